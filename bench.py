@@ -1,0 +1,389 @@
+"""Benchmark: aligned reads/s of FAME's single-end matching stage on GB300.
+
+Workload (default): 8 chromosomes / 300 Mbp synthetic genome with 8 %
+interspersed repeats, 5M bisulfite reads of 100 bp (1 % substitutions, 0.1 %
+indels), seeded (fame_gb300/synth.py).  One step = one CHUNKSIZE (300,000
+read) chunk through ReadQueue::matchReads semantics on the GPU: seeding and
+index gathers, Shift-And over every candidate window, uniqueness selection,
+banded DP and CpG tallies.  The first chunk (both orientations, strand vote)
+runs in the warm-up; timed steps are the following chunks in the decided
+orientation, as FAME's queryRoutine runs them.
+
+value: reads/s with reads resident in HBM (fame_gpu_match_reads_dev).
+e2e:   reads/s through fame_gpu_match_reads from pinned host buffers, host to
+       device copy of the chunk and device to host copy of the results timed.
+Both: per-step inputs are new reads, and each step gathers from a 5.2 GB index
+(4.3 GB bucket offsets + 1.2 GB entries), far larger than the 129 MB L2.
+
+--impl reference: the reference's own OpenMP matchReads (compiled from its
+sources by oracle/build_ref.sh) on the machine's host cores, on bounded samples of
+the same chunks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "aligned reads/s (single-end matching stage, bit-exact CpG report)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=12)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="se100_300mbp")
+    p.add_argument("--reads", type=int, default=0, help="override the workload's read count")
+    p.add_argument("--cpu-sample", type=int, default=60000, help="reads timed for the CPU baseline")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_init(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+def make_workload(name, n_reads):
+    from fame_gb300 import synth
+    spec = synth.WORKLOADS[name]
+    g = synth.make_genome(**spec["genome"])
+    rk = dict(spec["reads"])
+    if n_reads:
+        rk["n_reads"] = n_reads
+    rs = synth.make_reads(g, **rk)
+    return g, rs, rk.get("read_len", 100)
+
+
+def chunk_list(rs, chunk):
+    seq, offs = rs.concat()
+    n = len(rs)
+    out = []
+    for c0 in range(0, n, chunk):
+        c1 = min(n, c0 + chunk)
+        o = offs[c0:c1 + 1].copy()
+        out.append((int(o[0]), o - o[0]))
+    return np.frombuffer(seq, np.uint8), out
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(hi, seq, chunks, sample, readlen):
+    """The reference's OpenMP matchReads on a bounded sample of chunk 1 (steady state)."""
+    try:
+        from oracle import refbind
+        if not refbind.available():
+            raise RuntimeError("reference library not built")
+        L = refbind.RefLib()
+        if L.readlen != readlen:
+            raise RuntimeError("reference built for READLEN %d" % L.readlen)
+        t = hi.tables(sparse=False)
+
+        class Arrays:
+            pass
+
+        a = Arrays()
+        a.chrom_seqs = hi.chrom_seqs()
+        a.chrom_names = hi.chrom_names()
+        for k, v in t.items():
+            setattr(a, k, v)
+        a.tab_index64 = hi.tab_index64
+        ri = L.from_arrays(a)
+        base, o = chunks[1] if len(chunks) > 1 else chunks[0]
+        n = min(sample, len(o) - 1)
+        o = o[:n + 1]
+        s = seq[base:base + int(o[-1])].tobytes()
+        secs, cnt = ri.time_se(s, o, both_strands=False, match_r1_fwd=True)
+        ri.close()
+        return {"value": n / secs, "unit": "reads/s", "cores": L.corenum, "kind": "reference",
+                "sample": "%d reads of chunk 1 (300k-read CHUNKSIZE), decided orientation, matchReads only, "
+                          "CORENUM=%d OpenMP threads" % (n, L.corenum), "seconds": secs,
+                "succ": int(cnt[0])}
+    except Exception as e:
+        from oracle.oracle import OracleIndex  # single-threaded C restatement
+        return {"value": None, "unit": "reads/s", "cores": 1, "kind": "port",
+                "sample": "reference unavailable (%s)" % e}
+
+
+# ---------------------------------------------------------------------------
+def run_gb300(args):
+    import torch
+    from fame_gb300 import FAME_GET_STRANDED, FAME_MATCH_R1_FWD, GpuMatcher, HostIndex, CHUNKSIZE
+    rank, world, local = dist_init(args.gpus)
+    t0 = time.time()
+    g, rs, readlen = make_workload(args.workload, args.reads)
+    t_gen = time.time() - t0
+    t0 = time.time()
+    hi = HostIndex.build(g.seqs, readlen=readlen, threads=0)
+    t_build = time.time() - t0
+    t0 = time.time()
+    gm = GpuMatcher(hi, local)
+    t_open = time.time() - t0
+    seq, chunks = chunk_list(rs, CHUNKSIZE)
+    # device-resident copies of every chunk this rank handles (value) and pinned host copies (e2e)
+    mine = [i for i in range(len(chunks)) if i % world == rank] or [0]
+    dev = {}
+    pinned = {}
+    maxn = max(len(o) - 1 for _, o in chunks)
+    d_mat = gm.alloc(8 * maxn)
+    d_inv = gm.alloc(maxn)
+    for i in mine:
+        base, o = chunks[i]
+        nb = int(o[-1])
+        d_s = gm.alloc(nb)
+        d_o = gm.alloc(8 * len(o))
+        gm.memcpy(d_s, seq[base:].ctypes.data, nb, 1)
+        gm.memcpy(d_o, o.ctypes.data, 8 * len(o), 1)
+        dev[i] = (d_s, d_o, len(o) - 1)
+        hs = gm.host_alloc(nb)
+        ho = gm.host_alloc(8 * len(o)).view(np.uint64)
+        hs[:] = seq[base:base + nb]
+        ho[:] = o
+        pinned[i] = (hs, ho, len(o) - 1)
+    h_mat = gm.host_alloc(8 * maxn).view(np.uint64)
+    h_inv = gm.host_alloc(maxn)
+    p_stream = __import__("ctypes").c_void_p()
+    from fame_gb300._lib import lib as _L
+    _L().fame_gpu_stream(gm.h, __import__("ctypes").byref(p_stream))
+    stream = torch.cuda.ExternalStream(p_stream.value, device=local)
+    # warm-up: chunk 0 with the strand vote (getStranded), then decided orientation
+    first = mine[0]
+    d_s, d_o, n = dev[first]
+    c = gm.match_reads_dev(d_s, d_o, n, FAME_GET_STRANDED, d_mat, d_inv)
+    flags = FAME_MATCH_R1_FWD if c.r1_fwd > c.r1_rev else 0
+    steady = [i for i in mine if i != 0] or mine
+    for w in range(max(0, args.warmup - 1)):
+        d_s, d_o, n = dev[steady[w % len(steady)]]
+        gm.match_reads_dev(d_s, d_o, n, flags, d_mat, d_inv)
+    gm.set_timing(True)
+    # ---- timed: device-resident reads
+    stage = np.zeros(6)
+    reads = 0
+    gather = 0
+    scans = 0
+    launches = 0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        tw0 = time.perf_counter()
+        for k in range(args.steps):
+            d_s, d_o, n = dev[steady[k % len(steady)]]
+            c = gm.match_reads_dev(d_s, d_o, n, flags, d_mat, d_inv)
+            stage += gm.stage_times()
+            reads += n
+            gather += c.gather_bytes
+            scans += c.windows_scanned
+            launches += gm.last_launches()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        tw1 = time.perf_counter()
+    barrier(world)
+    t_dev = ev0.elapsed_time(ev1) / 1e3
+    t_max = allreduce_max(t_dev, world)
+    total_reads = reads * world
+    # ---- timed: end to end from pinned host memory
+    e_reads = 0
+    h2d = d2h = 0
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for k in range(args.steps):
+        hs, ho, n = pinned[steady[k % len(steady)]]
+        gm.match_reads(hs, ho, flags, mats=h_mat[:n], invalid=h_inv[:n])
+        e_reads += n
+        h2d += hs.nbytes + ho.nbytes
+        d2h += 9 * n
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = allreduce_max(ev0.elapsed_time(ev1) / 1e3, world)
+    gm.set_timing(False)
+    # ---- roofline of the index-gather (seeding) kernel and the Shift-And kernel
+    hbm, src = peaks()
+    names = ["read_prep", "seed_gather", "shift_and", "select_exact_cpg", "banded_dp", "seed_heavy"]
+    st = {names[i]: stage[i] / 1e3 for i in range(6)}
+    dominant = max(names, key=lambda k: st[k])
+    seed_s = st["seed_gather"] + st["seed_heavy"]
+    gbps = gather / seed_s / 1e9 if seed_s > 0 else 0.0
+    out = {
+        "metric": METRIC, "value": total_reads / t_max, "unit": "reads/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 integer",
+        "data": "synthetic (seeded; genome and bisulfite reads per the workload definition)",
+        "config": {"workload": args.workload, "genome_bp": int(g.total_len), "chromosomes": len(g.seqs),
+                   "reads_total": len(rs), "read_len": readlen, "chunk_reads": CHUNKSIZE,
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2: each step gathers from a 5.2 GB index and new reads"},
+        "e2e": {"value": e_reads * world / t_e2e, "unit": "reads/s", "h2d_bytes_per_step": int(h2d / args.steps),
+                "d2h_bytes_per_step": int(d2h / args.steps)},
+        "gpu_launches": launches,
+        "stage_seconds": st,
+        "dominant_kernel": dominant,
+        "roofline": {"kernel": "k_seed (index gathers)", "bound": "hbm", "achieved": gbps, "peak": hbm,
+                     "unit": "GB/s", "frac": gbps / hbm, "traffic": None,
+                     "note": "algorithmic bytes = 8 B bucket bounds + 4 B per bucket entry per k-mer; peak %s" % src},
+        "windows_scanned_per_read": scans / max(1, reads),
+        "clocks": clk.summary(),
+        "setup_seconds": {"generate": t_gen, "index_build": t_build, "upload": t_open},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(hi, seq, chunks, args.cpu_sample, readlen)
+    for i in mine:
+        gm.free(dev[i][0])
+        gm.free(dev[i][1])
+    gm.close()
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def run_reference(args):
+    rank, world, local = dist_init(args.gpus)
+    if rank != 0:
+        return
+    from fame_gb300 import CHUNKSIZE, HostIndex
+    g, rs, readlen = make_workload(args.workload, args.reads)
+    try:
+        from oracle import refbind
+        if not refbind.available():
+            import __graft_entry__
+            __graft_entry__.build()
+        if not refbind.available():
+            raise RuntimeError("reference sources not available to oracle/build_ref.sh")
+        L = refbind.RefLib()
+        fasta = "/tmp/fame_bench_%s.fa" % args.workload
+        g.write_fasta(fasta)
+        ri = L.build(fasta)  # the reference's own readReference + RefGenome constructor
+        kind = "reference"
+    except Exception as e:
+        print(json.dumps({"impl": "reference", "unavailable": "reference build failed: %s" % e}))
+        return
+    seq, chunks = chunk_list(rs, CHUNKSIZE)
+    sample = min(args.cpu_sample, CHUNKSIZE)
+    steady = list(range(1, len(chunks))) or [0]
+
+    def step(k):
+        base, o = chunks[steady[k % len(steady)]]
+        o = o[:sample + 1]
+        return ri.time_se(seq[base:base + int(o[-1])].tobytes(), o, both_strands=False, match_r1_fwd=True), len(o) - 1
+
+    for k in range(args.warmup):
+        step(k)
+    secs = 0.0
+    reads = 0
+    for k in range(args.steps):
+        (s, _), n = step(k)
+        secs += s
+        reads += n
+    v = reads / secs
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "reads/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 integer",
+        "data": "synthetic (seeded)", "config": {"workload": args.workload, "reads_per_step": sample},
+        "cpu_baseline": {"value": v, "unit": "reads/s", "cores": L.corenum, "kind": kind,
+                         "sample": "%d reads per step from consecutive 300k-read chunks, decided orientation"
+                                   % sample},
+        "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+    ri.close()
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)

@@ -1,0 +1,289 @@
+"""ctypes binding of libfame_gpu.so (the C ABI declared in include/fame_gpu.h).
+
+The library is the product; this module only marshals numpy buffers.  It
+raises on import-time use when the library has not been built, so no caller
+can silently run without the CUDA path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import numpy as np
+
+from . import build as _build
+
+_P = C.c_void_p
+HTABSIZE = 1 << 30
+CHUNKSIZE = 300000
+
+FAME_GET_STRANDED = 1
+FAME_BOTH_STRANDS = 2
+FAME_MATCH_R1_FWD = 4
+FAME_MAX_READ_LEN = 255
+
+ERRORS = {0: "FAME_OK", -1: "FAME_ERR_ARG", -2: "FAME_ERR_CUDA", -3: "FAME_ERR_NOMEM", -4: "FAME_ERR_INDEX",
+          -5: "FAME_ERR_READ", -6: "FAME_ERR_IO", -7: "FAME_ERR_TIMEOUT", -8: "FAME_ERR_BUSY"}
+
+
+class FameError(RuntimeError):
+    def __init__(self, code, msg=""):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class IndexView(C.Structure):
+    _fields_ = [("readlen", C.c_uint32), ("n_chrom", C.c_uint32), ("chrom_seq", _P), ("chrom_len", _P),
+                ("chrom_name", _P), ("n_cpg", C.c_uint64), ("cpg", _P), ("tab_index", _P), ("tab_index32", _P),
+                ("n_kmer", C.c_uint64), ("kmer", _P), ("strand_bits", _P), ("n_win", C.c_uint64), ("win", _P),
+                ("n_filtered", C.c_uint64), ("filtered", _P)]
+
+
+class Counters(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("succ", "nonunique", "unsucc", "r1_fwd", "r1_rev", "invalid_len",
+                                          "invalid_n", "gather_bytes", "windows_scanned", "dp_reads")]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+CPG_DT = np.dtype([("chrom", np.uint8), ("pos", np.uint32)], align=True)                 # 8 bytes
+WIN_DT = np.dtype([("start_pos", np.uint32), ("chrom", np.uint8), ("start_ind", np.uint32),
+                   ("end_ind", np.uint32)], align=True)                                   # 16 bytes
+KMER_DT = np.dtype([("meta", np.uint32), ("tmask", np.uint32)])
+
+EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_index_free", "fame_index_cpg_start",
+           "fame_gpu_open", "fame_gpu_close", "fame_gpu_last_error", "fame_gpu_match_reads",
+           "fame_gpu_match_reads_dev", "fame_gpu_tallies", "fame_gpu_alloc", "fame_gpu_free", "fame_gpu_memcpy",
+           "fame_gpu_host_alloc", "fame_gpu_host_free", "fame_gpu_stream", "fame_gpu_set_timing",
+           "fame_gpu_stage_times", "fame_gpu_last_launches"]
+
+_lib = None
+
+
+def lib(build_if_missing: bool = True):
+    """Load libfame_gpu.so (building it first when allowed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise ImportError("libfame_gpu.so is not built (run fame_gb300.build.build())")
+        _build.build()
+    L = C.CDLL(_build.LIB)
+    L.fame_index_read.argtypes = [C.c_char_p, _P]
+    L.fame_index_build.argtypes = [C.c_uint32, C.c_uint32, _P, _P, _P, C.c_int, C.c_int, _P]
+    L.fame_index_view_of.argtypes = [_P, _P]
+    L.fame_index_free.argtypes = [_P]
+    L.fame_index_free.restype = None
+    L.fame_index_cpg_start.argtypes = [_P, _P, C.c_uint64]
+    L.fame_index_cpg_start.restype = C.c_uint64
+    L.fame_gpu_open.argtypes = [_P, C.c_int, _P]
+    L.fame_gpu_close.argtypes = [_P]
+    L.fame_gpu_last_error.argtypes = [_P]
+    L.fame_gpu_last_error.restype = C.c_char_p
+    L.fame_gpu_match_reads.argtypes = [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]
+    L.fame_gpu_match_reads_dev.argtypes = [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]
+    L.fame_gpu_tallies.argtypes = [_P, _P, C.c_int]
+    L.fame_gpu_alloc.argtypes = [_P, C.c_size_t, _P]
+    L.fame_gpu_free.argtypes = [_P, _P]
+    L.fame_gpu_memcpy.argtypes = [_P, _P, _P, C.c_size_t, C.c_int]
+    L.fame_gpu_host_alloc.argtypes = [_P, C.c_size_t, _P]
+    L.fame_gpu_host_free.argtypes = [_P, _P]
+    L.fame_gpu_stream.argtypes = [_P, _P]
+    L.fame_gpu_set_timing.argtypes = [_P, C.c_int]
+    L.fame_gpu_stage_times.argtypes = [_P, _P, C.c_int]
+    L.fame_gpu_last_launches.argtypes = [_P]
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+def _check(rc, handle=None):
+    if rc != 0:
+        msg = lib().fame_gpu_last_error(handle).decode() if handle else ""
+        raise FameError(rc, msg)
+
+
+class HostIndex:
+    """A loaded (or built) FAME index in host memory, owned by the library."""
+
+    def __init__(self, handle):
+        self.h = _P(handle) if not isinstance(handle, _P) else handle
+        self.view = IndexView()
+        _check(lib().fame_index_view_of(self.h, C.byref(self.view)))
+
+    @classmethod
+    def read(cls, path: str) -> "HostIndex":
+        """The --load_index format (RefGenome::save / load)."""
+        h = _P()
+        _check(lib().fame_index_read(path.encode(), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def build(cls, chrom_seqs, readlen: int = 100, names=None, noloss: bool = False, threads: int = 0) -> "HostIndex":
+        """Index build from chromosome sequences (uint8 arrays or bytes)."""
+        arrs = [np.ascontiguousarray(np.frombuffer(s, np.uint8) if isinstance(s, (bytes, bytearray)) else s,
+                                     dtype=np.uint8) for s in chrom_seqs]
+        ptrs = (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        lens = np.array([len(a) for a in arrs], dtype=np.uint64)
+        nm = None
+        if names is not None:
+            enc = [n.encode() for n in names]
+            nm = (C.c_char_p * len(enc))(*enc)
+        h = _P()
+        _check(lib().fame_index_build(readlen, len(arrs), C.cast(ptrs, _P), _ptr(lens),
+                                      C.cast(nm, _P) if nm is not None else None, int(noloss), threads, C.byref(h)))
+        return cls(h)
+
+    def close(self):
+        if self.h:
+            lib().fame_index_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- numpy views of the tables (borrowed) ----
+    def _arr(self, addr, count, dtype):
+        if count == 0 or not addr:
+            return np.zeros(0, dtype=dtype)
+        buf = (C.c_char * (int(count) * np.dtype(dtype).itemsize)).from_address(addr)
+        return np.frombuffer(buf, dtype=dtype)
+
+    @property
+    def readlen(self) -> int:
+        return int(self.view.readlen)
+
+    @property
+    def n_cpg(self) -> int:
+        return int(self.view.n_cpg)
+
+    def chrom_names(self):
+        v = self.view
+        p = C.cast(v.chrom_name, C.POINTER(C.c_char_p))
+        return [p[i].decode() for i in range(v.n_chrom)]
+
+    def chrom_seqs(self):
+        v = self.view
+        sp = C.cast(v.chrom_seq, C.POINTER(C.c_void_p))
+        lens = self._arr(v.chrom_len, v.n_chrom, np.uint64)
+        return [self._arr(sp[i], int(lens[i]), np.uint8) for i in range(v.n_chrom)]
+
+    def tables(self, sparse: bool = True) -> dict:
+        """Index tables; with sparse=True the hash-table offsets are given as the
+        non-empty buckets (key, start, len), the layout of the oracle and the
+        golden files, otherwise omitted (see tab_index64)."""
+        v = self.view
+        cpg = self._arr(v.cpg, v.n_cpg, CPG_DT)
+        km = self._arr(v.kmer, v.n_kmer, KMER_DT)
+        win = self._arr(v.win, v.n_win, WIN_DT)
+        if sparse:
+            if v.tab_index32:
+                tab = self._arr(v.tab_index32, HTABSIZE + 1, np.uint32).astype(np.uint64)
+            else:
+                tab = self._arr(v.tab_index, HTABSIZE + 1, np.uint64)
+            ln = np.diff(tab)
+            keys = np.nonzero(ln)[0]
+        else:
+            tab = ln = keys = np.zeros(0, np.uint64)
+        sbits = self._arr(v.strand_bits, (v.n_kmer + 7) // 8, np.uint8)
+        strand = np.unpackbits(sbits, bitorder="little")[: v.n_kmer].astype(np.uint8)
+        ncs = lib().fame_index_cpg_start(self.h, None, 0)
+        cs = np.zeros(int(ncs), dtype=CPG_DT)
+        lib().fame_index_cpg_start(self.h, _ptr(cs), ncs)
+        return dict(cpg_chrom=np.ascontiguousarray(cpg["chrom"]), cpg_pos=np.ascontiguousarray(cpg["pos"]),
+                    cpgs_chrom=np.ascontiguousarray(cs["chrom"]), cpgs_pos=np.ascontiguousarray(cs["pos"]),
+                    bucket_key=keys.astype(np.uint32), bucket_start=tab[keys].astype(np.uint64),
+                    bucket_len=ln[keys].astype(np.uint32), kmer_meta=np.ascontiguousarray(km["meta"]),
+                    kmer_tmask=np.ascontiguousarray(km["tmask"]), strand=strand,
+                    win_start=np.ascontiguousarray(win["start_pos"]), win_chrom=np.ascontiguousarray(win["chrom"]),
+                    win_sind=np.ascontiguousarray(win["start_ind"]), win_eind=np.ascontiguousarray(win["end_ind"]),
+                    filtered=self._arr(v.filtered, v.n_filtered, np.uint64).copy())
+
+    def tab_index64(self):
+        v = self.view
+        if v.tab_index32:
+            return self._arr(v.tab_index32, HTABSIZE + 1, np.uint32).astype(np.uint64)
+        return self._arr(v.tab_index, HTABSIZE + 1, np.uint64)
+
+
+class GpuMatcher:
+    """The device context: index resident in HBM, chunk matching, tallies."""
+
+    def __init__(self, index: HostIndex, device: int = 0):
+        self.index = index
+        self.h = _P()
+        _check(lib().fame_gpu_open(C.byref(index.view), device, C.byref(self.h)))
+        self.n_cpg = index.n_cpg
+
+    def close(self):
+        if self.h:
+            lib().fame_gpu_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def match_reads(self, seq_bytes, offs, flags: int, mats=None, invalid=None):
+        offs = np.ascontiguousarray(offs, dtype=np.uint64)
+        n = len(offs) - 1
+        buf = np.frombuffer(seq_bytes, dtype=np.uint8) if isinstance(seq_bytes, (bytes, bytearray)) else seq_bytes
+        mats = np.zeros(n, np.uint64) if mats is None else mats
+        invalid = np.zeros(n, np.uint8) if invalid is None else invalid
+        cnt = Counters()
+        _check(lib().fame_gpu_match_reads(self.h, _ptr(buf), _ptr(offs), n, flags, _ptr(mats), _ptr(invalid),
+                                          C.byref(cnt)), self.h)
+        return mats, invalid, cnt
+
+    def match_reads_dev(self, seqs_dev, offs_dev, n: int, flags: int, mats_dev, invalid_dev):
+        cnt = Counters()
+        _check(lib().fame_gpu_match_reads_dev(self.h, seqs_dev, offs_dev, n, flags, mats_dev, invalid_dev,
+                                              C.byref(cnt)), self.h)
+        return cnt
+
+    def tallies(self, reset: bool = False) -> np.ndarray:
+        out = np.zeros(4 * self.n_cpg, np.uint16)
+        _check(lib().fame_gpu_tallies(self.h, _ptr(out), int(reset)), self.h)
+        return out.reshape(-1, 4)
+
+    def set_timing(self, on: bool):
+        _check(lib().fame_gpu_set_timing(self.h, int(on)), self.h)
+
+    def stage_times(self):
+        ms = np.zeros(6, np.float32)
+        lib().fame_gpu_stage_times(self.h, _ptr(ms), 6)
+        return ms
+
+    def last_launches(self) -> int:
+        return int(lib().fame_gpu_last_launches(self.h))
+
+    # device / pinned memory helpers
+    def alloc(self, nbytes: int) -> int:
+        p = _P()
+        _check(lib().fame_gpu_alloc(self.h, nbytes, C.byref(p)), self.h)
+        return p.value
+
+    def free(self, p):
+        _check(lib().fame_gpu_free(self.h, p), self.h)
+
+    def memcpy(self, dst, src, nbytes: int, kind: int):
+        _check(lib().fame_gpu_memcpy(self.h, dst, src, nbytes, kind), self.h)
+
+    def host_alloc(self, nbytes: int) -> np.ndarray:
+        p = _P()
+        _check(lib().fame_gpu_host_alloc(self.h, nbytes, C.byref(p)), self.h)
+        buf = (C.c_char * nbytes).from_address(p.value)
+        arr = np.frombuffer(buf, dtype=np.uint8)
+        return arr
+
+    def host_free(self, arr: np.ndarray):
+        _check(lib().fame_gpu_host_free(self.h, arr.ctypes.data), self.h)

@@ -1,0 +1,124 @@
+// Device-side data layout and helpers shared by the matching kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fame_const.h"
+
+namespace fame {
+
+// The index as it lives in HBM (read-only for the whole context lifetime).
+//   tab    : bucket start offsets, HTABSIZE + 1 x uint32 (tabIndex)
+//   entry  : one uint32 per k-mer entry: window id | forward-strand << 31
+//            (kmerTableSmall.meta with strandTable folded into bit 31; the
+//            start-CpG bit the reference reserves there is never set by the
+//            window index and is rejected on upload)
+//   gpack  : genome, 2 bits per base (A0 C1 G2 T3), 16 bases per word,
+//            chromosomes concatenated at 32-base aligned offsets
+//   gnmask : one bit per base, set for N
+//   win    : {startPos, chrom, startInd, endInd} per window (metaWindows)
+struct DevIndex {
+    uint32_t readlen;
+    uint32_t n_chrom;
+    const uint32_t* tab;
+    const uint32_t* entry;
+    const uint32_t* gpack;
+    const uint32_t* gnmask;
+    const uint64_t* chrom_off;
+    const uint64_t* chrom_len;
+    const uint4* win;
+    const uint32_t* cpg_pos;
+    const uint8_t* cpg_chrom;
+    uint64_t n_cpg;
+    uint64_t n_win;
+};
+
+// Per-chunk buffers.
+struct ChunkBufs {
+    const char* seqs;        // reads back to back
+    const uint64_t* offs;    // n + 1
+    uint32_t n;
+    uint32_t orient_mask;    // bit0 forward read, bit1 reverse complement
+    uint32_t stranded;       // count r1 votes (getStranded)
+    uint8_t* rflags;         // per read: bit0 too short, bit1 has N, bit2 too long
+    uint4* task_cand;        // per task (read*2 + orient): {cand offset, n forward-map, n reverse-map, -}
+    uint32_t* cand;          // candidate windows (entry encoding), in iteration order
+    uint32_t* cand_task;     // task of each candidate
+    uint32_t cand_cap;
+    uint32_t* hits;          // HIT_CAP per candidate: offset << 8 | errors
+    uint32_t* hit_n;         // number of hits of each candidate (may exceed HIT_CAP)
+    uint64_t* mats;
+    uint8_t* invalid;
+    uint32_t* dp_list;       // reads that need the banded DP: read
+    uint64_t* dp_mat;        // their match
+    uint8_t* dp_orient;
+    uint32_t* meth;          // 4 x n_cpg counters (uint16 semantics after the fact)
+    unsigned long long* ctr; // device counters, see CTR_*
+    uint32_t* heavy;         // tasks handed to the heavy path
+};
+
+enum {
+    CTR_CAND = 0,       // candidates allocated
+    CTR_HEAVY,          // heavy tasks
+    CTR_DP,             // DP reads
+    CTR_SUCC,
+    CTR_NONU,
+    CTR_UNSUCC,
+    CTR_R1F,
+    CTR_R1R,
+    CTR_INV_LEN,
+    CTR_INV_N,
+    CTR_GATHER_BYTES,
+    CTR_SCANS,
+    CTR_TOO_LONG,
+    CTR_ERRFLAG,        // a device-side capacity check failed
+    CTR_N
+};
+
+constexpr int HIT_CAP = 6;
+
+__device__ __forceinline__ uint64_t rotl64(uint64_t v, unsigned s)
+{
+    s &= 63u;
+    return s ? (v << s) | (v >> (64 - s)) : v;
+}
+
+// msTab value of a read byte (spaced_nthash/nthash.hpp:88-121)
+__device__ __forceinline__ uint64_t nt_val(uint8_t c)
+{
+    switch (c) {
+        case 'A': case 'a': case 4: return NT_SEED_A;
+        case 'C': case 'c': case 'T': case 't': case 1: case 7: return NT_SEED_T;
+        case 'G': case 'g': case 3: return NT_SEED_G;
+        default: return 0;
+    }
+}
+
+// reverse complement byte as matchReads builds revSeq (ReadQueue.cpp:448-484):
+// other letters leave the zero the string was resized with.
+__device__ __forceinline__ uint8_t rc_byte(uint8_t c)
+{
+    switch (c) {
+        case 'A': return 'T';
+        case 'C': return 'G';
+        case 'G': return 'C';
+        case 'T': return 'A';
+        default: return 0;
+    }
+}
+
+// Base of the packed genome: 0..3 for ACGT, 4 for N, 5 outside the chromosome.
+__device__ __forceinline__ int gbase(const DevIndex& ix, uint32_t chrom, int64_t pos)
+{
+    if (pos < 0 || (uint64_t)pos >= ix.chrom_len[chrom]) return 5;
+    const uint64_t g = ix.chrom_off[chrom] + (uint64_t)pos;
+    if ((__ldg(ix.gnmask + (g >> 5)) >> (g & 31)) & 1u) return 4;
+    return (int)((__ldg(ix.gpack + (g >> 4)) >> (2 * (g & 15))) & 3u);
+}
+
+__device__ __forceinline__ uint8_t base_char(int b)
+{
+    return b == 0 ? 'A' : b == 1 ? 'C' : b == 2 ? 'G' : b == 3 ? 'T' : b == 4 ? 'N' : 0;
+}
+
+}  // namespace fame

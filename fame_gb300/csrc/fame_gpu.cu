@@ -1,0 +1,539 @@
+// C ABI implementation: index upload, per-chunk matching pipeline, tallies.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/fame_gpu.h"
+#include "index_host.h"
+#include "kernels.cuh"
+
+using namespace fame;
+
+struct fame_gpu {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    DevIndex ix{};
+    std::vector<void*> index_allocs;
+    uint64_t n_cpg = 0;
+    uint32_t max_bucket = 0;
+    // chunk buffers
+    uint64_t cap_reads = 0, cap_bytes = 0, cap_cand = 0;
+    char* d_seqs = nullptr;
+    uint64_t* d_offs = nullptr;
+    uint8_t* d_rflags = nullptr;
+    uint4* d_task_cand = nullptr;
+    uint32_t *d_cand = nullptr, *d_cand_task = nullptr, *d_hits = nullptr, *d_hit_n = nullptr;
+    uint64_t* d_mats = nullptr;
+    uint8_t* d_invalid = nullptr;
+    uint32_t* d_dp_list = nullptr;
+    uint64_t* d_dp_mat = nullptr;
+    uint8_t* d_dp_orient = nullptr;
+    uint32_t* d_heavy = nullptr;
+    unsigned long long* d_ctr = nullptr;
+    unsigned long long* h_ctr = nullptr;  // pinned
+    uint32_t* d_meth = nullptr;
+    DpScratch dp{};
+    HeavyScratch hs{};
+    int timing = 0;
+    cudaEvent_t ev[8]{};
+    float stage_ms[6]{};
+    int launches = 0;
+    int sm_count = 0;
+    uint32_t wmask = 0x1e;  // Shift-And word counts present in the chunk (bit W)
+};
+
+namespace {
+
+int set_err(fame_gpu* g, int code, const std::string& msg)
+{
+    if (g) g->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return set_err(g, e_ == cudaErrorMemoryAllocation ? FAME_ERR_NOMEM : FAME_ERR_CUDA,    \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                     \
+    } while (0)
+
+template <class T>
+int dev_alloc(fame_gpu* g, T** p, uint64_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    CK(cudaMalloc((void**)p, count * sizeof(T)));
+    return FAME_OK;
+}
+
+template <class T>
+void dev_free(T*& p)
+{
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+int grow_chunk(fame_gpu* g, uint64_t n, uint64_t bytes, uint64_t cand)
+{
+    int rc;
+    if (n > g->cap_reads) {
+        const uint64_t c = std::max<uint64_t>(n, 1024);
+        dev_free(g->d_offs); dev_free(g->d_rflags); dev_free(g->d_task_cand); dev_free(g->d_mats);
+        dev_free(g->d_invalid); dev_free(g->d_dp_list); dev_free(g->d_dp_mat); dev_free(g->d_dp_orient);
+        dev_free(g->d_heavy);
+        if ((rc = dev_alloc(g, &g->d_offs, c + 1)) || (rc = dev_alloc(g, &g->d_rflags, c)) ||
+            (rc = dev_alloc(g, &g->d_task_cand, 2 * c)) || (rc = dev_alloc(g, &g->d_mats, c)) ||
+            (rc = dev_alloc(g, &g->d_invalid, c)) || (rc = dev_alloc(g, &g->d_dp_list, c)) ||
+            (rc = dev_alloc(g, &g->d_dp_mat, c)) || (rc = dev_alloc(g, &g->d_dp_orient, c)) ||
+            (rc = dev_alloc(g, &g->d_heavy, 2 * c)))
+            return rc;
+        g->cap_reads = c;
+    }
+    if (bytes > g->cap_bytes) {
+        const uint64_t c = std::max<uint64_t>(bytes, 1 << 20);
+        dev_free(g->d_seqs);
+        if ((rc = dev_alloc(g, &g->d_seqs, c))) return rc;
+        g->cap_bytes = c;
+    }
+    if (cand > g->cap_cand) {
+        const uint64_t c = std::max<uint64_t>(cand, 1 << 16);
+        dev_free(g->d_cand); dev_free(g->d_cand_task); dev_free(g->d_hits); dev_free(g->d_hit_n);
+        if ((rc = dev_alloc(g, &g->d_cand, c)) || (rc = dev_alloc(g, &g->d_cand_task, c)) ||
+            (rc = dev_alloc(g, &g->d_hits, c * HIT_CAP)) || (rc = dev_alloc(g, &g->d_hit_n, c)))
+            return rc;
+        g->cap_cand = c;
+    }
+    return FAME_OK;
+}
+
+uint32_t pow2_ceil_host(uint64_t v)
+{
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return (uint32_t)p;
+}
+
+}  // namespace
+
+extern "C" const char* fame_gpu_last_error(const fame_gpu* g) { return g ? g->err.c_str() : "null context"; }
+
+extern "C" int fame_gpu_close(fame_gpu* g)
+{
+    if (!g) return FAME_ERR_ARG;
+    cudaSetDevice(g->device);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    for (void* p : g->index_allocs) cudaFree(p);
+    dev_free(g->d_seqs); dev_free(g->d_offs); dev_free(g->d_rflags); dev_free(g->d_task_cand);
+    dev_free(g->d_cand); dev_free(g->d_cand_task); dev_free(g->d_hits); dev_free(g->d_hit_n);
+    dev_free(g->d_mats); dev_free(g->d_invalid); dev_free(g->d_dp_list); dev_free(g->d_dp_mat);
+    dev_free(g->d_dp_orient); dev_free(g->d_heavy); dev_free(g->d_ctr); dev_free(g->d_meth);
+    dev_free(g->dp.cells); dev_free(g->dp.align); dev_free(g->hs.base);
+    if (g->h_ctr) cudaFreeHost(g->h_ctr);
+    for (auto& e : g->ev) if (e) cudaEventDestroy(e);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+    return FAME_OK;
+}
+
+extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** out)
+{
+    if (!v || !out) return FAME_ERR_ARG;
+    *out = nullptr;
+    fame_gpu* g = new (std::nothrow) fame_gpu();
+    if (!g) return FAME_ERR_NOMEM;
+    auto fail = [&](int rc) { *out = nullptr; std::string m = g->err; fame_gpu_close(g); (void)m; return rc; };
+    g->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) return fail(set_err(g, FAME_ERR_CUDA, "cudaSetDevice failed"));
+    cudaDeviceGetAttribute(&g->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(set_err(g, FAME_ERR_CUDA, "cudaStreamCreate failed"));
+    for (auto& e : g->ev) cudaEventCreate(&e);
+    // ---- validate the view
+    if (v->n_chrom == 0 || v->n_chrom > 256 || !v->chrom_seq || !v->chrom_len || !v->kmer ||
+        (!v->tab_index && !v->tab_index32) || (!v->strand_bits && v->n_kmer) || !v->win ||
+        (!v->cpg && v->n_cpg) || v->readlen <= KMERLEN || v->readlen >= WINLEN)
+        return fail(set_err(g, FAME_ERR_INDEX, "incomplete index view"));
+    if (v->n_kmer >= 0xffffffffull || v->n_win >= 0x7fffffffull || v->n_cpg >= 0xffffffffull)
+        return fail(set_err(g, FAME_ERR_INDEX, "index tables exceed 32-bit device offsets"));
+    g->ix.readlen = v->readlen;
+    g->ix.n_chrom = v->n_chrom;
+    g->ix.n_cpg = v->n_cpg;
+    g->ix.n_win = v->n_win;
+    g->n_cpg = v->n_cpg;
+    auto alloc_idx = [&](void** p, uint64_t bytes) -> int {
+        if (cudaMalloc(p, std::max<uint64_t>(bytes, 16)) != cudaSuccess)
+            return set_err(g, FAME_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed");
+        g->index_allocs.push_back(*p);
+        return FAME_OK;
+    };
+    int rc;
+    // ---- tabIndex -> uint32 offsets
+    uint32_t* d_tab;
+    if ((rc = alloc_idx((void**)&d_tab, (HTABSIZE + 1) * 4))) return fail(rc);
+    const uint64_t CH = 1ull << 24;
+    std::vector<uint32_t> stage(CH);
+    if (v->tab_index32) {
+        if (v->tab_index32[HTABSIZE] != v->n_kmer) return fail(set_err(g, FAME_ERR_INDEX, "tabIndex end != k-mer count"));
+        if (cudaMemcpy(d_tab, v->tab_index32, (HTABSIZE + 1) * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(set_err(g, FAME_ERR_CUDA, "tabIndex upload failed"));
+    } else {
+        if (v->tab_index[HTABSIZE] != v->n_kmer) return fail(set_err(g, FAME_ERR_INDEX, "tabIndex end != k-mer count"));
+        for (uint64_t b = 0; b < HTABSIZE + 1; b += CH) {
+            const uint64_t e = std::min<uint64_t>(HTABSIZE + 1, b + CH);
+            for (uint64_t i = b; i < e; ++i) stage[i - b] = (uint32_t)v->tab_index[i];
+            if (cudaMemcpy(d_tab + b, stage.data(), (e - b) * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+                return fail(set_err(g, FAME_ERR_CUDA, "tabIndex upload failed"));
+        }
+    }
+    g->ix.tab = d_tab;
+    // ---- entries: window id | forward << 31
+    uint32_t* d_entry;
+    if ((rc = alloc_idx((void**)&d_entry, v->n_kmer * 4))) return fail(rc);
+    for (uint64_t b = 0; b < v->n_kmer; b += CH) {
+        const uint64_t e = std::min<uint64_t>(v->n_kmer, b + CH);
+        for (uint64_t i = b; i < e; ++i) {
+            const uint32_t meta = v->kmer[i].meta;
+            if ((meta >> 31) || meta >= v->n_win)
+                return fail(set_err(g, FAME_ERR_INDEX, "k-mer entry " + std::to_string(i) + " has a start-CpG flag or an unknown window"));
+            const uint32_t fwd = (v->strand_bits[i >> 3] >> (i & 7)) & 1u;
+            stage[i - b] = meta | (fwd << 31);
+        }
+        if (cudaMemcpy(d_entry + b, stage.data(), (e - b) * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(set_err(g, FAME_ERR_CUDA, "k-mer upload failed"));
+    }
+    g->ix.entry = d_entry;
+    // ---- genome: 2-bit codes + N mask, chromosomes at 32-base aligned offsets
+    std::vector<uint64_t> coff(v->n_chrom), clen(v->n_chrom);
+    uint64_t tot = 0;
+    for (uint32_t c = 0; c < v->n_chrom; ++c) { coff[c] = tot; clen[c] = v->chrom_len[c]; tot += (clen[c] + 31) / 32 * 32; }
+    {
+        std::vector<uint32_t> pack(tot / 16 + 1, 0), nm(tot / 32 + 1, 0);
+        for (uint32_t c = 0; c < v->n_chrom; ++c) {
+            const char* s = v->chrom_seq[c];
+            for (uint64_t i = 0; i < clen[c]; ++i) {
+                const uint64_t gi = coff[c] + i;
+                uint32_t code;
+                switch (s[i]) {
+                    case 'A': code = 0; break;
+                    case 'C': code = 1; break;
+                    case 'G': code = 2; break;
+                    case 'T': code = 3; break;
+                    case 'N': code = 0; nm[gi >> 5] |= 1u << (gi & 31); break;
+                    default:
+                        return fail(set_err(g, FAME_ERR_INDEX, "reference base outside ACGTN in chromosome " + std::to_string(c)));
+                }
+                pack[gi >> 4] |= code << (2 * (gi & 15));
+            }
+        }
+        uint32_t *d_pack, *d_nm;
+        uint64_t *d_coff, *d_clen;
+        if ((rc = alloc_idx((void**)&d_pack, pack.size() * 4)) || (rc = alloc_idx((void**)&d_nm, nm.size() * 4)) ||
+            (rc = alloc_idx((void**)&d_coff, coff.size() * 8)) || (rc = alloc_idx((void**)&d_clen, clen.size() * 8)))
+            return fail(rc);
+        if (cudaMemcpy(d_pack, pack.data(), pack.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(d_nm, nm.data(), nm.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(d_coff, coff.data(), coff.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(d_clen, clen.data(), clen.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(set_err(g, FAME_ERR_CUDA, "genome upload failed"));
+        g->ix.gpack = d_pack; g->ix.gnmask = d_nm; g->ix.chrom_off = d_coff; g->ix.chrom_len = d_clen;
+    }
+    // ---- windows and CpGs
+    {
+        std::vector<uint4> w(v->n_win);
+        for (uint64_t i = 0; i < v->n_win; ++i) {
+            if (v->win[i].chrom >= v->n_chrom) return fail(set_err(g, FAME_ERR_INDEX, "window on unknown chromosome"));
+            if (v->win[i].start_ind != CPGDUMMY && (v->win[i].start_ind >= v->n_cpg || (v->win[i].end_ind != CPGDUMMY && v->win[i].end_ind >= v->n_cpg)))
+                return fail(set_err(g, FAME_ERR_INDEX, "window CpG range outside cpgTable"));
+            w[i] = make_uint4(v->win[i].start_pos, v->win[i].chrom, v->win[i].start_ind, v->win[i].end_ind);
+        }
+        std::vector<uint32_t> pos(v->n_cpg);
+        std::vector<uint8_t> chr(v->n_cpg);
+        for (uint64_t i = 0; i < v->n_cpg; ++i) { pos[i] = v->cpg[i].pos; chr[i] = v->cpg[i].chrom; }
+        uint4* d_win;
+        uint32_t* d_pos;
+        uint8_t* d_chr;
+        if ((rc = alloc_idx((void**)&d_win, w.size() * 16)) || (rc = alloc_idx((void**)&d_pos, pos.size() * 4)) ||
+            (rc = alloc_idx((void**)&d_chr, chr.size())))
+            return fail(rc);
+        if (cudaMemcpy(d_win, w.data(), w.size() * 16, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(d_pos, pos.data(), pos.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(d_chr, chr.data(), chr.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(set_err(g, FAME_ERR_CUDA, "window/CpG upload failed"));
+        g->ix.win = d_win; g->ix.cpg_pos = d_pos; g->ix.cpg_chrom = d_chr;
+    }
+    // ---- largest bucket -> heavy-path scratch
+    {
+        unsigned int* d_mx;
+        if (cudaMalloc(&d_mx, 4) != cudaSuccess) return fail(set_err(g, FAME_ERR_NOMEM, "alloc"));
+        cudaMemset(d_mx, 0, 4);
+        k_max_bucket<<<g->sm_count * 8, 256, 0, g->stream>>>(d_tab, HTABSIZE, d_mx);
+        unsigned int mx = 0;
+        cudaMemcpyAsync(&mx, d_mx, 4, cudaMemcpyDeviceToHost, g->stream);
+        if (cudaStreamSynchronize(g->stream) != cudaSuccess) { cudaFree(d_mx); return fail(set_err(g, FAME_ERR_CUDA, "bucket scan failed")); }
+        cudaFree(d_mx);
+        g->max_bucket = mx;
+        const uint64_t ops_cap = std::max<uint64_t>(L_OPS + 1, std::min<uint64_t>((uint64_t)224 * std::max(1u, mx), 1ull << 24));
+        g->hs.ops_cap = (uint32_t)ops_cap;
+        g->hs.dt_cap = pow2_ceil_host(2 * ops_cap + 2);
+        g->hs.slot_cap = 2 * pow2_ceil_host(ops_cap + 1) + 64;
+        g->hs.bytes_per_warp = heavy_bytes_per_warp(g->hs.ops_cap, g->hs.dt_cap, g->hs.slot_cap);
+        g->hs.nwarps = (uint32_t)std::max<uint64_t>(8, std::min<uint64_t>(256, (4ull << 30) / g->hs.bytes_per_warp));
+        if (cudaMalloc(&g->hs.base, g->hs.bytes_per_warp * g->hs.nwarps) != cudaSuccess)
+            return fail(set_err(g, FAME_ERR_NOMEM, "heavy-path scratch allocation failed"));
+    }
+    // ---- tallies, counters, DP scratch
+    if ((rc = dev_alloc(g, &g->d_meth, 4 * std::max<uint64_t>(1, v->n_cpg)))) return fail(rc);
+    if (cudaMemset(g->d_meth, 0, 16 * std::max<uint64_t>(1, v->n_cpg)) != cudaSuccess) return fail(set_err(g, FAME_ERR_CUDA, "memset"));
+    if ((rc = dev_alloc(g, &g->d_ctr, CTR_N))) return fail(rc);
+    if (cudaMallocHost(&g->h_ctr, CTR_N * sizeof(unsigned long long)) != cudaSuccess) return fail(set_err(g, FAME_ERR_NOMEM, "pinned alloc"));
+    g->dp.nslots = 128u * (uint32_t)std::max(1, g->sm_count);
+    g->dp.cell_cap = (FAME_MAX_READ_LEN + 1) * (uint32_t)DPW;
+    g->dp.align_cap = 2 * FAME_MAX_READ_LEN + 4 * DP_BAND + 8;
+    if ((rc = dev_alloc(g, &g->dp.cells, (uint64_t)g->dp.cell_cap * g->dp.nslots)) ||
+        (rc = dev_alloc(g, &g->dp.align, (uint64_t)g->dp.align_cap * g->dp.nslots)))
+        return fail(rc);
+    if (cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * LightLayout::BYTES) != cudaSuccess)
+        return fail(set_err(g, FAME_ERR_CUDA, "shared memory attribute"));
+    *out = g;
+    return FAME_OK;
+}
+
+namespace {
+
+int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t n, uint32_t flags, uint64_t* d_mats,
+              uint8_t* d_invalid, fame_counters* cnt)
+{
+    const bool both = flags & FAME_BOTH_STRANDS, stranded = flags & FAME_GET_STRANDED;
+    const uint32_t omask = (both || stranded) ? 3u : ((flags & FAME_MATCH_R1_FWD) ? 1u : 2u);
+    const uint32_t norient = omask == 3u ? 2u : 1u;
+    int rc;
+    if ((rc = grow_chunk(g, n, 0, (uint64_t)n * norient * 4 + 4096))) return rc;
+    ChunkBufs cb{};
+    cb.seqs = d_seqs;
+    cb.offs = d_offs;
+    cb.n = n;
+    cb.orient_mask = omask;
+    cb.stranded = stranded ? 1u : 0u;
+    cb.rflags = g->d_rflags;
+    cb.task_cand = g->d_task_cand;
+    cb.mats = d_mats;
+    cb.invalid = d_invalid;
+    cb.dp_list = g->d_dp_list;
+    cb.dp_mat = g->d_dp_mat;
+    cb.dp_orient = g->d_dp_orient;
+    cb.meth = g->d_meth;
+    cb.ctr = g->d_ctr;
+    cb.heavy = g->d_heavy;
+    const int T = g->timing;
+    g->launches = 0;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        cb.cand = g->d_cand;
+        cb.cand_task = g->d_cand_task;
+        cb.cand_cap = (uint32_t)g->cap_cand;
+        cb.hits = g->d_hits;
+        cb.hit_n = g->d_hit_n;
+        CK(cudaMemsetAsync(g->d_ctr, 0, CTR_N * sizeof(unsigned long long), g->stream));
+        if (T) cudaEventRecord(g->ev[0], g->stream);
+        k_prep<<<(n + 255) / 256, 256, 0, g->stream>>>(cb, g->ix.readlen);
+        if (T) cudaEventRecord(g->ev[1], g->stream);
+        const uint32_t ntask = n * norient;
+        const uint32_t wpb = 4;
+        const uint32_t blocks = std::min<uint32_t>((ntask + wpb - 1) / wpb, (uint32_t)g->sm_count * 64);
+        if (ntask) k_seed<<<std::max(1u, blocks), wpb * 32, wpb * LightLayout::BYTES, g->stream>>>(g->ix, cb, ntask);
+        if (T) cudaEventRecord(g->ev[2], g->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
+        CK(cudaStreamSynchronize(g->stream));
+        g->launches += 2;
+        if (g->h_ctr[CTR_TOO_LONG]) return set_err(g, FAME_ERR_READ, "read longer than FAME_MAX_READ_LEN");
+        const uint64_t nheavy = g->h_ctr[CTR_HEAVY];
+        float heavy_ms = 0;
+        if (nheavy) {
+            if (T) cudaEventRecord(g->ev[6], g->stream);
+            const uint32_t hb = (g->hs.nwarps + 3) / 4;
+            k_seed_heavy<<<hb, 128, 0, g->stream>>>(g->ix, cb, g->hs, (uint32_t)nheavy);
+            if (T) cudaEventRecord(g->ev[7], g->stream);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
+            CK(cudaStreamSynchronize(g->stream));
+            if (T) cudaEventElapsedTime(&heavy_ms, g->ev[6], g->ev[7]);
+            g->launches += 1;
+            if (g->h_ctr[CTR_ERRFLAG]) return set_err(g, FAME_ERR_INDEX, "a read exceeded the heavy-path capacity");
+        }
+        const uint64_t ncand = g->h_ctr[CTR_CAND];
+        if (ncand > g->cap_cand) {
+            if ((rc = grow_chunk(g, n, 0, ncand + ncand / 4 + 4096))) return rc;
+            continue;  // nothing was tallied yet: redo the chunk with room for all candidates
+        }
+        if (T) {
+            cudaEventElapsedTime(&g->stage_ms[0], g->ev[0], g->ev[1]);
+            cudaEventElapsedTime(&g->stage_ms[1], g->ev[1], g->ev[2]);
+            g->stage_ms[5] = heavy_ms;
+            cudaEventRecord(g->ev[2], g->stream);
+        }
+        if (ncand) {
+            const uint32_t tb = 128;
+            const uint32_t grid = (uint32_t)std::min<uint64_t>((ncand + tb - 1) / tb, (uint64_t)g->sm_count * 32);
+            if (g->wmask & 2u) { k_shiftand<1><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+            if (g->wmask & 4u) { k_shiftand<2><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+            if (g->wmask & 8u) { k_shiftand<3><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+            if (g->wmask & 16u) { k_shiftand<4><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+        }
+        if (T) cudaEventRecord(g->ev[3], g->stream);
+        k_select<<<(n + 255) / 256, 256, 0, g->stream>>>(g->ix, cb);
+        if (T) cudaEventRecord(g->ev[4], g->stream);
+        k_dp<<<(g->dp.nslots + 127) / 128, 128, 0, g->stream>>>(g->ix, cb, g->dp);
+        if (T) cudaEventRecord(g->ev[5], g->stream);
+        g->launches += 2;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
+        CK(cudaStreamSynchronize(g->stream));
+        if (T) {
+            cudaEventElapsedTime(&g->stage_ms[2], g->ev[2], g->ev[3]);
+            cudaEventElapsedTime(&g->stage_ms[3], g->ev[3], g->ev[4]);
+            cudaEventElapsedTime(&g->stage_ms[4], g->ev[4], g->ev[5]);
+        }
+        if (g->h_ctr[CTR_ERRFLAG]) return set_err(g, FAME_ERR_INDEX, "a device capacity check failed");
+        if (cnt) {
+            const unsigned long long* h = g->h_ctr;
+            cnt->succ += h[CTR_SUCC];
+            cnt->nonunique += h[CTR_NONU];
+            cnt->unsucc += h[CTR_UNSUCC];
+            cnt->r1_fwd += h[CTR_R1F];
+            cnt->r1_rev += h[CTR_R1R];
+            cnt->invalid_len += h[CTR_INV_LEN];
+            cnt->invalid_n += h[CTR_INV_N];
+            cnt->gather_bytes += h[CTR_GATHER_BYTES];
+            cnt->windows_scanned += ncand;
+            cnt->dp_reads += h[CTR_DP];
+        }
+        return FAME_OK;
+    }
+    return set_err(g, FAME_ERR_NOMEM, "candidate buffer kept overflowing");
+}
+
+}  // namespace
+
+extern "C" int fame_gpu_match_reads_dev(fame_gpu* g, const char* seqs_dev, const uint64_t* offs_dev, uint32_t n,
+                                        uint32_t flags, uint64_t* mats_dev, uint8_t* invalid_dev, fame_counters* cnt)
+{
+    if (!g || (n && (!seqs_dev || !offs_dev || !mats_dev || !invalid_dev))) return FAME_ERR_ARG;
+    CK(cudaSetDevice(g->device));
+    if (n == 0) return FAME_OK;
+    return run_chunk(g, seqs_dev, offs_dev, n, flags, mats_dev, invalid_dev, cnt);
+}
+
+extern "C" int fame_gpu_match_reads(fame_gpu* g, const char* seqs, const uint64_t* offs, uint32_t n, uint32_t flags,
+                                    uint64_t* mats, uint8_t* invalid, fame_counters* cnt)
+{
+    if (!g || (n && (!seqs || !offs || !mats || !invalid))) return FAME_ERR_ARG;
+    CK(cudaSetDevice(g->device));
+    if (n == 0) return FAME_OK;
+    const uint64_t base = offs[0], bytes = offs[n] - offs[0];
+    int rc;
+    if ((rc = grow_chunk(g, n, bytes, 0))) return rc;
+    CK(cudaMemcpyAsync(g->d_seqs, seqs + base, bytes, cudaMemcpyHostToDevice, g->stream));
+    if (base == 0) {
+        CK(cudaMemcpyAsync(g->d_offs, offs, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, g->stream));
+    } else {
+        std::vector<uint64_t> o(offs, offs + n + 1);
+        for (auto& x : o) x -= base;
+        CK(cudaMemcpyAsync(g->d_offs, o.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, g->stream));
+        CK(cudaStreamSynchronize(g->stream));
+    }
+    g->wmask = 0;
+    for (uint32_t i = 0; i < n; ++i) g->wmask |= 1u << std::min<uint64_t>(4, (offs[i + 1] - offs[i]) / 64 + 1);
+    rc = run_chunk(g, g->d_seqs, g->d_offs, n, flags, g->d_mats, g->d_invalid, cnt);
+    g->wmask = 0x1e;
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(mats, g->d_mats, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaMemcpyAsync(invalid, g->d_invalid, n, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    return FAME_OK;
+}
+
+extern "C" int fame_gpu_tallies(fame_gpu* g, uint16_t* meth, int reset)
+{
+    if (!g) return FAME_ERR_ARG;
+    CK(cudaSetDevice(g->device));
+    const uint64_t n4 = 4 * g->n_cpg;
+    if (meth && n4) {
+        std::vector<uint32_t> h(n4);
+        CK(cudaMemcpyAsync(h.data(), g->d_meth, n4 * 4, cudaMemcpyDeviceToHost, g->stream));
+        CK(cudaStreamSynchronize(g->stream));
+        for (uint64_t i = 0; i < n4; ++i) meth[i] = (uint16_t)(h[i] & 0xffffu);  // uint16 wrap-around
+    }
+    if (reset && n4) {
+        CK(cudaMemsetAsync(g->d_meth, 0, n4 * 4, g->stream));
+        CK(cudaStreamSynchronize(g->stream));
+    }
+    return FAME_OK;
+}
+
+extern "C" int fame_gpu_alloc(fame_gpu* g, size_t bytes, void** p)
+{
+    if (!g || !p) return FAME_ERR_ARG;
+    CK(cudaSetDevice(g->device));
+    CK(cudaMalloc(p, std::max<size_t>(bytes, 16)));
+    return FAME_OK;
+}
+
+extern "C" int fame_gpu_free(fame_gpu* g, void* p)
+{
+    if (!g) return FAME_ERR_ARG;
+    if (p) CK(cudaFree(p));
+    return FAME_OK;
+}
+
+extern "C" int fame_gpu_memcpy(fame_gpu* g, void* dst, const void* src, size_t bytes, int kind)
+{
+    if (!g || (bytes && (!dst || !src))) return FAME_ERR_ARG;
+    const cudaMemcpyKind k = kind == 1 ? cudaMemcpyHostToDevice : kind == 2 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    CK(cudaMemcpyAsync(dst, src, bytes, k, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    return FAME_OK;
+}
+
+extern "C" int fame_gpu_host_alloc(fame_gpu* g, size_t bytes, void** p)
+{
+    if (!g || !p) return FAME_ERR_ARG;
+    CK(cudaMallocHost(p, std::max<size_t>(bytes, 16)));
+    return FAME_OK;
+}
+
+extern "C" int fame_gpu_host_free(fame_gpu* g, void* p)
+{
+    if (!g) return FAME_ERR_ARG;
+    if (p) CK(cudaFreeHost(p));
+    return FAME_OK;
+}
+
+extern "C" int fame_gpu_set_timing(fame_gpu* g, int enable)
+{
+    if (!g) return FAME_ERR_ARG;
+    g->timing = enable;
+    return FAME_OK;
+}
+
+extern "C" int fame_gpu_stage_times(fame_gpu* g, float* ms, int n)
+{
+    if (!g || !ms) return FAME_ERR_ARG;
+    for (int i = 0; i < n && i < 6; ++i) ms[i] = g->stage_ms[i];
+    return 6;
+}
+
+extern "C" int fame_gpu_last_launches(const fame_gpu* g) { return g ? g->launches : 0; }
+
+extern "C" int fame_gpu_stream(fame_gpu* g, void** stream)
+{
+    if (!g || !stream) return FAME_ERR_ARG;
+    *stream = (void*)g->stream;
+    return FAME_OK;
+}

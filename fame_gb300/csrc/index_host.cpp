@@ -1,0 +1,534 @@
+// Host side of the index boundary: the --load_index file reader and a
+// multi-threaded index builder producing the same tables as the reference's
+// RefGenome constructor (RefReader_istr.h:48-113, RefGenome.cpp:26-74,
+// 532-759, 1787-1989, 2191-2352) and save() (RefGenome.cpp:83-228).
+//
+// The builder keeps the reference's table contents and order exactly: within
+// a hash bucket the entries appear in reverse insertion order (the reference
+// fills by decrementing tabIndex, RefGenome.cpp:711-755), insertion order
+// being window, then N-free interval, then reverse strand before forward,
+// then k-mer position.  It parallelises the two hashing passes over windows
+// with atomic bucket counters and restores that order with a per-bucket sort.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/fame_gpu.h"
+#include "fame_const.h"
+#include "index_host.h"
+
+using namespace fame;
+
+namespace {
+
+inline uint64_t rotl64(uint64_t v, unsigned s) { s &= 63u; return s ? (v << s) | (v >> (64 - s)) : v; }
+
+// msTab (spaced_nthash/nthash.hpp:88-121)
+inline uint64_t nt_val(uint8_t c)
+{
+    switch (c) {
+        case 'A': case 'a': case 4: return NT_SEED_A;
+        case 'C': case 'c': case 'T': case 't': case 1: case 7: return NT_SEED_T;
+        case 'G': case 'g': case 3: return NT_SEED_G;
+        default: return 0;
+    }
+}
+
+// NTPS64 (nthash.hpp:480-498): full hash rolled, the four unseeded positions
+// (SEEDBITS zeros at 2, 7, 14, 30) removed.
+struct SpacedRoller {
+    uint64_t h = 0;
+    void init(const uint8_t* s) { h = 0; for (unsigned i = 0; i < KMERLEN; ++i) h ^= rotl64(nt_val(s[i]), 31 - i); }
+    void roll(uint8_t out, uint8_t in) { h = rotl64(h, 1) ^ rotl64(nt_val(out), KMERLEN) ^ nt_val(in); }
+    uint64_t spaced(const uint8_t* s) const
+    {
+        return h ^ rotl64(nt_val(s[2]), 29) ^ rotl64(nt_val(s[7]), 24) ^ rotl64(nt_val(s[14]), 17) ^ rotl64(nt_val(s[30]), 1);
+    }
+};
+
+template <class F>
+void parallel_for(uint64_t n, int threads, F fn)
+{
+    if (threads <= 1 || n < 2) { fn(0, n, 0); return; }
+    std::vector<std::thread> th;
+    const uint64_t step = (n + threads - 1) / threads;
+    for (int t = 0; t < threads; ++t) {
+        const uint64_t b = std::min<uint64_t>(n, t * step), e = std::min<uint64_t>(n, b + step);
+        if (b >= e) break;
+        th.emplace_back([=] { fn(b, e, t); });
+    }
+    for (auto& x : th) x.join();
+}
+
+// K-mers of one window in the reference's insertion order (RefGenome.cpp:621-759):
+// emit(key, offset, strand).  red/redr are scratch of WINLEN bytes.
+template <class Emit>
+void window_kmers(const fame_host_index& ix, uint64_t w, uint8_t* red, uint8_t* redr, uint32_t* iv, Emit emit)
+{
+    memset(red, 0, WINLEN);
+    memset(redr, 0, WINLEN);
+    const fame_window& win = ix.win[w];
+    const std::string& g = ix.seq[win.chrom];
+    const uint64_t sp = win.start_pos;
+    const uint64_t stop = std::min<uint64_t>(sp + WINLEN, g.size());
+    bool lastN = true;
+    uint32_t nStart = 0, niv = 0, j = 0;
+    for (uint64_t i = sp; i < stop; ++i, ++j) {
+        const uint32_t rp = WINLEN - 1 - j;
+        switch (g[i]) {
+            case 'N':
+                if (!lastN) { iv[2 * niv] = nStart; iv[2 * niv + 1] = j - 1; ++niv; }
+                lastN = true;
+                red[j] = 'N';
+                red[rp] = 'N';  // the reference writes the forward buffer here (RefGenome.cpp:646)
+                break;
+            case 'C': if (lastN) { nStart = j; lastN = false; } red[j] = 'T'; redr[rp] = 'G'; break;
+            case 'G': if (lastN) { nStart = j; lastN = false; } red[j] = 'G'; redr[rp] = 'T'; break;
+            case 'T': if (lastN) { nStart = j; lastN = false; } red[j] = 'T'; redr[rp] = 'A'; break;
+            case 'A': if (lastN) { nStart = j; lastN = false; } red[j] = 'A'; redr[rp] = 'T'; break;
+            default: break;
+        }
+    }
+    if (!lastN) { iv[2 * niv] = nStart; iv[2 * niv + 1] = j - 1; ++niv; }
+    SpacedRoller r;
+    for (uint32_t q = 0; q < niv; ++q) {
+        const uint32_t first = iv[2 * q], second = iv[2 * q + 1];
+        const uint32_t dist = second - first + 1;
+        if (dist < ix.readlen) continue;
+        for (int strand = 0; strand < 2; ++strand) {  // reverse strand first
+            const uint8_t* s = strand ? red + first : redr + (WINLEN - 1 - second);
+            uint32_t kp = strand ? first : WINLEN - first - KMERLEN;
+            r.init(s);
+            emit((uint32_t)(r.spaced(s) & HTAB_MASK), kp, strand);
+            for (uint32_t i = 0; i < dist - KMERLEN; ++i) {
+                kp = strand ? kp + 1 : kp - 1;
+                r.roll(s[i], s[i + KMERLEN]);
+                if (i % SKIPMOD) continue;
+                emit((uint32_t)(r.spaced(s + i + 1) & HTAB_MASK), kp, strand);
+            }
+        }
+    }
+}
+
+inline uint8_t base_at(const fame_host_index& ix, uint32_t c, uint64_t p)
+{
+    return p < ix.seq[c].size() ? (uint8_t)ix.seq[c][p] : 'N';  // past the chromosome end: no base
+}
+
+// reproduceKmerSeq (RefGenome.cpp:2028-2132)
+uint64_t kmer_seq(const fame_host_index& ix, uint32_t w, uint32_t off, int fwd)
+{
+    const uint32_t c = ix.win[w].chrom;
+    const uint64_t s0 = (uint64_t)ix.win[w].start_pos + off;
+    uint64_t k = 0;
+    for (unsigned i = 0; i < KMERLEN; ++i) {
+        k <<= 2;  // the reverse loop of the reference walks i = 32..1 with SEED[32 - i], i.e. the same seed index
+        if (!((SEEDBITS >> (31 - i)) & 1u)) continue;
+        if (fwd) {
+            const uint8_t ch = base_at(ix, c, s0 + i);
+            if (ch == 'C' || ch == 'T') k += 3; else if (ch == 'G') k += 2;
+        } else {
+            const uint8_t ch = base_at(ix, c, s0 + KMERLEN - 1 - i);
+            if (ch == 'G' || ch == 'A') k += 3; else if (ch == 'C') k += 2;
+        }
+    }
+    return k;
+}
+
+// reproduceTMask (RefGenome.cpp:2135-2189)
+uint32_t tmask_repro(const fame_host_index& ix, uint32_t w, uint32_t off, int fwd)
+{
+    const uint32_t c = ix.win[w].chrom;
+    const uint64_t s0 = (uint64_t)ix.win[w].start_pos + off;
+    uint32_t t = 0;
+    for (unsigned i = 0; i < KMERLEN; ++i) {
+        t <<= 1;
+        if (fwd) { if (base_at(ix, c, s0 + i) == 'T') t |= 1; }
+        else { if (base_at(ix, c, s0 + KMERLEN - 1 - i) == 'A') t |= 1; }
+    }
+    return t;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// builder
+// ---------------------------------------------------------------------------
+extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* const* seq, const uint64_t* len,
+                                const char* const* names, int noloss, int n_threads, fame_host_index** out)
+{
+    if (!out || !seq || !len || n_chrom == 0 || n_chrom > 256 || readlen <= KMERLEN || readlen >= WINLEN) return FAME_ERR_ARG;
+    *out = nullptr;
+    int T = n_threads > 0 ? n_threads : (int)std::max(1u, std::thread::hardware_concurrency());
+    fame_host_index* ix = new (std::nothrow) fame_host_index();
+    if (!ix) return FAME_ERR_NOMEM;
+    try {
+        ix->readlen = readlen;
+        ix->seq.resize(n_chrom);
+        ix->names.resize(n_chrom);
+        // readLine (RefReader_istr.h:48-113): case folding, other letters -> N,
+        // CpGs at C - READLEN + 2 (or at C when too close to the start).
+        std::vector<std::vector<fame_cpg>> cpg(n_chrom), cpgs(n_chrom);
+        parallel_for(n_chrom, std::min<int>(T, (int)n_chrom), [&](uint64_t b, uint64_t e, int) {
+            for (uint64_t c = b; c < e; ++c) {
+                std::string& s = ix->seq[c];
+                s.resize(len[c]);
+                bool lastC = false;
+                for (uint64_t i = 0; i < len[c]; ++i) {
+                    const char ch = seq[c][i];
+                    switch (ch) {
+                        case 'g': case 'G':
+                            if (lastC) {
+                                if (i >= readlen - 2) cpg[c].push_back({(uint8_t)c, (uint32_t)i - readlen + 1});
+                                else cpgs[c].push_back({(uint8_t)c, (uint32_t)i - 1});
+                                lastC = false;
+                            }
+                            s[i] = 'G';
+                            break;
+                        case 'c': case 'C': s[i] = 'C'; lastC = true; break;
+                        case 'a': case 'A': s[i] = 'A'; lastC = false; break;
+                        case 't': case 'T': s[i] = 'T'; lastC = false; break;
+                        default: s[i] = 'N'; lastC = false; break;
+                    }
+                }
+                ix->names[c] = names && names[c] ? std::string(names[c]) : ("chr" + std::to_string(c + 1));
+            }
+        });
+        for (uint32_t c = 0; c < n_chrom; ++c) {
+            ix->cpg.insert(ix->cpg.end(), cpg[c].begin(), cpg[c].end());
+            ix->cpg_start.insert(ix->cpg_start.end(), cpgs[c].begin(), cpgs[c].end());
+        }
+        // generateWindows (RefGenome.cpp:532-567); cpgTable[ci] is read even at
+        // ci == size there, which this treats as "no CpG".
+        {
+            const uint64_t ncpg = ix->cpg.size();
+            uint64_t ci = 0;
+            for (uint32_t c = 0; c < n_chrom; ++c) {
+                for (uint32_t ws = 0; ws < ix->seq[c].size(); ws = ws + WINLEN - readlen) {
+                    const uint32_t we = ws + WINLEN;
+                    uint32_t si = CPGDUMMY, ei = CPGDUMMY;
+                    while (ci < ncpg && ix->cpg[ci].chrom == c && ix->cpg[ci].pos <= we) {
+                        if (si == CPGDUMMY) si = (uint32_t)ci;
+                        ei = (uint32_t)ci;
+                        ++ci;
+                    }
+                    while (ci > 0 && ci < ncpg && ix->cpg[ci].chrom == c && ix->cpg[ci].pos >= we - readlen) --ci;
+                    if (ci > 0) ++ci;
+                    ix->win.push_back({ws, (uint8_t)c, si, ei});
+                }
+            }
+        }
+        const uint64_t nwin = ix->win.size();
+        // pass 1: bucket sizes (estimateTablesizes) and per-window entry counts
+        std::vector<uint32_t> cnt(HTABSIZE + 1, 0);
+        std::vector<uint32_t> wcount(nwin, 0);
+        parallel_for(nwin, T, [&](uint64_t b, uint64_t e, int) {
+            std::vector<uint8_t> red(WINLEN), redr(WINLEN);
+            std::vector<uint32_t> iv(2 * (WINLEN + 2));
+            for (uint64_t w = b; w < e; ++w) {
+                uint32_t k = 0;
+                window_kmers(*ix, w, red.data(), redr.data(), iv.data(), [&](uint32_t key, uint32_t, int) {
+                    __atomic_fetch_add(&cnt[key], 1u, __ATOMIC_RELAXED);
+                    ++k;
+                });
+                wcount[w] = k;
+            }
+        });
+        // bucket starts
+        uint64_t total = 0;
+        {
+            std::vector<uint64_t> part(T + 1, 0);
+            parallel_for(HTABSIZE, T, [&](uint64_t b, uint64_t e, int t) {
+                uint64_t s = 0;
+                for (uint64_t i = b; i < e; ++i) s += cnt[i];
+                part[t + 1] = s;
+            });
+            for (int t = 0; t < T; ++t) part[t + 1] += part[t];
+            total = part[T];
+            if (total >= 0xffffffffull) { delete ix; return FAME_ERR_INDEX; }
+            ix->tab32.assign(HTABSIZE + 1, 0);
+            parallel_for(HTABSIZE, T, [&](uint64_t b, uint64_t e, int t) {
+                uint64_t s = part[t];
+                for (uint64_t i = b; i < e; ++i) { ix->tab32[i] = (uint32_t)s; s += cnt[i]; cnt[i] = (uint32_t)(s - cnt[i]); }
+            });
+            ix->tab32[HTABSIZE] = (uint32_t)total;
+        }
+        // pass 2: fill with atomic cursors; order key = (window, position in window)
+        std::vector<uint64_t> ord(total);
+        std::vector<uint32_t> eoff(total);
+        std::vector<uint8_t> estr(total);
+        parallel_for(nwin, T, [&](uint64_t b, uint64_t e, int) {
+            std::vector<uint8_t> red(WINLEN), redr(WINLEN);
+            std::vector<uint32_t> iv(2 * (WINLEN + 2));
+            for (uint64_t w = b; w < e; ++w) {
+                uint32_t k = 0;
+                window_kmers(*ix, w, red.data(), redr.data(), iv.data(), [&](uint32_t key, uint32_t off, int strand) {
+                    const uint32_t slot = __atomic_fetch_add(&cnt[key], 1u, __ATOMIC_RELAXED);
+                    ord[slot] = (w << 32) | k;
+                    eoff[slot] = off;
+                    estr[slot] = (uint8_t)strand;
+                    ++k;
+                });
+            }
+        });
+        std::vector<uint32_t>().swap(cnt);
+        // per bucket: reverse insertion order, then the two filters.  keep[i]
+        // marks survivors; filtered k-mer sequences are collected per thread.
+        std::vector<uint8_t> keep(total, 1);
+        std::vector<std::vector<uint64_t>> filt(T);
+        std::vector<uint32_t> newlen(HTABSIZE, 0);
+        parallel_for(HTABSIZE, T, [&](uint64_t b, uint64_t e, int t) {
+            std::vector<uint64_t> tmp_o;
+            std::vector<uint32_t> tmp_off;
+            std::vector<uint8_t> tmp_s;
+            std::vector<uint64_t> ks, sorted;
+            std::vector<uint32_t> masks;
+            std::vector<uint32_t> idx;
+            for (uint64_t key = b; key < e; ++key) {
+                const uint32_t s0 = ix->tab32[key], s1 = ix->tab32[key + 1];
+                const uint32_t n = s1 - s0;
+                if (n == 0) continue;
+                if (n > 1) {
+                    idx.resize(n);
+                    for (uint32_t i = 0; i < n; ++i) idx[i] = i;
+                    std::sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) { return ord[s0 + x] > ord[s0 + y]; });
+                    tmp_o.resize(n); tmp_off.resize(n); tmp_s.resize(n);
+                    for (uint32_t i = 0; i < n; ++i) { tmp_o[i] = ord[s0 + idx[i]]; tmp_off[i] = eoff[s0 + idx[i]]; tmp_s[i] = estr[s0 + idx[i]]; }
+                    for (uint32_t i = 0; i < n; ++i) { ord[s0 + i] = tmp_o[i]; eoff[s0 + i] = tmp_off[i]; estr[s0 + i] = tmp_s[i]; }
+                }
+                // filterHashTable (RefGenome.cpp:2267-2352)
+                if (!noloss && n >= KMERCUTOFF) {
+                    ks.resize(n); sorted.resize(n);
+                    for (uint32_t i = 0; i < n; ++i)
+                        ks[i] = sorted[i] = kmer_seq(*ix, (uint32_t)(ord[s0 + i] >> 32), eoff[s0 + i], estr[s0 + i]);
+                    std::sort(sorted.begin(), sorted.end());
+                    for (uint32_t i = 0; i < n; ++i) {
+                        auto r = std::equal_range(sorted.begin(), sorted.end(), ks[i]);
+                        if ((uint64_t)(r.second - r.first) >= KMERCUTOFF) { keep[s0 + i] = 0; filt[t].push_back(ks[i]); }
+                    }
+                }
+                // filterRedundancyInHashTable (RefGenome.cpp:2191-2264)
+                uint64_t prevMeta = ~0ull;
+                int prevFwd = 0;
+                masks.clear();
+                uint32_t kept = 0;
+                for (uint32_t i = 0; i < n; ++i) {
+                    if (!keep[s0 + i]) continue;
+                    const uint32_t w = (uint32_t)(ord[s0 + i] >> 32);
+                    const int fwd = estr[s0 + i];
+                    const uint32_t tm = tmask_repro(*ix, w, eoff[s0 + i], fwd);
+                    if (w != prevMeta || fwd != prevFwd) {
+                        masks.clear();
+                        masks.push_back(tm);
+                        prevMeta = w;
+                        prevFwd = fwd;
+                        ++kept;
+                    } else if (std::find(masks.begin(), masks.end(), tm) == masks.end()) {
+                        masks.push_back(tm);
+                        ++kept;
+                    } else {
+                        keep[s0 + i] = 0;
+                    }
+                }
+                newlen[key] = kept;
+            }
+        });
+        // compaction
+        uint64_t nk = 0;
+        {
+            std::vector<uint64_t> part(T + 1, 0);
+            parallel_for(HTABSIZE, T, [&](uint64_t b, uint64_t e, int t) {
+                uint64_t s = 0;
+                for (uint64_t i = b; i < e; ++i) s += newlen[i];
+                part[t + 1] = s;
+            });
+            for (int t = 0; t < T; ++t) part[t + 1] += part[t];
+            nk = part[T];
+            ix->kmer.resize(nk);
+            std::vector<uint8_t> kstr(nk);
+            std::vector<uint32_t> koff(nk);
+            // the old start of each thread's first key after its range, read
+            // before any thread rewrites tab32 (same partition as parallel_for)
+            std::vector<uint32_t> bound(T, 0);
+            {
+                const uint64_t step = (HTABSIZE + T - 1) / T;
+                for (int t = 0; t < T; ++t) bound[t] = ix->tab32[std::min<uint64_t>(HTABSIZE, (uint64_t)t * step + step)];
+            }
+            parallel_for(HTABSIZE, T, [&](uint64_t b, uint64_t e, int t) {
+                uint64_t o = part[t];
+                for (uint64_t key = b; key < e; ++key) {
+                    const uint32_t s0 = ix->tab32[key], s1 = key + 1 == e ? bound[t] : ix->tab32[key + 1];
+                    ix->tab32[key] = (uint32_t)o;
+                    for (uint32_t i = s0; i < s1; ++i) {
+                        if (!keep[i]) continue;
+                        ix->kmer[o].meta = (uint32_t)(ord[i] >> 32);
+                        kstr[o] = estr[i];
+                        koff[o] = eoff[i];
+                        ++o;
+                    }
+                }
+            });
+            ix->tab32[HTABSIZE] = (uint32_t)nk;
+            // strandTable
+            ix->strand_bits.assign((nk + 7) / 8, 0);
+            for (uint64_t i = 0; i < nk; ++i) if (kstr[i]) ix->strand_bits[i >> 3] |= (uint8_t)(1u << (i & 7));
+            // getTMask at save time (RefGenome.h:62-100): strand taken at
+            // strandTable[window id]; the reverse loop skips base 0.
+            parallel_for(nk, T, [&](uint64_t b, uint64_t e, int) {
+                for (uint64_t k = b; k < e; ++k) {
+                    const uint32_t w = ix->kmer[k].meta & 0x7fffffffu;
+                    const uint32_t c = ix->win[w].chrom;
+                    const uint64_t s0 = (uint64_t)ix->win[w].start_pos + koff[k];
+                    const int fwd = w < nk ? kstr[w] : 0;
+                    uint32_t tm = 0;
+                    if (fwd) { for (unsigned i = 0; i < KMERLEN; ++i) { tm <<= 1; if (base_at(*ix, c, s0 + i) == 'T') tm |= 1; } }
+                    else { for (unsigned i = KMERLEN - 1; i > 0; --i) { tm <<= 1; if (base_at(*ix, c, s0 + i) == 'A') tm |= 1; } }
+                    ix->kmer[k].tmask = tm;
+                }
+            });
+        }
+        for (auto& f : filt) ix->filtered.insert(ix->filtered.end(), f.begin(), f.end());
+        std::sort(ix->filtered.begin(), ix->filtered.end());
+        ix->filtered.erase(std::unique(ix->filtered.begin(), ix->filtered.end()), ix->filtered.end());
+    } catch (const std::bad_alloc&) {
+        delete ix;
+        return FAME_ERR_NOMEM;
+    }
+    *out = ix;
+    return FAME_OK;
+}
+
+// ---------------------------------------------------------------------------
+// --load_index reader (RefGenome.cpp:230-433)
+// ---------------------------------------------------------------------------
+namespace {
+struct Reader {
+    FILE* f;
+    bool ok = true;
+    template <class T> T get() { T v{}; if (fread(&v, sizeof(T), 1, f) != 1) ok = false; return v; }
+    void bytes(void* p, uint64_t n) { if (n && fread(p, 1, n, f) != n) ok = false; }
+};
+}  // namespace
+
+extern "C" int fame_index_read(const char* path, fame_host_index** out)
+{
+    if (!path || !out) return FAME_ERR_ARG;
+    *out = nullptr;
+    FILE* f = fopen(path, "rb");
+    if (!f) return FAME_ERR_IO;
+    fame_host_index* ix = new (std::nothrow) fame_host_index();
+    if (!ix) { fclose(f); return FAME_ERR_NOMEM; }
+    Reader r{f};
+    int rc = FAME_OK;
+    try {
+        const uint64_t htabs = r.get<uint64_t>();
+        const uint32_t readl = r.get<uint32_t>(), winl = r.get<uint32_t>(), kmerl = r.get<uint32_t>();
+        const uint64_t kmerc = r.get<uint64_t>();
+        const uint32_t seedbits = r.get<uint32_t>();
+        if (!r.ok || htabs != HTABSIZE || winl != WINLEN || kmerl != KMERLEN || kmerc != KMERCUTOFF ||
+            seedbits != SEEDBITS || readl <= KMERLEN || readl >= WINLEN) {
+            rc = FAME_ERR_IO;
+        } else {
+            ix->readlen = readl;
+            uint64_t n = r.get<uint64_t>();
+            ix->cpg.resize(n); r.bytes(ix->cpg.data(), n * sizeof(fame_cpg));
+            n = r.get<uint64_t>();
+            ix->cpg_start.resize(n); r.bytes(ix->cpg_start.data(), n * sizeof(fame_cpg));
+            n = r.get<uint64_t>();
+            if (n > 256) throw std::bad_alloc();
+            ix->seq.resize(n);
+            for (auto& s : ix->seq) { uint64_t l = r.get<uint64_t>(); s.resize(l); r.bytes(&s[0], l); }
+            n = r.get<uint64_t>();
+            ix->tab64.resize(n); r.bytes(ix->tab64.data(), n * 8);
+            n = r.get<uint64_t>();
+            ix->kmer.resize(n); r.bytes(ix->kmer.data(), n * sizeof(fame_kmer));
+            uint64_t m = r.get<uint64_t>();      // metaCpGs (unused by the window index)
+            fseek(f, (long)(m * 8), SEEK_CUR);
+            m = r.get<uint64_t>();               // metaStartCpGs
+            fseek(f, (long)(m * 8), SEEK_CUR);
+            n = r.get<uint64_t>();
+            ix->win.resize(n); r.bytes(ix->win.data(), n * sizeof(fame_window));
+            n = r.get<uint64_t>();
+            ix->filtered.resize(n); r.bytes(ix->filtered.data(), n * 8);
+            std::sort(ix->filtered.begin(), ix->filtered.end());
+            n = r.get<uint64_t>();
+            ix->names.assign(ix->seq.size(), std::string());
+            for (uint64_t i = 0; i < n && r.ok; ++i) {
+                const uint8_t id = r.get<uint8_t>();
+                const uint64_t l = r.get<uint64_t>();
+                std::string s(l, '\0');
+                r.bytes(&s[0], l);
+                if (id < ix->names.size()) ix->names[id] = s;
+            }
+            if (!r.ok || ix->tab64.size() != HTABSIZE + 1 || ix->tab64.back() != ix->kmer.size()) rc = FAME_ERR_IO;
+        }
+    } catch (const std::bad_alloc&) {
+        rc = FAME_ERR_NOMEM;
+    }
+    fclose(f);
+    if (rc == FAME_OK) {
+        const std::string sp = std::string(path) + "_strands";
+        FILE* g = fopen(sp.c_str(), "rb");
+        if (!g) rc = FAME_ERR_IO;
+        else {
+            Reader rs{g};
+            const uint64_t n = rs.get<uint64_t>();
+            ix->strand_bits.resize((n + 7) / 8);
+            rs.bytes(ix->strand_bits.data(), ix->strand_bits.size());
+            if (!rs.ok || n != ix->kmer.size()) rc = FAME_ERR_IO;
+            fclose(g);
+        }
+    }
+    if (rc != FAME_OK) { delete ix; return rc; }
+    *out = ix;
+    return FAME_OK;
+}
+
+extern "C" int fame_index_view_of(const fame_host_index* cix, fame_index_view* v)
+{
+    if (!cix || !v) return FAME_ERR_ARG;
+    fame_host_index* ix = const_cast<fame_host_index*>(cix);
+    ix->seq_ptrs.resize(ix->seq.size());
+    ix->seq_lens.resize(ix->seq.size());
+    ix->name_ptrs.resize(ix->seq.size());
+    if (ix->names.size() < ix->seq.size()) ix->names.resize(ix->seq.size());
+    for (size_t c = 0; c < ix->seq.size(); ++c) {
+        ix->seq_ptrs[c] = ix->seq[c].data();
+        ix->seq_lens[c] = ix->seq[c].size();
+        ix->name_ptrs[c] = ix->names[c].c_str();
+    }
+    memset(v, 0, sizeof(*v));
+    v->readlen = ix->readlen;
+    v->n_chrom = (uint32_t)ix->seq.size();
+    v->chrom_seq = ix->seq_ptrs.data();
+    v->chrom_len = ix->seq_lens.data();
+    v->chrom_name = ix->name_ptrs.data();
+    v->n_cpg = ix->cpg.size();
+    v->cpg = ix->cpg.data();
+    v->tab_index = ix->tab64.empty() ? nullptr : ix->tab64.data();
+    v->tab_index32 = ix->tab32.empty() ? nullptr : ix->tab32.data();
+    v->n_kmer = ix->kmer.size();
+    v->kmer = ix->kmer.data();
+    v->strand_bits = ix->strand_bits.data();
+    v->n_win = ix->win.size();
+    v->win = ix->win.data();
+    v->n_filtered = ix->filtered.size();
+    v->filtered = ix->filtered.data();
+    return FAME_OK;
+}
+
+extern "C" void fame_index_free(fame_host_index* ix) { delete ix; }
+
+// Start CpGs (never reported, RefReader_istr.h:66-76) for the index file writer and tests.
+extern "C" uint64_t fame_index_cpg_start(const fame_host_index* ix, fame_cpg* out, uint64_t cap)
+{
+    if (!ix) return 0;
+    for (uint64_t i = 0; i < ix->cpg_start.size() && i < cap; ++i) out[i] = ix->cpg_start[i];
+    return ix->cpg_start.size();
+}

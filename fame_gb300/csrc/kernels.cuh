@@ -1,0 +1,731 @@
+// Matching kernels after seeding: Shift-And window scans, candidate
+// selection with the exact-match CpG calls, and the banded DP CpG calls.
+#pragma once
+#include "seed.cuh"
+
+namespace fame {
+
+// ---------------------------------------------------------------------------
+// ShiftAnd<6> (ShiftAnd.h:121-432).  State bit s of layer e: a prefix of s
+// pattern characters aligns with <= e edits ending at the current text base.
+// A read T also sets the mask of a reference C (bisulfite asymmetry,
+// ShiftAnd.h:399-402).  W = pLen / 64 + 1 words; only bits <= pLen matter.
+// ---------------------------------------------------------------------------
+template <int W>
+struct ShiftAndState {
+    uint64_t m[4][W];
+    uint64_t acc;          // accepted bit of word W - 1
+    uint64_t a[NERR + 1][W];
+    uint32_t plen;
+
+    __device__ __forceinline__ void load(const char* raw, uint32_t len, int orient)
+    {
+        plen = len;
+        acc = 1ull << (len % 64);
+        uint64_t mA = ~0ull, mC = ~0ull, mG = ~0ull, mT = ~0ull;
+#pragma unroll
+        for (int w = 0; w < W; ++w) { m[0][w] = m[1][w] = m[2][w] = m[3][w] = 0; }
+        for (uint32_t i = len; i > 0;) {
+            mA <<= 1; mC <<= 1; mG <<= 1; mT <<= 1;
+            const uint8_t c = orient ? rc_byte((uint8_t)raw[len - i]) : (uint8_t)raw[i - 1];
+            switch (c) {
+                case 'A': mA |= 1; break;
+                case 'C': mC |= 1; break;
+                case 'G': mG |= 1; break;
+                case 'T': mT |= 1; mC |= 1; break;
+                default: break;
+            }
+            if (i % 64 == 0) {
+                const int w = (int)(i / 64);
+#pragma unroll
+                for (int q = 0; q < W; ++q)
+                    if (q == w) { m[0][q] = mA; m[1][q] = mC; m[2][q] = mG; m[3][q] = mT; }
+                mA = mC = mG = mT = ~0ull;
+            }
+            --i;
+        }
+        m[0][0] = (mA << 1) | 1; m[1][0] = (mC << 1) | 1; m[2][0] = (mG << 1) | 1; m[3][0] = (mT << 1) | 1;
+    }
+
+    __device__ __forceinline__ void reset()
+    {
+#pragma unroll
+        for (int i = 0; i <= (int)NERR; ++i) {
+#pragma unroll
+            for (int j = 1; j < W; ++j) a[i][j] = 0;
+            a[i][0] = (1ull << (i + 1)) - 1;
+        }
+    }
+
+    // queryLetter (ShiftAnd.h:276-318)
+    __device__ __forceinline__ void letter(int b)
+    {
+        uint64_t mk[W];
+#pragma unroll
+        for (int j = 0; j < W; ++j) mk[j] = b == 0 ? m[0][j] : b == 1 ? m[1][j] : b == 2 ? m[2][j] : m[3][j];
+#pragma unroll
+        for (int i = NERR; i > 0; --i) {
+#pragma unroll
+            for (int j = W - 1; j > 0; --j)
+                a[i][j] = (((a[i][j] << 1) | (a[i][j - 1] >> 63)) & mk[j]) | a[i - 1][j] |
+                          ((a[i - 1][j] << 1) | (a[i - 1][j - 1] >> 63));
+            a[i][0] = (((a[i][0] << 1) | 1) & mk[0]) | a[i - 1][0] | (a[i - 1][0] << 1);
+        }
+#pragma unroll
+        for (int j = W - 1; j > 0; --j) a[0][j] = ((a[0][j] << 1) | (a[0][j - 1] >> 63)) & mk[j];
+        a[0][0] = ((a[0][0] << 1) | 1) & mk[0];
+#pragma unroll
+        for (int i = 1; i <= (int)NERR; ++i) {
+#pragma unroll
+            for (int j = W - 1; j > 0; --j) a[i][j] |= (a[i - 1][j] << 1) | (a[i - 1][j - 1] >> 63);
+            a[i][0] |= a[i - 1][0] << 1;
+        }
+    }
+
+    // isMatch (ShiftAnd.h:323-341): smallest layer with the accepting state
+    __device__ __forceinline__ int match() const
+    {
+#pragma unroll
+        for (int i = 0; i <= (int)NERR; ++i)
+            if (a[i][W - 1] & acc) return i;
+        return -1;
+    }
+};
+
+// Scan of one candidate window (querySeq / queryRevSeq, ShiftAnd.h:130-255, on
+// the text spans of saQuerySeedSetRef, ReadQueue.cpp:1953-1962, 2048-2058).
+// emit(offset, errors) is called once per run of consecutive accepting bases,
+// with the last position holding the run's smallest error count.
+template <int W, class Emit>
+__device__ void scan_window(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t wid, int fwd, Emit emit)
+{
+    const uint4 wi = ix.win[wid];
+    const uint32_t sp = wi.x, ch = wi.y;
+    const int64_t L = (int64_t)ix.chrom_len[ch];
+    const uint64_t g0 = ix.chrom_off[ch];
+    sa.reset();
+    bool was = false;
+    uint32_t cur_off = 0;
+    int cur_err = 0;
+    uint32_t ncl = 0;
+    const uint32_t gate = sa.plen - NERR;
+    if (fwd) {
+        int64_t e = (int64_t)sp + WIN_TEXT;
+        if (e > L) e = L;
+        uint64_t g = g0 + sp;
+        uint32_t wpack = __ldg(ix.gpack + (g >> 4)), wn = __ldg(ix.gnmask + (g >> 5));
+        for (int64_t t = sp; t < e; ++t, ++g) {
+            if ((g & 15) == 0) wpack = __ldg(ix.gpack + (g >> 4));
+            if ((g & 31) == 0) wn = __ldg(ix.gnmask + (g >> 5));
+            if ((wn >> (g & 31)) & 1u) { sa.reset(); continue; }
+            sa.letter((int)((wpack >> (2 * (g & 15))) & 3u));
+            if (++ncl < gate) continue;
+            const int er = sa.match();
+            const uint32_t off = (uint32_t)(t - sp) + MISCOUNT;
+            if (er >= 0) {
+                if (was) { if (er <= cur_err) { cur_off = off; cur_err = er; } }
+                else { was = true; cur_off = off; cur_err = er; }
+            } else if (was) {
+                emit(cur_off, cur_err);
+                was = false;
+            }
+        }
+    } else {
+        const int64_t lo = sp > 0 ? (int64_t)sp - 1 : 0;
+        int64_t hi = (int64_t)sp + WIN_TEXT;
+        if (hi >= L) hi = L - 1;
+        uint64_t g = g0 + (uint64_t)hi;
+        uint32_t wpack = __ldg(ix.gpack + (g >> 4)), wn = __ldg(ix.gnmask + (g >> 5));
+        for (int64_t t = hi; t != lo; --t, --g) {
+            if ((g & 15) == 15) wpack = __ldg(ix.gpack + (g >> 4));
+            if ((g & 31) == 31) wn = __ldg(ix.gnmask + (g >> 5));
+            if ((wn >> (g & 31)) & 1u) { sa.reset(); continue; }
+            sa.letter(3 - (int)((wpack >> (2 * (g & 15))) & 3u));
+            if (++ncl < gate) continue;
+            const int er = sa.match();
+            const uint32_t off = (uint32_t)(t - lo) + sa.plen - 1 + MISCOUNT;
+            if (er >= 0) {
+                if (was) { if (er <= cur_err) { cur_off = off; cur_err = er; } }
+                else { was = true; cur_off = off; cur_err = er; }
+            } else if (was) {
+                emit(cur_off, cur_err);
+                was = false;
+            }
+        }
+    }
+    if (was) emit(cur_off, cur_err);
+}
+
+template <int W>
+__device__ void shiftand_one(const DevIndex& ix, const ChunkBufs& cb, uint32_t c)
+{
+    const uint32_t task = cb.cand_task[c];
+    const uint32_t r = task >> 1, o = task & 1;
+    const uint64_t off0 = cb.offs[r];
+    const uint32_t len = (uint32_t)(cb.offs[r + 1] - off0);
+    ShiftAndState<W> sa;
+    sa.load(cb.seqs + off0, len, (int)o);
+    const uint32_t e = cb.cand[c];
+    uint32_t n = 0;
+    uint32_t* out = cb.hits + (uint64_t)c * HIT_CAP;
+    scan_window<W>(ix, sa, e & 0x7fffffffu, (int)(e >> 31), [&](uint32_t off, int err) {
+        if (n < HIT_CAP) out[n] = (off << 8) | (uint32_t)err;
+        ++n;
+    });
+    cb.hit_n[c] = n;
+}
+
+// One launch per pattern word count W: each handles the candidates whose read
+// length needs W words, so the register file is sized for that W only.
+template <int W>
+__global__ void k_shiftand(DevIndex ix, ChunkBufs cb, uint32_t ncand)
+{
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncand; c += gridDim.x * blockDim.x) {
+        const uint32_t task = cb.cand_task[c];
+        const uint32_t r = task >> 1;
+        const uint32_t len = (uint32_t)(cb.offs[r + 1] - cb.offs[r]);
+        if ((int)(len / 64 + 1) == W) shiftand_one<W>(ix, cb, c);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// selection: saQuerySeedSetRef's uniqueness walk (ReadQueue.cpp:1928-2160) and
+// matchReads' orientation choice (ReadQueue.cpp:629-923)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t mk_match(uint32_t off, uint32_t err, uint64_t fwd, uint64_t meta)
+{
+    return (uint64_t)(off & 0xffffu) | ((uint64_t)(err & 0xffu) << 16) | (fwd << 24) | (meta << 32);
+}
+
+struct Uniq {
+    uint8_t multi[NERR + 1];
+    uint64_t uniq[NERR + 1];
+    uint32_t prevChr;
+    uint64_t prevOff;
+    bool abort;  // a second zero-error hit: return -1
+};
+
+// One hit of candidate window w (dir = forward window); idx = hit index in the window.
+__device__ __forceinline__ void uniq_hit(const DevIndex& ix, Uniq& u, uint32_t w, uint32_t sp, int dir, uint32_t off,
+                                         uint32_t err)
+{
+    if (u.multi[err]) {
+        const uint64_t m2 = u.uniq[err];
+        const bool m2fwd = (m2 >> 24) & 1ull, m2start = (m2 >> 25) & 1ull;
+        const bool same_dir = dir ? m2fwd : !m2fwd;
+        if (same_dir && !m2start &&
+            (uint64_t)ix.win[(uint32_t)(m2 >> 32)].x + (m2 & 0xffffull) == (uint64_t)sp + off)
+            return;
+        if (err == 0) { u.abort = true; return; }
+        u.multi[err] = 2;
+    } else {
+        u.uniq[err] = mk_match(off, err, (uint64_t)dir, w);
+        u.multi[err] = 1;
+    }
+}
+
+template <int W>
+__device__ __noinline__ void rescan_into(const DevIndex& ix, const ChunkBufs& cb, uint32_t task, uint32_t w, int dir, Uniq& u,
+                            uint32_t sp, uint32_t ch, uint32_t& nh, uint32_t& last)
+{
+    const uint32_t r = task >> 1, o = task & 1;
+    const uint64_t off0 = cb.offs[r];
+    const uint32_t len = (uint32_t)(cb.offs[r + 1] - off0);
+    ShiftAndState<W> sa;
+    sa.load(cb.seqs + off0, len, (int)o);
+    scan_window<W>(ix, sa, w, dir, [&](uint32_t off, int err) {
+        if (u.abort) return;
+        if (!(nh == 0 && (uint64_t)off + sp == u.prevOff && ch == u.prevChr)) uniq_hit(ix, u, w, sp, dir, off, (uint32_t)err);
+        last = off;
+        ++nh;
+    });
+}
+
+// returns 1 / 0 / -1 like saQuerySeedSetRef; *mat as the reference leaves it
+__device__ int select_task(const DevIndex& ix, const ChunkBufs& cb, uint32_t task, uint64_t* mat)
+{
+    const uint4 tc = cb.task_cand[task];
+    const uint32_t base = tc.x, nf = tc.y, nt = tc.y + tc.z;
+    Uniq u;
+#pragma unroll
+    for (int i = 0; i <= (int)NERR; ++i) { u.multi[i] = 0; u.uniq[i] = 0; }
+    u.abort = false;
+    const uint32_t r = task >> 1;
+    const uint32_t len = (uint32_t)(cb.offs[r + 1] - cb.offs[r]);
+    for (uint32_t k = 0; k < nt; ++k) {
+        if (k == 0 || k == nf) { u.prevChr = 0; u.prevOff = 0xffffffffffffffffull; }
+        const uint32_t c = base + k;
+        const uint32_t e = cb.cand[c];
+        const uint32_t w = e & 0x7fffffffu;
+        const int dir = (int)(e >> 31);
+        const uint4 wi = ix.win[w];
+        const uint32_t sp = wi.x, ch = wi.y;
+        const uint32_t n = cb.hit_n[c];
+        uint32_t last = 0, nh = 0;
+        if (n <= HIT_CAP) {
+            const uint32_t* h = cb.hits + (uint64_t)c * HIT_CAP;
+            for (uint32_t i = 0; i < n && !u.abort; ++i) {
+                const uint32_t off = h[i] >> 8, err = h[i] & 0xffu;
+                if (!(i == 0 && (uint64_t)off + sp == u.prevOff && ch == u.prevChr)) uniq_hit(ix, u, w, sp, dir, off, err);
+                last = off;
+            }
+            nh = n;
+        } else {
+            switch (len / 64 + 1) {
+                case 1: rescan_into<1>(ix, cb, task, w, dir, u, sp, ch, nh, last); break;
+                case 2: rescan_into<2>(ix, cb, task, w, dir, u, sp, ch, nh, last); break;
+                case 3: rescan_into<3>(ix, cb, task, w, dir, u, sp, ch, nh, last); break;
+                default: rescan_into<4>(ix, cb, task, w, dir, u, sp, ch, nh, last); break;
+            }
+        }
+        if (u.abort) return -1;
+        if (nh > 0) { u.prevChr = ch; u.prevOff = (uint64_t)sp + last; }
+        else { u.prevChr = 0; u.prevOff = 0xffffffffffffffffull; }
+    }
+    for (int i = 0; i <= (int)NERR; ++i) {
+        if (!u.multi[i]) continue;
+        *mat = u.uniq[i];
+        return u.multi[i] > 1 ? -1 : 1;
+    }
+    return 0;
+}
+
+__device__ __forceinline__ uint8_t oriented_char(const char* raw, uint32_t len, int orient, uint32_t i)
+{
+    return orient ? rc_byte((uint8_t)raw[len - 1 - i]) : (uint8_t)raw[i];
+}
+
+// computeMethLvl for a hit without errors (ReadQueue.cpp:3293-3484)
+__device__ void meth_exact(const DevIndex& ix, const ChunkBufs& cb, uint32_t r, int orient, uint64_t mat)
+{
+    const uint32_t meta = (uint32_t)(mat >> 32);
+    const int isFwd = (int)((mat >> 24) & 1ull);
+    const uint16_t offset = (uint16_t)(mat & 0xffffull);
+    const uint4 wi = ix.win[meta];
+    const uint32_t metaPos = wi.x, sind = wi.z, eind = wi.w;
+    const uint64_t off0 = cb.offs[r];
+    const uint32_t size = (uint32_t)(cb.offs[r + 1] - off0);
+    const char* raw = cb.seqs + off0;
+    const uint32_t RL = ix.readlen;
+    const uint32_t minPos = (uint32_t)(metaPos + offset - (size - 1));
+    const uint32_t maxPos = metaPos + offset;
+    for (uint32_t id = sind; id <= eind; ++id) {
+        const uint32_t pos = ix.cpg_pos[id];
+        if (pos + RL - 2 < minPos) continue;
+        if (isFwd) { if (pos + RL - 2 > maxPos) break; }
+        else { if (pos + RL - 1 > maxPos) break; }
+        const uint32_t trueCpGPos = pos - 1 + RL - 1;
+        const uint32_t readCpGPos = (uint32_t)(size - (uint32_t)(metaPos + offset - trueCpGPos) - 1);
+        if (isFwd) {
+            if ((uint32_t)(readCpGPos + MISCOUNT) >= size) continue;
+            const uint8_t c = oriented_char(raw, size, orient, (uint32_t)(readCpGPos + MISCOUNT));
+            if (c == 'T') atomicAdd(cb.meth + 4ull * id + 1, 1u);
+            else if (c == 'C') atomicAdd(cb.meth + 4ull * id + 0, 1u);
+        } else {
+            if ((uint32_t)(readCpGPos + 1 + MISCOUNT + 2) > size) continue;
+            const uint8_t c = oriented_char(raw, size, orient, size - readCpGPos - 1 - MISCOUNT - 2);
+            if (c == 'T') atomicAdd(cb.meth + 4ull * id + 3, 1u);
+            else if (c == 'C') atomicAdd(cb.meth + 4ull * id + 2, 1u);
+        }
+    }
+}
+
+__global__ void k_select(DevIndex ix, ChunkBufs cb)
+{
+    __shared__ unsigned long long sc[8];
+    if (threadIdx.x < 8) sc[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < cb.n) {
+        const uint8_t f = cb.rflags[r];
+        uint64_t mat = 0;
+        bool ok = false;
+        int orient = 0;
+        if (f & 1u) atomicAdd(&sc[0], 1ull);
+        else if (f & 2u) atomicAdd(&sc[1], 1ull);
+        if (!(f & 7u)) {
+            const bool runF = cb.orient_mask & 1u, runR = (cb.orient_mask >> 1) & 1u;
+            uint64_t mF = 0, mR = 0;
+            int sF = 0, sR = 0;
+            if (runF) sF = select_task(ix, cb, 2 * r, &mF);
+            if (runR) sR = select_task(ix, cb, 2 * r + 1, &mR);
+            const uint32_t eF = (uint32_t)((mF >> 16) & 0xff), eR = (uint32_t)((mR >> 16) & 0xff);
+            int vote = 0;  // 1 fwd, 2 rev
+            if (sF == 1 && sR == 1) {
+                if (eF < eR) { ok = true; mat = mF; orient = 0; vote = 1; }
+                else if (eF > eR) { ok = true; mat = mR; orient = 1; vote = 2; }
+                else {
+                    const uint32_t p1 = ix.win[(uint32_t)(mF >> 32)].x + (uint32_t)(mF & 0xffff);
+                    const uint32_t p2 = ix.win[(uint32_t)(mR >> 32)].x + (uint32_t)(mR & 0xffff);
+                    if (((mF >> 24) & 1) == ((mR >> 24) & 1) && p1 == p2) { ok = true; mat = mF; orient = 0; vote = 1; }
+                    else atomicAdd(&sc[3], 1ull);
+                }
+            } else if (sF == 1) {
+                if (sR == -1 && !(eF < eR)) atomicAdd(&sc[3], 1ull);
+                else { ok = true; mat = mF; orient = 0; vote = 1; }
+            } else if (sR == 1) {
+                if (sF == -1 && !(eR < eF)) atomicAdd(&sc[3], 1ull);
+                else { ok = true; mat = mR; orient = 1; vote = 2; }
+            } else {
+                if (sF == -1 || sR == -1) atomicAdd(&sc[3], 1ull);
+                else atomicAdd(&sc[4], 1ull);
+            }
+            if (ok) {
+                atomicAdd(&sc[2], 1ull);
+                if (cb.stranded) atomicAdd(&sc[vote == 1 ? 5 : 6], 1ull);
+            }
+        }
+        cb.mats[r] = ok ? mat : 0;
+        cb.invalid[r] = ok ? 0 : 1;
+        if (ok) {
+            const uint32_t meta = (uint32_t)(mat >> 32);
+            if (ix.win[meta].z != CPGDUMMY) {
+                if (((mat >> 16) & 0xff) == 0) meth_exact(ix, cb, r, orient, mat);
+                else {
+                    const uint32_t slot = (uint32_t)atomicAdd(cb.ctr + CTR_DP, 1ull);
+                    cb.dp_list[slot] = r;
+                    cb.dp_mat[slot] = mat;
+                    cb.dp_orient[slot] = (uint8_t)orient;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int map[7] = {CTR_INV_LEN, CTR_INV_N, CTR_SUCC, CTR_NONU, CTR_UNSUCC, CTR_R1F, CTR_R1R};
+        for (int i = 0; i < 7; ++i) if (sc[i]) atomicAdd(cb.ctr + map[i], sc[i]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// banded DP (LevenshtDP<uint16_t, 8>, LevenshtDP.h:191-544) over the storage
+// layout of BandedMatrix<uint16_t, 9> (BandedMatrix.h:67-75), then the CpG walk
+// of computeMethLvl (ReadQueue.cpp:3620-3944).  The matrix of each thread
+// lives in global scratch interleaved across threads (cell-major) so that a
+// warp's accesses to one cell coalesce.
+// ---------------------------------------------------------------------------
+struct DpScratch {
+    uint16_t* cells;    // [cell][slot]
+    uint8_t* align;     // [step][slot]
+    uint32_t nslots;
+    uint32_t cell_cap;  // cells per slot
+    uint32_t align_cap; // alignment steps per slot
+};
+
+constexpr long DPB = DP_BAND;      // band
+constexpr long DPS = DP_BAND + 1;  // storage band
+constexpr long DPW = 2 * DPS + 1;  // cells per stored row
+
+__device__ __forceinline__ long dp_idx(long i, long j)
+{
+    return i * DPW + (DPS - i > 0 ? DPS - i : 0) + (j - i + DPS);
+}
+
+__device__ __forceinline__ uint16_t cmp_fwd(uint8_t r, uint8_t g)  // CompiFwd, ReadQueue.h:295-307
+{
+    if (r == 'T' && g == 'C') return 0;
+    return r == g ? 0 : 1;
+}
+__device__ __forceinline__ uint16_t cmp_rev(uint8_t r, uint8_t g)  // CompiRev, ReadQueue.h:309-338
+{
+    switch (r) {
+        case 'T': if (g == 'A' || g == 'G') return 0; break;
+        case 'G': if (g == 'C') return 0; break;
+        case 'A': if (g == 'T') return 0; break;
+        case 'C': if (g == 'G') return 0; break;
+    }
+    return 1;
+}
+
+struct DpView {
+    uint16_t* c;
+    uint32_t stride;
+    long msize;
+    __device__ __forceinline__ uint16_t get(long i, long j) const
+    {
+        const long k = dp_idx(i, j);
+        return (k >= 0 && k < msize) ? c[(uint64_t)k * stride] : (uint16_t)0xffff;
+    }
+    __device__ __forceinline__ void set(long i, long j, uint16_t v) const
+    {
+        const long k = dp_idx(i, j);
+        if (k >= 0 && k < msize) c[(uint64_t)k * stride] = v;
+    }
+};
+
+__device__ void meth_dp(const DevIndex& ix, const ChunkBufs& cb, const DpScratch& ds, uint32_t slot, uint32_t r,
+                        int orient, uint64_t mat)
+{
+    const uint32_t meta = (uint32_t)(mat >> 32);
+    const int isFwd = (int)((mat >> 24) & 1ull);
+    const uint16_t offset = (uint16_t)(mat & 0xffffull);
+    const uint4 wi = ix.win[meta];
+    const uint32_t metaPos = wi.x, sind = wi.z, eind = wi.w;
+    const uint64_t off0 = cb.offs[r];
+    const uint32_t size = (uint32_t)(cb.offs[r + 1] - off0);
+    const char* raw = cb.seqs + off0;
+    const uint32_t RL = ix.readlen;
+    const uint32_t chrom = ix.cpg_chrom[sind];
+    const int64_t base = (int64_t)metaPos + offset;
+    const long n = (long)size;
+    DpView dv{ds.cells + slot, ds.nslots, (n + 1) * DPW};
+    if ((uint64_t)dv.msize > ds.cell_cap) { atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull); return; }
+    for (long k = 0; k < dv.msize; ++k) dv.c[(uint64_t)k * ds.nslots] = 0xffff;
+    // runDPFill / runDPFillRev (LevenshtDP.h:205-323)
+    dv.set(0, 0, 0);
+    for (long c = 1; c <= DPB; ++c) dv.set(0, c, (uint16_t)c);
+    for (long rr = 1; rr <= DPB; ++rr) dv.set(rr, 0, (uint16_t)rr);
+    for (long c = 0; c < n - DPB; ++c) dv.set(c + DPB + 1, c, (uint16_t)(65535 - c - DPB - 1));
+    for (long rr = 0; rr < n; ++rr) dv.set(rr, rr + DPB + 1, (uint16_t)(65535 - rr - DPB - 1));
+    for (long row = 1; row <= n; ++row) {
+        const uint8_t rc = oriented_char(raw, size, orient, isFwd ? (uint32_t)(n - row) : (uint32_t)(row - 1));
+        for (long o = -DPB; o <= DPB; ++o) {
+            const long j = row + o;
+            if (j <= 0) continue;
+            const uint8_t g = base_char(gbase(ix, chrom, base + 1 - j));
+            const int mm = isFwd ? cmp_fwd(rc, g) : cmp_rev(rc, g);
+            int v = dv.get(row - 1, j) + 1;
+            const int v2 = dv.get(row, j - 1) + 1;
+            const int v3 = dv.get(row - 1, j - 1) + mm;
+            if (v2 < v) v = v2;
+            if (v3 < v) v = v3;
+            dv.set(row, j, (uint16_t)v);
+        }
+    }
+    // backtrackDP / backtrackDPRev (LevenshtDP.h:327-544)
+    uint8_t* al = ds.align + slot;
+    uint32_t alen = 0;
+    {
+        uint16_t mn = 0xffff;
+        long col = 0;
+        for (long o = -DPB; o <= DPB; ++o) {
+            const uint16_t v = dv.get(n, n + o);
+            if (v < mn) { col = n + o; mn = v; }
+        }
+        for (long row = n; row > 0;) {
+            const uint8_t rc = oriented_char(raw, size, orient, isFwd ? (uint32_t)(n - row) : (uint32_t)(row - 1));
+            const uint8_t g = base_char(gbase(ix, chrom, base + 1 - col));
+            const int mm = isFwd ? cmp_fwd(rc, g) : cmp_rev(rc, g);
+            const uint16_t up = dv.get(row - 1, col), left = dv.get(row, col - 1), dg = dv.get(row - 1, col - 1);
+            uint8_t code;
+            if (up < left) {
+                if ((int)up + 1 < (int)dg + mm) { code = 2; --row; }
+                else { code = mm ? 1 : 0; --row; --col; }
+            } else {
+                if ((int)left + 1 < (int)dg + mm) { code = 3; --col; }
+                else { code = mm ? 1 : 0; --row; --col; }
+            }
+            if (alen >= ds.align_cap) { atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull); return; }
+            al[(uint64_t)alen * ds.nslots] = code;
+            ++alen;
+        }
+        while (col > 0) {
+            if (alen >= ds.align_cap) { atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull); return; }
+            al[(uint64_t)alen * ds.nslots] = 3;
+            ++alen;
+            --col;
+        }
+    }
+    // CpG range and walk (ReadQueue.cpp:3631-3944)
+    const uint32_t minPos = (uint32_t)(metaPos + offset - (size - 1));
+    const uint32_t maxPos = metaPos + offset;
+    int32_t minIndex = (int32_t)sind, maxIndex = (int32_t)eind;
+    for (int32_t id = (int32_t)sind; (uint32_t)id <= eind; ++id) {
+        const uint32_t pos = ix.cpg_pos[id];
+        if (pos + RL - 2 < minPos) ++minIndex;
+        else if (pos + RL - 2 > maxPos) { maxIndex = id - 1; break; }
+    }
+    uint32_t refSeqPos = metaPos + offset;
+    int32_t readSeqPos = (int32_t)size - 1;
+    int32_t alignPos = (int32_t)alen - 1;
+    for (int32_t id = maxIndex; id >= minIndex; --id) {
+        const uint32_t cpos = ix.cpg_pos[id] + RL - 2;
+        while (cpos < refSeqPos && alignPos >= 0) {
+            switch (al[(uint64_t)alignPos * ds.nslots]) {
+                case 0: case 1: --readSeqPos; --refSeqPos; break;
+                case 3: --refSeqPos; break;
+                default: --readSeqPos; break;
+            }
+            if (readSeqPos < 0) break;
+            --alignPos;
+        }
+        if (readSeqPos < 0) break;
+        if (isFwd) {
+            const uint8_t c = oriented_char(raw, size, orient, (uint32_t)readSeqPos);
+            if (c == 'C') atomicAdd(cb.meth + 4ull * id + 0, 1u);
+            else if (c == 'T') atomicAdd(cb.meth + 4ull * id + 1, 1u);
+        } else {
+            // the sequence was reversed in place (ReadQueue.cpp:3796); index size reads '\0'
+            const uint32_t k = (uint32_t)readSeqPos + 1;
+            const uint8_t c = k < size ? oriented_char(raw, size, orient, size - 1 - k) : 0;
+            if (c == 'C') atomicAdd(cb.meth + 4ull * id + 2, 1u);
+            else if (c == 'T') atomicAdd(cb.meth + 4ull * id + 3, 1u);
+        }
+    }
+}
+
+__global__ void k_dp(DevIndex ix, ChunkBufs cb, DpScratch ds)
+{
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= ds.nslots) return;
+    const uint32_t ndp = (uint32_t)cb.ctr[CTR_DP];
+    for (uint32_t i = slot; i < ndp; i += ds.nslots) meth_dp(ix, cb, ds, slot, cb.dp_list[i], cb.dp_orient[i], cb.dp_mat[i]);
+}
+
+// ---------------------------------------------------------------------------
+// read checks (ReadQueue.cpp:428-490)
+// ---------------------------------------------------------------------------
+__global__ void k_prep(ChunkBufs cb, uint32_t readlen)
+{
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= cb.n) return;
+    const uint64_t o0 = cb.offs[r];
+    const uint32_t len = (uint32_t)(cb.offs[r + 1] - o0);
+    uint8_t f = 0;
+    if (len < readlen - 20) f = 1;
+    else {
+        for (uint32_t i = 0; i < len; ++i) if (cb.seqs[o0 + i] == 'N') { f = 2; break; }
+        if (!f && len > FAME_MAX_READ_LEN) { f = 4; atomicAdd(cb.ctr + CTR_TOO_LONG, 1ull); }
+    }
+    cb.rflags[r] = f;
+    cb.task_cand[2 * r] = make_uint4(0, 0, 0, 0);
+    cb.task_cand[2 * r + 1] = make_uint4(0, 0, 0, 0);
+}
+
+// Light path: one warp per task, working memory in shared memory.
+constexpr uint32_t L_OPS = 256, L_DT = 512, L_SLOT = 512 + NBHD - 1, L_OVF = 32;
+struct LightLayout {
+    // per warp, in bytes
+    static constexpr uint32_t KST = 0;                          // 224 x u32
+    static constexpr uint32_t KPRE = KST + 224 * 4;             // 225 x u32
+    static constexpr uint32_t INS = KPRE + 228 * 4;             // L_OPS x u32
+    static constexpr uint32_t INSC = INS + L_OPS * 4;           // L_OPS x u32
+    static constexpr uint32_t U = INSC + L_OPS * 4;             // union region
+    // phase A (hash/gather/count): seq, ops, opk, dt
+    static constexpr uint32_t SEQ = U;                          // 256 B
+    static constexpr uint32_t OPS = SEQ + 256;                  // L_OPS x u32
+    static constexpr uint32_t OPK = OPS + L_OPS * 4;            // L_OPS x u8
+    static constexpr uint32_t DTK = OPK + L_OPS;                // L_DT x u32
+    static constexpr uint32_t DTF = DTK + L_DT * 4;
+    static constexpr uint32_t DTC = DTF + L_DT * 4;
+    static constexpr uint32_t END_A = DTC + L_DT * 4;
+    // phase B (replay): slot, stk, ovf, stage
+    static constexpr uint32_t SLOT = U;
+    static constexpr uint32_t STK = SLOT + ((L_SLOT * 4 + 15) / 16) * 16;
+    static constexpr uint32_t OVF = STK + L_OPS * 4;
+    static constexpr uint32_t STAGE = OVF + L_OVF * 4;
+    static constexpr uint32_t END_B = STAGE + L_OPS * 4;
+    static constexpr uint32_t BYTES = ((END_A > END_B ? END_A : END_B) + 15) / 16 * 16;
+};
+
+__device__ __forceinline__ SeedMem light_mem(uint8_t* base)
+{
+    SeedMem s;
+    s.kst = (uint32_t*)(base + LightLayout::KST);
+    s.kpre = (uint32_t*)(base + LightLayout::KPRE);
+    s.ins = (uint32_t*)(base + LightLayout::INS);
+    s.ins_cnt = (uint32_t*)(base + LightLayout::INSC);
+    s.seq = base + LightLayout::SEQ;
+    s.ops = (uint32_t*)(base + LightLayout::OPS);
+    s.opk = base + LightLayout::OPK;
+    s.dt_key = (uint32_t*)(base + LightLayout::DTK);
+    s.dt_first = (uint32_t*)(base + LightLayout::DTF);
+    s.dt_cnt = (uint32_t*)(base + LightLayout::DTC);
+    s.slot = (uint32_t*)(base + LightLayout::SLOT);
+    s.stk = (uint32_t*)(base + LightLayout::STK);
+    s.ovf = (uint32_t*)(base + LightLayout::OVF);
+    s.stage = (uint32_t*)(base + LightLayout::STAGE);
+    s.ops_cap = L_OPS; s.dt_cap = L_DT; s.slot_cap = L_SLOT; s.stk_cap = L_OPS; s.ovf_cap = L_OVF;
+    return s;
+}
+
+// tasks: all (read, orientation) pairs of the chunk in orientation-major order
+__global__ void k_seed(DevIndex ix, ChunkBufs cb, uint32_t ntask)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const uint32_t wib = threadIdx.x >> 5;
+    const SeedMem s = light_mem(smem + wib * LightLayout::BYTES);
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    const int norient = __popc(cb.orient_mask);
+    const uint32_t first_o = (cb.orient_mask & 1u) ? 0 : 1;
+    for (uint32_t t = blockIdx.x * (blockDim.x >> 5) + wib; t < ntask; t += nwarps) {
+        const uint32_t r = norient == 2 ? (t >> 1) : t;
+        const uint32_t o = norient == 2 ? (t & 1) : first_o;
+        if (cb.rflags[r]) continue;
+        const uint32_t task = 2 * r + o;
+        const int heavy = seed_task(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES);
+        if (heavy && (threadIdx.x & 31) == 0) {
+            const uint32_t h = (uint32_t)atomicAdd(cb.ctr + CTR_HEAVY, 1ull);
+            cb.heavy[h] = task;
+        }
+        __syncwarp();
+    }
+}
+
+// Heavy path: one warp per task with its working memory in global scratch.
+struct HeavyScratch {
+    uint8_t* base;
+    uint64_t bytes_per_warp;
+    uint32_t nwarps;
+    uint32_t ops_cap, dt_cap, slot_cap;
+};
+
+__device__ __forceinline__ SeedMem heavy_mem(const HeavyScratch& hs, uint32_t w)
+{
+    uint8_t* b = hs.base + (uint64_t)w * hs.bytes_per_warp;
+    SeedMem s;
+    const uint64_t oc = hs.ops_cap, dc = hs.dt_cap, sc = hs.slot_cap;
+    uint64_t o = 0;
+    auto take = [&](uint64_t bytes) { uint8_t* p = b + o; o += (bytes + 15) / 16 * 16; return p; };
+    s.seq = take(256);
+    s.kst = (uint32_t*)take(256 * 4);
+    s.kpre = (uint32_t*)take(260 * 4);
+    s.ops = (uint32_t*)take(oc * 4);
+    s.opk = take(oc);
+    s.dt_key = (uint32_t*)take(dc * 4);
+    s.dt_first = (uint32_t*)take(dc * 4);
+    s.dt_cnt = (uint32_t*)take(dc * 4);
+    s.ins = (uint32_t*)take(oc * 4);
+    s.ins_cnt = (uint32_t*)take(oc * 4);
+    s.slot = (uint32_t*)take(sc * 4);
+    s.stk = (uint32_t*)take(oc * 4);
+    s.ovf = (uint32_t*)take(oc * 4);
+    s.stage = (uint32_t*)take(oc * 4);
+    s.ops_cap = hs.ops_cap; s.dt_cap = hs.dt_cap; s.slot_cap = hs.slot_cap; s.stk_cap = hs.ops_cap; s.ovf_cap = hs.ops_cap;
+    return s;
+}
+
+__host__ __device__ inline uint64_t heavy_bytes_per_warp(uint64_t ops_cap, uint64_t dt_cap, uint64_t slot_cap)
+{
+    auto al = [](uint64_t x) { return (x + 15) / 16 * 16; };
+    return al(256) + al(256 * 4) + al(260 * 4) + al(ops_cap * 4) + al(ops_cap) + 3 * al(dt_cap * 4) +
+           2 * al(ops_cap * 4) + al(slot_cap * 4) + 3 * al(ops_cap * 4);
+}
+
+__global__ void k_seed_heavy(DevIndex ix, ChunkBufs cb, HeavyScratch hs, uint32_t nheavy)
+{
+    const uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (w >= hs.nwarps) return;
+    const SeedMem s = heavy_mem(hs, w);
+    for (uint32_t i = w; i < nheavy; i += hs.nwarps) {
+        const uint32_t task = cb.heavy[i];
+        const int bad = seed_task(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES);
+        if (bad && (threadIdx.x & 31) == 0) {
+            atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull);
+            cb.task_cand[task] = make_uint4(0, 0, 0, 0);
+        }
+        __syncwarp();
+    }
+}
+
+// Largest bucket of the index (sizes the heavy path).
+__global__ void k_max_bucket(const uint32_t* tab, uint64_t n, unsigned int* out)
+{
+    uint32_t mx = 0;
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        mx = max(mx, tab[k + 1] - tab[k]);
+    for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
+}
+
+}  // namespace fame

@@ -1,0 +1,123 @@
+"""Host-side mirror of FAME's ReadQueue (ReadQueue.h:58-131) over the C ABI.
+
+The names, argument meaning and loop structure follow the reference so that
+tests read like its own: parse_chunk (parseChunk, ReadQueue.cpp:218-296),
+match_reads (matchReads, 404-933, on the GPU), decide_strand (376-400),
+print_methylation_levels (1860-1893) and query_routine (main.cpp:363-399).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from ._lib import CHUNKSIZE, FAME_BOTH_STRANDS, FAME_GET_STRANDED, FAME_MATCH_R1_FWD, GpuMatcher, HostIndex
+
+
+class _FastqSource:
+    """parseChunk's reading: four getline calls per record, sequence = line 2."""
+
+    def __init__(self, path: str, is_gz: bool = False):
+        import gzip
+        self.f = gzip.open(path, "rb") if is_gz else open(path, "rb")
+
+    def take(self, n):
+        seqs = []
+        while len(seqs) < n:
+            hdr = self.f.readline()
+            if not hdr:
+                break
+            seq = self.f.readline().rstrip(b"\n")
+            self.f.readline()
+            self.f.readline()
+            seqs.append(seq)
+        return seqs
+
+
+class _ListSource:
+    def __init__(self, seqs):
+        self.seqs = seqs
+        self.i = 0
+
+    def take(self, n):
+        out = self.seqs[self.i:self.i + n]
+        self.i += len(out)
+        return out
+
+
+class ReadQueue:
+    def __init__(self, reads, index: HostIndex, gpu: GpuMatcher, is_gz: bool = False, both_strands: bool = False,
+                 chunk_size: int = CHUNKSIZE):
+        if isinstance(reads, str):
+            self.src = _FastqSource(reads, is_gz)
+        else:
+            self.src = _ListSource(list(reads))
+        self.index = index
+        self.gpu = gpu
+        self.chunk_size = chunk_size
+        self.both_strands_flag = both_strands
+        self.r1_fwd_matches = 0
+        self.r1_rev_matches = 0
+        self.match_r1_fwd = True
+        self.buffer = []
+        self.mats = np.zeros(0, np.uint64)
+        self.invalid = np.zeros(0, np.uint8)
+
+    def parse_chunk(self):
+        """Returns (procReads, more): more is True iff a full chunk was read."""
+        self.buffer = self.src.take(self.chunk_size)
+        n = len(self.buffer)
+        return n, n >= self.chunk_size
+
+    def match_reads(self, proc_reads: int, get_stranded: bool):
+        """Match buffer[:proc_reads]; returns (succ, nonunique, unsucc) of this call."""
+        seqs = self.buffer[:proc_reads]
+        offs = np.zeros(len(seqs) + 1, dtype=np.uint64)
+        np.cumsum([len(s) for s in seqs], out=offs[1:])
+        flags = (FAME_GET_STRANDED if get_stranded else 0) | (FAME_BOTH_STRANDS if self.both_strands_flag else 0) | \
+            (FAME_MATCH_R1_FWD if self.match_r1_fwd else 0)
+        mats, inval, cnt = self.gpu.match_reads(b"".join(seqs), offs, flags)
+        self.mats, self.invalid = mats, inval
+        self.r1_fwd_matches += cnt.r1_fwd
+        self.r1_rev_matches += cnt.r1_rev
+        return cnt
+
+    def decide_strand(self):
+        self.match_r1_fwd = self.r1_fwd_matches > self.r1_rev_matches
+
+    def methylation_levels(self) -> np.ndarray:
+        return self.gpu.tallies(reset=False)
+
+    def print_methylation_levels(self, basename: str):
+        """<basename>_cpg.tsv: chrom, C position, methFwd, unmethFwd, methRev, unmethRev."""
+        write_cpg_report(basename + "_cpg.tsv", self.index, self.gpu.tallies(reset=False))
+
+    def query_routine(self):
+        """main.cpp:363-399; returns the summed counters."""
+        tot = dict(succ=0, nonunique=0, unsucc=0)
+
+        def add(c):
+            tot["succ"] += c.succ
+            tot["nonunique"] += c.nonunique
+            tot["unsucc"] += c.unsucc
+
+        if not self.both_strands_flag:
+            n, _ = self.parse_chunk()
+            add(self.match_reads(n, True))
+            self.decide_strand()
+        while True:
+            n, more = self.parse_chunk()
+            if not more:
+                break
+            add(self.match_reads(n, False))
+        add(self.match_reads(n, False))
+        return tot
+
+
+def write_cpg_report(path: str, index: HostIndex, meth: np.ndarray):
+    """printMethylationLevels (ReadQueue.cpp:1860-1893)."""
+    t = index.tables()
+    names = np.array(index.chrom_names(), dtype=object)
+    pos = t["cpg_pos"].astype(np.int64) + index.readlen - 2
+    with open(path, "w") as f:
+        for i in range(len(pos)):
+            m = meth[i]
+            f.write("%s\t%d\t%d\t%d\t%d\t%d\n" % (names[t["cpg_chrom"][i]], pos[i], m[0], m[1], m[2], m[3]))

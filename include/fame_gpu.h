@@ -1,0 +1,163 @@
+/* fame_gpu.h — C ABI of the GB300 read-matching library for FAME.
+ *
+ * The library replaces the body of FAME's single-end matching stage
+ * (ReadQueue::matchReads, ReadQueue.cpp:404-933, and everything it calls:
+ * getSeedRefs 2325-2461, saQuerySeedSetRef 1928-2160, ShiftAnd.h,
+ * computeMethLvl 3278-3947, LevenshtDP.h) with CUDA kernels for sm_103a.
+ * FAME's host (CLI, parseChunk, decideStrand, printMethylationLevels, the
+ * --load_index reader) stays as it is and calls these functions.
+ *
+ * Conventions: plain C types, host pointers unless a name ends in _dev,
+ * every function returns FAME_OK (0) or a negative FAME_ERR_* code and never
+ * exits; fame_gpu_last_error() returns a message for the last failure.
+ * One fame_gpu context is used by one host thread at a time.
+ */
+#ifndef FAME_GPU_H
+#define FAME_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    FAME_OK = 0,
+    FAME_ERR_ARG = -1,        /* bad argument (null pointer, size)              */
+    FAME_ERR_CUDA = -2,       /* CUDA runtime failure (message has the detail)  */
+    FAME_ERR_NOMEM = -3,      /* device or host allocation failed               */
+    FAME_ERR_INDEX = -4,      /* index tables inconsistent or unsupported       */
+    FAME_ERR_READ = -5,       /* a read is longer than FAME_MAX_READ_LEN        */
+    FAME_ERR_IO = -6,         /* index file missing, truncated or mismatched    */
+    FAME_ERR_TIMEOUT = -7,    /* a bounded device wait gave up                  */
+    FAME_ERR_BUSY = -8        /* serving queue full / admission refused         */
+};
+
+/* Longest read the kernels accept (the reference has no limit; FAME's
+ * CONST.h READLEN is 100 or 150 for the workloads it is run on). */
+#define FAME_MAX_READ_LEN 255
+
+/* Match flags of fame_gpu_match_reads, the three inputs of the orientation
+ * choice at ReadQueue.cpp:529 and :591. */
+#define FAME_GET_STRANDED 1u  /* matchReads(..., getStranded = true): both orientations, count r1 votes */
+#define FAME_BOTH_STRANDS 2u  /* bothStrandsFlag (--unord_reads)                                      */
+#define FAME_MATCH_R1_FWD 4u  /* matchR1Fwd after decideStrand (ReadQueue.cpp:376-400)               */
+
+/* Layout-compatible with the reference's structs (structs.h:40-72, 118-125). */
+typedef struct { uint8_t chrom; uint32_t pos; } fame_cpg;                            /* struct CpG   */
+typedef struct { uint32_t start_pos; uint8_t chrom; uint32_t start_ind; uint32_t end_ind; } fame_window; /* metaWindow */
+typedef struct { uint32_t meta; uint32_t tmask; } fame_kmer;                        /* KMER_S::kmer */
+
+/* A loaded index: the public members of RefGenome after load()
+ * (RefGenome.h:193-227, RefGenome.cpp:230-387), as host pointers the caller
+ * keeps alive for the duration of fame_gpu_open.  Exactly one of tab_index
+ * (the reference's uint64 offsets) or tab_index32 must be given; both hold
+ * 2^30 + 1 entries.  strand_bits is strandTable packed LSB first, the layout
+ * of the <index>_strands side file (RefGenome.cpp:392-433). */
+typedef struct {
+    uint32_t readlen;                 /* MyConst::READLEN of the index (CONST.h:35) */
+    uint32_t n_chrom;
+    const char* const* chrom_seq;     /* fullSeq[c].data()                          */
+    const uint64_t* chrom_len;
+    const char* const* chrom_name;    /* chrMap (may be NULL)                       */
+    uint64_t n_cpg;
+    const fame_cpg* cpg;              /* cpgTable                                   */
+    const uint64_t* tab_index;        /* tabIndex (uint64)                          */
+    const uint32_t* tab_index32;      /* or the same offsets as uint32              */
+    uint64_t n_kmer;
+    const fame_kmer* kmer;            /* kmerTableSmall                             */
+    const uint8_t* strand_bits;       /* strandTable                                */
+    uint64_t n_win;
+    const fame_window* win;           /* metaWindows                                */
+    uint64_t n_filtered;
+    const uint64_t* filtered;         /* filteredKmers (paired path only)           */
+} fame_index_view;
+
+/* Per-call statistics: the counters matchReads updates (ReadQueue.cpp:408-416,
+ * 926-932) plus the strand votes of the first chunk (r1FwdMatches/r1RevMatches). */
+typedef struct {
+    uint64_t succ;
+    uint64_t nonunique;
+    uint64_t unsucc;
+    uint64_t r1_fwd;
+    uint64_t r1_rev;
+    uint64_t invalid_len;     /* reads rejected by the length gate (ReadQueue.cpp:430) */
+    uint64_t invalid_n;       /* reads rejected for an N (ReadQueue.cpp:487)            */
+    uint64_t gather_bytes;    /* algorithmic index-gather bytes of the call             */
+    uint64_t windows_scanned; /* Shift-And window scans of the call                     */
+    uint64_t dp_reads;        /* reads aligned with the banded DP                       */
+} fame_counters;
+
+typedef struct fame_gpu fame_gpu;
+
+/* ---- host-side index (the --load_index format and the index build) ---- */
+typedef struct fame_host_index fame_host_index;
+
+/* Read <path> and <path>_strands as written by RefGenome::save
+ * (RefGenome.cpp:83-228); the header constants must equal the library's
+ * (RefGenome.cpp:239-280 exits on a mismatch, this returns FAME_ERR_IO). */
+int fame_index_read(const char* path, fame_host_index** out);
+
+/* Build the index from chromosome sequences the way readReference +
+ * RefGenome(cpgTab, ...) do (RefReader_istr.h:48-113, RefGenome.cpp:26-74,
+ * 532-759, 1787-1989, 2191-2352), on n_threads host threads (0 = all). */
+int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* const* seq, const uint64_t* len,
+                     const char* const* names, int noloss, int n_threads, fame_host_index** out);
+
+/* Borrow a view of a host index (valid until fame_index_free). */
+int fame_index_view_of(const fame_host_index* ix, fame_index_view* view);
+void fame_index_free(fame_host_index* ix);
+/* cpgStartTable (CpGs too close to a chromosome start to be reported,
+ * RefReader_istr.h:66-76); returns the count, copies up to cap entries. */
+uint64_t fame_index_cpg_start(const fame_host_index* ix, fame_cpg* out, uint64_t cap);
+
+/* ---- device context ----------------------------------------------------- */
+/* Copy the index into HBM on `device` (resident until fame_gpu_close). */
+int fame_gpu_open(const fame_index_view* ix, int device, fame_gpu** out);
+int fame_gpu_close(fame_gpu* g);
+const char* fame_gpu_last_error(const fame_gpu* g);
+
+/* ReadQueue::matchReads for one chunk of reads: seqs holds the sequences back
+ * to back, read i is seqs[offs[i] .. offs[i+1]).  Per read it writes the match
+ * (MATCH::match encoding, structs.h:154-192; 0 when invalid) and the invalid
+ * flag (Read::isInvalid), accumulates the CpG tallies in device memory and
+ * adds to *cnt.  Synchronous. */
+int fame_gpu_match_reads(fame_gpu* g, const char* seqs, const uint64_t* offs, uint32_t n, uint32_t flags,
+                         uint64_t* mats, uint8_t* invalid, fame_counters* cnt);
+
+/* The same with the reads, offsets and outputs already in device memory
+ * (allocated by fame_gpu_alloc or by the caller). */
+int fame_gpu_match_reads_dev(fame_gpu* g, const char* seqs_dev, const uint64_t* offs_dev, uint32_t n,
+                             uint32_t flags, uint64_t* mats_dev, uint8_t* invalid_dev, fame_counters* cnt);
+
+/* Copy out the methylation tallies as methLevels (ReadQueue.h:354-367): four
+ * uint16 per CpG in cpgTable order {methFwd, unmethFwd, methRev, unmethRev}
+ * with the reference's 16-bit wrap-around; reset != 0 zeroes them afterwards
+ * (printSCMethylationLevels, ReadQueue.cpp:1894-1921). */
+int fame_gpu_tallies(fame_gpu* g, uint16_t* meth, int reset);
+
+/* Device memory helpers for the _dev entry points, and page-locked host
+ * buffers (a host that parses its chunks straight into these gets the fast
+ * host-to-device copy path). */
+int fame_gpu_alloc(fame_gpu* g, size_t bytes, void** ptr_dev);
+int fame_gpu_free(fame_gpu* g, void* ptr_dev);
+int fame_gpu_memcpy(fame_gpu* g, void* dst, const void* src, size_t bytes, int kind /* 1 H2D, 2 D2H, 3 D2D */);
+int fame_gpu_host_alloc(fame_gpu* g, size_t bytes, void** ptr);
+int fame_gpu_host_free(fame_gpu* g, void* ptr);
+/* The CUDA stream (cudaStream_t) all work of the context runs on. */
+int fame_gpu_stream(fame_gpu* g, void** stream);
+
+/* Per-stage device time of the last match call, in milliseconds, measured with
+ * CUDA events on the library's stream when enabled.  Stages: 0 read prep,
+ * 1 seed/gather/order, 2 Shift-And, 3 select + exact CpG calls, 4 banded DP +
+ * CpG calls, 5 heavy-read seeding.  Returns the number of stages. */
+int fame_gpu_set_timing(fame_gpu* g, int enable);
+int fame_gpu_stage_times(fame_gpu* g, float* ms, int n);
+/* Number of kernel launches of the last match call. */
+int fame_gpu_last_launches(const fame_gpu* g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FAME_GPU_H */

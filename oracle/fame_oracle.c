@@ -728,9 +728,10 @@ static void compute_meth(const orc_index* ix, uint64_t mat, uint8_t* seq, uint32
         if (pos + RL - 2 < minPos) ++minIndex;
         else if (pos + RL - 2 > maxPos) { maxIndex = id - 1; break; }
     }
-    uint8_t* al = (uint8_t*)malloc((size_t)size + 4 * DP_BAND + 8);
+    const uint32_t alcap = 2 * size + 2 * DP_BAND + 8; /* every backtrack step lowers row or column */
+    uint8_t* al = (uint8_t*)malloc(alcap);
     lev_fill(&L, !isFwd, isFwd ? 1 : 2);
-    const uint32_t alen = lev_back(&L, !isFwd, isFwd ? 1 : 2, al, size + 4 * DP_BAND + 8);
+    const uint32_t alen = lev_back(&L, !isFwd, isFwd ? 1 : 2, al, alcap);
     uint32_t refSeqPos = metaPos + offset;
     int32_t readSeqPos = (int32_t)size - 1;
     int32_t alignPos = (int32_t)alen - 1;
@@ -785,7 +786,7 @@ static void match_chunk(const orc_index* ix, const uint8_t* seqs, const uint64_t
     hits h = {0};
     for (uint32_t r = 0; r < n; ++r) {
         const uint32_t size = (uint32_t)(offs[r + 1] - offs[r]);
-        uint8_t* fw = (uint8_t*)malloc(size + 1);
+        uint8_t* fw = (uint8_t*)calloc(size + 1, 1); /* std::string keeps a NUL at [size] */
         uint8_t* rv = (uint8_t*)calloc(size + 1, 1);
         memcpy(fw, seqs + offs[r], size);
         invalid[r] = 0;

@@ -357,3 +357,36 @@ int fame_ref_hopscotch(const uint32_t* keys, uint32_t n, uint32_t bucket_count, 
     return (int)k;
 }
 }
+
+extern "C" {
+// Steady-state timing of ReadQueue::matchReads (ReadQueue.cpp:404-933): the
+// orientation is already decided (matchR1Fwd given, getStranded false), as for
+// every chunk after the first in queryRoutine (main.cpp:383-388).  Only the
+// matchReads calls are timed.  counters: [succ, nonunique, unsucc]
+int fame_ref_time_se(void* ref, const char* seqs, const uint64_t* offs, uint32_t n, int both_strands,
+                     int match_r1_fwd, uint64_t* counters, double* seconds)
+{
+    RefGenome& r = *static_cast<RefGenome*>(ref);
+    ReadQueue* rq = in_tmp([&] { return new ReadQueue("/dev/null", r, false, both_strands != 0); });
+    rq->matchR1Fwd = match_r1_fwd != 0;
+    uint64_t succ = 0, nonu = 0, unsucc = 0;
+    double secs = 0.0;
+    std::string id("r");
+    const uint32_t chunk = MyConst::CHUNKSIZE;
+    for (uint32_t c0 = 0; c0 < n; c0 += chunk) {
+        const uint32_t cn = std::min<uint32_t>(chunk, n - c0);
+        for (uint32_t j = 0; j < cn; ++j) {
+            std::string s(seqs + offs[c0 + j], seqs + offs[c0 + j + 1]);
+            rq->readBuffer[j] = Read(s, id);
+        }
+        auto t0 = std::chrono::steady_clock::now();
+        rq->matchReads(cn, succ, nonu, unsucc, false);
+        auto t1 = std::chrono::steady_clock::now();
+        secs += std::chrono::duration<double>(t1 - t0).count();
+    }
+    counters[0] = succ; counters[1] = nonu; counters[2] = unsucc;
+    *seconds = secs;
+    delete rq;
+    return 0;
+}
+}

@@ -132,6 +132,19 @@ class RefIndex:
                                      _ptr(mats), _ptr(inval), _ptr(meth), _ptr(cnt), _ptr(secs))
         return dict(mat=mats, invalid=inval, meth=meth.reshape(-1, 4), counters=cnt, seconds=float(secs[0]))
 
+    def time_se(self, seq_bytes: bytes, offs: np.ndarray, both_strands: bool = False, match_r1_fwd: bool = True):
+        """Seconds spent in matchReads for already-stranded chunks, and [succ, nonunique, unsucc]."""
+        import ctypes as C
+        f = self.L.lib.fame_ref_time_se
+        f.argtypes = [_P, _P, _P, C.c_uint32, C.c_int, C.c_int, _P, _P]
+        n = len(offs) - 1
+        cnt = np.zeros(3, np.uint64)
+        secs = np.zeros(1, np.float64)
+        buf = np.frombuffer(seq_bytes, dtype=np.uint8)
+        offs = np.ascontiguousarray(offs, dtype=np.uint64)
+        f(self.h, _ptr(buf), _ptr(offs), n, int(both_strands), int(match_r1_fwd), _ptr(cnt), _ptr(secs))
+        return float(secs[0]), cnt
+
     def seed_order(self, seq: bytes, cap: int = 1 << 20):
         keys = np.zeros(cap, np.uint32)
         cnts = np.zeros(cap, np.uint32)

@@ -1,0 +1,58 @@
+"""The C ABI library: it builds, loads, exports every declared entry point and
+reports argument and I/O errors (no GPU needed)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from fame_gb300 import _lib
+from fame_gb300 import build as fbuild
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "fame_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*|uint64_t)\s+(fame_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+    assert os.path.exists(fbuild.LIB)
+
+
+def test_argument_errors_without_gpu():
+    L = _lib.lib()
+    assert L.fame_gpu_open(None, 0, None) == -1
+    assert L.fame_gpu_close(None) == -1
+    assert L.fame_gpu_match_reads(None, None, None, 0, 0, None, None, None) == -1
+    assert L.fame_gpu_tallies(None, None, 0) == -1
+    assert L.fame_index_read(None, None) == -1
+
+
+def test_index_read_errors(tmp_path):
+    L = _lib.lib()
+    h = C.c_void_p()
+    assert L.fame_index_read(str(tmp_path / "missing.idx").encode(), C.byref(h)) == -6
+    bad = tmp_path / "bad.idx"
+    bad.write_bytes(b"\x00" * 64)   # wrong HTABSIZE in the header
+    assert L.fame_index_read(str(bad).encode(), C.byref(h)) == -6
+    import struct
+    hdr = struct.pack("<QIIIQI", 1 << 30, 100, 2048, 32, 1500, 0xDEFDFFFD)
+    trunc = tmp_path / "trunc.idx"
+    trunc.write_bytes(hdr + struct.pack("<Q", 5))   # announces 5 CpGs, ends there
+    assert L.fame_index_read(str(trunc).encode(), C.byref(h)) == -6
+    wrongseed = tmp_path / "seed.idx"
+    wrongseed.write_bytes(struct.pack("<QIIIQI", 1 << 30, 100, 2048, 32, 1500, 0x12345678))
+    assert L.fame_index_read(str(wrongseed).encode(), C.byref(h)) == -6
+
+
+def test_lib_rebuild_is_noop_when_fresh():
+    fbuild.build()
+    assert fbuild.up_to_date()
