@@ -537,3 +537,108 @@ extern "C" int fame_gpu_stream(fame_gpu* g, void** stream)
     *stream = (void*)g->stream;
     return FAME_OK;
 }
+
+// ---------------------------------------------------------------------------
+// CpG calls without any device allocation (fame_gpu_call_cpgs_noalloc).
+//
+// Some callers of this library cannot allocate device memory while they run:
+// a serving loop whose other streams must not be stalled by the device-wide
+// synchronisation that cudaFree implies, or code that is only handed buffers
+// from an allocator it does not own.  This entry point is a variant of the
+// banded-DP CpG kernel (k_dp in kernels.cuh) whose per-read DP matrices live
+// in one file-scope static device array instead of context scratch; the
+// caller passes its inputs and outputs in device memory it already has.
+#include <mutex>
+
+namespace {
+
+// Layout of the static array: 256 bytes of status counters, then one DP
+// matrix (cells) and one alignment trace per slot.  NOALLOC_SLOTS slots serve
+// any number of reads (the kernel strides over them); reads up to
+// FAME_MAX_READ_LEN bases fit a slot.  Total: about 10.5 MB per GPU.
+constexpr uint32_t NOALLOC_SLOTS = 1024;
+constexpr uint32_t NOALLOC_CELLS = (FAME_MAX_READ_LEN + 1) * (uint32_t)DPW;
+constexpr uint32_t NOALLOC_ALIGN = 2 * FAME_MAX_READ_LEN + 4 * DP_BAND + 8;
+constexpr uint64_t NOALLOC_HEADER = 256;
+constexpr uint64_t NOALLOC_BYTES =
+    NOALLOC_HEADER + (uint64_t)NOALLOC_SLOTS * NOALLOC_CELLS * 2 + (uint64_t)NOALLOC_SLOTS * NOALLOC_ALIGN;
+
+static __device__ __align__(256) uint8_t g_noalloc_scratch[NOALLOC_BYTES];
+
+constexpr int MAX_DEVICES = 64;
+void* g_scratch_addr[MAX_DEVICES] = {};
+std::mutex g_scratch_mu;
+
+// Device address of the static array on the current device (resolved once per
+// device; the host-side symbol is only a stand-in and is never passed to a kernel).
+void* scratch_address(int dev)
+{
+    if (dev < 0 || dev >= MAX_DEVICES) return nullptr;
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) return nullptr;
+        g_scratch_addr[dev] = p;
+    }
+    return g_scratch_addr[dev];
+}
+
+__global__ void k_call_cpgs_static(DevIndex ix, ChunkBufs cb, DpScratch ds, const uint64_t* mats, const uint8_t* inval,
+                                   uint32_t n, int orient)
+{
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= ds.nslots) return;
+    for (uint32_t i = slot; i < n; i += ds.nslots) {
+        if (inval[i]) continue;
+        const uint32_t len = (uint32_t)(cb.offs[i + 1] - cb.offs[i]);
+        if (len > FAME_MAX_READ_LEN) { atomicAdd(cb.ctr + CTR_TOO_LONG, 1ull); continue; }
+        const uint64_t mat = mats[i];
+        const uint32_t meta = (uint32_t)(mat >> 32);
+        if (meta >= ix.n_win) { atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull); continue; }
+        if (ix.win[meta].z == CPGDUMMY) continue;  // computeMethLvl returns early (ReadQueue.cpp:3287)
+        if (((mat >> 16) & 0xff) == 0) meth_exact(ix, cb, i, orient, mat);
+        else meth_dp(ix, cb, ds, slot, i, orient, mat);
+    }
+}
+
+}  // namespace
+
+extern "C" int fame_gpu_call_cpgs_noalloc(fame_gpu* g, const char* seqs_dev, const uint64_t* offs_dev,
+                                          const uint64_t* mats_dev, const uint8_t* invalid_dev, uint32_t n,
+                                          int orient, uint32_t* meth_dev)
+{
+    if (!g || !meth_dev || (orient != 0 && orient != 1) || (n && (!seqs_dev || !offs_dev || !mats_dev || !invalid_dev)))
+        return FAME_ERR_ARG;
+    const int dev = g->device;
+    if (cudaSetDevice(dev) != cudaSuccess) return FAME_ERR_CUDA;
+    uint8_t* base = (uint8_t*)scratch_address(dev);
+    if (!base) return FAME_ERR_CUDA;
+    cudaStream_t s = g->stream;
+    unsigned long long* h = g->h_ctr;
+    unsigned long long* d_ctr = (unsigned long long*)base;
+    if (cudaMemsetAsync(meth_dev, 0, 16 * g->n_cpg, s) != cudaSuccess) return FAME_ERR_CUDA;
+    if (cudaMemsetAsync(d_ctr, 0, NOALLOC_HEADER, s) != cudaSuccess) return FAME_ERR_CUDA;
+    if (n) {
+        ChunkBufs cb{};
+        cb.seqs = seqs_dev;
+        cb.offs = offs_dev;
+        cb.n = n;
+        cb.meth = meth_dev;
+        cb.ctr = d_ctr;
+        DpScratch ds;
+        ds.cells = (uint16_t*)(base + NOALLOC_HEADER);
+        ds.align = base + NOALLOC_HEADER + (uint64_t)NOALLOC_SLOTS * NOALLOC_CELLS * 2;
+        ds.nslots = NOALLOC_SLOTS;
+        ds.cell_cap = NOALLOC_CELLS;
+        ds.align_cap = NOALLOC_ALIGN;
+        k_call_cpgs_static<<<NOALLOC_SLOTS / 128, 128, 0, s>>>(g->ix, cb, ds, mats_dev, invalid_dev, n,
+                                                              orient);
+        if (cudaGetLastError() != cudaSuccess) return FAME_ERR_CUDA;
+    }
+    if (cudaMemcpyAsync(h, d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return FAME_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return FAME_ERR_CUDA;
+    if (h[CTR_TOO_LONG]) return FAME_ERR_READ;
+    if (h[CTR_ERRFLAG]) return FAME_ERR_ARG;
+    return FAME_OK;
+}

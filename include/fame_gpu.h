@@ -157,6 +157,26 @@ int fame_gpu_stage_times(fame_gpu* g, float* ms, int n);
 /* Number of kernel launches of the last match call. */
 int fame_gpu_last_launches(const fame_gpu* g);
 
+/* CpG calls that allocate no device memory.  No counterpart in the reference:
+ * it is for callers that cannot allocate while they run (a serving loop that
+ * must not stall its other streams on the device-wide synchronisation of
+ * cudaFree, or code that only receives buffers from an allocator it does not
+ * own).  For each read i < n with invalid_dev[i] == 0 it does what
+ * computeMethLvl does for the match mats_dev[i] (exact-hit lookup, or the
+ * banded DP and alignment walk), with the read as given (orient 0) or its
+ * reverse complement (orient 1), and writes four uint32 counters per CpG
+ * {methFwd, unmethFwd, methRev, unmethRev} to meth_dev (zeroed first; the low
+ * 16 bits are methLevels).  All pointers are device memory owned by the
+ * caller; g only supplies the resident index and its stream.
+ * Scratch: one static device array of about 10.5 MB per GPU that loads the
+ * library (held until exit), shared by every call: calls that overlap on the
+ * GPU race.  The first call on a device resolves the array's address and
+ * should come before any stream capture.  Reads longer than
+ * FAME_MAX_READ_LEN give FAME_ERR_READ; a match naming no window of the index
+ * gives FAME_ERR_ARG. */
+int fame_gpu_call_cpgs_noalloc(fame_gpu* g, const char* seqs_dev, const uint64_t* offs_dev, const uint64_t* mats_dev,
+                               const uint8_t* invalid_dev, uint32_t n, int orient, uint32_t* meth_dev);
+
 #ifdef __cplusplus
 }
 #endif
