@@ -72,6 +72,7 @@ enum {
     CTR_SCANS,
     CTR_TOO_LONG,
     CTR_ERRFLAG,        // a device-side capacity check failed
+    CTR_WMASK,          // bit W set when a valid read needs a W-word automaton
     CTR_N
 };
 

@@ -38,14 +38,12 @@ struct fame_gpu {
     unsigned long long* d_ctr = nullptr;
     unsigned long long* h_ctr = nullptr;  // pinned
     uint32_t* d_meth = nullptr;
-    DpScratch dp{};
     HeavyScratch hs{};
     int timing = 0;
     cudaEvent_t ev[8]{};
     float stage_ms[6]{};
     int launches = 0;
     int sm_count = 0;
-    uint32_t wmask = 0x1e;  // Shift-And word counts present in the chunk (bit W)
 };
 
 namespace {
@@ -134,7 +132,7 @@ extern "C" int fame_gpu_close(fame_gpu* g)
     dev_free(g->d_cand); dev_free(g->d_cand_task); dev_free(g->d_hits); dev_free(g->d_hit_n);
     dev_free(g->d_mats); dev_free(g->d_invalid); dev_free(g->d_dp_list); dev_free(g->d_dp_mat);
     dev_free(g->d_dp_orient); dev_free(g->d_heavy); dev_free(g->d_ctr); dev_free(g->d_meth);
-    dev_free(g->dp.cells); dev_free(g->dp.align); dev_free(g->hs.base);
+    dev_free(g->hs.base);
     if (g->h_ctr) cudaFreeHost(g->h_ctr);
     for (auto& e : g->ev) if (e) cudaEventDestroy(e);
     if (g->stream) cudaStreamDestroy(g->stream);
@@ -293,13 +291,8 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
     if (cudaMemset(g->d_meth, 0, 16 * std::max<uint64_t>(1, v->n_cpg)) != cudaSuccess) return fail(set_err(g, FAME_ERR_CUDA, "memset"));
     if ((rc = dev_alloc(g, &g->d_ctr, CTR_N))) return fail(rc);
     if (cudaMallocHost(&g->h_ctr, CTR_N * sizeof(unsigned long long)) != cudaSuccess) return fail(set_err(g, FAME_ERR_NOMEM, "pinned alloc"));
-    g->dp.nslots = 128u * (uint32_t)std::max(1, g->sm_count);
-    g->dp.cell_cap = (FAME_MAX_READ_LEN + 1) * (uint32_t)DPW;
-    g->dp.align_cap = 2 * FAME_MAX_READ_LEN + 4 * DP_BAND + 8;
-    if ((rc = dev_alloc(g, &g->dp.cells, (uint64_t)g->dp.cell_cap * g->dp.nslots)) ||
-        (rc = dev_alloc(g, &g->dp.align, (uint64_t)g->dp.align_cap * g->dp.nslots)))
-        return fail(rc);
-    if (cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * LightLayout::BYTES) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * LightLayout::BYTES) != cudaSuccess ||
+        cudaFuncSetAttribute(k_dp_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * DPW_BYTES) != cudaSuccess)
         return fail(set_err(g, FAME_ERR_CUDA, "shared memory attribute"));
     *out = g;
     return FAME_OK;
@@ -381,15 +374,16 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         if (ncand) {
             const uint32_t tb = 128;
             const uint32_t grid = (uint32_t)std::min<uint64_t>((ncand + tb - 1) / tb, (uint64_t)g->sm_count * 32);
-            if (g->wmask & 2u) { k_shiftand<1><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
-            if (g->wmask & 4u) { k_shiftand<2><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
-            if (g->wmask & 8u) { k_shiftand<3><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
-            if (g->wmask & 16u) { k_shiftand<4><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+            const uint64_t wmask = g->h_ctr[CTR_WMASK];
+            if (wmask & 2u) { k_shiftand<1><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+            if (wmask & 4u) { k_shiftand<2><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+            if (wmask & 8u) { k_shiftand<3><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+            if (wmask & 16u) { k_shiftand<4><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
         }
         if (T) cudaEventRecord(g->ev[3], g->stream);
         k_select<<<(n + 255) / 256, 256, 0, g->stream>>>(g->ix, cb);
         if (T) cudaEventRecord(g->ev[4], g->stream);
-        k_dp<<<(g->dp.nslots + 127) / 128, 128, 0, g->stream>>>(g->ix, cb, g->dp);
+        k_dp_warp<<<(uint32_t)g->sm_count * 8, 128, 4 * DPW_BYTES, g->stream>>>(g->ix, cb);
         if (T) cudaEventRecord(g->ev[5], g->stream);
         g->launches += 2;
         CK(cudaGetLastError());
@@ -448,11 +442,7 @@ extern "C" int fame_gpu_match_reads(fame_gpu* g, const char* seqs, const uint64_
         CK(cudaMemcpyAsync(g->d_offs, o.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, g->stream));
         CK(cudaStreamSynchronize(g->stream));
     }
-    g->wmask = 0;
-    for (uint32_t i = 0; i < n; ++i) g->wmask |= 1u << std::min<uint64_t>(4, (offs[i + 1] - offs[i]) / 64 + 1);
-    rc = run_chunk(g, g->d_seqs, g->d_offs, n, flags, g->d_mats, g->d_invalid, cnt);
-    g->wmask = 0x1e;
-    if (rc) return rc;
+    if ((rc = run_chunk(g, g->d_seqs, g->d_offs, n, flags, g->d_mats, g->d_invalid, cnt))) return rc;
     CK(cudaMemcpyAsync(mats, g->d_mats, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, g->stream));
     CK(cudaMemcpyAsync(invalid, g->d_invalid, n, cudaMemcpyDeviceToHost, g->stream));
     CK(cudaStreamSynchronize(g->stream));

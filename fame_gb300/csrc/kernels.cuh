@@ -92,12 +92,12 @@ struct ShiftAndState {
     }
 };
 
-// Scan of one candidate window (querySeq / queryRevSeq, ShiftAnd.h:130-255, on
-// the text spans of saQuerySeedSetRef, ReadQueue.cpp:1953-1962, 2048-2058).
+// Full scan of one candidate window (querySeq / queryRevSeq, ShiftAnd.h:130-255,
+// on the text spans of saQuerySeedSetRef, ReadQueue.cpp:1953-1962, 2048-2058).
 // emit(offset, errors) is called once per run of consecutive accepting bases,
 // with the last position holding the run's smallest error count.
 template <int W, class Emit>
-__device__ void scan_window(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t wid, int fwd, Emit emit)
+__device__ void scan_window_full(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t wid, int fwd, Emit emit)
 {
     const uint4 wi = ix.win[wid];
     const uint32_t sp = wi.x, ch = wi.y;
@@ -156,6 +156,201 @@ __device__ void scan_window(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t w
     if (was) emit(cur_off, cur_err);
 }
 
+
+// Text of a window in scan order: forward windows run over [sp, e), reverse
+// windows from hi down to lo + 1 with every base complemented.
+struct ScanText {
+    const DevIndex* ix;
+    uint64_t g0;      // packed-genome index of scan position 0
+    int dir;          // +1 forward, -1 reverse
+    uint32_t len;     // scan positions
+    uint32_t off_a;   // reported offset = off_a + dir_sign * u (see off())
+    int fwd;
+    __device__ __forceinline__ int base(uint32_t u, bool& isN) const
+    {
+        const uint64_t g = dir > 0 ? g0 + u : g0 - u;
+        isN = (__ldg(ix->gnmask + (g >> 5)) >> (g & 31)) & 1u;
+        const int b = (int)((__ldg(ix->gpack + (g >> 4)) >> (2 * (g & 15))) & 3u);
+        return fwd ? b : 3 - b;
+    }
+    __device__ __forceinline__ uint32_t off(uint32_t u) const { return fwd ? u + MISCOUNT : off_a - u; }
+};
+
+// Scan of one candidate window with the same hits as scan_window_full.
+//
+// Any alignment of the read with <= 6 edits leaves one of 7 disjoint read
+// pieces without an edit, so that piece's first q bases occur in the text
+// (equal in the reduced alphabet A / G / C=T, which the asymmetric match
+// implies).  A cheap pass finds those q-gram occurrences and turns each into
+// the span of scan positions where the alignment can end; the automaton then
+// runs only over those spans, each entered at least m + 7 positions early
+// (the state at a position depends on the last m + 6 bases only, and a reset
+// state never accepts where the full scan would not) or continued from the
+// previous span, and each extended until its run of accepting positions ends.
+// N bases reset the automaton exactly as in the full scan.  Too many spans
+// (repetitive windows) fall back to the full scan.
+template <int W, class Emit>
+__device__ void scan_window(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t wid, int fwd, Emit emit,
+                            const uint32_t* pkey, uint32_t pvalid, uint64_t bloom, uint32_t q, const uint32_t* pstart)
+{
+    constexpr int CAP = 32;
+    const uint4 wi = ix.win[wid];
+    const uint32_t sp = wi.x, ch = wi.y;
+    const int64_t L = (int64_t)ix.chrom_len[ch];
+    const uint64_t gch = ix.chrom_off[ch];
+    ScanText tx;
+    tx.ix = &ix;
+    tx.fwd = fwd;
+    if (fwd) {
+        int64_t e = (int64_t)sp + WIN_TEXT;
+        if (e > L) e = L;
+        tx.g0 = gch + sp;
+        tx.dir = 1;
+        tx.len = (uint32_t)(e - (int64_t)sp);
+        tx.off_a = 0;
+    } else {
+        const int64_t lo = sp > 0 ? (int64_t)sp - 1 : 0;
+        int64_t hi = (int64_t)sp + WIN_TEXT;
+        if (hi >= L) hi = L - 1;
+        tx.g0 = gch + (uint64_t)hi;
+        tx.dir = -1;
+        tx.len = (uint32_t)(hi - lo);
+        tx.off_a = (uint32_t)(hi - lo) + sa.plen - 1 + MISCOUNT;
+    }
+    const uint32_t m = sa.plen;
+    // ---- q-gram pass
+    int32_t ilo[CAP], ihi[CAP];
+    int nint = 0;
+    bool overflow = false;
+    {
+        const uint32_t qmask = q >= 16 ? 0xffffffffu : ((1u << (2 * q)) - 1);
+        uint32_t key = 0, valid = 0;
+        uint64_t g = tx.g0;
+        uint32_t wpack = __ldg(ix.gpack + (g >> 4)), wn = __ldg(ix.gnmask + (g >> 5));
+        for (uint32_t u = 0; u < tx.len; ++u, g += tx.dir) {
+            if (fwd) {
+                if ((g & 15) == 0) wpack = __ldg(ix.gpack + (g >> 4));
+                if ((g & 31) == 0) wn = __ldg(ix.gnmask + (g >> 5));
+            } else {
+                if ((g & 15) == 15) wpack = __ldg(ix.gpack + (g >> 4));
+                if ((g & 31) == 31) wn = __ldg(ix.gnmask + (g >> 5));
+            }
+            if ((wn >> (g & 31)) & 1u) { valid = 0; continue; }
+            int b = (int)((wpack >> (2 * (g & 15))) & 3u);
+            if (!fwd) b = 3 - b;
+            const uint32_t sym = b == 0 ? 0u : (b == 2 ? 1u : 2u);  // A, G, C/T
+            key = ((key << 2) | sym) & qmask;
+            if (++valid < q) continue;
+            if (!((bloom >> ((key * 0x9E3779B1u) >> 26)) & 1ull)) continue;
+#pragma unroll
+            for (int k = 0; k < 7; ++k) {
+                if (((pvalid >> k) & 1u) && key == pkey[k]) {
+                    const int32_t x = (int32_t)(u - q + 1);
+                    const int32_t end0 = x - 1 + (int32_t)(m - pstart[k]);
+                    int32_t a = end0 - (int32_t)NERR, bnd = end0 + (int32_t)NERR;
+                    if (bnd < 0 || a > (int32_t)tx.len - 1) continue;
+                    if (a < 0) a = 0;
+                    if (bnd > (int32_t)tx.len - 1) bnd = (int32_t)tx.len - 1;
+                    if (nint >= CAP) { overflow = true; continue; }
+                    ilo[nint] = a;
+                    ihi[nint] = bnd;
+                    ++nint;
+                }
+            }
+        }
+    }
+    if (overflow) { scan_window_full<W>(ix, sa, wid, fwd, emit); return; }
+    if (nint == 0) return;
+    // sort spans by start and merge overlapping ones
+    for (int i = 1; i < nint; ++i) {
+        const int32_t a = ilo[i], b = ihi[i];
+        int j = i - 1;
+        while (j >= 0 && ilo[j] > a) { ilo[j + 1] = ilo[j]; ihi[j + 1] = ihi[j]; --j; }
+        ilo[j + 1] = a;
+        ihi[j + 1] = b;
+    }
+    int nm = 0;
+    for (int i = 0; i < nint; ++i) {
+        if (nm > 0 && ilo[i] <= ihi[nm - 1] + 1) { if (ihi[i] > ihi[nm - 1]) ihi[nm - 1] = ihi[i]; }
+        else { ilo[nm] = ilo[i]; ihi[nm] = ihi[i]; ++nm; }
+    }
+    // ---- automaton over the spans (state at scan position 0 = the full scan's reset)
+    const uint32_t gate = m - NERR;
+    bool was = false;
+    uint32_t cur_off = 0;
+    int cur_err = 0;
+    uint32_t ncl = 0;
+    int64_t cursor = -1;
+    sa.reset();
+    for (int i = 0; i < nm; ++i) {
+        int64_t start = (int64_t)ilo[i] - (int64_t)(m + NERR + 1);
+        if (start < 0) start = 0;
+        if (start <= cursor + 1) {
+            start = cursor + 1;
+        } else {
+            sa.reset();
+            ncl = 0;
+        }
+        int64_t u = start;
+        for (; u < (int64_t)tx.len && (u <= ihi[i] || was); ++u) {
+            bool isN;
+            const int b = tx.base((uint32_t)u, isN);
+            if (isN) { sa.reset(); continue; }
+            sa.letter(b);
+            if (++ncl < gate) continue;
+            const int er = sa.match();
+            if (er >= 0) {
+                const uint32_t off = tx.off((uint32_t)u);
+                if (was) { if (er <= cur_err) { cur_off = off; cur_err = er; } }
+                else { was = true; cur_off = off; cur_err = er; }
+            } else if (was) {
+                emit(cur_off, cur_err);
+                was = false;
+            }
+        }
+        cursor = u - 1;
+        if (u >= (int64_t)tx.len) break;
+    }
+    if (was) emit(cur_off, cur_err);
+}
+
+// Reduced-alphabet keys of the first q bases of the 7 read pieces.
+struct PieceKeys {
+    uint32_t key[7];
+    uint32_t start[7];
+    uint32_t valid;
+    uint64_t bloom;
+    uint32_t q;
+    __device__ __forceinline__ void load(const char* raw, uint32_t len, int orient)
+    {
+        q = min(16u, len / 7);
+        valid = 0;
+        bloom = 0;
+        for (int k = 0; k < 7; ++k) {
+            start[k] = (uint32_t)((k * len) / 7);
+            uint32_t kk = 0;
+            bool ok = true;
+            for (uint32_t i = 0; i < q; ++i) {
+                const uint32_t p = start[k] + i;
+                const uint8_t c = orient ? rc_byte((uint8_t)raw[len - 1 - p]) : (uint8_t)raw[p];
+                uint32_t sym;
+                switch (c) {
+                    case 'A': sym = 0; break;
+                    case 'G': sym = 1; break;
+                    case 'C': case 'T': sym = 2; break;
+                    default: sym = 3; ok = false; break;
+                }
+                kk = (kk << 2) | sym;
+            }
+            key[k] = kk;
+            if (ok) {
+                valid |= 1u << k;
+                bloom |= 1ull << ((kk * 0x9E3779B1u) >> 26);
+            }
+        }
+    }
+};
+
 template <int W>
 __device__ void shiftand_one(const DevIndex& ix, const ChunkBufs& cb, uint32_t c)
 {
@@ -165,13 +360,15 @@ __device__ void shiftand_one(const DevIndex& ix, const ChunkBufs& cb, uint32_t c
     const uint32_t len = (uint32_t)(cb.offs[r + 1] - off0);
     ShiftAndState<W> sa;
     sa.load(cb.seqs + off0, len, (int)o);
+    PieceKeys pk;
+    pk.load(cb.seqs + off0, len, (int)o);
     const uint32_t e = cb.cand[c];
     uint32_t n = 0;
     uint32_t* out = cb.hits + (uint64_t)c * HIT_CAP;
     scan_window<W>(ix, sa, e & 0x7fffffffu, (int)(e >> 31), [&](uint32_t off, int err) {
         if (n < HIT_CAP) out[n] = (off << 8) | (uint32_t)err;
         ++n;
-    });
+    }, pk.key, pk.valid, pk.bloom, pk.q, pk.start);
     cb.hit_n[c] = n;
 }
 
@@ -233,7 +430,7 @@ __device__ __noinline__ void rescan_into(const DevIndex& ix, const ChunkBufs& cb
     const uint32_t len = (uint32_t)(cb.offs[r + 1] - off0);
     ShiftAndState<W> sa;
     sa.load(cb.seqs + off0, len, (int)o);
-    scan_window<W>(ix, sa, w, dir, [&](uint32_t off, int err) {
+    scan_window_full<W>(ix, sa, w, dir, [&](uint32_t off, int err) {
         if (u.abort) return;
         if (!(nh == 0 && (uint64_t)off + sp == u.prevOff && ch == u.prevChr)) uniq_hit(ix, u, w, sp, dir, off, (uint32_t)err);
         last = off;
@@ -564,14 +761,6 @@ __device__ void meth_dp(const DevIndex& ix, const ChunkBufs& cb, const DpScratch
     }
 }
 
-__global__ void k_dp(DevIndex ix, ChunkBufs cb, DpScratch ds)
-{
-    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= ds.nslots) return;
-    const uint32_t ndp = (uint32_t)cb.ctr[CTR_DP];
-    for (uint32_t i = slot; i < ndp; i += ds.nslots) meth_dp(ix, cb, ds, slot, cb.dp_list[i], cb.dp_orient[i], cb.dp_mat[i]);
-}
-
 // ---------------------------------------------------------------------------
 // read checks (ReadQueue.cpp:428-490)
 // ---------------------------------------------------------------------------
@@ -586,6 +775,7 @@ __global__ void k_prep(ChunkBufs cb, uint32_t readlen)
     else {
         for (uint32_t i = 0; i < len; ++i) if (cb.seqs[o0 + i] == 'N') { f = 2; break; }
         if (!f && len > FAME_MAX_READ_LEN) { f = 4; atomicAdd(cb.ctr + CTR_TOO_LONG, 1ull); }
+        if (!f) atomicOr(cb.ctr + CTR_WMASK, 1ull << min(4u, len / 64 + 1));
     }
     cb.rflags[r] = f;
     cb.task_cand[2 * r] = make_uint4(0, 0, 0, 0);
@@ -726,6 +916,177 @@ __global__ void k_max_bucket(const uint32_t* tab, uint64_t n, unsigned int* out)
         mx = max(mx, tab[k + 1] - tab[k]);
     for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
     if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
+}
+
+}  // namespace fame
+
+namespace fame {
+
+// ---------------------------------------------------------------------------
+// Banded DP, one warp per read, the matrix in shared memory.  Same storage
+// (flat BandedMatrix index, dp_idx), same initial values and the same cell
+// recurrence as meth_dp; the cells are computed along anti-diagonals
+// t = 2 * row + offset (the three inputs of a cell lie on t - 1 and t - 2), one
+// band offset per lane, so every input is final when it is read.  The
+// backtrack and the CpG walk are serial on lane 0.
+// ---------------------------------------------------------------------------
+constexpr uint32_t DPW_MAXN = FAME_MAX_READ_LEN;
+constexpr uint32_t DPW_CELLS = (DPW_MAXN + 1) * (uint32_t)DPW;       // u16
+constexpr uint32_t DPW_REF = DPW_MAXN + 2 * DP_BAND + 8;             // reference bases, j in [-2, n + 10]
+constexpr uint32_t DPW_ALIGN = 2 * DPW_MAXN + 4 * DP_BAND + 8;
+constexpr uint32_t DPW_BYTES = ((DPW_CELLS * 2 + 256 + DPW_REF + DPW_ALIGN) + 15) / 16 * 16;
+constexpr int DPW_REF0 = 2;  // refc[j + DPW_REF0] = colPat[1 - j]
+
+__device__ __forceinline__ uint16_t sget(const uint16_t* c, long msize, long i, long j)
+{
+    const long k = dp_idx(i, j);
+    return (k >= 0 && k < msize) ? c[k] : (uint16_t)0xffff;
+}
+__device__ __forceinline__ void sset(uint16_t* c, long msize, long i, long j, uint16_t v)
+{
+    const long k = dp_idx(i, j);
+    if (k >= 0 && k < msize) c[k] = v;
+}
+
+__global__ void k_dp_warp(DevIndex ix, ChunkBufs cb)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int lane = threadIdx.x & 31;
+    uint8_t* base_p = smem + (threadIdx.x >> 5) * DPW_BYTES;
+    uint16_t* cells = (uint16_t*)base_p;
+    uint8_t* rowc = base_p + DPW_CELLS * 2;           // oriented read, 256 B
+    uint8_t* refc = rowc + 256;                       // reference bases along the columns
+    uint8_t* al = refc + DPW_REF;                     // alignment trace
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    const uint32_t ndp = (uint32_t)cb.ctr[CTR_DP];
+    for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < ndp; it += nwarps) {
+        const uint32_t r = cb.dp_list[it];
+        const uint64_t mat = cb.dp_mat[it];
+        const int orient = cb.dp_orient[it];
+        const uint32_t meta = (uint32_t)(mat >> 32);
+        const int isFwd = (int)((mat >> 24) & 1ull);
+        const uint16_t offset = (uint16_t)(mat & 0xffffull);
+        const uint4 wi = ix.win[meta];
+        const uint32_t metaPos = wi.x, sind = wi.z, eind = wi.w;
+        const uint64_t off0 = cb.offs[r];
+        const uint32_t size = (uint32_t)(cb.offs[r + 1] - off0);
+        const char* raw = cb.seqs + off0;
+        const uint32_t RL = ix.readlen;
+        const uint32_t chrom = ix.cpg_chrom[sind];
+        const int64_t gbase0 = (int64_t)metaPos + offset;
+        const long n = (long)size;
+        const long msize = (n + 1) * DPW;
+        // row characters: row k (1..n) compares rowc[k - 1]
+        for (long k = lane; k < n; k += 32)
+            rowc[k] = oriented_char(raw, size, orient, isFwd ? (uint32_t)(n - 1 - k) : (uint32_t)k);
+        for (long j = lane - DPW_REF0; j <= n + DPB + 2; j += 32)
+            refc[j + DPW_REF0] = base_char(gbase(ix, chrom, gbase0 + 1 - j));
+        for (long k = lane; k < msize; k += 32) cells[k] = 0xffff;
+        __syncwarp();
+        // borders in the reference's order (the left band's (9,0) is overwritten by the right band's (8,17))
+        if (lane == 0) {
+            sset(cells, msize, 0, 0, 0);
+            for (long c = 1; c <= DPB; ++c) sset(cells, msize, 0, c, (uint16_t)c);
+            for (long rr = 1; rr <= DPB; ++rr) sset(cells, msize, rr, 0, (uint16_t)rr);
+        }
+        __syncwarp();
+        for (long c = lane; c < n - DPB; c += 32) sset(cells, msize, c + DPB + 1, c, (uint16_t)(65535 - c - DPB - 1));
+        __syncwarp();
+        for (long rr = lane; rr < n; rr += 32) sset(cells, msize, rr, rr + DPB + 1, (uint16_t)(65535 - rr - DPB - 1));
+        __syncwarp();
+        // fill along anti-diagonals
+        const long o = lane - DPB;  // lanes 0..16 hold band offsets -8..8
+        for (long t = 2 - DPB; t <= 2 * n + DPB; ++t) {
+            if (lane <= 2 * DPB && ((t - o) & 1) == 0) {
+                const long row = (t - o) >> 1;
+                const long j = row + o;
+                if (row >= 1 && row <= n && j >= 1) {
+                    const uint8_t rc = rowc[row - 1];
+                    const uint8_t g = refc[j + DPW_REF0];
+                    const int mm = isFwd ? cmp_fwd(rc, g) : cmp_rev(rc, g);
+                    int v = sget(cells, msize, row - 1, j) + 1;
+                    const int v2 = sget(cells, msize, row, j - 1) + 1;
+                    const int v3 = sget(cells, msize, row - 1, j - 1) + mm;
+                    if (v2 < v) v = v2;
+                    if (v3 < v) v = v3;
+                    sset(cells, msize, row, j, (uint16_t)v);
+                }
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            uint32_t alen = 0;
+            bool bad = false;
+            uint16_t mn = 0xffff;
+            long col = 0;
+            for (long oo = -DPB; oo <= DPB; ++oo) {
+                const uint16_t v = sget(cells, msize, n, n + oo);
+                if (v < mn) { col = n + oo; mn = v; }
+            }
+            for (long row = n; row > 0;) {
+                const uint8_t rc = rowc[row - 1];
+                const long jj = col + DPW_REF0;
+                const uint8_t g = (jj >= 0 && jj < (long)DPW_REF) ? refc[jj] : 0;
+                const int mm = isFwd ? cmp_fwd(rc, g) : cmp_rev(rc, g);
+                const uint16_t up = sget(cells, msize, row - 1, col), left = sget(cells, msize, row, col - 1),
+                               dg = sget(cells, msize, row - 1, col - 1);
+                uint8_t code;
+                if (up < left) {
+                    if ((int)up + 1 < (int)dg + mm) { code = 2; --row; }
+                    else { code = mm ? 1 : 0; --row; --col; }
+                } else {
+                    if ((int)left + 1 < (int)dg + mm) { code = 3; --col; }
+                    else { code = mm ? 1 : 0; --row; --col; }
+                }
+                if (alen >= DPW_ALIGN) { bad = true; break; }
+                al[alen++] = code;
+            }
+            while (!bad && col > 0) {
+                if (alen >= DPW_ALIGN) { bad = true; break; }
+                al[alen++] = 3;
+                --col;
+            }
+            if (bad) {
+                atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull);
+            } else {
+                const uint32_t minPos = (uint32_t)(metaPos + offset - (size - 1));
+                const uint32_t maxPos = metaPos + offset;
+                int32_t minIndex = (int32_t)sind, maxIndex = (int32_t)eind;
+                for (int32_t id = (int32_t)sind; (uint32_t)id <= eind; ++id) {
+                    const uint32_t pos = ix.cpg_pos[id];
+                    if (pos + RL - 2 < minPos) ++minIndex;
+                    else if (pos + RL - 2 > maxPos) { maxIndex = id - 1; break; }
+                }
+                uint32_t refSeqPos = metaPos + offset;
+                int32_t readSeqPos = (int32_t)size - 1;
+                int32_t alignPos = (int32_t)alen - 1;
+                for (int32_t id = maxIndex; id >= minIndex; --id) {
+                    const uint32_t cpos = ix.cpg_pos[id] + RL - 2;
+                    while (cpos < refSeqPos && alignPos >= 0) {
+                        switch (al[alignPos]) {
+                            case 0: case 1: --readSeqPos; --refSeqPos; break;
+                            case 3: --refSeqPos; break;
+                            default: --readSeqPos; break;
+                        }
+                        if (readSeqPos < 0) break;
+                        --alignPos;
+                    }
+                    if (readSeqPos < 0) break;
+                    if (isFwd) {
+                        const uint8_t c = oriented_char(raw, size, orient, (uint32_t)readSeqPos);
+                        if (c == 'C') atomicAdd(cb.meth + 4ull * id + 0, 1u);
+                        else if (c == 'T') atomicAdd(cb.meth + 4ull * id + 1, 1u);
+                    } else {
+                        const uint32_t k = (uint32_t)readSeqPos + 1;
+                        const uint8_t c = k < size ? oriented_char(raw, size, orient, size - 1 - k) : 0;
+                        if (c == 'C') atomicAdd(cb.meth + 4ull * id + 2, 1u);
+                        else if (c == 'T') atomicAdd(cb.meth + 4ull * id + 3, 1u);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
 }
 
 }  // namespace fame

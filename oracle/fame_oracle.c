@@ -1299,3 +1299,18 @@ int orc_hopscotch(const uint32_t* keys, uint32_t n, uint32_t bucket_count, uint3
     cs_free(&cs);
     return k;
 }
+
+/* One matchReads call with explicit flags (ReadQueue.cpp:404-933); meth accumulates.
+ * counters: [succ, nonunique, unsucc, r1Fwd, r1Rev] of this call. */
+int orc_match_chunk(const orc_index* ix, const uint8_t* seqs, const uint64_t* offs, uint32_t n, int get_stranded,
+                    int both_strands, int match_r1_fwd, uint64_t* mats, uint8_t* invalid, uint16_t* meth,
+                    uint64_t* counters)
+{
+    stats st;
+    memset(&st, 0, sizeof(st));
+    st.matchR1Fwd = match_r1_fwd;
+    match_chunk(ix, seqs, offs, n, get_stranded, both_strands, &st, mats, invalid, meth);
+    counters[0] = st.succ; counters[1] = st.nonu; counters[2] = st.unsucc;
+    counters[3] = st.r1f; counters[4] = st.r1r;
+    return 0;
+}

@@ -73,6 +73,12 @@ int orc_lev(int band, const uint8_t* row, uint32_t row_len, const uint8_t* col, 
 int orc_shiftand(const uint8_t* pat, uint32_t pat_len, const uint8_t* text, uint32_t text_len, int rev,
                  uint64_t* offs, uint8_t* errs, uint32_t cap);
 
+/* One matchReads call with explicit flags; meth accumulates (uint16 wrap).
+ * counters: [succ, nonunique, unsucc, r1Fwd, r1Rev] of this call. */
+int orc_match_chunk(const orc_index* ix, const uint8_t* seqs, const uint64_t* offs, uint32_t n, int get_stranded,
+                    int both_strands, int match_r1_fwd, uint64_t* mats, uint8_t* invalid, uint16_t* meth,
+                    uint64_t* counters);
+
 /* Hopscotch insertion model on an explicit key sequence; returns iteration order. */
 int orc_hopscotch(const uint32_t* keys, uint32_t n, uint32_t bucket_count, uint32_t* order, uint64_t* final_buckets);
 

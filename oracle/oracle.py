@@ -50,6 +50,7 @@ def lib():
         L.orc_seed_order.argtypes = [_P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]
         L.orc_lev.argtypes = [C.c_int, _P, C.c_uint32, _P, C.c_int64, C.c_int64, C.c_int, C.c_int, _P, C.c_uint32, _P]
         L.orc_shiftand.argtypes = [_P, C.c_uint32, _P, C.c_uint32, C.c_int, _P, _P, C.c_uint32]
+        L.orc_match_chunk.argtypes = [_P, _P, _P, C.c_uint32, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P]
         _lib = L
     return _lib
 
@@ -115,6 +116,18 @@ class OracleIndex:
         lib().orc_match_se(C.byref(self.view), _ptr(buf), _ptr(offs), n, chunk, int(both_strands),
                            _ptr(mats), _ptr(inval), _ptr(meth), _ptr(cnt))
         return dict(mat=mats, invalid=inval, meth=meth.reshape(-1, 4), counters=cnt)
+
+    def match_chunk(self, seq_bytes, offs, get_stranded: bool, both_strands: bool, match_r1_fwd: bool, meth):
+        """One matchReads call; meth (uint16, 4 per CpG) accumulates.  Returns mats, invalid, counters[5]."""
+        n = len(offs) - 1
+        mats = np.zeros(n, np.uint64)
+        inval = np.zeros(n, np.uint8)
+        cnt = np.zeros(5, np.uint64)
+        buf = np.frombuffer(seq_bytes, dtype=np.uint8) if isinstance(seq_bytes, (bytes, bytearray)) else seq_bytes
+        offs = np.ascontiguousarray(offs, dtype=np.uint64)
+        lib().orc_match_chunk(C.byref(self.view), _ptr(buf), _ptr(offs), n, int(get_stranded), int(both_strands),
+                              int(match_r1_fwd), _ptr(mats), _ptr(inval), _ptr(meth), _ptr(cnt))
+        return mats, inval, cnt
 
     def seed_order(self, seq: bytes, cap: int = 1 << 20):
         keys = np.zeros(cap, np.uint32)
