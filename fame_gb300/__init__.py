@@ -7,8 +7,8 @@ and a host-side mirror of FAME's ReadQueue interface.
 """
 from ._lib import (CHUNKSIZE, FAME_BOTH_STRANDS, FAME_GET_STRANDED, FAME_MATCH_R1_FWD, FAME_MAX_READ_LEN,
                    Counters, FameError, GpuMatcher, HostIndex, lib)
-from .readqueue import ReadQueue, write_cpg_report
+from .readqueue import ReadQueue, SingleCellQueue, read_sc_meta, write_cpg_report
 from . import synth
 
 __all__ = ["CHUNKSIZE", "FAME_BOTH_STRANDS", "FAME_GET_STRANDED", "FAME_MATCH_R1_FWD", "FAME_MAX_READ_LEN",
-           "Counters", "FameError", "GpuMatcher", "HostIndex", "lib", "ReadQueue", "write_cpg_report"]
+           "Counters", "FameError", "GpuMatcher", "HostIndex", "lib", "ReadQueue", "SingleCellQueue", "read_sc_meta", "write_cpg_report"]

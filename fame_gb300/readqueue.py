@@ -121,3 +121,57 @@ def write_cpg_report(path: str, index: HostIndex, meth: np.ndarray):
         for i in range(len(pos)):
             m = meth[i]
             f.write("%s\t%d\t%d\t%d\t%d\t%d\n" % (names[t["cpg_chrom"][i]], pos[i], m[0], m[1], m[2], m[3]))
+
+
+class SingleCellQueue:
+    """Single-cell batches (matchSCBatch, ReadQueue.cpp:1660-1748, and
+    printSCMethylationLevels, 1894-1921; queryRoutineSC, main.cpp:443-468).
+
+    Per cell: the strand votes restart at zero, the cell's reads run through
+    the chunk loop (first chunk with getStranded unless both_strands), then the
+    cell's four count rows are written and the counters zeroed.  As in the
+    reference, the final bulk report after all cells is therefore all zeros,
+    and the fourth row is labelled "unmethFwd" (ReadQueue.cpp:1915)."""
+
+    def __init__(self, out_path: str, index: HostIndex, gpu: GpuMatcher, both_strands: bool = False,
+                 chunk_size: int = CHUNKSIZE):
+        self.index = index
+        self.gpu = gpu
+        self.both = both_strands
+        self.chunk_size = chunk_size
+        self.out = open(out_path, "w")
+        t = index.tables(sparse=False)
+        names = index.chrom_names()
+        self.out.write("\nSC_ID\tCount_Type\t")
+        self.out.write("".join("%s\t" % names[c] for c in t["cpg_chrom"]))
+        self.out.write("\nSC_ID\tCount_Type\t")
+        self.out.write("".join("%d\t" % (p + index.readlen - 2) for p in t["cpg_pos"].astype(np.int64)))
+
+    def match_sc_batch(self, reads, sc_id: str):
+        rq = ReadQueue(reads, self.index, self.gpu, both_strands=self.both, chunk_size=self.chunk_size)
+        tot = rq.query_routine()
+        self.print_sc_methylation_levels(sc_id)
+        return tot
+
+    def print_sc_methylation_levels(self, sc_id: str):
+        meth = self.gpu.tallies(reset=True)
+        for col, label in ((0, "methFwd"), (1, "unmethFwd"), (2, "methRev"), (3, "unmethFwd")):
+            self.out.write("\n%s\t%s\t" % (sc_id, label))
+            self.out.write("".join("%d\t" % v for v in meth[:, col]))
+
+    def close(self):
+        self.out.close()
+
+
+def read_sc_meta(path: str):
+    """queryRoutineSC's meta file: '<id> <fastq path>' per line, split on spaces (main.cpp:454-458)."""
+    out = []
+    with open(path) as f:
+        for line in f:
+            line = line.rstrip("\n")
+            p = line.find(" ")
+            sc_id = line[:p] if p >= 0 else line
+            rest = line[p + 1:] if p >= 0 else ""
+            q = rest.find(" ")
+            out.append((sc_id, rest[:q] if q >= 0 else rest))
+    return out

@@ -256,3 +256,46 @@ WORKLOADS = {
                                          length_sampler=_uneven_len, error_sampler=_per_read_err,
                                          sub_rate=0.01, indel_rate=0.001, repeat_read_frac=0.05)),
 }
+
+
+def make_pairs(genome: Genome, n_pairs, seed, read_len=100, inner=(20, 400), sub_rate=0.01, indel_rate=0.001):
+    """Paired-end bisulfite reads: a fragment of read_len + inner + read_len bases
+    (inner uniform in the closed range) from a random strand; mate 1 is the
+    fragment's first read_len bases, mate 2 the reverse complement of its last
+    read_len bases (the opposite strand).  Errors are drawn per mate."""
+    rng = np.random.default_rng(seed)
+
+    def frag_len(r, n):
+        return read_len + r.integers(inner[0], inner[1] + 1, size=n) + read_len
+
+    fr = make_reads(genome, n_pairs, seed=int(rng.integers(1 << 31)), read_len=read_len + inner[1] + read_len,
+                    length_sampler=frag_len, sub_rate=0.0, indel_rate=0.0)
+    m1 = np.zeros((n_pairs, read_len), np.uint8)
+    m2 = np.zeros((n_pairs, read_len), np.uint8)
+    for i in range(n_pairs):
+        f = fr.seqs[i, : fr.lens[i]]
+        m1[i] = f[:read_len]
+        m2[i] = _COMP[f[-read_len:][::-1]]
+    lens = np.full(n_pairs, read_len, np.int32)
+
+    def errs(mat):
+        out = mat.copy()
+        sub = rng.random(out.shape) < sub_rate
+        ns = int(sub.sum())
+        if ns:
+            out[sub] = BASES[(_IDX[out[sub]] + rng.integers(1, 4, size=ns)) % 4]
+        for i in np.nonzero(rng.random(n_pairs) < indel_rate * read_len)[0]:
+            p = int(rng.integers(0, read_len))
+            row = list(out[i])
+            if rng.random() < 0.5:
+                del row[p]
+                row.append(int(BASES[rng.integers(0, 4)]))
+            else:
+                row.insert(p, int(BASES[rng.integers(0, 4)]))
+                row = row[:read_len]
+            out[i] = np.array(row, np.uint8)
+        return out
+
+    r1 = ReadSet(errs(m1), lens.copy(), fr.chrom, fr.start, fr.fwd)
+    r2 = ReadSet(errs(m2), lens.copy(), fr.chrom, fr.start, ~fr.fwd)
+    return r1, r2

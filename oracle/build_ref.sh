@@ -15,6 +15,7 @@ SRC="$OUT/src"
 REF="${FAME_REFERENCE_DIR:-/root/reference}"
 CORES="${FAME_REF_CORENUM:-$(nproc)}"
 READLEN="${FAME_REF_READLEN:-100}"
+MAXPDIST="${FAME_REF_MAXPDIST:-550}"
 
 mkdir -p "$OUT"
 if [ -f "$REF/ReadQueue.cpp" ]; then
@@ -34,12 +35,13 @@ if [ ! -f "$SRC/ReadQueue.cpp" ]; then
   echo "build_ref: reference sources not available (neither $REF nor a staged copy)" >&2
   exit 3
 fi
-# per-machine thread count and read length (CONST.h:35, 38)
+# per-machine thread count, read length and pair distance (CONST.h:35, 38, 42)
 sed -i -E "s/^#define CORENUM .*/#define CORENUM ${CORES}/" "$SRC/CONST.h"
 sed -i -E "s/^constexpr unsigned int READLEN = .*;/constexpr unsigned int READLEN = ${READLEN};/" "$SRC/CONST.h"
+sed -i -E "s/^constexpr uint32_t MAXPDIST = .*;/constexpr uint32_t MAXPDIST = ${MAXPDIST};/" "$SRC/CONST.h"
 
 CXXFLAGS="-std=c++14 -O3 -fopenmp -fPIC -w -Dprivate=public -I$SRC -I$SRC/hopscotch-map/include/tsl"
 g++ $CXXFLAGS -shared -o "$OUT/libfame_ref.so" \
     "$HERE/ref_driver.cpp" "$SRC/RefGenome.cpp" "$SRC/RefReader_istr.cpp" "$SRC/Read.cpp" \
     "$SRC/CONST.cpp" "$SRC/DnaBitStr.cpp" "$SRC/gzstream/gzstream.C" -lz
-echo "build_ref: built $OUT/libfame_ref.so (CORENUM=$CORES READLEN=$READLEN)"
+echo "build_ref: built $OUT/libfame_ref.so (CORENUM=$CORES READLEN=$READLEN MAXPDIST=$MAXPDIST)"

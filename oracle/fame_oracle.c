@@ -1314,3 +1314,590 @@ int orc_match_chunk(const orc_index* ix, const uint8_t* seqs, const uint64_t* of
     counters[3] = st.r1f; counters[4] = st.r1r;
     return 0;
 }
+
+/* ====================================================================== */
+/* paired-end path (ReadQueue.cpp:935-1655, 2167-2323, 2468-3164, 3255-3275, */
+/* 4538-4776)                                                               */
+/* ====================================================================== */
+#define KMERDIST 10 /* CONST.h:104 */
+
+/* value of a paired map entry: tuple<uint8 count1, uint8 count2, bool f2, bool f3> */
+#define PC1(v) ((v) & 0xffu)
+#define PC2(v) (((v) >> 8) & 0xffu)
+#define PF2 (1u << 16)
+#define PF3 (1u << 17)
+
+typedef struct { uint64_t cap; uint32_t* k; uint32_t* v; uint8_t* used; } vmap;
+
+static void vm_init(vmap* s, uint64_t n)
+{
+    s->cap = 16;
+    while (s->cap < 2 * n + 16) s->cap <<= 1;
+    s->k = (uint32_t*)malloc(s->cap * sizeof(uint32_t));
+    s->v = (uint32_t*)calloc(s->cap, sizeof(uint32_t));
+    s->used = (uint8_t*)calloc(s->cap, 1);
+}
+static void vm_free(vmap* s) { free(s->k); free(s->v); free(s->used); }
+static uint32_t* vm_find(vmap* s, uint32_t key)
+{
+    uint64_t h = (key * 0x9E3779B97F4A7C15ULL) >> 20;
+    for (uint64_t i = h & (s->cap - 1);; i = (i + 1) & (s->cap - 1)) {
+        if (!s->used[i]) return NULL;
+        if (s->k[i] == key) return &s->v[i];
+    }
+}
+static uint32_t* vm_add(vmap* s, uint32_t key)
+{
+    uint64_t h = (key * 0x9E3779B97F4A7C15ULL) >> 20;
+    for (uint64_t i = h & (s->cap - 1);; i = (i + 1) & (s->cap - 1)) {
+        if (!s->used[i]) { s->used[i] = 1; s->k[i] = key; s->v[i] = 0; return &s->v[i]; }
+        if (s->k[i] == key) return &s->v[i];
+    }
+}
+
+/* one tsl::hopscotch_map<uint32_t, tuple<...>>: positions + values */
+typedef struct { hmap hm; vmap vm; } pmap;
+
+static void pm_init(pmap* p, uint64_t bucket_count, uint64_t expect) { hm_init(&p->hm, bucket_count); vm_init(&p->vm, expect); }
+static void pm_free(pmap* p) { hm_free(&p->hm); vm_free(&p->vm); }
+static uint32_t* pm_find(pmap* p, uint32_t key) { return vm_find(&p->vm, key); }
+static uint32_t* pm_at(pmap* p, uint32_t key) /* operator[] */
+{
+    uint32_t* v = vm_find(&p->vm, key);
+    if (v) return v;
+    v = vm_add(&p->vm, key);
+    hm_insert_at(&p->hm, key & p->hm.mask, key);
+    return vm_find(&p->vm, key);
+}
+static uint64_t pm_size(const pmap* p) { return p->hm.nb_elem; }
+
+/* libstdc++ std::sort (introsort: median-of-three unguarded partition, heap
+ * sort below the depth limit, final insertion sort with a 16-element
+ * threshold) for the paired candidate lists; comp(a, b) = count(a) > count(b)
+ * (CompiMetaFirst / CompiMetaSecond, ReadQueue.h:340-353). */
+typedef struct { uint32_t key; uint32_t v; } pent;
+static int pcomp(const pent* a, const pent* b, int second)
+{
+    return second ? PC2(a->v) > PC2(b->v) : PC1(a->v) > PC1(b->v);
+}
+static void pswap(pent* a, pent* b) { pent t = *a; *a = *b; *b = t; }
+static void ps_insertion(pent* f, pent* l, int sec)
+{
+    if (f == l) return;
+    for (pent* i = f + 1; i != l; ++i) {
+        pent val = *i;
+        if (pcomp(&val, f, sec)) {
+            memmove(f + 1, f, (size_t)(i - f) * sizeof(pent));
+            *f = val;
+        } else {
+            pent* last = i;
+            pent* next = i - 1;
+            while (pcomp(&val, next, sec)) { *last = *next; last = next; --next; }
+            *last = val;
+        }
+    }
+}
+static void ps_unguarded_insertion(pent* f, pent* l, int sec)
+{
+    for (pent* i = f; i != l; ++i) {
+        pent val = *i;
+        pent* last = i;
+        pent* next = i - 1;
+        while (pcomp(&val, next, sec)) { *last = *next; last = next; --next; }
+        *last = val;
+    }
+}
+static void ps_push_heap(pent* f, long hole, long top, pent val, int sec)
+{
+    long parent = (hole - 1) / 2;
+    while (hole > top && pcomp(f + parent, &val, sec)) {
+        f[hole] = f[parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    f[hole] = val;
+}
+static void ps_adjust_heap(pent* f, long hole, long len, pent val, int sec)
+{
+    const long top = hole;
+    long child = hole;
+    while (child < (len - 1) / 2) {
+        child = 2 * (child + 1);
+        if (pcomp(f + child, f + (child - 1), sec)) child--;
+        f[hole] = f[child];
+        hole = child;
+    }
+    if ((len & 1) == 0 && child == (len - 2) / 2) {
+        child = 2 * (child + 1);
+        f[hole] = f[child - 1];
+        hole = child - 1;
+    }
+    ps_push_heap(f, hole, top, val, sec);
+}
+static void ps_make_heap(pent* f, pent* l, int sec)
+{
+    const long len = l - f;
+    if (len < 2) return;
+    long parent = (len - 2) / 2;
+    while (1) {
+        pent val = f[parent];
+        ps_adjust_heap(f, parent, len, val, sec);
+        if (parent == 0) return;
+        parent--;
+    }
+}
+static void ps_pop_heap(pent* f, pent* l, pent* result, int sec)
+{
+    pent val = *result;
+    *result = *f;
+    ps_adjust_heap(f, 0, l - f, val, sec);
+}
+static void ps_partial_sort(pent* f, pent* m, pent* l, int sec)
+{
+    ps_make_heap(f, m, sec);
+    for (pent* i = m; i < l; ++i)
+        if (pcomp(i, f, sec)) ps_pop_heap(f, m, i, sec);
+    while (m - f > 1) { --m; ps_pop_heap(f, m, m, sec); }
+}
+static void ps_move_median_first(pent* r, pent* a, pent* b, pent* c, int sec)
+{
+    if (pcomp(a, b, sec)) {
+        if (pcomp(b, c, sec)) pswap(r, b);
+        else if (pcomp(a, c, sec)) pswap(r, c);
+        else pswap(r, a);
+    } else if (pcomp(a, c, sec)) pswap(r, a);
+    else if (pcomp(b, c, sec)) pswap(r, c);
+    else pswap(r, b);
+}
+static pent* ps_unguarded_partition(pent* f, pent* l, pent* pivot, int sec)
+{
+    while (1) {
+        while (pcomp(f, pivot, sec)) ++f;
+        --l;
+        while (pcomp(pivot, l, sec)) --l;
+        if (!(f < l)) return f;
+        pswap(f, l);
+        ++f;
+    }
+}
+static void ps_introsort(pent* f, pent* l, long depth, int sec)
+{
+    while (l - f > 16) {
+        if (depth == 0) { ps_partial_sort(f, l, l, sec); return; }
+        --depth;
+        pent* mid = f + (l - f) / 2;
+        ps_move_median_first(f, f + 1, mid, l - 1, sec);
+        pent* cut = ps_unguarded_partition(f + 1, l, f, sec);
+        ps_introsort(cut, l, depth, sec);
+        l = cut;
+    }
+}
+static void std_sort_desc(pent* f, long n, int sec)
+{
+    if (n <= 1) return;
+    long lg = 0;
+    while ((1l << (lg + 1)) <= n) ++lg;
+    ps_introsort(f, f + n, 2 * lg, sec);
+    if (n > 16) {
+        ps_insertion(f, f + 16, sec);
+        ps_unguarded_insertion(f + 16, f + n, sec);
+    } else {
+        ps_insertion(f, f + n, sec);
+    }
+}
+
+int orc_sort_desc(const uint32_t* keys, const uint8_t* counts, uint32_t n, uint32_t* out)
+{
+    pent* v = (pent*)malloc((n + 1) * sizeof(pent));
+    for (uint32_t i = 0; i < n; ++i) { v[i].key = keys[i]; v[i].v = counts[i]; }
+    std_sort_desc(v, n, 0);
+    for (uint32_t i = 0; i < n; ++i) out[i] = v[i].key;
+    free(v);
+    return 0;
+}
+
+static int filtered_has(const orc_pe_extra* px, uint64_t k)
+{
+    uint64_t lo = 0, hi = px->n_filtered;
+    while (lo < hi) { uint64_t mid = (lo + hi) >> 1; if (px->filtered[mid] < k) lo = mid + 1; else hi = mid; }
+    return lo < px->n_filtered && px->filtered[lo] == k;
+}
+
+static inline uint32_t kseq_code(uint8_t c) { return (c == 'C' || c == 'T') ? 3u : (c == 'G' ? 2u : 0u); }
+
+/* getSeedRefsFirstRead (ReadQueue.cpp:2468-2794) */
+static void pe_first_read(const orc_index* ix, const orc_pe_extra* px, const uint8_t* seq, uint32_t size, pmap* pm)
+{
+    const uint32_t nk = size - KMERLEN + 1;
+    uint32_t bucket_count = 0;
+    uint64_t total = 0;
+    uint64_t* keys = (uint64_t*)malloc(nk * sizeof(uint64_t));
+    for (uint32_t p = 0; p < nk; ++p) {
+        uint64_t st, ln;
+        keys[p] = spaced_hash(seq + p) & HTAB_MASK;
+        bucket_of(ix, keys[p], &st, &ln);
+        bucket_count += (uint32_t)ln;
+        total += ln;
+    }
+    bucket_count /= 5;
+    pmap tmp[2];
+    for (int s = 0; s < 2; ++s) pm_init(&tmp[s], bucket_count, total);
+    uint32_t cMask = 0, kSeq = 0;
+    for (uint32_t i = 0; i < KMERLEN; ++i) {
+        cMask = (cMask << 1) | (seq[i] == 'C');
+        kSeq = (kSeq << 2) + kseq_code(seq[i]);
+    }
+    const uint32_t maxQPos = size - KMERLEN + 1 - QTHRESH;
+    for (uint32_t p = 0; p < nk; ++p) {
+        if (p > 0) {
+            const uint32_t cIdx = p - 1;
+            kSeq = (kSeq << 2) + kseq_code(seq[KMERLEN + cIdx]);
+            cMask = (cMask << 1) | (seq[KMERLEN + cIdx] == 'C');
+            if (filtered_has(px, kSeq)) continue;
+        }
+        uint64_t st, ln;
+        bucket_of(ix, keys[p], &st, &ln);
+        uint64_t lastId = 0xffffffffffffffffULL;
+        int wasFwd = 0, wasStart = 0;
+        for (uint64_t i = st; i < st + ln; ++i) {
+            const uint32_t meta = ix->kmer_meta[i];
+            const uint32_t metaId = meta & 0x7fffffffu;
+            if (cMask & SEEDBITS & px->kmer_tmask[i]) continue;
+            const int isFwd = ix->strand[i] != 0;
+            const int isStart = (int)(meta >> 31);
+            if (metaId == lastId && isFwd == wasFwd && isStart == wasStart) continue;
+            lastId = metaId; wasFwd = isFwd; wasStart = isStart;
+            if (p == 0 || p - 1 < maxQPos) {
+                uint32_t* v = pm_at(&tmp[isFwd], metaId);
+                *v = (*v & ~0xffu) | ((PC1(*v) + 1) & 0xffu);
+            } else {
+                uint32_t* v = pm_find(&tmp[isFwd], metaId);
+                if (v) *v = (*v & ~0xffu) | ((PC1(*v) + 1) & 0xffu);
+            }
+        }
+    }
+    free(keys);
+    /* keep count1 >= qThreshold in new maps of 20 buckets, in the old order */
+    for (int s = 0; s < 2; ++s) {
+        pm_init(&pm[s], 20, 64);
+        uint32_t* order = (uint32_t*)malloc((tmp[s].hm.nb_elem + 1) * sizeof(uint32_t));
+        uint64_t n = map_order(&tmp[s].hm, order);
+        for (uint64_t q = 0; q < n; ++q) {
+            const uint32_t v = *pm_find(&tmp[s], order[q]);
+            if (PC1(v) >= QTHRESH) *pm_at(&pm[s], order[q]) = PC1(v);
+        }
+        free(order);
+        pm_free(&tmp[s]);
+    }
+}
+
+/* getSeedRefsSecondRead (ReadQueue.cpp:2801-3164); returns hasCpG */
+static int pe_second_read(const orc_index* ix, const orc_pe_extra* px, const uint8_t* seq, uint32_t size, pmap* pm)
+{
+    const int ctx = (int)((double)px->maxpdist / WINLEN) + 1;
+    const uint32_t nk = size - KMERLEN + 1;
+    uint32_t cMask = 0, kSeq = 0;
+    for (uint32_t i = 0; i < KMERLEN; ++i) {
+        cMask = (cMask << 1) | (seq[i] == 'C');
+        kSeq = (kSeq << 2) + kseq_code(seq[i]);
+    }
+    const uint32_t maxQPos = size - KMERLEN + 1 - QTHRESH;
+    for (uint32_t p = 0; p < nk; ++p) {
+        if (p > 0) {
+            const uint32_t cIdx = p - 1;
+            kSeq = (kSeq << 2) + kseq_code(seq[KMERLEN + cIdx]);
+            cMask = (cMask << 1) | (seq[KMERLEN + cIdx] == 'C');
+            if (filtered_has(px, kSeq)) continue;
+        }
+        uint64_t st, ln;
+        bucket_of(ix, spaced_hash(seq + p) & HTAB_MASK, &st, &ln);
+        uint64_t lastId = 0xffffffffffffffffULL;
+        int wasFwd = 0;
+        for (uint64_t i = st; i < st + ln; ++i) {
+            const uint32_t metaId = ix->kmer_meta[i] & 0x7fffffffu;
+            if (cMask & SEEDBITS & px->kmer_tmask[i]) continue;
+            const int isFwd = ix->strand[i] != 0;
+            if (metaId == lastId && isFwd == wasFwd) continue;
+            lastId = metaId; wasFwd = isFwd;
+            if (p == 0 || p - 1 < maxQPos) {
+                for (int c = -ctx; c <= ctx; ++c) {
+                    if (pm_find(&pm[isFwd], metaId + (uint32_t)c)) {
+                        uint32_t* v = pm_at(&pm[isFwd], metaId);
+                        *v = (*v & ~0xff00u) | (((PC2(*v) + 1) & 0xffu) << 8);
+                        break;
+                    }
+                }
+            } else {
+                uint32_t* v = pm_find(&pm[isFwd], metaId);
+                if (v) *v = (*v & ~0xff00u) | (((PC2(*v) + 1) & 0xffu) << 8);
+            }
+        }
+    }
+    for (int dir = 1; dir >= 0; --dir) {
+        uint32_t* order = (uint32_t*)malloc((pm[dir].hm.nb_elem + 1) * sizeof(uint32_t));
+        uint64_t n = map_order(&pm[dir].hm, order);
+        for (uint64_t q = 0; q < n; ++q) {
+            uint32_t* v = pm_find(&pm[dir], order[q]);
+            if (PC2(*v) >= QTHRESH) {
+                *v |= PF2;
+                for (int c = 1; c <= ctx; ++c) {
+                    uint32_t* w = pm_find(&pm[dir], order[q] + (uint32_t)c);
+                    if (w) *w |= PF2;
+                    w = pm_find(&pm[dir], order[q] - (uint32_t)c);
+                    if (w) *w |= PF2;
+                }
+            }
+        }
+        free(order);
+    }
+    for (int dir = 1; dir >= 0; --dir) {
+        uint32_t* order = (uint32_t*)malloc((pm[dir].hm.nb_elem + 1) * sizeof(uint32_t));
+        uint64_t n = map_order(&pm[dir].hm, order);
+        for (uint64_t q = 0; q < n; ++q) {
+            if ((*pm_find(&pm[dir], order[q]) & PF2) && ix->win_sind[order[q]] != CPGDUMMY) { free(order); return 1; }
+        }
+        free(order);
+    }
+    return 0;
+}
+
+typedef struct { uint64_t* m; uint32_t n, cap; } mvec;
+static void mv_push(mvec* v, uint64_t x)
+{
+    if (v->n == v->cap) { v->cap = v->cap ? 2 * v->cap : 8; v->m = (uint64_t*)realloc(v->m, v->cap * 8); }
+    v->m[v->n++] = x;
+}
+
+/* matchFwdFirst / matchRevFirst / matchFwdSecond / matchRevSecond (ReadQueue.cpp:4538-4776) */
+static int pe_match_one(const orc_index* ix, const orc_pe_extra* px, pent* meta, int dir, int second, uint8_t* prevChr,
+                        uint64_t* prevOff, mvec* mats, int32_t* bmCount, sa_t* sa, hits* h, pmap* pm)
+{
+    const int ctx = (int)((double)px->maxpdist / WINLEN) + 1;
+    const int32_t cnt = (int32_t)(second ? PC2(meta->v) : PC1(meta->v));
+    const int32_t thr = *bmCount - KMERDIST > (int32_t)QTHRESH ? *bmCount - KMERDIST : (int32_t)QTHRESH;
+    if (cnt < thr) return 0;
+    if (!(meta->v & (second ? PF3 : PF2))) return 1;
+    const uint32_t w = meta->key;
+    const uint32_t sp = ix->win_start[w];
+    const uint8_t ch = ix->win_chrom[w];
+    const uint8_t* g = ix->chrom_seq[ch];
+    const int64_t L = (int64_t)ix->chrom_len[ch];
+    if (dir) {
+        int64_t e = (int64_t)sp + WINLEN + MISCOUNT + ADDMIS - 1;
+        if (e > L) e = L;
+        sa_query_fwd(sa, g + sp, (uint64_t)(e - (int64_t)sp), h);
+    } else {
+        /* matchRevSecond leaves the start unguarded (startPos - 1 for window 0, ReadQueue.cpp:4736) */
+        int64_t lo = second ? (int64_t)sp - 1 : (sp > 0 ? (int64_t)sp - 1 : 0);
+        int64_t hi = (int64_t)sp + WINLEN + MISCOUNT + ADDMIS - 1;
+        if (hi >= L) hi = L - 1;
+        sa_query_rev(sa, g, hi, lo, h);
+    }
+    uint32_t i = 0;
+    if (h->n > 0 && h->off[0] + sp == *prevOff && ch == *prevChr) ++i;
+    for (; i < h->n; ++i) mv_push(mats, mk_match((uint16_t)h->off[i], h->err[i], (uint64_t)dir, 0, w));
+    if (h->n > 0) {
+        if (cnt > *bmCount) *bmCount = cnt;
+        if (!second) {
+            *pm_find(&pm[dir], w) |= PF3;
+            for (int c = 1; c <= ctx; ++c) {
+                uint32_t* x = pm_find(&pm[dir], w + (uint32_t)c);
+                if (x) *x |= PF3;
+                x = pm_find(&pm[dir], w - (uint32_t)c);
+                if (x) *x |= PF3;
+            }
+        }
+        *prevChr = ch;
+        *prevOff = sp + h->off[h->n - 1];
+    } else {
+        *prevChr = 0;
+        *prevOff = 0xffffffffffffffffULL;
+    }
+    return 1;
+}
+
+/* saQuerySeedSetRefFirst / Second (ReadQueue.cpp:2167-2323) */
+static void pe_query(const orc_index* ix, const orc_pe_extra* px, pmap* pm, int second, sa_t* sa, hits* h, mvec* mats)
+{
+    pent* lists[2];
+    uint64_t nl[2];
+    for (int dir = 0; dir < 2; ++dir) {
+        uint32_t* order = (uint32_t*)malloc((pm[dir].hm.nb_elem + 1) * sizeof(uint32_t));
+        nl[dir] = map_order(&pm[dir].hm, order);
+        lists[dir] = (pent*)malloc((nl[dir] + 1) * sizeof(pent));
+        for (uint64_t q = 0; q < nl[dir]; ++q) { lists[dir][q].key = order[q]; lists[dir][q].v = *pm_find(&pm[dir], order[q]); }
+        free(order);
+        std_sort_desc(lists[dir], (long)nl[dir], second);
+    }
+    int32_t bmCount = 0;
+    uint8_t prevChr = 0;
+    uint64_t prevOff = 0xffffffffffffffffULL;
+    int order2[2];
+    int nwalk = 0;
+    if (nl[1] > 0) {
+        if (nl[0] > 0) {
+            /* both walks compare count1 of the heads (ReadQueue.cpp:2185, 2265) */
+            if (PC1(lists[1][0].v) > PC1(lists[0][0].v)) { order2[0] = 1; order2[1] = 0; }
+            else { order2[0] = 0; order2[1] = 1; }
+            nwalk = 2;
+        } else { order2[0] = 1; nwalk = 1; }
+    } else if (nl[0] > 0) { order2[0] = 0; nwalk = 1; }
+    for (int wk = 0; wk < nwalk; ++wk) {
+        const int dir = order2[wk];
+        if (wk == 1) { prevChr = 0; prevOff = 0xffffffffffffffffULL; }
+        for (uint64_t q = 0; q < nl[dir]; ++q)
+            if (!pe_match_one(ix, px, &lists[dir][q], dir, second, &prevChr, &prevOff, mats, &bmCount, sa, h, pm)) break;
+    }
+    free(lists[0]);
+    free(lists[1]);
+}
+
+static int pe_extract(const orc_index* ix, const orc_pe_extra* px, uint64_t m1, uint64_t m2)
+{
+    if (ix->win_chrom[M_META(m1)] != ix->win_chrom[M_META(m2)]) return -1;
+    const uint32_t p1 = (uint32_t)(ix->win_start[M_META(m1)] + M_OFF(m1));
+    const uint32_t p2 = (uint32_t)(ix->win_start[M_META(m2)] + M_OFF(m2));
+    const uint32_t d = p2 > p1 ? p2 - p1 : p1 - p2;
+    if (d <= px->maxpdist + ix->readlen) return (int)(M_ERR(m1) + M_ERR(m2));
+    return -1;
+}
+
+typedef struct { uint64_t succ, nonu, unsucc, paired, tooShort, r1f, r1r; int matchR1Fwd; } pstats;
+
+static int rc_read(const uint8_t* s, uint32_t n, uint8_t* out)
+{
+    int bad = 0;
+    for (uint32_t p = 0, q = n - 1; p < n; ++p, --q) {
+        switch (s[p]) {
+            case 'A': out[q] = 'T'; break;
+            case 'C': out[q] = 'G'; break;
+            case 'G': out[q] = 'C'; break;
+            case 'T': out[q] = 'A'; break;
+            default: bad = 1; break; /* N and other letters invalidate a mate */
+        }
+    }
+    return bad;
+}
+
+static void pe_chunk(const orc_index* ix, const orc_pe_extra* px, const uint8_t* s1, const uint64_t* o1, const uint8_t* s2,
+                     const uint64_t* o2, uint32_t n, int getStranded, int both, pstats* st, uint64_t* mats1,
+                     uint64_t* mats2, uint8_t* inv1, uint8_t* inv2, uint16_t* meth)
+{
+    sa_t sa;
+    hits h = {0};
+    const float minlen = ceilf((float)ix->readlen * 0.75f);
+    for (uint32_t r = 0; r < n; ++r) {
+        const uint32_t n1 = (uint32_t)(o1[r + 1] - o1[r]), n2 = (uint32_t)(o2[r + 1] - o2[r]);
+        uint8_t* f1 = (uint8_t*)calloc(n1 + 1, 1);
+        uint8_t* f2 = (uint8_t*)calloc(n2 + 1, 1);
+        uint8_t* r1 = (uint8_t*)calloc(n1 + 1, 1);
+        uint8_t* r2 = (uint8_t*)calloc(n2 + 1, 1);
+        memcpy(f1, s1 + o1[r], n1);
+        memcpy(f2, s2 + o2[r], n2);
+        int bad1 = (float)n1 < minlen, bad2 = (float)n2 < minlen;
+        mats1[r] = mats2[r] = 0;
+        if (bad1 || bad2) st->tooShort++;
+        if (n1 && rc_read(f1, n1, r1)) bad1 = 1;
+        if (n2 && rc_read(f2, n2, r2)) bad2 = 1;
+        inv1[r] = (uint8_t)bad1;
+        inv2[r] = (uint8_t)bad2;
+        if (bad1 || bad2) { st->tooShort += 2; goto next; }
+        {
+            mvec m1F = {0}, m2R = {0}, m1R = {0}, m2F = {0};
+            for (int o = 0; o < 2; ++o) {
+                const int run = o == 0 ? (both || getStranded || st->matchR1Fwd) : (both || getStranded || !st->matchR1Fwd);
+                if (!run) continue;
+                uint8_t* first = o == 0 ? f1 : r1;
+                uint8_t* sec = o == 0 ? r2 : f2;
+                mvec* ma = o == 0 ? &m1F : &m1R;
+                mvec* mb = o == 0 ? &m2R : &m2F;
+                pmap pm[2];
+                pe_first_read(ix, px, first, n1, pm);
+                if (pm_size(&pm[1]) || pm_size(&pm[0])) {
+                    if (pe_second_read(ix, px, sec, n2, pm)) {
+                        sa_load(&sa, first, n1);
+                        pe_query(ix, px, pm, 0, &sa, &h, ma);
+                        if (ma->n) {
+                            sa_load(&sa, sec, n2);
+                            pe_query(ix, px, pm, 1, &sa, &h, mb);
+                        }
+                    }
+                }
+                pm_free(&pm[0]);
+                pm_free(&pm[1]);
+            }
+            if ((m1F.n == 0 && m1R.n == 0) || (m2F.n == 0 && m2R.n == 0)) {
+                inv1[r] = inv2[r] = 1;
+                st->unsucc += 2;
+            } else {
+                const int WORST = 2 * (MISCOUNT + ADDMIS) + 1;
+                int best = WORST, nonUnique = 0, orig = 1;
+                uint64_t b1 = 0, b2 = 0;
+                if (both || getStranded || st->matchR1Fwd)
+                    for (uint32_t a = 0; a < m1F.n; ++a)
+                        for (uint32_t b = 0; b < m2R.n; ++b) {
+                            const int e = pe_extract(ix, px, m1F.m[a], m2R.m[b]);
+                            if (e < 0) continue;
+                            if (e == best) nonUnique = 1;
+                            else if (e < best) { best = e; b1 = m1F.m[a]; b2 = m2R.m[b]; nonUnique = 0; }
+                        }
+                if (both || getStranded || !st->matchR1Fwd)
+                    for (uint32_t a = 0; a < m1R.n; ++a)
+                        for (uint32_t b = 0; b < m2F.n; ++b) {
+                            const int e = pe_extract(ix, px, m1R.m[a], m2F.m[b]);
+                            if (e < 0) continue;
+                            if (e == best) nonUnique = 1;
+                            else if (e < best) { best = e; b1 = m1R.m[a]; b2 = m2F.m[b]; orig = 0; nonUnique = 0; }
+                        }
+                if (best == WORST) { inv1[r] = inv2[r] = 1; st->unsucc += 2; }
+                else if (nonUnique) { st->nonu += 2; inv1[r] = inv2[r] = 1; }
+                else {
+                    mats1[r] = b1;
+                    mats2[r] = b2;
+                    if (orig) {
+                        if (getStranded) st->r1f++;
+                        compute_meth(ix, b1, f1, n1, meth);
+                        compute_meth(ix, b2, r2, n2, meth);
+                    } else {
+                        if (getStranded) st->r1r++;
+                        compute_meth(ix, b1, r1, n1, meth);
+                        compute_meth(ix, b2, f2, n2, meth);
+                    }
+                    const int d1 = ix->win_sind[M_META(b1)] == CPGDUMMY, d2 = ix->win_sind[M_META(b2)] == CPGDUMMY;
+                    if (d1 && d2) st->tooShort += 2;
+                    else if (d1 || d2) { st->tooShort++; st->succ++; }
+                    else { st->paired++; st->succ += 2; }
+                }
+            }
+            free(m1F.m); free(m2R.m); free(m1R.m); free(m2F.m);
+        }
+    next:
+        if (inv1[r]) mats1[r] = 0;
+        if (inv2[r]) mats2[r] = 0;
+        free(f1); free(f2); free(r1); free(r2);
+    }
+    free(h.off);
+    free(h.err);
+}
+
+/* queryRoutinePaired loop (main.cpp:400-441) */
+int orc_match_pe(const orc_index* ix, const orc_pe_extra* px, const uint8_t* s1, const uint64_t* o1, const uint8_t* s2,
+                 const uint64_t* o2, uint32_t n, uint32_t chunk, int both_strands, uint64_t* mats1, uint64_t* mats2,
+                 uint8_t* inv1, uint8_t* inv2, uint16_t* meth, uint64_t* counters)
+{
+    pstats st;
+    memset(&st, 0, sizeof(st));
+    st.matchR1Fwd = 1;
+    if (chunk == 0) chunk = 300000;
+    memset(meth, 0, sizeof(uint16_t) * 4 * ix->n_cpg);
+    for (uint32_t c0 = 0, ci = 0; c0 < n; c0 += chunk, ++ci) {
+        const uint32_t cn = n - c0 < chunk ? n - c0 : chunk;
+        const int stranded = ci == 0 && !both_strands;
+        pe_chunk(ix, px, s1, o1 + c0, s2, o2 + c0, cn, stranded, both_strands, &st, mats1 + c0, mats2 + c0, inv1 + c0,
+                 inv2 + c0, meth);
+        if (stranded) st.matchR1Fwd = st.r1f > st.r1r;
+    }
+    counters[0] = st.succ; counters[1] = st.nonu; counters[2] = st.unsucc; counters[3] = st.paired;
+    counters[4] = st.tooShort; counters[5] = st.r1f; counters[6] = st.r1r; counters[7] = (uint64_t)st.matchR1Fwd;
+    return 0;
+}

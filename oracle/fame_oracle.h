@@ -38,6 +38,15 @@ typedef struct {
     const uint32_t* win_eind;
 } orc_index;
 
+/* Paired-end extras: T masks (kmerTableSmall.tmask), filteredKmers (sorted) and
+ * MyConst::MAXPDIST (CONST.h:42). */
+typedef struct {
+    const uint32_t* kmer_tmask;
+    uint64_t n_filtered;
+    const uint64_t* filtered;
+    uint32_t maxpdist;
+} orc_pe_extra;
+
 /* ---- index build (RefReader_istr.h:48-113, RefGenome.cpp:26-74) ---------- */
 typedef struct orc_built orc_built;
 orc_built* orc_build(uint32_t readlen, uint32_t n_chrom, const uint8_t* const* raw_seq, const uint64_t* raw_len,
@@ -78,6 +87,16 @@ int orc_shiftand(const uint8_t* pat, uint32_t pat_len, const uint8_t* text, uint
 int orc_match_chunk(const orc_index* ix, const uint8_t* seqs, const uint64_t* offs, uint32_t n, int get_stranded,
                     int both_strands, int match_r1_fwd, uint64_t* mats, uint8_t* invalid, uint16_t* meth,
                     uint64_t* counters);
+
+/* Paired-end matching (matchPairedReads, ReadQueue.cpp:935-1655) with the loop
+ * of queryRoutinePaired (main.cpp:400-441).  counters: [succ, nonunique,
+ * unsucc, succPaired, tooShort, r1Fwd, r1Rev, matchR1Fwd] */
+int orc_match_pe(const orc_index* ix, const orc_pe_extra* px, const uint8_t* s1, const uint64_t* o1, const uint8_t* s2,
+                 const uint64_t* o2, uint32_t n, uint32_t chunk, int both_strands, uint64_t* mats1, uint64_t* mats2,
+                 uint8_t* inv1, uint8_t* inv2, uint16_t* meth, uint64_t* counters);
+
+/* libstdc++ std::sort of (key, count) by count descending; keys out in order. */
+int orc_sort_desc(const uint32_t* keys, const uint8_t* counts, uint32_t n, uint32_t* out);
 
 /* Hopscotch insertion model on an explicit key sequence; returns iteration order. */
 int orc_hopscotch(const uint32_t* keys, uint32_t n, uint32_t bucket_count, uint32_t* order, uint64_t* final_buckets);

@@ -51,8 +51,22 @@ def lib():
         L.orc_lev.argtypes = [C.c_int, _P, C.c_uint32, _P, C.c_int64, C.c_int64, C.c_int, C.c_int, _P, C.c_uint32, _P]
         L.orc_shiftand.argtypes = [_P, C.c_uint32, _P, C.c_uint32, C.c_int, _P, _P, C.c_uint32]
         L.orc_match_chunk.argtypes = [_P, _P, _P, C.c_uint32, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P]
+        L.orc_match_pe.argtypes = [_P, _P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_int, _P, _P, _P, _P, _P, _P]
+        L.orc_sort_desc.argtypes = [_P, _P, C.c_uint32, _P]
         _lib = L
     return _lib
+
+
+class _PeExtra(C.Structure):
+    _fields_ = [("kmer_tmask", _P), ("n_filtered", C.c_uint64), ("filtered", _P), ("maxpdist", C.c_uint32)]
+
+
+def sort_desc(keys, counts):
+    keys = np.ascontiguousarray(keys, np.uint32)
+    counts = np.ascontiguousarray(counts, np.uint8)
+    out = np.zeros(len(keys), np.uint32)
+    lib().orc_sort_desc(_ptr(keys), _ptr(counts), len(keys), _ptr(out))
+    return out
 
 
 class OracleIndex:
@@ -128,6 +142,24 @@ class OracleIndex:
         lib().orc_match_chunk(C.byref(self.view), _ptr(buf), _ptr(offs), n, int(get_stranded), int(both_strands),
                               int(match_r1_fwd), _ptr(mats), _ptr(inval), _ptr(meth), _ptr(cnt))
         return mats, inval, cnt
+
+    def match_pe(self, s1: bytes, o1, s2: bytes, o2, chunk: int = 0, both_strands: bool = False,
+                 maxpdist: int = 550) -> dict:
+        n = len(o1) - 1
+        px = _PeExtra(_ptr(self.t["kmer_tmask"]), len(self.t["filtered"]), _ptr(self.t["filtered"]), maxpdist)
+        m1 = np.zeros(n, np.uint64)
+        m2 = np.zeros(n, np.uint64)
+        i1 = np.zeros(n, np.uint8)
+        i2 = np.zeros(n, np.uint8)
+        meth = np.zeros(4 * self.n_cpg, np.uint16)
+        cnt = np.zeros(8, np.uint64)
+        b1 = np.frombuffer(s1, np.uint8)
+        b2 = np.frombuffer(s2, np.uint8)
+        o1 = np.ascontiguousarray(o1, np.uint64)
+        o2 = np.ascontiguousarray(o2, np.uint64)
+        lib().orc_match_pe(C.byref(self.view), C.byref(px), _ptr(b1), _ptr(o1), _ptr(b2), _ptr(o2), n, chunk,
+                           int(both_strands), _ptr(m1), _ptr(m2), _ptr(i1), _ptr(i2), _ptr(meth), _ptr(cnt))
+        return dict(mat1=m1, mat2=m2, inv1=i1, inv2=i2, meth=meth.reshape(-1, 4), counters=cnt)
 
     def seed_order(self, seq: bytes, cap: int = 1 << 20):
         keys = np.zeros(cap, np.uint32)

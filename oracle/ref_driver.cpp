@@ -390,3 +390,67 @@ int fame_ref_time_se(void* ref, const char* seqs, const uint64_t* offs, uint32_t
     return 0;
 }
 }
+
+extern "C" {
+int fame_ref_maxpdist() { return (int)MyConst::MAXPDIST; }
+
+// Paired-end run with the loop structure of queryRoutinePaired (main.cpp:400-441):
+// chunk 0 with getStranded unless both_strands, decideStrand, later chunks in the
+// decided orientation.  counters: [succ, nonunique, unsucc, succPaired, tooShort,
+// r1Fwd, r1Rev, matchR1Fwd]
+int fame_ref_match_pe(void* ref, const char* s1, const uint64_t* o1, const char* s2, const uint64_t* o2, uint32_t n,
+                      uint32_t chunk, int both_strands, uint64_t* mats1, uint64_t* mats2, uint8_t* inv1,
+                      uint8_t* inv2, uint16_t* meth, uint64_t* counters, double* seconds)
+{
+    RefGenome& r = *static_cast<RefGenome*>(ref);
+    ReadQueue* rq = in_tmp([&] { return new ReadQueue("/dev/null", "/dev/null", r, false, both_strands != 0); });
+    if (chunk == 0 || chunk > MyConst::CHUNKSIZE) chunk = MyConst::CHUNKSIZE;
+    uint64_t succ = 0, nonu = 0, unsucc = 0, paired = 0, tooShort = 0;
+    double secs = 0.0;
+    std::string id("r");
+    for (uint32_t c0 = 0, ci = 0; c0 < n; c0 += chunk, ++ci) {
+        const uint32_t cn = std::min<uint32_t>(chunk, n - c0);
+        for (uint32_t j = 0; j < cn; ++j) {
+            std::string a(s1 + o1[c0 + j], s1 + o1[c0 + j + 1]);
+            std::string b(s2 + o2[c0 + j], s2 + o2[c0 + j + 1]);
+            rq->readBuffer[j] = Read(a, id);
+            rq->readBuffer2[j] = Read(b, id);
+        }
+        const bool stranded = (ci == 0) && !both_strands;
+        auto t0 = std::chrono::steady_clock::now();
+        rq->matchPairedReads(cn, succ, nonu, unsucc, paired, tooShort, stranded);
+        auto t1 = std::chrono::steady_clock::now();
+        secs += std::chrono::duration<double>(t1 - t0).count();
+        if (stranded) rq->decideStrand();
+        for (uint32_t j = 0; j < cn; ++j) {
+            inv1[c0 + j] = rq->readBuffer[j].isInvalid ? 1 : 0;
+            inv2[c0 + j] = rq->readBuffer2[j].isInvalid ? 1 : 0;
+            mats1[c0 + j] = rq->readBuffer[j].isInvalid ? 0 : rq->readBuffer[j].mat;
+            mats2[c0 + j] = rq->readBuffer2[j].isInvalid ? 0 : rq->readBuffer2[j].mat;
+        }
+    }
+    for (size_t i = 0; i < r.cpgTable.size(); ++i) {
+        meth[4 * i + 0] = rq->methLevels[i].methFwd;
+        meth[4 * i + 1] = rq->methLevels[i].unmethFwd;
+        meth[4 * i + 2] = rq->methLevels[i].methRev;
+        meth[4 * i + 3] = rq->methLevels[i].unmethRev;
+    }
+    counters[0] = succ; counters[1] = nonu; counters[2] = unsucc; counters[3] = paired; counters[4] = tooShort;
+    counters[5] = rq->r1FwdMatches; counters[6] = rq->r1RevMatches; counters[7] = rq->matchR1Fwd ? 1 : 0;
+    if (seconds) *seconds = secs;
+    delete rq;
+    return 0;
+}
+
+// std::sort with the paired path's comparator (cmpMetaFirst, ReadQueue.h:340-346):
+// input in the given order, output the keys in sorted order (pins the tie order).
+int fame_ref_sort_desc(const uint32_t* keys, const uint8_t* counts, uint32_t n, uint32_t* out)
+{
+    std::vector<std::pair<uint32_t, std::tuple<uint8_t, uint8_t, bool, bool>>> v;
+    for (uint32_t i = 0; i < n; ++i) v.push_back({keys[i], std::make_tuple(counts[i], (uint8_t)0, false, false)});
+    ReadQueue::CompiMetaFirst c;
+    std::sort(v.begin(), v.end(), c);
+    for (uint32_t i = 0; i < n; ++i) out[i] = v[i].first;
+    return 0;
+}
+}

@@ -145,6 +145,28 @@ class RefIndex:
         f(self.h, _ptr(buf), _ptr(offs), n, int(both_strands), int(match_r1_fwd), _ptr(cnt), _ptr(secs))
         return float(secs[0]), cnt
 
+    def match_pe(self, s1: bytes, o1, s2: bytes, o2, chunk: int = 0, both_strands: bool = False):
+        import ctypes as C
+        f = self.L.lib.fame_ref_match_pe
+        f.argtypes = [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_int, _P, _P, _P, _P, _P, _P, _P]
+        sz = np.zeros(7, dtype=np.uint64)
+        self.L.lib.fame_ref_sizes(self.h, _ptr(sz))
+        n = len(o1) - 1
+        m1 = np.zeros(n, np.uint64)
+        m2 = np.zeros(n, np.uint64)
+        i1 = np.zeros(n, np.uint8)
+        i2 = np.zeros(n, np.uint8)
+        meth = np.zeros(4 * int(sz[0]), np.uint16)
+        cnt = np.zeros(8, np.uint64)
+        secs = np.zeros(1, np.float64)
+        b1 = np.frombuffer(s1, np.uint8)
+        b2 = np.frombuffer(s2, np.uint8)
+        o1 = np.ascontiguousarray(o1, np.uint64)
+        o2 = np.ascontiguousarray(o2, np.uint64)
+        f(self.h, _ptr(b1), _ptr(o1), _ptr(b2), _ptr(o2), n, chunk, int(both_strands), _ptr(m1), _ptr(m2), _ptr(i1),
+          _ptr(i2), _ptr(meth), _ptr(cnt), _ptr(secs))
+        return dict(mat1=m1, mat2=m2, inv1=i1, inv2=i2, meth=meth.reshape(-1, 4), counters=cnt, seconds=float(secs[0]))
+
     def seed_order(self, seq: bytes, cap: int = 1 << 20):
         keys = np.zeros(cap, np.uint32)
         cnts = np.zeros(cap, np.uint32)

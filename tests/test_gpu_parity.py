@@ -210,3 +210,33 @@ def test_device_resident_entry_point(gpu, golden):
     ref = run_mode(gpu, seq.tobytes(), offs, 0, True)
     assert np.array_equal(mats, ref["mat"]) and np.array_equal(inv, ref["invalid"])
     assert np.array_equal(meth, ref["meth"]) and cnt.succ == ref["counters"][0]
+
+
+def test_single_cell_batches(golden, product_index, gpu, oracle_index, tmp_path):
+    """Two cells through SingleCellQueue: each cell's printed rows equal an
+    independent run of the reference path on that cell's reads (votes restart
+    per cell), and the bulk counters are left at zero."""
+    from fame_gb300 import SingleCellQueue
+    seq = golden["read_seq"].tobytes()
+    offs = golden["read_offs"]
+    reads = [seq[int(offs[i]):int(offs[i + 1])] for i in range(len(offs) - 1)]
+    cells = [("cellA", reads[:2500]), ("cellB", reads[2500:])]
+    gpu.tallies(reset=True)
+    out = tmp_path / "sc.tsv"
+    sc = SingleCellQueue(str(out), product_index, gpu, both_strands=False, chunk_size=1000)
+    for cid, rr in cells:
+        sc.match_sc_batch(rr, cid)
+    sc.close()
+    assert not gpu.tallies(reset=False).any()
+    lines = out.read_text().split("\n")
+    assert lines[0] == "" and lines[1].startswith("SC_ID\tCount_Type\t") and lines[2].startswith("SC_ID\tCount_Type\t")
+    rows = {}
+    for ln in lines[3:]:
+        parts = ln.split("\t")
+        rows[(parts[0], len([k for k in rows if k[0] == parts[0]]))] = np.array(parts[2:-1], dtype=np.int64)
+    for cid, rr in cells:
+        o = np.zeros(len(rr) + 1, np.uint64)
+        np.cumsum([len(r) for r in rr], out=o[1:])
+        ref = oracle_index.match_se(b"".join(rr), o, chunk=1000, both_strands=False)["meth"]
+        for col in range(4):
+            assert np.array_equal(rows[(cid, col)], ref[:, col].astype(np.int64)), (cid, col)
