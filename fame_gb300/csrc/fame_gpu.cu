@@ -44,6 +44,7 @@ struct fame_gpu {
     float stage_ms[6]{};
     int launches = 0;
     int sm_count = 0;
+    uint32_t dp_grid = 0;   // resident blocks of k_dp_warp on the whole device
 };
 
 namespace {
@@ -294,6 +295,12 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
     if (cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * LightLayout::BYTES) != cudaSuccess ||
         cudaFuncSetAttribute(k_dp_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * DPW_BYTES) != cudaSuccess)
         return fail(set_err(g, FAME_ERR_CUDA, "shared memory attribute"));
+    {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dp_warp, 128, 4 * DPW_BYTES) != cudaSuccess || nb < 1)
+            return fail(set_err(g, FAME_ERR_CUDA, "k_dp_warp does not fit an SM"));
+        g->dp_grid = (uint32_t)(g->sm_count * nb);
+    }
     *out = g;
     return FAME_OK;
 }
@@ -383,7 +390,7 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         if (T) cudaEventRecord(g->ev[3], g->stream);
         k_select<<<(n + 255) / 256, 256, 0, g->stream>>>(g->ix, cb);
         if (T) cudaEventRecord(g->ev[4], g->stream);
-        k_dp_warp<<<(uint32_t)g->sm_count * 8, 128, 4 * DPW_BYTES, g->stream>>>(g->ix, cb);
+        k_dp_warp<<<g->dp_grid, 128, 4 * DPW_BYTES, g->stream>>>(g->ix, cb);
         if (T) cudaEventRecord(g->ev[5], g->stream);
         g->launches += 2;
         CK(cudaGetLastError());

@@ -1,6 +1,7 @@
 // Matching kernels after seeding: Shift-And window scans, candidate
 // selection with the exact-match CpG calls, and the banded DP CpG calls.
 #pragma once
+#include "qgram.h"
 #include "seed.cuh"
 
 namespace fame {
@@ -191,7 +192,7 @@ struct ScanText {
 // (repetitive windows) fall back to the full scan.
 template <int W, class Emit>
 __device__ void scan_window(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t wid, int fwd, Emit emit,
-                            const uint32_t* pkey, uint32_t pvalid, uint64_t bloom, uint32_t q, const uint32_t* pstart)
+                            const uint32_t* pkey, uint32_t pvalid, uint32_t q, const uint32_t* pstart)
 {
     constexpr int CAP = 32;
     const uint4 wi = ix.win[wid];
@@ -220,46 +221,9 @@ __device__ void scan_window(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t w
     const uint32_t m = sa.plen;
     // ---- q-gram pass
     int32_t ilo[CAP], ihi[CAP];
-    int nint = 0;
-    bool overflow = false;
-    {
-        const uint32_t qmask = q >= 16 ? 0xffffffffu : ((1u << (2 * q)) - 1);
-        uint32_t key = 0, valid = 0;
-        uint64_t g = tx.g0;
-        uint32_t wpack = __ldg(ix.gpack + (g >> 4)), wn = __ldg(ix.gnmask + (g >> 5));
-        for (uint32_t u = 0; u < tx.len; ++u, g += tx.dir) {
-            if (fwd) {
-                if ((g & 15) == 0) wpack = __ldg(ix.gpack + (g >> 4));
-                if ((g & 31) == 0) wn = __ldg(ix.gnmask + (g >> 5));
-            } else {
-                if ((g & 15) == 15) wpack = __ldg(ix.gpack + (g >> 4));
-                if ((g & 31) == 31) wn = __ldg(ix.gnmask + (g >> 5));
-            }
-            if ((wn >> (g & 31)) & 1u) { valid = 0; continue; }
-            int b = (int)((wpack >> (2 * (g & 15))) & 3u);
-            if (!fwd) b = 3 - b;
-            const uint32_t sym = b == 0 ? 0u : (b == 2 ? 1u : 2u);  // A, G, C/T
-            key = ((key << 2) | sym) & qmask;
-            if (++valid < q) continue;
-            if (!((bloom >> ((key * 0x9E3779B1u) >> 26)) & 1ull)) continue;
-#pragma unroll
-            for (int k = 0; k < 7; ++k) {
-                if (((pvalid >> k) & 1u) && key == pkey[k]) {
-                    const int32_t x = (int32_t)(u - q + 1);
-                    const int32_t end0 = x - 1 + (int32_t)(m - pstart[k]);
-                    int32_t a = end0 - (int32_t)NERR, bnd = end0 + (int32_t)NERR;
-                    if (bnd < 0 || a > (int32_t)tx.len - 1) continue;
-                    if (a < 0) a = 0;
-                    if (bnd > (int32_t)tx.len - 1) bnd = (int32_t)tx.len - 1;
-                    if (nint >= CAP) { overflow = true; continue; }
-                    ilo[nint] = a;
-                    ihi[nint] = bnd;
-                    ++nint;
-                }
-            }
-        }
-    }
-    if (overflow) { scan_window_full<W>(ix, sa, wid, fwd, emit); return; }
+    const uint64_t G0 = fwd ? tx.g0 : tx.g0 + 1 - tx.len, G1 = G0 + tx.len;
+    const int nint = qgram_spans<CAP>(ix.gpack, ix.gnmask, G0, G1, fwd, m, q, pkey, pvalid, pstart, ilo, ihi);
+    if (nint < 0) { scan_window_full<W>(ix, sa, wid, fwd, emit); return; }
     if (nint == 0) return;
     // sort spans by start and merge overlapping ones
     for (int i = 1; i < nint; ++i) {
@@ -319,13 +283,11 @@ struct PieceKeys {
     uint32_t key[7];
     uint32_t start[7];
     uint32_t valid;
-    uint64_t bloom;
     uint32_t q;
     __device__ __forceinline__ void load(const char* raw, uint32_t len, int orient)
     {
         q = min(16u, len / 7);
         valid = 0;
-        bloom = 0;
         for (int k = 0; k < 7; ++k) {
             start[k] = (uint32_t)((k * len) / 7);
             uint32_t kk = 0;
@@ -343,10 +305,7 @@ struct PieceKeys {
                 kk = (kk << 2) | sym;
             }
             key[k] = kk;
-            if (ok) {
-                valid |= 1u << k;
-                bloom |= 1ull << ((kk * 0x9E3779B1u) >> 26);
-            }
+            if (ok) valid |= 1u << k;
         }
     }
 };
@@ -368,7 +327,7 @@ __device__ void shiftand_one(const DevIndex& ix, const ChunkBufs& cb, uint32_t c
     scan_window<W>(ix, sa, e & 0x7fffffffu, (int)(e >> 31), [&](uint32_t off, int err) {
         if (n < HIT_CAP) out[n] = (off << 8) | (uint32_t)err;
         ++n;
-    }, pk.key, pk.valid, pk.bloom, pk.q, pk.start);
+    }, pk.key, pk.valid, pk.q, pk.start);
     cb.hit_n[c] = n;
 }
 
@@ -923,126 +882,161 @@ __global__ void k_max_bucket(const uint32_t* tab, uint64_t n, unsigned int* out)
 namespace fame {
 
 // ---------------------------------------------------------------------------
-// Banded DP, one warp per read, the matrix in shared memory.  Same storage
-// (flat BandedMatrix index, dp_idx), same initial values and the same cell
-// recurrence as meth_dp; the cells are computed along anti-diagonals
-// t = 2 * row + offset (the three inputs of a cell lie on t - 1 and t - 2), one
-// band offset per lane, so every input is final when it is read.  The
-// backtrack and the CpG walk are serial on lane 0.
+// Banded DP for the CpG calls of erroneous hits, three reads per warp.
+//
+// LevenshtDP<uint16_t, 8> (LevenshtDP.h:205-544) fills a 17-cell band per row
+// from three neighbours and then backtracks from the smallest cell of the last
+// row.  Every cell inside the band is written once and its three inputs are
+// final when it is computed, and a computed cell never exceeds n + 8 while the
+// band's border cells hold at least 65518, so the backtrack never leaves the
+// band: its choice at a cell is a function of that cell's own inputs.  The fill
+// therefore records the choice per cell (two bits, as two warp ballots per
+// anti-diagonal) instead of the matrix, and keeps the values in registers:
+// cells are computed along anti-diagonals
+// t = 2 * row + offset, lane k of a 9-lane group holding offset 2k - 8 (even t)
+// or 2k - 7 (odd t), so the up and left inputs are neighbour lanes' values of
+// step t - 1 (shuffles) and the diagonal input is the lane's own value of step
+// t - 2.  Border values follow the reference's initialisation, including its
+// storage overlap: cell (9, 0) reads 65518, the value the right border writes
+// over it.  Column-0 cells of rows 1..8 always backtrack as insertions.
 // ---------------------------------------------------------------------------
-constexpr uint32_t DPW_MAXN = FAME_MAX_READ_LEN;
-constexpr uint32_t DPW_CELLS = (DPW_MAXN + 1) * (uint32_t)DPW;       // u16
-constexpr uint32_t DPW_REF = DPW_MAXN + 2 * DP_BAND + 8;             // reference bases, j in [-2, n + 10]
-constexpr uint32_t DPW_ALIGN = 2 * DPW_MAXN + 4 * DP_BAND + 8;
-constexpr uint32_t DPW_BYTES = ((DPW_CELLS * 2 + 256 + DPW_REF + DPW_ALIGN) + 15) / 16 * 16;
-constexpr int DPW_REF0 = 2;  // refc[j + DPW_REF0] = colPat[1 - j]
-
-__device__ __forceinline__ uint16_t sget(const uint16_t* c, long msize, long i, long j)
-{
-    const long k = dp_idx(i, j);
-    return (k >= 0 && k < msize) ? c[k] : (uint16_t)0xffff;
-}
-__device__ __forceinline__ void sset(uint16_t* c, long msize, long i, long j, uint16_t v)
-{
-    const long k = dp_idx(i, j);
-    if (k >= 0 && k < msize) c[k] = v;
-}
+constexpr uint32_t DP3_GROUPS = 3;                                     // reads per warp
+constexpr uint32_t DP3_MAXN = FAME_MAX_READ_LEN;
+constexpr uint32_t DP3_STEPS = 2 * DP3_MAXN + DP_BAND + 2;            // anti-diagonals, rounded up to even
+constexpr uint32_t DP3_REF = 288;                                      // reference bases, j in [-2, n + 10]
+constexpr uint32_t DP3_ALIGN = 2 * DP3_MAXN + 4 * DP_BAND + 10;       // alignment trace
+constexpr uint32_t DP3_GROUP_BYTES = 48 + 256 + DP3_REF + DP3_ALIGN + 8; // row-n values, read, reference, trace
+constexpr uint32_t DPW_BYTES = DP3_STEPS * 8 + DP3_GROUPS * DP3_GROUP_BYTES;   // per warp
+constexpr int DPW_REF0 = 2;
+static_assert(DP3_GROUP_BYTES % 16 == 0 && (DP3_STEPS * 8) % 16 == 0, "16-byte aligned shared-memory regions");
+static_assert(DP3_MAXN + DP_BAND + 2 + DPW_REF0 < DP3_REF, "reference bases fit");
 
 __global__ void k_dp_warp(DevIndex ix, ChunkBufs cb)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const int lane = threadIdx.x & 31;
-    uint8_t* base_p = smem + (threadIdx.x >> 5) * DPW_BYTES;
-    uint16_t* cells = (uint16_t*)base_p;
-    uint8_t* rowc = base_p + DPW_CELLS * 2;           // oriented read, 256 B
-    uint8_t* refc = rowc + 256;                       // reference bases along the columns
-    uint8_t* al = refc + DPW_REF;                     // alignment trace
+    const int grp = lane / 9;                   // 3 groups of 9 lanes, lanes 27..31 idle
+    const int k = lane - 9 * grp;
+    const bool in_grp = grp < (int)DP3_GROUPS;
+    uint8_t* warp_p = smem + (threadIdx.x >> 5) * DPW_BYTES;
+    uint2* steps = (uint2*)warp_p;              // per anti-diagonal: ballots of the two choice bits
+    uint8_t* gbase_p = warp_p + DP3_STEPS * 8 + (in_grp ? grp : 0) * DP3_GROUP_BYTES;
+    uint16_t* rown = (uint16_t*)gbase_p;        // row n, offsets -8..8
+    uint8_t* rowc = gbase_p + 48;
+    uint8_t* refc = rowc + 256;
+    uint8_t* al = refc + DP3_REF;
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     const uint32_t ndp = (uint32_t)cb.ctr[CTR_DP];
-    for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < ndp; it += nwarps) {
-        const uint32_t r = cb.dp_list[it];
-        const uint64_t mat = cb.dp_mat[it];
-        const int orient = cb.dp_orient[it];
-        const uint32_t meta = (uint32_t)(mat >> 32);
-        const int isFwd = (int)((mat >> 24) & 1ull);
-        const uint16_t offset = (uint16_t)(mat & 0xffffull);
-        const uint4 wi = ix.win[meta];
-        const uint32_t metaPos = wi.x, sind = wi.z, eind = wi.w;
-        const uint64_t off0 = cb.offs[r];
-        const uint32_t size = (uint32_t)(cb.offs[r + 1] - off0);
+    const uint32_t RL = ix.readlen;
+    for (uint32_t it0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * DP3_GROUPS; it0 < ndp;
+         it0 += nwarps * DP3_GROUPS) {
+        const uint32_t it = it0 + (in_grp ? grp : 0);
+        const bool have = in_grp && it < ndp;
+        uint32_t r = 0, size = 0, metaPos = 0, sind = 0, eind = 0, chrom = 0;
+        uint64_t mat = 0, off0 = 0;
+        int orient = 0, isFwd = 0;
+        uint16_t offset = 0;
+        if (have) {
+            r = cb.dp_list[it];
+            mat = cb.dp_mat[it];
+            orient = cb.dp_orient[it];
+            const uint32_t meta = (uint32_t)(mat >> 32);
+            isFwd = (int)((mat >> 24) & 1ull);
+            offset = (uint16_t)(mat & 0xffffull);
+            const uint4 wi = ix.win[meta];
+            metaPos = wi.x; sind = wi.z; eind = wi.w;
+            off0 = cb.offs[r];
+            size = (uint32_t)(cb.offs[r + 1] - off0);
+            chrom = ix.cpg_chrom[sind];
+        }
         const char* raw = cb.seqs + off0;
-        const uint32_t RL = ix.readlen;
-        const uint32_t chrom = ix.cpg_chrom[sind];
-        const int64_t gbase0 = (int64_t)metaPos + offset;
         const long n = (long)size;
-        const long msize = (n + 1) * DPW;
-        // row characters: row k (1..n) compares rowc[k - 1]
-        for (long k = lane; k < n; k += 32)
-            rowc[k] = oriented_char(raw, size, orient, isFwd ? (uint32_t)(n - 1 - k) : (uint32_t)k);
-        for (long j = lane - DPW_REF0; j <= n + DPB + 2; j += 32)
-            refc[j + DPW_REF0] = base_char(gbase(ix, chrom, gbase0 + 1 - j));
-        for (long k = lane; k < msize; k += 32) cells[k] = 0xffff;
-        __syncwarp();
-        // borders in the reference's order (the left band's (9,0) is overwritten by the right band's (8,17))
-        if (lane == 0) {
-            sset(cells, msize, 0, 0, 0);
-            for (long c = 1; c <= DPB; ++c) sset(cells, msize, 0, c, (uint16_t)c);
-            for (long rr = 1; rr <= DPB; ++rr) sset(cells, msize, rr, 0, (uint16_t)rr);
+        const int64_t gb0 = (int64_t)metaPos + offset;
+        if (have) {
+            // row characters: row i (1..n) compares rowc[i - 1]; reference columns j in [-2, n + 10]
+            for (long q = k; q < n; q += 9)
+                rowc[q] = oriented_char(raw, size, orient, isFwd ? (uint32_t)(n - 1 - q) : (uint32_t)q);
+            for (long j = k - DPW_REF0; j <= n + DPB + 2; j += 9)
+                refc[j + DPW_REF0] = base_char(gbase(ix, chrom, gb0 + 1 - j));
         }
         __syncwarp();
-        for (long c = lane; c < n - DPB; c += 32) sset(cells, msize, c + DPB + 1, c, (uint16_t)(65535 - c - DPB - 1));
-        __syncwarp();
-        for (long rr = lane; rr < n; rr += 32) sset(cells, msize, rr, rr + DPB + 1, (uint16_t)(65535 - rr - DPB - 1));
-        __syncwarp();
-        // fill along anti-diagonals
-        const long o = lane - DPB;  // lanes 0..16 hold band offsets -8..8
-        for (long t = 2 - DPB; t <= 2 * n + DPB; ++t) {
-            if (lane <= 2 * DPB && ((t - o) & 1) == 0) {
+        // fill: steps t = 0 .. 2 * nmax + 8 over the group's anti-diagonals
+        long nmax = n;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) nmax = max(nmax, (long)__shfl_xor_sync(0xffffffffu, (int)nmax, d));
+        int cur1 = 0xffff, cur2 = 0xffff;   // own values of steps t - 1 and t - 2
+        const int base_lane = 9 * (in_grp ? grp : 0);
+        for (long t = 0; t <= 2 * nmax + DPB; ++t) {
+            const int par = (int)(t & 1);
+            const long o = 2 * k - 8 + par;
+            // neighbour values of step t - 1: up (row - 1, o + 1), left (row, o - 1)
+            const int upl = par ? k + 1 : k;
+            const int lfl = par ? k : k - 1;
+            const int v_up = __shfl_sync(0xffffffffu, cur1, base_lane + min(max(upl, 0), 8));
+            const int v_lf = __shfl_sync(0xffffffffu, cur1, base_lane + min(max(lfl, 0), 8));
+            int val = 0xffff;
+            uint32_t mycode = 0;
+            if (have && o <= DPB && ((t - o) & 1) == 0) {
                 const long row = (t - o) >> 1;
                 const long j = row + o;
-                if (row >= 1 && row <= n && j >= 1) {
+                if (row == 0 && o >= 0) {
+                    val = (int)o;                                    // first row: 0..8
+                } else if (row >= 1 && row <= n && j == 0) {
+                    val = (int)row;                                  // first column, rows 1..8
+                } else if (row >= 1 && row <= n && j >= 1) {
+                    const int up = (o == DPB) ? 65535 - (int)(row - 1) - (int)DPB - 1 : v_up;
+                    const int lf = (o == -DPB) ? (row == DPB + 1 ? 65535 - DPB - (int)DPB - 1 : 65535 - (int)row) : v_lf;
+                    const int dg = cur2;
                     const uint8_t rc = rowc[row - 1];
                     const uint8_t g = refc[j + DPW_REF0];
                     const int mm = isFwd ? cmp_fwd(rc, g) : cmp_rev(rc, g);
-                    int v = sget(cells, msize, row - 1, j) + 1;
-                    const int v2 = sget(cells, msize, row, j - 1) + 1;
-                    const int v3 = sget(cells, msize, row - 1, j - 1) + mm;
-                    if (v2 < v) v = v2;
-                    if (v3 < v) v = v3;
-                    sset(cells, msize, row, j, (uint16_t)v);
+                    int v = up + 1;
+                    if (lf + 1 < v) v = lf + 1;
+                    if (dg + mm < v) v = dg + mm;
+                    val = v & 0xffff;
+                    uint8_t code;
+                    if (up < lf) code = (up + 1 < dg + mm) ? 2 : (mm ? 1 : 0);
+                    else code = (lf + 1 < dg + mm) ? 3 : (mm ? 1 : 0);
+                    mycode = code;
+                    if (row == n) rown[o + DPB] = (uint16_t)val;
                 }
             }
-            __syncwarp();
+            const uint32_t b0 = __ballot_sync(0xffffffffu, mycode & 1);
+            const uint32_t b1 = __ballot_sync(0xffffffffu, mycode & 2);
+            if (lane == 0) steps[t] = make_uint2(b0, b1);
+            cur2 = cur1;
+            cur1 = val;
         }
-        if (lane == 0) {
+        __syncwarp();
+        if (have && k == 0) {
+            // backtrackDP / backtrackDPRev over the recorded choices
             uint32_t alen = 0;
             bool bad = false;
             uint16_t mn = 0xffff;
             long col = 0;
             for (long oo = -DPB; oo <= DPB; ++oo) {
-                const uint16_t v = sget(cells, msize, n, n + oo);
+                const uint16_t v = rown[oo + DPB];
                 if (v < mn) { col = n + oo; mn = v; }
             }
             for (long row = n; row > 0;) {
-                const uint8_t rc = rowc[row - 1];
-                const long jj = col + DPW_REF0;
-                const uint8_t g = (jj >= 0 && jj < (long)DPW_REF) ? refc[jj] : 0;
-                const int mm = isFwd ? cmp_fwd(rc, g) : cmp_rev(rc, g);
-                const uint16_t up = sget(cells, msize, row - 1, col), left = sget(cells, msize, row, col - 1),
-                               dg = sget(cells, msize, row - 1, col - 1);
                 uint8_t code;
-                if (up < left) {
-                    if ((int)up + 1 < (int)dg + mm) { code = 2; --row; }
-                    else { code = mm ? 1 : 0; --row; --col; }
-                } else {
-                    if ((int)left + 1 < (int)dg + mm) { code = 3; --col; }
-                    else { code = mm ? 1 : 0; --row; --col; }
+                if (col == 0 && row <= DPB) code = 2;
+                else {
+                    const long oo = col - row;
+                    if (oo < -DPB || oo > DPB || col < 1) { bad = true; break; }
+                    const long tt = 2 * row + oo;
+                    const uint2 m = steps[tt];
+                    const int bit = 9 * grp + (int)((oo + DPB - (tt & 1)) >> 1);
+                    code = (uint8_t)(((m.x >> bit) & 1u) | (((m.y >> bit) & 1u) << 1));
                 }
-                if (alen >= DPW_ALIGN) { bad = true; break; }
+                if (alen >= DP3_ALIGN) { bad = true; break; }
                 al[alen++] = code;
+                if (code == 2) --row;
+                else if (code == 3) --col;
+                else { --row; --col; }
             }
             while (!bad && col > 0) {
-                if (alen >= DPW_ALIGN) { bad = true; break; }
+                if (alen >= DP3_ALIGN) { bad = true; break; }
                 al[alen++] = 3;
                 --col;
             }
@@ -1077,8 +1071,8 @@ __global__ void k_dp_warp(DevIndex ix, ChunkBufs cb)
                         if (c == 'C') atomicAdd(cb.meth + 4ull * id + 0, 1u);
                         else if (c == 'T') atomicAdd(cb.meth + 4ull * id + 1, 1u);
                     } else {
-                        const uint32_t k = (uint32_t)readSeqPos + 1;
-                        const uint8_t c = k < size ? oriented_char(raw, size, orient, size - 1 - k) : 0;
+                        const uint32_t kk = (uint32_t)readSeqPos + 1;
+                        const uint8_t c = kk < size ? oriented_char(raw, size, orient, size - 1 - kk) : 0;
                         if (c == 'C') atomicAdd(cb.meth + 4ull * id + 2, 1u);
                         else if (c == 'T') atomicAdd(cb.meth + 4ull * id + 3, 1u);
                     }
