@@ -46,6 +46,14 @@ class Counters(C.Structure):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
+class PairCounters(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("succ", "nonunique", "unsucc", "paired", "too_short", "r1_fwd", "r1_rev",
+                                          "dp_reads", "heavy_pairs")]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
 CPG_DT = np.dtype([("chrom", np.uint8), ("pos", np.uint32)], align=True)                 # 8 bytes
 WIN_DT = np.dtype([("start_pos", np.uint32), ("chrom", np.uint8), ("start_ind", np.uint32),
                    ("end_ind", np.uint32)], align=True)                                   # 16 bytes
@@ -55,7 +63,7 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_gpu_open", "fame_gpu_close", "fame_gpu_last_error", "fame_gpu_match_reads",
            "fame_gpu_match_reads_dev", "fame_gpu_tallies", "fame_gpu_alloc", "fame_gpu_free", "fame_gpu_memcpy",
            "fame_gpu_host_alloc", "fame_gpu_host_free", "fame_gpu_stream", "fame_gpu_set_timing",
-           "fame_gpu_stage_times", "fame_gpu_last_launches"]
+           "fame_gpu_stage_times", "fame_gpu_last_launches", "fame_gpu_match_pairs"]
 
 _lib = None
 
@@ -93,6 +101,7 @@ def lib(build_if_missing: bool = True):
     L.fame_gpu_set_timing.argtypes = [_P, C.c_int]
     L.fame_gpu_stage_times.argtypes = [_P, _P, C.c_int]
     L.fame_gpu_last_launches.argtypes = [_P]
+    L.fame_gpu_match_pairs.argtypes = [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]
     _lib = L
     return L
 
@@ -243,6 +252,23 @@ class GpuMatcher:
         _check(lib().fame_gpu_match_reads(self.h, _ptr(buf), _ptr(offs), n, flags, _ptr(mats), _ptr(invalid),
                                           C.byref(cnt)), self.h)
         return mats, invalid, cnt
+
+    def match_pairs(self, seq1, offs1, seq2, offs2, flags: int, maxpdist: int):
+        """One chunk of read pairs (fame_gpu_match_pairs); returns
+        (mats1, mats2, invalid1, invalid2, PairCounters)."""
+        offs1 = np.ascontiguousarray(offs1, dtype=np.uint64)
+        offs2 = np.ascontiguousarray(offs2, dtype=np.uint64)
+        n = len(offs1) - 1
+        if len(offs2) != n + 1:
+            raise ValueError("mate offset arrays differ in length")
+        b1 = np.frombuffer(seq1, dtype=np.uint8) if isinstance(seq1, (bytes, bytearray)) else seq1
+        b2 = np.frombuffer(seq2, dtype=np.uint8) if isinstance(seq2, (bytes, bytearray)) else seq2
+        m1, m2 = np.zeros(n, np.uint64), np.zeros(n, np.uint64)
+        i1, i2 = np.zeros(n, np.uint8), np.zeros(n, np.uint8)
+        cnt = PairCounters()
+        _check(lib().fame_gpu_match_pairs(self.h, _ptr(b1), _ptr(offs1), _ptr(b2), _ptr(offs2), n, flags, maxpdist,
+                                          _ptr(m1), _ptr(m2), _ptr(i1), _ptr(i2), C.byref(cnt)), self.h)
+        return m1, m2, i1, i2, cnt
 
     def match_reads_dev(self, seqs_dev, offs_dev, n: int, flags: int, mats_dev, invalid_dev):
         cnt = Counters()

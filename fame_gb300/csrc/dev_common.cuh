@@ -73,6 +73,8 @@ enum {
     CTR_TOO_LONG,
     CTR_ERRFLAG,        // a device-side capacity check failed
     CTR_WMASK,          // bit W set when a valid read needs a W-word automaton
+    CTR_PAIRED,         // pairs with both mates in CpG windows
+    CTR_TOOSHORT,       // the paired path's tooShort count
     CTR_N
 };
 

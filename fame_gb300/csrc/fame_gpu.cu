@@ -10,7 +10,7 @@
 
 #include "../../include/fame_gpu.h"
 #include "index_host.h"
-#include "kernels.cuh"
+#include "pe.cuh"
 
 using namespace fame;
 
@@ -45,6 +45,13 @@ struct fame_gpu {
     int launches = 0;
     int sm_count = 0;
     uint32_t dp_grid = 0;   // resident blocks of k_dp_warp on the whole device
+    // paired path
+    PeIndex px{};
+    uint64_t pe_warp_bytes = 0;          // shared memory per warp of k_pe
+    uint32_t pe_grid[5]{};               // resident blocks of k_pe<W>
+    uint8_t* d_pe_heavy = nullptr;       // global scratch of k_pe_heavy
+    uint64_t pe_heavy_warp_bytes = 0;
+    uint32_t pe_heavy_warps = 0;
 };
 
 namespace {
@@ -134,6 +141,7 @@ extern "C" int fame_gpu_close(fame_gpu* g)
     dev_free(g->d_mats); dev_free(g->d_invalid); dev_free(g->d_dp_list); dev_free(g->d_dp_mat);
     dev_free(g->d_dp_orient); dev_free(g->d_heavy); dev_free(g->d_ctr); dev_free(g->d_meth);
     dev_free(g->hs.base);
+    dev_free(g->d_pe_heavy);
     if (g->h_ctr) cudaFreeHost(g->h_ctr);
     for (auto& e : g->ev) if (e) cudaEventDestroy(e);
     if (g->stream) cudaStreamDestroy(g->stream);
@@ -208,6 +216,27 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
             return fail(set_err(g, FAME_ERR_CUDA, "k-mer upload failed"));
     }
     g->ix.entry = d_entry;
+    // ---- paired path: tmask per entry (kmerTableSmall.tmask), filteredKmers sorted
+    {
+        uint32_t* d_tm;
+        if ((rc = alloc_idx((void**)&d_tm, v->n_kmer * 4))) return fail(rc);
+        for (uint64_t b = 0; b < v->n_kmer; b += CH) {
+            const uint64_t e = std::min<uint64_t>(v->n_kmer, b + CH);
+            for (uint64_t i = b; i < e; ++i) stage[i - b] = v->kmer[i].tmask;
+            if (cudaMemcpy(d_tm + b, stage.data(), (e - b) * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+                return fail(set_err(g, FAME_ERR_CUDA, "tmask upload failed"));
+        }
+        std::vector<uint64_t> f;
+        if (v->n_filtered && v->filtered) f.assign(v->filtered, v->filtered + v->n_filtered);
+        std::sort(f.begin(), f.end());
+        uint64_t* d_f;
+        if ((rc = alloc_idx((void**)&d_f, f.size() * 8))) return fail(rc);
+        if (!f.empty() && cudaMemcpy(d_f, f.data(), f.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(set_err(g, FAME_ERR_CUDA, "filteredKmers upload failed"));
+        g->px.tmask = d_tm;
+        g->px.filtered = d_f;
+        g->px.n_filtered = f.size();
+    }
     // ---- genome: 2-bit codes + N mask, chromosomes at 32-base aligned offsets
     std::vector<uint64_t> coff(v->n_chrom), clen(v->n_chrom);
     uint64_t tot = 0;
@@ -300,6 +329,16 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dp_warp, 128, 4 * DPW_BYTES) != cudaSuccess || nb < 1)
             return fail(set_err(g, FAME_ERR_CUDA, "k_dp_warp does not fit an SM"));
         g->dp_grid = (uint32_t)(g->sm_count * nb);
+        uint64_t off[23];
+        g->pe_warp_bytes = pe_layout(PE_LIGHT, off);
+        const size_t pe_smem = 4 * g->pe_warp_bytes;
+        void (*kp[5])(DevIndex, PeIndex, ChunkBufs, uint32_t) = {nullptr, k_pe<1>, k_pe<2>, k_pe<3>, k_pe<4>};
+        for (int w = 1; w <= 4; ++w) {
+            if (cudaFuncSetAttribute(kp[w], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pe_smem) != cudaSuccess ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kp[w], 128, pe_smem) != cudaSuccess || nb < 1)
+                return fail(set_err(g, FAME_ERR_CUDA, "k_pe does not fit an SM"));
+            g->pe_grid[w] = (uint32_t)(g->sm_count * nb);
+        }
     }
     *out = g;
     return FAME_OK;
@@ -452,6 +491,120 @@ extern "C" int fame_gpu_match_reads(fame_gpu* g, const char* seqs, const uint64_
     if ((rc = run_chunk(g, g->d_seqs, g->d_offs, n, flags, g->d_mats, g->d_invalid, cnt))) return rc;
     CK(cudaMemcpyAsync(mats, g->d_mats, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, g->stream));
     CK(cudaMemcpyAsync(invalid, g->d_invalid, n, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    return FAME_OK;
+}
+
+namespace {
+
+// Heavy-pair caps: keys per map and phase, value-table slots, replayed buckets
+// (bucket_count = summed bucket sizes / 5 <= 224 k-mers x KMERCUTOFF / 5).
+constexpr PeCaps PE_HEAVY{16384, 65536, 131072 + NBHD - 1 + 64, 4096, 4096};
+constexpr uint32_t PE_HEAVY_WARPS = 128;
+
+// Mates of pair r are reads r and n + r of (d_seqs, d_offs); mats and invalid
+// hold 2n entries in the same order.
+int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t n, uint32_t flags, uint32_t maxpdist,
+              uint64_t* d_mats, uint8_t* d_invalid, fame_pair_counters* cnt)
+{
+    const bool both = flags & FAME_BOTH_STRANDS, stranded = flags & FAME_GET_STRANDED;
+    const uint32_t omask = (both || stranded) ? 3u : ((flags & FAME_MATCH_R1_FWD) ? 1u : 2u);
+    int rc;
+    if ((rc = grow_chunk(g, 2ull * n, 0, 0))) return rc;
+    ChunkBufs cb{};
+    cb.seqs = d_seqs;
+    cb.offs = d_offs;
+    cb.n = n;
+    cb.orient_mask = omask;
+    cb.stranded = stranded ? 1u : 0u;
+    cb.rflags = g->d_rflags;
+    cb.mats = d_mats;
+    cb.invalid = d_invalid;
+    cb.dp_list = g->d_dp_list;
+    cb.dp_mat = g->d_dp_mat;
+    cb.dp_orient = g->d_dp_orient;
+    cb.meth = g->d_meth;
+    cb.ctr = g->d_ctr;
+    cb.heavy = g->d_heavy;
+    PeIndex px = g->px;
+    px.ctx = (uint32_t)((double)maxpdist / WINLEN) + 1;
+    px.maxdist = maxpdist + g->ix.readlen;
+    g->launches = 0;
+    CK(cudaMemsetAsync(g->d_ctr, 0, CTR_N * sizeof(unsigned long long), g->stream));
+    k_pe_prep<<<(n + 255) / 256, 256, 0, g->stream>>>(cb, g->ix.readlen);
+    g->launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    if (g->h_ctr[CTR_TOO_LONG]) return set_err(g, FAME_ERR_READ, "mate longer than FAME_MAX_READ_LEN");
+    const uint64_t wmask = g->h_ctr[CTR_WMASK];
+    const size_t smem = 4 * g->pe_warp_bytes;
+    const uint32_t wb = (uint32_t)g->pe_warp_bytes;
+    if (wmask & 2u) { k_pe<1><<<g->pe_grid[1], 128, smem, g->stream>>>(g->ix, px, cb, wb); g->launches++; }
+    if (wmask & 4u) { k_pe<2><<<g->pe_grid[2], 128, smem, g->stream>>>(g->ix, px, cb, wb); g->launches++; }
+    if (wmask & 8u) { k_pe<3><<<g->pe_grid[3], 128, smem, g->stream>>>(g->ix, px, cb, wb); g->launches++; }
+    if (wmask & 16u) { k_pe<4><<<g->pe_grid[4], 128, smem, g->stream>>>(g->ix, px, cb, wb); g->launches++; }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    if (g->h_ctr[CTR_HEAVY]) {
+        if (!g->d_pe_heavy) {
+            uint64_t off[23];
+            g->pe_heavy_warp_bytes = pe_layout(PE_HEAVY, off);
+            g->pe_heavy_warps = PE_HEAVY_WARPS;
+            CK(cudaMalloc((void**)&g->d_pe_heavy, g->pe_heavy_warp_bytes * g->pe_heavy_warps));
+        }
+        k_pe_heavy<<<g->pe_heavy_warps / 4, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_heavy,
+                                                                  g->pe_heavy_warp_bytes, PE_HEAVY);
+        g->launches++;
+        CK(cudaGetLastError());
+    }
+    k_dp_warp<<<g->dp_grid, 128, 4 * DPW_BYTES, g->stream>>>(g->ix, cb);
+    g->launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    if (g->h_ctr[CTR_ERRFLAG]) return set_err(g, FAME_ERR_INDEX, "a read pair exceeds the paired path's capacities");
+    if (cnt) {
+        const unsigned long long* h = g->h_ctr;
+        cnt->succ += h[CTR_SUCC];
+        cnt->nonunique += h[CTR_NONU];
+        cnt->unsucc += h[CTR_UNSUCC];
+        cnt->paired += h[CTR_PAIRED];
+        cnt->too_short += h[CTR_TOOSHORT];
+        cnt->r1_fwd += h[CTR_R1F];
+        cnt->r1_rev += h[CTR_R1R];
+        cnt->dp_reads += h[CTR_DP];
+        cnt->heavy_pairs += h[CTR_HEAVY];
+    }
+    return FAME_OK;
+}
+
+}  // namespace
+
+extern "C" int fame_gpu_match_pairs(fame_gpu* g, const char* seqs1, const uint64_t* offs1, const char* seqs2,
+                                    const uint64_t* offs2, uint32_t n, uint32_t flags, uint32_t maxpdist,
+                                    uint64_t* mats1, uint64_t* mats2, uint8_t* invalid1, uint8_t* invalid2,
+                                    fame_pair_counters* cnt)
+{
+    if (!g || (n && (!seqs1 || !offs1 || !seqs2 || !offs2 || !mats1 || !mats2 || !invalid1 || !invalid2)))
+        return FAME_ERR_ARG;
+    CK(cudaSetDevice(g->device));
+    if (n == 0) return FAME_OK;
+    const uint64_t b1 = offs1[0], n1 = offs1[n] - offs1[0], b2 = offs2[0], n2 = offs2[n] - offs2[0];
+    int rc;
+    if ((rc = grow_chunk(g, 2ull * n, n1 + n2, 0))) return rc;
+    std::vector<uint64_t> o(2ull * n + 1);
+    for (uint32_t i = 0; i <= n; ++i) o[i] = offs1[i] - b1;
+    for (uint32_t i = 1; i <= n; ++i) o[n + i] = n1 + offs2[i] - b2;
+    CK(cudaMemcpyAsync(g->d_seqs, seqs1 + b1, n1, cudaMemcpyHostToDevice, g->stream));
+    CK(cudaMemcpyAsync(g->d_seqs + n1, seqs2 + b2, n2, cudaMemcpyHostToDevice, g->stream));
+    CK(cudaMemcpyAsync(g->d_offs, o.data(), o.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, g->stream));
+    if ((rc = run_pairs(g, g->d_seqs, g->d_offs, n, flags, maxpdist, g->d_mats, g->d_invalid, cnt))) return rc;
+    CK(cudaMemcpyAsync(mats1, g->d_mats, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaMemcpyAsync(mats2, g->d_mats + n, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaMemcpyAsync(invalid1, g->d_invalid, n, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaMemcpyAsync(invalid2, g->d_invalid + n, n, cudaMemcpyDeviceToHost, g->stream));
     CK(cudaStreamSynchronize(g->stream));
     return FAME_OK;
 }

@@ -97,8 +97,11 @@ struct ShiftAndState {
 // on the text spans of saQuerySeedSetRef, ReadQueue.cpp:1953-1962, 2048-2058).
 // emit(offset, errors) is called once per run of consecutive accepting bases,
 // with the last position holding the run's smallest error count.
+// unguarded: the reverse scan starts at startPos - 1 even for a window at
+// position 0 (matchRevSecond, ReadQueue.cpp:4736), i.e. it includes base 0.
 template <int W, class Emit>
-__device__ void scan_window_full(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t wid, int fwd, Emit emit)
+__device__ void scan_window_full(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t wid, int fwd, Emit emit,
+                                 bool unguarded = false)
 {
     const uint4 wi = ix.win[wid];
     const uint32_t sp = wi.x, ch = wi.y;
@@ -132,7 +135,7 @@ __device__ void scan_window_full(const DevIndex& ix, ShiftAndState<W>& sa, uint3
             }
         }
     } else {
-        const int64_t lo = sp > 0 ? (int64_t)sp - 1 : 0;
+        const int64_t lo = (sp > 0 || unguarded) ? (int64_t)sp - 1 : 0;
         int64_t hi = (int64_t)sp + WIN_TEXT;
         if (hi >= L) hi = L - 1;
         uint64_t g = g0 + (uint64_t)hi;
@@ -192,7 +195,8 @@ struct ScanText {
 // (repetitive windows) fall back to the full scan.
 template <int W, class Emit>
 __device__ void scan_window(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t wid, int fwd, Emit emit,
-                            const uint32_t* pkey, uint32_t pvalid, uint32_t q, const uint32_t* pstart)
+                            const uint32_t* pkey, uint32_t pvalid, uint32_t q, const uint32_t* pstart,
+                            bool unguarded = false)
 {
     constexpr int CAP = 32;
     const uint4 wi = ix.win[wid];
@@ -210,7 +214,7 @@ __device__ void scan_window(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t w
         tx.len = (uint32_t)(e - (int64_t)sp);
         tx.off_a = 0;
     } else {
-        const int64_t lo = sp > 0 ? (int64_t)sp - 1 : 0;
+        const int64_t lo = (sp > 0 || unguarded) ? (int64_t)sp - 1 : 0;
         int64_t hi = (int64_t)sp + WIN_TEXT;
         if (hi >= L) hi = L - 1;
         tx.g0 = gch + (uint64_t)hi;
@@ -223,7 +227,7 @@ __device__ void scan_window(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t w
     int32_t ilo[CAP], ihi[CAP];
     const uint64_t G0 = fwd ? tx.g0 : tx.g0 + 1 - tx.len, G1 = G0 + tx.len;
     const int nint = qgram_spans<CAP>(ix.gpack, ix.gnmask, G0, G1, fwd, m, q, pkey, pvalid, pstart, ilo, ihi);
-    if (nint < 0) { scan_window_full<W>(ix, sa, wid, fwd, emit); return; }
+    if (nint < 0) { scan_window_full<W>(ix, sa, wid, fwd, emit, unguarded); return; }
     if (nint == 0) return;
     // sort spans by start and merge overlapping ones
     for (int i = 1; i < nint; ++i) {
@@ -905,7 +909,8 @@ constexpr uint32_t DP3_MAXN = FAME_MAX_READ_LEN;
 constexpr uint32_t DP3_STEPS = 2 * DP3_MAXN + DP_BAND + 2;            // anti-diagonals, rounded up to even
 constexpr uint32_t DP3_REF = 288;                                      // reference bases, j in [-2, n + 10]
 constexpr uint32_t DP3_ALIGN = 2 * DP3_MAXN + 4 * DP_BAND + 10;       // alignment trace
-constexpr uint32_t DP3_GROUP_BYTES = 48 + 256 + DP3_REF + DP3_ALIGN + 8; // row-n values, read, reference, trace
+// row-n values, read, reference, trace; + 16 so that the groups' arrays start in different banks
+constexpr uint32_t DP3_GROUP_BYTES = 48 + 256 + DP3_REF + DP3_ALIGN + 8 + 16;
 constexpr uint32_t DPW_BYTES = DP3_STEPS * 8 + DP3_GROUPS * DP3_GROUP_BYTES;   // per warp
 constexpr int DPW_REF0 = 2;
 static_assert(DP3_GROUP_BYTES % 16 == 0 && (DP3_STEPS * 8) % 16 == 0, "16-byte aligned shared-memory regions");

@@ -1,0 +1,875 @@
+// Paired-end matching: one warp per read pair.
+//
+// Follows matchPairedReads (ReadQueue.cpp:940-1658) per pair and orientation:
+//   getSeedRefsFirstRead  (ReadQueue.cpp:2468-2794)   first mate's window counts
+//   getSeedRefsSecondRead (ReadQueue.cpp:2801-3164)   mate counts near those windows
+//   saQuerySeedSetRefFirst / Second (ReadQueue.cpp:2167-2323) with
+//   matchFwd/RevFirst/Second (ReadQueue.cpp:4538-4776)  sorted, pruned walks
+//   extractPairedMatch (ReadQueue.cpp:3255-3275) and the pair choice (1300-1638)
+//
+// The maps of the reference (tsl::hopscotch_map<uint32_t, tuple<u8 count1,
+// u8 count2, bool f2, bool f3>>, one per window strand) are kept as a value
+// table for lookups plus the sequence of insertions; the iteration order,
+// which decides the order of the candidate lists before their (unstable)
+// std::sort, is reproduced by replaying those insertions (seed.cuh).  The
+// first mate's map is rebuilt after counting into a map of 20 buckets holding
+// the windows with count1 >= QTHRESH in the old map's order, and the second
+// mate inserts new windows into that map, so the final order is the replay of
+// [kept keys in the first map's order] ++ [keys the second mate inserted].
+//
+// Lanes hash and look up the k-mers; lane 0 applies the map operations in the
+// reference's order, replays, sorts and walks.  Pairs whose working set
+// exceeds the shared-memory caps are handed to a launch with global scratch.
+#pragma once
+#include "kernels.cuh"
+
+namespace fame {
+
+constexpr uint32_t KMERDIST = 10;  // CONST.h:104
+
+// paired-path tables
+struct PeIndex {
+    const uint32_t* tmask;     // per k-mer entry (kmerTableSmall.tmask)
+    const uint64_t* filtered;  // filteredKmers, sorted
+    uint64_t n_filtered;
+    uint32_t ctx;              // contextWLen = floor(MAXPDIST / WINLEN) + 1
+    uint32_t maxdist;          // MAXPDIST + READLEN
+};
+
+// value of a map entry
+constexpr uint32_t PV_PRESENT = 1u << 31;
+constexpr uint32_t PV_F2 = 1u << 16;
+constexpr uint32_t PV_F3 = 1u << 17;
+__device__ __forceinline__ uint32_t pv_c1(uint32_t v) { return v & 0xffu; }
+__device__ __forceinline__ uint32_t pv_c2(uint32_t v) { return (v >> 8) & 0xffu; }
+
+constexpr uint32_t PE_KMAX = FAME_MAX_READ_LEN - KMERLEN + 1;   // k-mers of the longest read
+
+// Capacities of one warp's working memory.
+struct PeCaps {
+    uint32_t icap;      // keys per map and phase
+    uint32_t vcap;      // value-table slots per strand (power of two, >= 4 * icap)
+    uint32_t slot_cap;  // replayed bucket array
+    uint32_t ovf_cap;
+    uint32_t hcap;      // hits per mate and orientation
+};
+
+struct PeMem {
+    uint8_t* rd[2];       // oriented first and second mate
+    uint32_t* kst;        // per k-mer: bucket start
+    uint32_t* kln;        //            bucket size
+    uint32_t* kcm;        //            C mask
+    uint8_t* kfl;         //            in filteredKmers
+    uint32_t* vk[2];      // value tables per window strand (0 reverse, 1 forward)
+    uint32_t* vv[2];
+    uint32_t* ins1[2];    // first-mate insertions
+    uint32_t* ins2[2];    // second-mate insertions
+    uint32_t* seq;        // one replay's insertion sequence
+    uint32_t* ord[2];     // final iteration order
+    uint32_t* slot;
+    uint32_t* stk;
+    uint32_t* ovf;
+    uint2* list[2];       // (key, value) candidate lists
+    uint64_t* hits[4];    // m1F, m2R, m1R, m2F
+    PeCaps c;
+};
+
+__host__ __device__ inline uint64_t pe_align16(uint64_t x) { return (x + 15) & ~15ull; }
+
+// Byte layout of PeMem for the given caps; returns the total.
+__host__ __device__ inline uint64_t pe_layout(PeCaps c, uint64_t* off)
+{
+    uint64_t o = 0;
+    int i = 0;
+    auto put = [&](uint64_t bytes) { off[i++] = o; o = pe_align16(o + bytes); };
+    put(8ull * c.hcap * 4);                 // 0 hits
+    put(8ull * c.icap * 2);                 // 1 list[0]
+    put(8ull * c.icap * 2);                 // 2 list[1]
+    put(4ull * c.vcap);                     // 3 vk[0]
+    put(4ull * c.vcap);                     // 4 vk[1]
+    put(4ull * c.vcap);                     // 5 vv[0]
+    put(4ull * c.vcap);                     // 6 vv[1]
+    put(4ull * c.icap);                     // 7 ins1[0]
+    put(4ull * c.icap);                     // 8 ins1[1]
+    put(4ull * c.icap);                     // 9 ins2[0]
+    put(4ull * c.icap);                     // 10 ins2[1]
+    put(4ull * c.icap * 2);                 // 11 seq
+    put(4ull * c.icap * 2);                 // 12 ord[0]
+    put(4ull * c.icap * 2);                 // 13 ord[1]
+    put(4ull * c.slot_cap);                 // 14 slot
+    put(4ull * c.icap * 2);                 // 15 stk
+    put(4ull * c.ovf_cap);                  // 16 ovf
+    put(4ull * PE_KMAX);                    // 17 kst
+    put(4ull * PE_KMAX);                    // 18 kln
+    put(4ull * PE_KMAX);                    // 19 kcm
+    put(PE_KMAX);                           // 20 kfl
+    put(256);                               // 21 rd[0]
+    put(256);                               // 22 rd[1]
+    return o;
+}
+
+__device__ inline PeMem pe_mem(uint8_t* base, PeCaps c)
+{
+    uint64_t off[23];
+    pe_layout(c, off);
+    PeMem s;
+    s.c = c;
+    uint64_t* h = (uint64_t*)(base + off[0]);
+    for (int k = 0; k < 4; ++k) s.hits[k] = h + (uint64_t)k * c.hcap;
+    s.list[0] = (uint2*)(base + off[1]);
+    s.list[1] = (uint2*)(base + off[2]);
+    s.vk[0] = (uint32_t*)(base + off[3]);
+    s.vk[1] = (uint32_t*)(base + off[4]);
+    s.vv[0] = (uint32_t*)(base + off[5]);
+    s.vv[1] = (uint32_t*)(base + off[6]);
+    s.ins1[0] = (uint32_t*)(base + off[7]);
+    s.ins1[1] = (uint32_t*)(base + off[8]);
+    s.ins2[0] = (uint32_t*)(base + off[9]);
+    s.ins2[1] = (uint32_t*)(base + off[10]);
+    s.seq = (uint32_t*)(base + off[11]);
+    s.ord[0] = (uint32_t*)(base + off[12]);
+    s.ord[1] = (uint32_t*)(base + off[13]);
+    s.slot = (uint32_t*)(base + off[14]);
+    s.stk = (uint32_t*)(base + off[15]);
+    s.ovf = (uint32_t*)(base + off[16]);
+    s.kst = (uint32_t*)(base + off[17]);
+    s.kln = (uint32_t*)(base + off[18]);
+    s.kcm = (uint32_t*)(base + off[19]);
+    s.kfl = base + off[20];
+    s.rd[0] = base + off[21];
+    s.rd[1] = base + off[22];
+    return s;
+}
+
+// shared-memory caps (one warp)
+constexpr PeCaps PE_LIGHT{96, 256, 512 + NBHD - 1, 64, 32};
+
+__device__ __forceinline__ uint32_t vt_hash(uint32_t k, uint32_t mask) { return (k * 0x9E3779B1u) >> 8 & mask; }
+
+// Lane-0 state of one pair and orientation.
+struct PeState {
+    uint32_t nkeys[2];   // keys held by each value table
+    uint32_t n1[2];      // first-mate insertions
+    uint32_t n2[2];      // second-mate insertions
+    uint32_t nord[2];
+    bool over;           // a capacity was exceeded
+};
+
+// slot of key in the strand's table when present, else -1
+__device__ __forceinline__ int pm_find(const PeMem& s, int dir, uint32_t key)
+{
+    if (key == EMPTY_KEY) return -1;
+    const uint32_t mask = s.c.vcap - 1;
+    for (uint32_t h = vt_hash(key, mask);; h = (h + 1) & mask) {
+        const uint32_t k = s.vk[dir][h];
+        if (k == key) return (s.vv[dir][h] & PV_PRESENT) ? (int)h : -1;
+        if (k == EMPTY_KEY) return -1;
+    }
+}
+
+// operator[]: the key's slot, inserted (and recorded) when absent; -1 when full
+__device__ __forceinline__ int pm_at(const PeMem& s, PeState& st, int dir, uint32_t key, int phase)
+{
+    const uint32_t mask = s.c.vcap - 1;
+    uint32_t h = vt_hash(key, mask);
+    for (;; h = (h + 1) & mask) {
+        const uint32_t k = s.vk[dir][h];
+        if (k == key) break;
+        if (k == EMPTY_KEY) {
+            if (4 * (st.nkeys[dir] + 1) > 3 * s.c.vcap) { st.over = true; return -1; }
+            s.vk[dir][h] = key;
+            s.vv[dir][h] = 0;
+            st.nkeys[dir]++;
+            break;
+        }
+    }
+    if (!(s.vv[dir][h] & PV_PRESENT)) {
+        uint32_t& n = phase == 1 ? st.n1[dir] : st.n2[dir];
+        if (n >= s.c.icap) { st.over = true; return -1; }
+        (phase == 1 ? s.ins1[dir] : s.ins2[dir])[n++] = key;
+        s.vv[dir][h] = PV_PRESENT;
+    }
+    return (int)h;
+}
+
+__device__ __forceinline__ bool filtered_has(const PeIndex& px, uint64_t k)
+{
+    uint64_t lo = 0, hi = px.n_filtered;
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (__ldg(px.filtered + mid) < k) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo < px.n_filtered && __ldg(px.filtered + lo) == k;
+}
+
+// Warp: per k-mer bucket bounds, C mask and filteredKmers flag of the read in
+// rd; returns the summed bucket sizes (the maps' bucket_count * 5).
+__device__ uint32_t pe_kmers(const DevIndex& ix, const PeIndex& px, const PeMem& s, const uint8_t* rd, uint32_t len)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nk = len - KMERLEN + 1;
+    uint32_t sigma = 0;
+    for (uint32_t p = lane; p < nk; p += 32) {
+        uint64_t h = 0;
+        uint32_t cm = 0, kq = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < KMERLEN; ++i) {
+            const uint8_t c = rd[p + i];
+            if ((SEEDBITS >> (31 - i)) & 1u) h ^= rotl64(nt_val(c), 31 - i);
+            cm = (cm << 1) | (c == 'C' ? 1u : 0u);
+            kq = (kq << 2) + ((c == 'C' || c == 'T') ? 3u : (c == 'G' ? 2u : 0u));
+        }
+        const uint32_t key = (uint32_t)(h & HTAB_MASK);
+        const uint32_t b0 = __ldg(ix.tab + key), b1 = __ldg(ix.tab + key + 1);
+        s.kst[p] = b0;
+        s.kln[p] = b1 - b0;
+        s.kcm[p] = cm;
+        s.kfl[p] = (p > 0 && filtered_has(px, kq)) ? 1 : 0;
+        sigma += b1 - b0;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) sigma += __shfl_xor_sync(0xffffffffu, sigma, d);
+    __syncwarp();
+    return sigma;
+}
+
+// Iteration order of a map that received seq[0..n) by insertion into
+// bucket_count buckets; false when the replay exceeds a cap.
+__device__ bool pe_replay(const PeMem& s, const uint32_t* seq, uint32_t n, uint32_t bucket_count, uint32_t* out,
+                          uint32_t& nout)
+{
+    SeedMem sm{};
+    sm.ins = (uint32_t*)seq;
+    sm.slot = s.slot;
+    sm.stk = s.stk;
+    sm.ovf = s.ovf;
+    sm.slot_cap = s.c.slot_cap;
+    sm.stk_cap = 2 * s.c.icap;
+    sm.ovf_cap = s.c.ovf_cap;
+    MapSim m;
+    sim_init(m, bucket_count);
+    m.nb = 0; m.novf = 0; m.sp = 0;
+    if (m.size > s.c.slot_cap) return false;
+    for (uint32_t b = 0; b < m.size; ++b) s.slot[b] = EMPTY_KEY;
+    for (uint32_t x = 0; x < n; ++x) {
+        if (m.sp >= sm.stk_cap) return false;
+        s.stk[m.sp++] = x;
+        while (m.sp > 0)
+            if (!sim_step(m, sm)) return false;
+    }
+    nout = 0;
+    for (uint32_t b = 0; b < m.size; ++b)
+        if (s.slot[b] != EMPTY_KEY) out[nout++] = seq[s.slot[b]];
+    for (uint32_t i = 0; i < m.novf; ++i) out[nout++] = seq[s.ovf[i]];
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// std::sort of libstdc++ (introsort with median-of-three pivot, heap sort past
+// the depth limit, final insertion sort with a 16-element threshold) with
+// comp(a, b) = count(a) > count(b) (CompiMetaFirst / CompiMetaSecond,
+// ReadQueue.h:340-353).  The sort is not stable, so its exact steps decide the
+// order of equal counts.
+// ---------------------------------------------------------------------------
+struct PeCmp {
+    int second;
+    __device__ __forceinline__ bool operator()(const uint2& a, const uint2& b) const
+    {
+        return second ? pv_c2(a.y) > pv_c2(b.y) : pv_c1(a.y) > pv_c1(b.y);
+    }
+};
+
+__device__ inline void ps_swap(uint2* a, uint2* b) { const uint2 t = *a; *a = *b; *b = t; }
+
+__device__ inline void ps_insertion(uint2* f, uint2* l, PeCmp cmp)
+{
+    if (f == l) return;
+    for (uint2* i = f + 1; i != l; ++i) {
+        const uint2 val = *i;
+        if (cmp(val, *f)) {
+            for (uint2* j = i; j != f; --j) *j = *(j - 1);
+            *f = val;
+        } else {
+            uint2* last = i;
+            uint2* next = i - 1;
+            while (cmp(val, *next)) { *last = *next; last = next; --next; }
+            *last = val;
+        }
+    }
+}
+
+__device__ inline void ps_unguarded_insertion(uint2* f, uint2* l, PeCmp cmp)
+{
+    for (uint2* i = f; i != l; ++i) {
+        const uint2 val = *i;
+        uint2* last = i;
+        uint2* next = i - 1;
+        while (cmp(val, *next)) { *last = *next; last = next; --next; }
+        *last = val;
+    }
+}
+
+__device__ inline void ps_adjust_heap(uint2* f, long hole, long len, uint2 val, PeCmp cmp)
+{
+    const long top = hole;
+    long child = hole;
+    while (child < (len - 1) / 2) {
+        child = 2 * (child + 1);
+        if (cmp(f[child], f[child - 1])) --child;
+        f[hole] = f[child];
+        hole = child;
+    }
+    if ((len & 1) == 0 && child == (len - 2) / 2) {
+        child = 2 * (child + 1);
+        f[hole] = f[child - 1];
+        hole = child - 1;
+    }
+    long parent = (hole - 1) / 2;
+    while (hole > top && cmp(f[parent], val)) {
+        f[hole] = f[parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    f[hole] = val;
+}
+
+__device__ inline void ps_heap_select_sort(uint2* f, uint2* m, uint2* l, PeCmp cmp)
+{
+    // make_heap on [f, m)
+    const long len = m - f;
+    if (len >= 2) {
+        for (long parent = (len - 2) / 2;; --parent) {
+            ps_adjust_heap(f, parent, len, f[parent], cmp);
+            if (parent == 0) break;
+        }
+    }
+    for (uint2* i = m; i < l; ++i)
+        if (cmp(*i, *f)) {
+            const uint2 val = *i;
+            *i = *f;
+            ps_adjust_heap(f, 0, len, val, cmp);
+        }
+    // sort_heap
+    for (uint2* e = m; e - f > 1;) {
+        --e;
+        const uint2 val = *e;
+        *e = *f;
+        ps_adjust_heap(f, 0, e - f, val, cmp);
+    }
+}
+
+__device__ inline void ps_median_first(uint2* r, uint2* a, uint2* b, uint2* c, PeCmp cmp)
+{
+    if (cmp(*a, *b)) {
+        if (cmp(*b, *c)) ps_swap(r, b);
+        else if (cmp(*a, *c)) ps_swap(r, c);
+        else ps_swap(r, a);
+    } else if (cmp(*a, *c)) ps_swap(r, a);
+    else if (cmp(*b, *c)) ps_swap(r, c);
+    else ps_swap(r, b);
+}
+
+__device__ inline uint2* ps_partition(uint2* f, uint2* l, uint2* pivot, PeCmp cmp)
+{
+    while (true) {
+        while (cmp(*f, *pivot)) ++f;
+        --l;
+        while (cmp(*pivot, *l)) --l;
+        if (!(f < l)) return f;
+        ps_swap(f, l);
+        ++f;
+    }
+}
+
+// introsort loop with an explicit stack (the recursion goes right, the loop left)
+__device__ inline void ps_introsort(uint2* f, uint2* l, long depth, PeCmp cmp)
+{
+    struct Frame { uint2* f; uint2* l; long depth; };
+    Frame stk[64];
+    int sp = 0;
+    stk[sp++] = {f, l, depth};
+    while (sp > 0) {
+        Frame fr = stk[--sp];
+        uint2* a = fr.f;
+        uint2* b = fr.l;
+        long d = fr.depth;
+        while (b - a > 16) {
+            if (d == 0) { ps_heap_select_sort(a, b, b, cmp); break; }
+            --d;
+            uint2* mid = a + (b - a) / 2;
+            ps_median_first(a, a + 1, mid, b - 1, cmp);
+            uint2* cut = ps_partition(a + 1, b, a, cmp);
+            if (sp < 64) stk[sp++] = {cut, b, d};
+            b = cut;
+        }
+    }
+}
+
+__device__ inline void pe_sort(uint2* f, long n, PeCmp cmp)
+{
+    if (n <= 1) return;
+    long lg = 0;
+    while ((1l << (lg + 1)) <= n) ++lg;
+    ps_introsort(f, f + n, 2 * lg, cmp);
+    if (n > 16) {
+        ps_insertion(f, f + 16, cmp);
+        ps_unguarded_insertion(f + 16, f + n, cmp);
+    } else {
+        ps_insertion(f, f + n, cmp);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// lane 0: map operations of one mate (getSeedRefsFirstRead / SecondRead)
+// ---------------------------------------------------------------------------
+__device__ void pe_count_first(const DevIndex& ix, const PeIndex& px, const PeMem& s, PeState& st, uint32_t len)
+{
+    const uint32_t nk = len - KMERLEN + 1;
+    const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
+    for (uint32_t p = 0; p < nk && !st.over; ++p) {
+        if (s.kfl[p]) continue;
+        const uint32_t b0 = s.kst[p], n = s.kln[p], cm = s.kcm[p];
+        bool have = false;
+        uint32_t lastId = 0, lastFwd = 0;
+        for (uint32_t i = b0; i < b0 + n; ++i) {
+            if (cm & SEEDBITS & __ldg(px.tmask + i)) continue;
+            const uint32_t e = __ldg(ix.entry + i);
+            const uint32_t id = e & 0x7fffffffu, fwd = e >> 31;
+            if (have && id == lastId && fwd == lastFwd) continue;
+            have = true; lastId = id; lastFwd = fwd;
+            int h;
+            if (p == 0 || p - 1 < maxQPos) {
+                h = pm_at(s, st, (int)fwd, id, 1);
+                if (h < 0) return;
+            } else {
+                h = pm_find(s, (int)fwd, id);
+            }
+            if (h >= 0) {
+                const uint32_t v = s.vv[fwd][h];
+                s.vv[fwd][h] = (v & ~0xffu) | ((pv_c1(v) + 1) & 0xffu);
+            }
+        }
+    }
+}
+
+__device__ void pe_count_second(const DevIndex& ix, const PeIndex& px, const PeMem& s, PeState& st, uint32_t len)
+{
+    const uint32_t nk = len - KMERLEN + 1;
+    const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
+    const int ctx = (int)px.ctx;
+    for (uint32_t p = 0; p < nk && !st.over; ++p) {
+        if (s.kfl[p]) continue;
+        const uint32_t b0 = s.kst[p], n = s.kln[p], cm = s.kcm[p];
+        bool have = false;
+        uint32_t lastId = 0, lastFwd = 0;
+        for (uint32_t i = b0; i < b0 + n; ++i) {
+            if (cm & SEEDBITS & __ldg(px.tmask + i)) continue;
+            const uint32_t e = __ldg(ix.entry + i);
+            const uint32_t id = e & 0x7fffffffu, fwd = e >> 31;
+            if (have && id == lastId && fwd == lastFwd) continue;
+            have = true; lastId = id; lastFwd = fwd;
+            int h = -1;
+            if (p == 0 || p - 1 < maxQPos) {
+                for (int c = -ctx; c <= ctx; ++c) {
+                    if (pm_find(s, (int)fwd, id + (uint32_t)c) >= 0) {
+                        h = pm_at(s, st, (int)fwd, id, 2);
+                        if (h < 0) return;
+                        break;
+                    }
+                }
+            } else {
+                h = pm_find(s, (int)fwd, id);
+            }
+            if (h >= 0) {
+                const uint32_t v = s.vv[fwd][h];
+                s.vv[fwd][h] = (v & ~0xff00u) | (((pv_c2(v) + 1) & 0xffu) << 8);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// lane 0: one query walk (saQuerySeedSetRefFirst / Second)
+// ---------------------------------------------------------------------------
+template <int W>
+__device__ __noinline__ void pe_walk(const DevIndex& ix, const PeIndex& px, const PeMem& s, PeState& st,
+                                     const ChunkBufs& cb, uint32_t r_idx, int orient, int second, uint64_t* hits,
+                                     uint32_t& nh)
+{
+    const uint64_t off0 = cb.offs[r_idx];
+    const uint32_t len = (uint32_t)(cb.offs[r_idx + 1] - off0);
+    const char* raw = cb.seqs + off0;
+    ShiftAndState<W> sa;
+    sa.load(raw, len, orient);
+    PieceKeys pk;
+    pk.load(raw, len, orient);
+    const PeCmp cmp{second};
+    uint32_t nl[2];
+    for (int dir = 0; dir < 2; ++dir) {
+        nl[dir] = st.nord[dir];
+        for (uint32_t q = 0; q < nl[dir]; ++q) {
+            const uint32_t key = s.ord[dir][q];
+            const int h = pm_find(s, dir, key);
+            s.list[dir][q] = make_uint2(key, h >= 0 ? s.vv[dir][h] : 0u);
+        }
+        pe_sort(s.list[dir], (long)nl[dir], cmp);
+    }
+    int order2[2] = {0, 1};
+    int nwalk = 0;
+    if (nl[1] > 0) {
+        if (nl[0] > 0) {
+            // both walks compare the heads' count1 (ReadQueue.cpp:2185, 2265)
+            if (pv_c1(s.list[1][0].y) > pv_c1(s.list[0][0].y)) { order2[0] = 1; order2[1] = 0; }
+            nwalk = 2;
+        } else {
+            order2[0] = 1;
+            nwalk = 1;
+        }
+    } else if (nl[0] > 0) {
+        order2[0] = 0;
+        nwalk = 1;
+    }
+    int32_t bmCount = 0;
+    uint32_t prevChr = 0;
+    uint64_t prevOff = 0xffffffffffffffffull;
+    const int ctx = (int)px.ctx;
+    for (int wk = 0; wk < nwalk; ++wk) {
+        const int dir = order2[wk];
+        if (wk == 1) { prevChr = 0; prevOff = 0xffffffffffffffffull; }
+        for (uint32_t q = 0; q < nl[dir]; ++q) {
+            const uint2 e = s.list[dir][q];
+            const int32_t cnt = (int32_t)(second ? pv_c2(e.y) : pv_c1(e.y));
+            const int32_t thr = bmCount - (int32_t)KMERDIST > (int32_t)QTHRESH ? bmCount - (int32_t)KMERDIST : (int32_t)QTHRESH;
+            if (cnt < thr) break;
+            if (!(e.y & (second ? PV_F3 : PV_F2))) continue;
+            const uint32_t w = e.x;
+            const uint4 wi = ix.win[w];
+            const uint32_t sp = wi.x, ch = wi.y;
+            uint32_t n = 0, last = 0;
+            scan_window<W>(ix, sa, w, dir, [&](uint32_t off, int err) {
+                if (!(n == 0 && (uint64_t)off + sp == prevOff && ch == prevChr)) {
+                    if (nh >= s.c.hcap) st.over = true;
+                    else hits[nh++] = mk_match(off, (uint32_t)err, (uint64_t)dir, w);
+                }
+                last = off;
+                ++n;
+            }, pk.key, pk.valid, pk.q, pk.start, second && dir == 0);
+            if (st.over) return;
+            if (n > 0) {
+                if (cnt > bmCount) bmCount = cnt;
+                if (!second) {
+                    int h = pm_find(s, dir, w);
+                    if (h >= 0) s.vv[dir][h] |= PV_F3;
+                    for (int c = 1; c <= ctx; ++c) {
+                        h = pm_find(s, dir, w + (uint32_t)c);
+                        if (h >= 0) s.vv[dir][h] |= PV_F3;
+                        h = pm_find(s, dir, w - (uint32_t)c);
+                        if (h >= 0) s.vv[dir][h] |= PV_F3;
+                    }
+                }
+                prevChr = ch;
+                prevOff = (uint64_t)sp + last;
+            } else {
+                prevChr = 0;
+                prevOff = 0xffffffffffffffffull;
+            }
+        }
+    }
+}
+
+template <int WMAX>
+__device__ __forceinline__ void pe_walk_any(const DevIndex& ix, const PeIndex& px, const PeMem& s, PeState& st,
+                                            const ChunkBufs& cb, uint32_t r_idx, int orient, int second,
+                                            uint64_t* hits, uint32_t& nh)
+{
+    const uint32_t len = (uint32_t)(cb.offs[r_idx + 1] - cb.offs[r_idx]);
+    const int w = (int)(len / 64 + 1);
+    if (w == 1 || WMAX == 1) pe_walk<1>(ix, px, s, st, cb, r_idx, orient, second, hits, nh);
+    else if (w == 2 || WMAX == 2) pe_walk<(WMAX >= 2 ? 2 : 1)>(ix, px, s, st, cb, r_idx, orient, second, hits, nh);
+    else if (w == 3 || WMAX == 3) pe_walk<(WMAX >= 3 ? 3 : 1)>(ix, px, s, st, cb, r_idx, orient, second, hits, nh);
+    else pe_walk<(WMAX >= 4 ? 4 : 1)>(ix, px, s, st, cb, r_idx, orient, second, hits, nh);
+}
+
+// ---------------------------------------------------------------------------
+// one pair (warp); returns false when a cap was exceeded before any output
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int pe_extract(const DevIndex& ix, const PeIndex& px, uint64_t m1, uint64_t m2)
+{
+    const uint4 w1 = ix.win[(uint32_t)(m1 >> 32)], w2 = ix.win[(uint32_t)(m2 >> 32)];
+    if (w1.y != w2.y) return -1;
+    const uint32_t p1 = w1.x + (uint32_t)(m1 & 0xffffu), p2 = w2.x + (uint32_t)(m2 & 0xffffu);
+    const uint32_t d = p2 > p1 ? p2 - p1 : p1 - p2;
+    if (d <= px.maxdist) return (int)(((m1 >> 16) & 0xffu) + ((m2 >> 16) & 0xffu));
+    return -1;
+}
+
+__device__ __forceinline__ void pe_meth(const DevIndex& ix, const ChunkBufs& cb, uint32_t idx, int orient, uint64_t mat)
+{
+    if (ix.win[(uint32_t)(mat >> 32)].z == CPGDUMMY) return;
+    if (((mat >> 16) & 0xffu) == 0) {
+        meth_exact(ix, cb, idx, orient, mat);
+    } else {
+        const uint32_t slot = (uint32_t)atomicAdd(cb.ctr + CTR_DP, 1ull);
+        cb.dp_list[slot] = idx;
+        cb.dp_mat[slot] = mat;
+        cb.dp_orient[slot] = (uint8_t)orient;
+    }
+}
+
+// Writes the oriented mate into rd: orient 0 as read, 1 reverse complement.
+__device__ __forceinline__ void pe_orient(uint8_t* rd, const char* raw, uint32_t len, int orient)
+{
+    const int lane = threadIdx.x & 31;
+    for (uint32_t p = lane; p < len; p += 32) rd[p] = oriented_char(raw, len, orient, p);
+}
+
+template <int WMAX>
+__device__ bool pe_pair(const DevIndex& ix, const PeIndex& px, const ChunkBufs& cb, const PeMem& s, uint32_t r)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t n = cb.n;                 // pairs; mate 2 of pair r is read n + r
+    const uint32_t i1 = r, i2 = n + r;
+    const uint32_t n1 = (uint32_t)(cb.offs[i1 + 1] - cb.offs[i1]);
+    const uint32_t n2 = (uint32_t)(cb.offs[i2 + 1] - cb.offs[i2]);
+    uint32_t nh[4] = {0, 0, 0, 0};
+    // mates were validated by k_pe_prep: rflags bit0 length, bit1 non-ACGT
+    const uint8_t f1 = cb.rflags[i1], f2 = cb.rflags[i2];
+    if ((f1 | f2) & 3u) return true;     // counted and written by k_pe_prep
+    for (int o = 0; o < 2; ++o) {
+        if (!((cb.orient_mask >> o) & 1u)) continue;
+        // first = mate 1 (o = 0) or its reverse complement; second = the other strand of mate 2
+        pe_orient(s.rd[0], cb.seqs + cb.offs[i1], n1, o);
+        pe_orient(s.rd[1], cb.seqs + cb.offs[i2], n2, 1 - o);
+        for (uint32_t i = lane; i < s.c.vcap; i += 32) {
+            s.vk[0][i] = EMPTY_KEY;
+            s.vk[1][i] = EMPTY_KEY;
+            s.vv[0][i] = 0;
+            s.vv[1][i] = 0;
+        }
+        __syncwarp();
+        const uint32_t sigma = pe_kmers(ix, px, s, s.rd[0], n1);
+        PeState st{};
+        if (lane == 0) {
+            pe_count_first(ix, px, s, st, n1);
+            // rebuild: keep count1 >= QTHRESH
+            if (!st.over)
+                for (int dir = 0; dir < 2; ++dir)
+                    for (uint32_t x = 0; x < st.n1[dir]; ++x) {
+                        const int h = pm_find(s, dir, s.ins1[dir][x]);
+                        if (pv_c1(s.vv[dir][h]) < QTHRESH) s.vv[dir][h] = 0;
+                        else s.vv[dir][h] = PV_PRESENT | pv_c1(s.vv[dir][h]);
+                    }
+        }
+        bool over = __shfl_sync(0xffffffffu, st.over, 0);
+        if (over) return false;
+        bool any = false;
+        if (lane == 0)
+            for (int dir = 0; dir < 2 && !any; ++dir)
+                for (uint32_t x = 0; x < st.n1[dir]; ++x)
+                    if (pm_find(s, dir, s.ins1[dir][x]) >= 0) { any = true; break; }
+        any = __shfl_sync(0xffffffffu, any, 0);
+        if (!any) continue;
+        __syncwarp();
+        pe_kmers(ix, px, s, s.rd[1], n2);
+        bool hasCpG = false;
+        if (lane == 0) {
+            pe_count_second(ix, px, s, st, n2);
+            if (!st.over) {
+                // f2 flags (order-independent) and hasCpG
+                const int ctx = (int)px.ctx;
+                for (int dir = 0; dir < 2; ++dir)
+                    for (uint32_t hh = 0; hh < s.c.vcap; ++hh) {
+                        const uint32_t v = s.vv[dir][hh];
+                        const uint32_t key = s.vk[dir][hh];
+                        if (key == EMPTY_KEY || !(v & PV_PRESENT) || pv_c2(v) < QTHRESH) continue;
+                        s.vv[dir][hh] |= PV_F2;
+                        for (int c = 1; c <= ctx; ++c) {
+                            int h2 = pm_find(s, dir, key + (uint32_t)c);
+                            if (h2 >= 0) s.vv[dir][h2] |= PV_F2;
+                            h2 = pm_find(s, dir, key - (uint32_t)c);
+                            if (h2 >= 0) s.vv[dir][h2] |= PV_F2;
+                        }
+                    }
+                for (int dir = 0; dir < 2 && !hasCpG; ++dir)
+                    for (uint32_t hh = 0; hh < s.c.vcap; ++hh) {
+                        const uint32_t v = s.vv[dir][hh];
+                        const uint32_t key = s.vk[dir][hh];
+                        if (key != EMPTY_KEY && (v & PV_PRESENT) && (v & PV_F2) && ix.win[key].z != CPGDUMMY) {
+                            hasCpG = true;
+                            break;
+                        }
+                    }
+            }
+            if (hasCpG && !st.over) {
+                // final iteration orders: replay of the first map, kept keys, then the second mate's insertions
+                for (int dir = 0; dir < 2 && !st.over; ++dir) {
+                    uint32_t nt = 0;
+                    if (!pe_replay(s, s.ins1[dir], st.n1[dir], sigma / 5, s.ord[dir], nt)) { st.over = true; break; }
+                    uint32_t ns = 0;
+                    for (uint32_t q = 0; q < nt; ++q) {
+                        const uint32_t key = s.ord[dir][q];
+                        const int h = pm_find(s, dir, key);
+                        // kept keys are present with count1 >= QTHRESH; keys the second mate re-inserted
+                        // after the rebuild dropped them come later, from ins2
+                        if (h >= 0 && pv_c1(s.vv[dir][h]) >= QTHRESH) s.seq[ns++] = key;
+                    }
+                    for (uint32_t x = 0; x < st.n2[dir]; ++x) s.seq[ns++] = s.ins2[dir][x];
+                    if (!pe_replay(s, s.seq, ns, 20, s.ord[dir], st.nord[dir])) { st.over = true; break; }
+                }
+                if (!st.over) {
+                    uint64_t* ha = s.hits[o == 0 ? 0 : 2];
+                    uint64_t* hb = s.hits[o == 0 ? 1 : 3];
+                    pe_walk_any<WMAX>(ix, px, s, st, cb, i1, o, 0, ha, nh[o == 0 ? 0 : 2]);
+                    if (!st.over && nh[o == 0 ? 0 : 2] > 0)
+                        pe_walk_any<WMAX>(ix, px, s, st, cb, i2, 1 - o, 1, hb, nh[o == 0 ? 1 : 3]);
+                }
+            }
+        }
+        over = __shfl_sync(0xffffffffu, st.over, 0);
+        if (over) return false;
+        __syncwarp();
+    }
+    if (lane == 0) {
+        uint64_t* m1F = s.hits[0];
+        uint64_t* m2R = s.hits[1];
+        uint64_t* m1R = s.hits[2];
+        uint64_t* m2F = s.hits[3];
+        uint64_t mat1 = 0, mat2 = 0;
+        bool ok = false;
+        if ((nh[0] == 0 && nh[2] == 0) || (nh[1] == 0 && nh[3] == 0)) {
+            atomicAdd(cb.ctr + CTR_UNSUCC, 2ull);
+        } else {
+            const int WORST = 2 * (int)(MISCOUNT + ADDMIS) + 1;
+            int best = WORST;
+            bool nonUnique = false, orig = true;
+            uint64_t b1 = 0, b2 = 0;
+            if (cb.orient_mask & 1u)
+                for (uint32_t a = 0; a < nh[0]; ++a)
+                    for (uint32_t b = 0; b < nh[1]; ++b) {
+                        const int e = pe_extract(ix, px, m1F[a], m2R[b]);
+                        if (e < 0) continue;
+                        if (e == best) nonUnique = true;
+                        else if (e < best) { best = e; b1 = m1F[a]; b2 = m2R[b]; nonUnique = false; }
+                    }
+            if (cb.orient_mask & 2u)
+                for (uint32_t a = 0; a < nh[2]; ++a)
+                    for (uint32_t b = 0; b < nh[3]; ++b) {
+                        const int e = pe_extract(ix, px, m1R[a], m2F[b]);
+                        if (e < 0) continue;
+                        if (e == best) nonUnique = true;
+                        else if (e < best) { best = e; b1 = m1R[a]; b2 = m2F[b]; orig = false; nonUnique = false; }
+                    }
+            if (best == WORST) {
+                atomicAdd(cb.ctr + CTR_UNSUCC, 2ull);
+            } else if (nonUnique) {
+                atomicAdd(cb.ctr + CTR_NONU, 2ull);
+            } else {
+                ok = true;
+                mat1 = b1;
+                mat2 = b2;
+                if (cb.stranded) atomicAdd(cb.ctr + (orig ? CTR_R1F : CTR_R1R), 1ull);
+                pe_meth(ix, cb, i1, orig ? 0 : 1, b1);
+                pe_meth(ix, cb, i2, orig ? 1 : 0, b2);
+                const bool d1 = ix.win[(uint32_t)(b1 >> 32)].z == CPGDUMMY, d2 = ix.win[(uint32_t)(b2 >> 32)].z == CPGDUMMY;
+                if (d1 && d2) atomicAdd(cb.ctr + CTR_TOOSHORT, 2ull);
+                else if (d1 || d2) { atomicAdd(cb.ctr + CTR_TOOSHORT, 1ull); atomicAdd(cb.ctr + CTR_SUCC, 1ull); }
+                else { atomicAdd(cb.ctr + CTR_PAIRED, 1ull); atomicAdd(cb.ctr + CTR_SUCC, 2ull); }
+            }
+        }
+        cb.mats[i1] = ok ? mat1 : 0;
+        cb.mats[i2] = ok ? mat2 : 0;
+        cb.invalid[i1] = ok ? 0 : 1;
+        cb.invalid[i2] = ok ? 0 : 1;
+    }
+    __syncwarp();
+    return true;
+}
+
+// Mate checks of every pair (matchPairedReads, ReadQueue.cpp:968-1080): a mate
+// shorter than ceil(0.75 * READLEN) or with a letter other than ACGT is
+// invalid.  Pairs with an invalid mate are finished here: tooShort grows by 1
+// for a short mate and by 2 more for any invalid pair (the reference's
+// counting).  Sets CTR_WMASK bit W for the automaton width of valid pairs.
+__global__ void k_pe_prep(ChunkBufs cb, uint32_t readlen)
+{
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= cb.n) return;
+    const float minlen = ceilf((float)readlen * 0.75f);
+    uint32_t wmax = 0;
+    uint8_t f[2];
+    for (int m = 0; m < 2; ++m) {
+        const uint32_t i = m == 0 ? r : cb.n + r;
+        const uint64_t o0 = cb.offs[i];
+        const uint32_t len = (uint32_t)(cb.offs[i + 1] - o0);
+        uint8_t fl = 0;
+        if ((float)len < minlen) fl |= 1;
+        if (len > FAME_MAX_READ_LEN) fl |= 4;
+        for (uint32_t p = 0; p < len && !(fl & 2); ++p) {
+            const char c = cb.seqs[o0 + p];
+            if (c != 'A' && c != 'C' && c != 'G' && c != 'T') fl |= 2;
+        }
+        f[m] = fl;
+        cb.rflags[i] = fl;
+        wmax = max(wmax, len / 64 + 1);
+    }
+    const uint32_t i2 = cb.n + r;
+    // a mate longer than the widest automaton fails the whole call on the host
+    if ((f[0] | f[1]) & 4) atomicAdd(cb.ctr + CTR_TOO_LONG, 1ull);
+    if ((f[0] | f[1]) & 7) {
+        unsigned long long ts = 0;
+        if ((f[0] | f[1]) & 1) ts += 1;
+        ts += 2;
+        atomicAdd(cb.ctr + CTR_TOOSHORT, ts);
+        cb.mats[r] = 0;
+        cb.mats[i2] = 0;
+        cb.invalid[r] = (f[0] & 7) ? 1 : 0;
+        cb.invalid[i2] = (f[1] & 7) ? 1 : 0;
+        return;
+    }
+    atomicOr(cb.ctr + CTR_WMASK, 1ull << wmax);
+}
+
+// Pairs whose widest mate needs WMAX words; warp per pair, working memory in
+// shared memory, pairs over the caps go to the heavy list.
+template <int WMAX>
+__global__ void k_pe(DevIndex ix, PeIndex px, ChunkBufs cb, uint32_t warp_bytes)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int lane = threadIdx.x & 31;
+    const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+    const PeMem s = pe_mem(smem + (threadIdx.x >> 5) * warp_bytes, PE_LIGHT);
+    for (uint32_t r = wid; r < cb.n; r += nw) {
+        const uint32_t l1 = (uint32_t)(cb.offs[r + 1] - cb.offs[r]);
+        const uint32_t l2 = (uint32_t)(cb.offs[cb.n + r + 1] - cb.offs[cb.n + r]);
+        if ((cb.rflags[r] | cb.rflags[cb.n + r]) & 7u) continue;
+        if ((int)(max(l1, l2) / 64 + 1) != WMAX) continue;
+        if (!pe_pair<WMAX>(ix, px, cb, s, r)) {
+            if (lane == 0) {
+                const uint32_t k = (uint32_t)atomicAdd(cb.ctr + CTR_HEAVY, 1ull);
+                cb.heavy[k] = r;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Heavy pairs: same code with large caps in global scratch.
+__global__ void k_pe_heavy(DevIndex ix, PeIndex px, ChunkBufs cb, uint8_t* scratch, uint64_t warp_bytes, PeCaps caps)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+    const PeMem s = pe_mem(scratch + (uint64_t)wid * warp_bytes, caps);
+    const uint32_t nheavy = (uint32_t)cb.ctr[CTR_HEAVY];
+    for (uint32_t k = wid; k < nheavy; k += nw) {
+        const uint32_t r = cb.heavy[k];
+        if (!pe_pair<4>(ix, px, cb, s, r)) {
+            if (lane == 0) atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull);
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace fame

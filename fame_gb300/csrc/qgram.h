@@ -56,8 +56,6 @@ FAME_HD uint32_t qg_symrev(uint32_t key, uint32_t q)
     return r;
 }
 
-FAME_HD uint32_t qg_bloom_bit(uint32_t key) { return (key * 0x9E3779B1u) >> 26; }
-
 // Spans for one window whose text is the packed-genome range [G0, G1)
 // (forward: scan position u = genome G0 + u; reverse: u = genome G1 - 1 - u).
 // pkey[k]: scan-order key of piece k (first symbol most significant), valid
@@ -68,19 +66,27 @@ FAME_HD int qgram_spans(const uint32_t* gpack, const uint32_t* gnmask, uint64_t 
                         uint32_t q, const uint32_t* pkey, uint32_t pvalid, const uint32_t* pstart, int32_t* ilo,
                         int32_t* ihi)
 {
-    if (G1 <= G0 || q == 0 || q > 16) return 0;
+    if (G1 <= G0 || q == 0 || q > 16 || !(pvalid & ((1u << QG_PIECES) - 1))) return 0;
+    pvalid &= (1u << QG_PIECES) - 1;
     const int32_t len = (int32_t)(G1 - G0);
-    uint32_t ckey[QG_PIECES];
-    uint64_t bloom = 0;
-    for (int k = 0; k < QG_PIECES; ++k) {
-        ckey[k] = fwd ? qg_symrev(pkey[k], q) : pkey[k];
-        if ((pvalid >> k) & 1u) bloom |= 1ull << qg_bloom_bit(ckey[k]);
-    }
-    if (!bloom) return 0;
     const uint32_t qmask = q >= 16 ? 0xffffffffu : ((1u << (2 * q)) - 1);
+    // compare keys in genome order; an invalid piece repeats the key of the
+    // first valid one (the hit path skips it)
+#if defined(__CUDA_ARCH__)
+    const int kv = __ffs(pvalid) - 1;
+#else
+    const int kv = __builtin_ctz(pvalid);
+#endif
+    const uint32_t kfill = fwd ? qg_symrev(pkey[kv], q) : pkey[kv];
+    uint32_t ckey[QG_PIECES];
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int k = 0; k < QG_PIECES; ++k)
+        ckey[k] = ((pvalid >> k) & 1u) ? (fwd ? qg_symrev(pkey[k], q) : pkey[k]) : kfill;
     const uint32_t nq = (1u << q) - 1;
     const uint64_t w0 = G0 >> 4, w1 = (G1 - 1) >> 4;
-    uint64_t catS = 0;          // reduced symbols: previous word in bits 0..31, current in 32..63
+    uint64_t catS = 0;           // reduced symbols: previous word in bits 0..31, current in 32..63
     uint32_t catN = 0xffffffffu; // excluded bases (N or outside the window), one bit per base, same layout
     int n = 0;
     for (uint64_t wi = w0; wi <= w1; ++wi) {
@@ -92,12 +98,24 @@ FAME_HD int qgram_spans(const uint32_t* gpack, const uint32_t* gnmask, uint64_t 
         // q-gram ending at base i of this word starts at bit 17 + i - q
         const uint64_t sS = catS >> (2 * (17 - q));
         const uint32_t sN = catN >> (17 - q);
-        const bool anyN = sN != 0;
+        // positions whose key equals a piece key (branch-free; hits are rare)
+        uint32_t hm = 0;
+#if defined(__CUDA_ARCH__)
 #pragma unroll
+#endif
         for (int i = 0; i < 16; ++i) {
-            if (anyN && ((sN >> i) & nq)) continue;
             const uint32_t key = (uint32_t)(sS >> (2 * i)) & qmask;
-            if (!((bloom >> qg_bloom_bit(key)) & 1ull)) continue;
+            bool eq = false;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+            for (int k = 0; k < QG_PIECES; ++k) eq |= key == ckey[k];
+            hm |= (eq ? 1u : 0u) << i;
+        }
+        if (!hm) continue;
+        for (int i = 0; i < 16; ++i) {
+            if (!((hm >> i) & 1u) || ((sN >> i) & nq)) continue;
+            const uint32_t key = (uint32_t)(sS >> (2 * i)) & qmask;
             const int64_t A = (int64_t)(16 * wi + (uint64_t)i) - (int64_t)q + 1;   // genome start of the q-gram
             const int32_t x = fwd ? (int32_t)(A - (int64_t)G0) : (int32_t)((int64_t)G1 - A - (int64_t)q);
             for (int k = 0; k < QG_PIECES; ++k) {

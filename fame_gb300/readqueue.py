@@ -112,6 +112,81 @@ class ReadQueue:
         return tot
 
 
+class PairedReadQueue:
+    """Paired-end chunk loop: the two-file ReadQueue with matchPairedReads
+    (ReadQueue.cpp:940-1658) on the GPU and queryRoutinePaired
+    (main.cpp:400-441).  maxpdist is the MAXPDIST of the reference build
+    (CONST.h:42)."""
+
+    def __init__(self, reads1, reads2, index: HostIndex, gpu: GpuMatcher, maxpdist: int, is_gz: bool = False,
+                 both_strands: bool = False, chunk_size: int = CHUNKSIZE):
+        self.src = [(_FastqSource(r, is_gz) if isinstance(r, str) else _ListSource(list(r))) for r in (reads1, reads2)]
+        self.index = index
+        self.gpu = gpu
+        self.maxpdist = maxpdist
+        self.chunk_size = chunk_size
+        self.both_strands_flag = both_strands
+        self.r1_fwd_matches = 0
+        self.r1_rev_matches = 0
+        self.match_r1_fwd = True
+        self.buffer = ([], [])
+        self.mats = (np.zeros(0, np.uint64), np.zeros(0, np.uint64))
+        self.invalid = (np.zeros(0, np.uint8), np.zeros(0, np.uint8))
+
+    def parse_chunk(self):
+        """Returns (procReads, more): the pairs read, more iff a full chunk was read."""
+        b1 = self.src[0].take(self.chunk_size)
+        b2 = self.src[1].take(len(b1))
+        if len(b2) != len(b1):
+            raise ValueError("mate files hold different numbers of reads")
+        self.buffer = (b1, b2)
+        return len(b1), len(b1) >= self.chunk_size
+
+    def match_paired_reads(self, proc_reads: int, get_stranded: bool):
+        """Match pairs buffer[:proc_reads]; returns this call's PairCounters."""
+        packed = []
+        for mates in self.buffer:
+            seqs = mates[:proc_reads]
+            offs = np.zeros(len(seqs) + 1, dtype=np.uint64)
+            np.cumsum([len(x) for x in seqs], out=offs[1:])
+            packed.append((b"".join(seqs), offs))
+        flags = (FAME_GET_STRANDED if get_stranded else 0) | (FAME_BOTH_STRANDS if self.both_strands_flag else 0) | \
+            (FAME_MATCH_R1_FWD if self.match_r1_fwd else 0)
+        m1, m2, i1, i2, cnt = self.gpu.match_pairs(packed[0][0], packed[0][1], packed[1][0], packed[1][1], flags,
+                                                   self.maxpdist)
+        self.mats, self.invalid = (m1, m2), (i1, i2)
+        self.r1_fwd_matches += cnt.r1_fwd
+        self.r1_rev_matches += cnt.r1_rev
+        return cnt
+
+    def decide_strand(self):
+        self.match_r1_fwd = self.r1_fwd_matches > self.r1_rev_matches
+
+    def print_methylation_levels(self, basename: str):
+        write_cpg_report(basename + "_cpg.tsv", self.index, self.gpu.tallies(reset=False))
+
+    def query_routine_paired(self):
+        """main.cpp:400-441; returns the summed counters."""
+        keys = ("succ", "nonunique", "unsucc", "paired", "too_short")
+        tot = dict.fromkeys(keys, 0)
+
+        def add(c):
+            for k in keys:
+                tot[k] += getattr(c, k)
+
+        if not self.both_strands_flag:
+            n, _ = self.parse_chunk()
+            add(self.match_paired_reads(n, True))
+            self.decide_strand()
+        while True:
+            n, more = self.parse_chunk()
+            if not more:
+                break
+            add(self.match_paired_reads(n, False))
+        add(self.match_paired_reads(n, False))
+        return tot
+
+
 def write_cpg_report(path: str, index: HostIndex, meth: np.ndarray):
     """printMethylationLevels (ReadQueue.cpp:1860-1893)."""
     t = index.tables()

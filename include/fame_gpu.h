@@ -131,6 +131,36 @@ int fame_gpu_match_reads(fame_gpu* g, const char* seqs, const uint64_t* offs, ui
 int fame_gpu_match_reads_dev(fame_gpu* g, const char* seqs_dev, const uint64_t* offs_dev, uint32_t n,
                              uint32_t flags, uint64_t* mats_dev, uint8_t* invalid_dev, fame_counters* cnt);
 
+/* Counters of the paired path (matchPairedReads' statistics): mates counted as
+ * the reference counts them (a uniquely paired pair adds 2 to succ). */
+typedef struct {
+    uint64_t succ;        /* successfully matched mates                          */
+    uint64_t nonunique;   /* mates of pairs with two equally good pairings       */
+    uint64_t unsucc;      /* mates of pairs without a pairing                    */
+    uint64_t paired;      /* pairs with both mates in windows holding CpGs       */
+    uint64_t too_short;   /* tooShort: short or invalid mates, mates without CpG windows */
+    uint64_t r1_fwd;      /* getStranded votes: the first mate matched forward   */
+    uint64_t r1_rev;
+    uint64_t dp_reads;    /* mates whose CpG calls needed the banded DP          */
+    uint64_t heavy_pairs; /* pairs run with the large-capacity scratch           */
+} fame_pair_counters;
+
+/* Paired-end matching of one chunk of n read pairs, replacing the body of
+ * ReadQueue::matchPairedReads (ReadQueue.cpp:940-1658; called per chunk by
+ * queryRoutinePaired, main.cpp:400-441).  Mate 1 of pair i is
+ * seqs1[offs1[i] .. offs1[i+1]), mate 2 likewise in seqs2; flags as for
+ * fame_gpu_match_reads (FAME_GET_STRANDED on the first chunk unless
+ * FAME_BOTH_STRANDS; FAME_MATCH_R1_FWD after decideStrand).  maxpdist is the
+ * MAXPDIST the reference is compiled with (CONST.h:42): it sets the mate
+ * context (contextWLen = floor(maxpdist / 2048) + 1 windows) and the pairing
+ * distance (maxpdist + READLEN, extractPairedMatch, ReadQueue.cpp:3255-3275).
+ * Outputs per pair: the MATCH::match of each mate (0 when invalid) and the
+ * isInvalid flags; CpG calls of uniquely paired mates go to the tallies.
+ * Mates longer than FAME_MAX_READ_LEN give FAME_ERR_READ. */
+int fame_gpu_match_pairs(fame_gpu* g, const char* seqs1, const uint64_t* offs1, const char* seqs2,
+                         const uint64_t* offs2, uint32_t n, uint32_t flags, uint32_t maxpdist, uint64_t* mats1,
+                         uint64_t* mats2, uint8_t* invalid1, uint8_t* invalid2, fame_pair_counters* cnt);
+
 /* Copy out the methylation tallies as methLevels (ReadQueue.h:354-367): four
  * uint16 per CpG in cpgTable order {methFwd, unmethFwd, methRev, unmethRev}
  * with the reference's 16-bit wrap-around; reset != 0 zeroes them afterwards

@@ -49,3 +49,8 @@ def oracle_index(golden_genome):
 def product_index(golden_genome):
     from fame_gb300 import HostIndex
     return HostIndex.build(golden_genome, readlen=100)
+
+
+@pytest.fixture(scope="session")
+def pe_golden():
+    return dict(np.load(os.path.join(GOLDEN, "pe_small.npz"), allow_pickle=True))

@@ -83,3 +83,18 @@ def test_matching_matches_reference(golden, oracle_index):
     c = golden["default_counters"]
     assert c[0] > 5000 and c[1] > 0 and c[2] > 0
     assert golden["default_meth"].astype(np.int64).sum() > 3000
+
+
+PE_MODES = (("default", 0, False), ("chunk700", 700, False), ("both", 900, True))
+
+
+def test_paired_matching_matches_reference(pe_golden, oracle_index):
+    """matchPairedReads per chunk (queryRoutinePaired) on the paired fixture:
+    per-mate matches, invalid flags, tallies and counters equal the reference's."""
+    g = pe_golden
+    s1, o1 = g["read_seq1"].tobytes(), g["read_offs1"]
+    s2, o2 = g["read_seq2"].tobytes(), g["read_offs2"]
+    for name, chunk, both in PE_MODES:
+        r = oracle_index.match_pe(s1, o1, s2, o2, chunk=chunk, both_strands=both, maxpdist=int(g["maxpdist"]))
+        for k in ("mat1", "mat2", "inv1", "inv2", "meth", "counters"):
+            assert np.array_equal(r[k], g["%s_%s" % (name, k)]), (name, k)
