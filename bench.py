@@ -130,6 +130,17 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
+def make_pair_workload(name, n_pairs):
+    from fame_gb300 import synth
+    spec = synth.WORKLOADS[name]
+    g = synth.make_genome(**spec["genome"])
+    pk = dict(spec["pairs"])
+    if n_pairs:
+        pk["n_pairs"] = n_pairs
+    r1, r2 = synth.make_pairs(g, **pk)
+    return g, r1, r2
+
+
 def make_workload(name, n_reads):
     from fame_gb300 import synth
     spec = synth.WORKLOADS[name]
@@ -330,6 +341,142 @@ def run_gb300(args):
         print(json.dumps(out))
 
 
+PE_METRIC = "aligned read pairs/s (paired-end matching stage, bit-exact CpG report)"
+PE_MAXPDIST = 550   # the MAXPDIST the reference library is compiled with (CONST.h:42)
+
+
+def run_gb300_pe(args):
+    """Paired-end form: one step = one 300k-pair chunk through matchPairedReads
+    semantics (fame_gpu_match_pairs_dev; mates resident in HBM), e2e through
+    fame_gpu_match_pairs from pinned host buffers."""
+    import ctypes
+    import torch
+    from fame_gb300 import FAME_GET_STRANDED, FAME_MATCH_R1_FWD, GpuMatcher, HostIndex, CHUNKSIZE
+    from fame_gb300._lib import lib as _L
+    t0 = time.time()
+    g, r1, r2 = make_pair_workload(args.workload, args.reads)
+    t_gen = time.time() - t0
+    t0 = time.time()
+    hi = HostIndex.build(g.seqs, readlen=100, threads=0)
+    t_build = time.time() - t0
+    gm = GpuMatcher(hi, 0)
+    s1, o1 = r1.concat()
+    s2, o2 = r2.concat()
+    n = len(o1) - 1
+    chunks = [(c0, min(n, c0 + CHUNKSIZE)) for c0 in range(0, n, CHUNKSIZE)]
+    dev, pinned = [], []
+    maxn = max(b - a for a, b in chunks)
+    d_mat = gm.alloc(16 * maxn)
+    d_inv = gm.alloc(2 * maxn)
+    for a, b in chunks:
+        m1 = np.frombuffer(s1, np.uint8)[int(o1[a]):int(o1[b])]
+        m2 = np.frombuffer(s2, np.uint8)[int(o2[a]):int(o2[b])]
+        oo = np.concatenate([o1[a:b + 1] - o1[a], (o2[a + 1:b + 1] - o2[a]) + (o1[b] - o1[a])]).astype(np.uint64)
+        buf = np.concatenate([m1, m2])
+        d_s = gm.alloc(len(buf))
+        d_o = gm.alloc(8 * len(oo))
+        gm.memcpy(d_s, buf.ctypes.data, len(buf), 1)
+        gm.memcpy(d_o, oo.ctypes.data, 8 * len(oo), 1)
+        dev.append((d_s, d_o, b - a))
+        h1 = gm.host_alloc(len(m1)); h1[:] = m1
+        h2 = gm.host_alloc(len(m2)); h2[:] = m2
+        ho1 = gm.host_alloc(8 * (b - a + 1)).view(np.uint64); ho1[:] = o1[a:b + 1] - o1[a]
+        ho2 = gm.host_alloc(8 * (b - a + 1)).view(np.uint64); ho2[:] = o2[a:b + 1] - o2[a]
+        pinned.append((h1, ho1, h2, ho2, b - a))
+    p_stream = ctypes.c_void_p()
+    _L().fame_gpu_stream(gm.h, ctypes.byref(p_stream))
+    stream = torch.cuda.ExternalStream(p_stream.value, device=0)
+    d_s, d_o, nn = dev[0]
+    c = gm.match_pairs_dev(d_s, d_o, nn, FAME_GET_STRANDED, PE_MAXPDIST, d_mat, d_inv)
+    flags = FAME_MATCH_R1_FWD if c.r1_fwd > c.r1_rev else 0
+    steady = list(range(1, len(chunks))) or [0]
+    for w in range(max(0, args.warmup - 1)):
+        d_s, d_o, nn = dev[steady[w % len(steady)]]
+        gm.match_pairs_dev(d_s, d_o, nn, flags, PE_MAXPDIST, d_mat, d_inv)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pairs = 0
+    launches = 0
+    heavy = 0
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        ev0.record(stream)
+        for k in range(args.steps):
+            d_s, d_o, nn = dev[steady[k % len(steady)]]
+            c = gm.match_pairs_dev(d_s, d_o, nn, flags, PE_MAXPDIST, d_mat, d_inv)
+            pairs += nn
+            heavy += c.heavy_pairs
+            launches += gm.last_launches()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    t_dev = ev0.elapsed_time(ev1) / 1e3
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    e_pairs = h2d = d2h = 0
+    for k in range(args.steps):
+        h1, ho1, h2, ho2, nn = pinned[steady[k % len(steady)]]
+        gm.match_pairs(h1, ho1, h2, ho2, flags, PE_MAXPDIST)
+        e_pairs += nn
+        h2d += h1.nbytes + h2.nbytes + 16 * (nn + 1)
+        d2h += 18 * nn
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = ev0.elapsed_time(ev1) / 1e3
+    out = {
+        "metric": PE_METRIC, "value": pairs / t_dev, "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 integer",
+        "data": "synthetic (seeded; genome and bisulfite read pairs per the workload definition)",
+        "config": {"workload": args.workload, "genome_bp": int(g.total_len), "pairs_total": n, "read_len": 100,
+                   "chunk_pairs": CHUNKSIZE, "maxpdist": PE_MAXPDIST, "parallelism": "single GPU",
+                   "l2": "inputs larger than L2: each step gathers from a 6.5 GB index and new pairs"},
+        "e2e": {"value": e_pairs / t_e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d / args.steps),
+                "d2h_bytes_per_step": int(d2h / args.steps)},
+        "gpu_launches": launches, "heavy_pairs": heavy, "clocks": clk.summary(),
+        "setup_seconds": {"generate": t_gen, "index_build": t_build},
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_pe(hi, s1, o1, s2, o2, chunks, args.cpu_sample)
+    for d_s, d_o, _ in dev:
+        gm.free(d_s)
+        gm.free(d_o)
+    gm.close()
+    print(json.dumps(out))
+
+
+def cpu_baseline_pe(hi, s1, o1, s2, o2, chunks, sample):
+    """The reference's OpenMP matchPairedReads on a bounded sample of chunk 1."""
+    try:
+        from oracle import refbind
+        if not refbind.available():
+            raise RuntimeError("reference library not built")
+        L = refbind.RefLib()
+        t = hi.tables(sparse=False)
+
+        class Arrays:
+            pass
+
+        a = Arrays()
+        a.chrom_seqs = hi.chrom_seqs()
+        a.chrom_names = hi.chrom_names()
+        for k, v in t.items():
+            setattr(a, k, v)
+        a.tab_index64 = hi.tab_index64
+        ri = L.from_arrays(a)
+        c0, c1 = chunks[1] if len(chunks) > 1 else chunks[0]
+        nn = min(sample, c1 - c0)
+        p1 = o1[c0:c0 + nn + 1]
+        p2 = o2[c0:c0 + nn + 1]
+        secs, cnt = ri.time_pe(s1[int(p1[0]):int(p1[-1])], p1 - p1[0], s2[int(p2[0]):int(p2[-1])], p2 - p2[0],
+                               both_strands=False, match_r1_fwd=True)
+        ri.close()
+        return {"value": nn / secs, "unit": "pairs/s", "cores": L.corenum, "kind": "reference",
+                "sample": "%d pairs of chunk 1, decided orientation, matchPairedReads only, CORENUM=%d OpenMP "
+                          "threads, MAXPDIST %d" % (nn, L.corenum, L.maxpdist()), "seconds": secs,
+                "succ": int(cnt[0])}
+    except Exception as e:
+        return {"value": None, "unit": "pairs/s", "cores": 1, "kind": "port", "sample": "reference unavailable (%s)" % e}
+
+
 def run_reference(args):
     rank, world, local = dist_init(args.gpus)
     if rank != 0:
@@ -385,5 +532,7 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload.startswith("pe"):
+        run_gb300_pe(a)
     else:
         run_gb300(a)

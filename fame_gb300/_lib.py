@@ -63,7 +63,7 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_gpu_open", "fame_gpu_close", "fame_gpu_last_error", "fame_gpu_match_reads",
            "fame_gpu_match_reads_dev", "fame_gpu_tallies", "fame_gpu_alloc", "fame_gpu_free", "fame_gpu_memcpy",
            "fame_gpu_host_alloc", "fame_gpu_host_free", "fame_gpu_stream", "fame_gpu_set_timing",
-           "fame_gpu_stage_times", "fame_gpu_last_launches", "fame_gpu_match_pairs"]
+           "fame_gpu_stage_times", "fame_gpu_last_launches", "fame_gpu_match_pairs", "fame_gpu_match_pairs_dev"]
 
 _lib = None
 
@@ -102,6 +102,7 @@ def lib(build_if_missing: bool = True):
     L.fame_gpu_stage_times.argtypes = [_P, _P, C.c_int]
     L.fame_gpu_last_launches.argtypes = [_P]
     L.fame_gpu_match_pairs.argtypes = [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]
+    L.fame_gpu_match_pairs_dev.argtypes = [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P]
     _lib = L
     return L
 
@@ -269,6 +270,12 @@ class GpuMatcher:
         _check(lib().fame_gpu_match_pairs(self.h, _ptr(b1), _ptr(offs1), _ptr(b2), _ptr(offs2), n, flags, maxpdist,
                                           _ptr(m1), _ptr(m2), _ptr(i1), _ptr(i2), C.byref(cnt)), self.h)
         return m1, m2, i1, i2, cnt
+
+    def match_pairs_dev(self, seqs_dev, offs_dev, n: int, flags: int, maxpdist: int, mats_dev, invalid_dev):
+        cnt = PairCounters()
+        _check(lib().fame_gpu_match_pairs_dev(self.h, seqs_dev, offs_dev, n, flags, maxpdist, mats_dev, invalid_dev,
+                                              C.byref(cnt)), self.h)
+        return cnt
 
     def match_reads_dev(self, seqs_dev, offs_dev, n: int, flags: int, mats_dev, invalid_dev):
         cnt = Counters()

@@ -582,6 +582,16 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
 
 }  // namespace
 
+extern "C" int fame_gpu_match_pairs_dev(fame_gpu* g, const char* seqs_dev, const uint64_t* offs_dev, uint32_t n,
+                                        uint32_t flags, uint32_t maxpdist, uint64_t* mats_dev, uint8_t* invalid_dev,
+                                        fame_pair_counters* cnt)
+{
+    if (!g || (n && (!seqs_dev || !offs_dev || !mats_dev || !invalid_dev))) return FAME_ERR_ARG;
+    CK(cudaSetDevice(g->device));
+    if (n == 0) return FAME_OK;
+    return run_pairs(g, seqs_dev, offs_dev, n, flags, maxpdist, mats_dev, invalid_dev, cnt);
+}
+
 extern "C" int fame_gpu_match_pairs(fame_gpu* g, const char* seqs1, const uint64_t* offs1, const char* seqs2,
                                     const uint64_t* offs2, uint32_t n, uint32_t flags, uint32_t maxpdist,
                                     uint64_t* mats1, uint64_t* mats2, uint8_t* invalid1, uint8_t* invalid2,

@@ -173,7 +173,9 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
         else s.seq[len - 1 - p] = rc_byte(c);
     }
     __syncwarp();
-    // 1. hashes and bucket bounds (getSeedRefs pass 1, ReadQueue.cpp:2331-2354)
+    // 1. hashes and bucket bounds (getSeedRefs pass 1, ReadQueue.cpp:2331-2354):
+    //    every lane first hashes its k-mers, then issues all of its bucket
+    //    reads before using any, so their DRAM latencies overlap
     const uint32_t nk = len - KMERLEN + 1;
     uint32_t sigma = 0;
     unsigned long long gb = 0;
@@ -182,12 +184,30 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
 #pragma unroll
         for (uint32_t i = 0; i < KMERLEN; ++i)
             if ((SEEDBITS >> (31 - i)) & 1u) h ^= rotl64(nt_val(s.seq[p + i]), 31 - i);
-        const uint32_t key = (uint32_t)(h & HTAB_MASK);
-        const uint32_t b0 = __ldg(ix.tab + key), b1 = __ldg(ix.tab + key + 1);
-        s.kst[p] = b0;
-        s.kpre[p] = b1 - b0;
-        sigma += b1 - b0;
-        gb += 8 + 4ull * (b1 - b0);
+        s.kst[p] = (uint32_t)(h & HTAB_MASK);
+    }
+    {
+        constexpr int KPL = (FAME_MAX_READ_LEN - KMERLEN + 1 + 31) / 32;   // k-mers per lane, at most
+        uint32_t b0[KPL], b1[KPL];
+#pragma unroll
+        for (int j = 0; j < KPL; ++j) {
+            const uint32_t p = lane + 32 * j;
+            if (p < nk) {
+                const uint32_t key = s.kst[p];
+                b0[j] = __ldg(ix.tab + key);
+                b1[j] = __ldg(ix.tab + key + 1);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < KPL; ++j) {
+            const uint32_t p = lane + 32 * j;
+            if (p < nk) {
+                s.kst[p] = b0[j];
+                s.kpre[p] = b1[j] - b0[j];
+                sigma += b1[j] - b0[j];
+                gb += 8 + 4ull * (b1[j] - b0[j]);
+            }
+        }
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -216,12 +236,27 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
     const uint32_t T = s.kpre[nk];
     if (T > s.ops_cap) return 1;
     if (lane == 0) atomicAdd(gather_bytes_acc, gb);
-    // 2. gather entries (getSeedRefs pass 2, ReadQueue.cpp:2361-2460)
+    // 2. gather entries (getSeedRefs pass 2, ReadQueue.cpp:2361-2460): the
+    //    k-mer of every op first, then the entry reads, up to 8 per lane in flight
     for (uint32_t p = lane; p < nk; p += 32) {
-        const uint32_t b = s.kpre[p], n = s.kpre[p + 1] - b, st = s.kst[p];
-        for (uint32_t j = 0; j < n; ++j) {
-            s.ops[b + j] = __ldg(ix.entry + st + j);
-            s.opk[b + j] = (uint8_t)p;
+        const uint32_t b = s.kpre[p], n = s.kpre[p + 1] - b;
+        for (uint32_t j = 0; j < n; ++j) s.opk[b + j] = (uint8_t)p;
+    }
+    __syncwarp();
+    for (uint32_t base = 0; base < T; base += 256) {
+        uint32_t e[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint32_t i = base + lane + 32 * j;
+            if (i < T) {
+                const uint32_t p = s.opk[i];
+                e[j] = __ldg(ix.entry + s.kst[p] + (i - s.kpre[p]));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint32_t i = base + lane + 32 * j;
+            if (i < T) s.ops[i] = e[j];
         }
     }
     // 3. distinct keys with counts and first op (consecutive duplicates within a
@@ -287,6 +322,27 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
     uint32_t nstage = 0, nf = 0;
     bool fail = false;
     for (int dir = 1; dir >= 0; --dir) {
+        // A map with at most one candidate (count >= QTHRESH) needs no replay:
+        // its walk sees that candidate alone, wherever the other keys sit.
+        uint32_t ndc = 0, only = 0;
+        for (uint32_t b0 = 0; b0 < nins; b0 += 32) {
+            const uint32_t x = b0 + lane;
+            const uint32_t v = x < nins ? s.ins[x] : 0u;
+            const bool take = x < nins && (v >> 31) == (uint32_t)dir && (s.ins_cnt[x] & 0xffffu) >= QTHRESH;
+            const unsigned bm = __ballot_sync(0xffffffffu, take);
+            if (bm) {
+                const uint32_t first = __shfl_sync(0xffffffffu, v, __ffs(bm) - 1);
+                if (ndc == 0) only = first;
+            }
+            ndc += __popc(bm);
+        }
+        if (ndc <= 1) {
+            if (ndc == 1 && lane == 0) s.stage[nstage] = only;
+            nstage += ndc;
+            __syncwarp();
+            if (dir == 1) nf = nstage;
+            continue;
+        }
         MapSim m;
         sim_init(m, sigma / 5);
         m.nb = 0; m.novf = 0; m.sp = 0;

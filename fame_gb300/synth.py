@@ -249,6 +249,9 @@ WORKLOADS = {
     "se100_300mbp": dict(genome=dict(chrom_lengths=[37_500_000] * 8, seed=11, meth_p=0.7,
                                      repeat_frac=0.08),
                          reads=dict(n_reads=5_000_000, seed=12, sub_rate=0.01, indel_rate=0.001)),
+    # the 300 Mbp genome above, 1.5M pairs of 2 x 100 bp, inner distance U[20, 400]
+    "pe100_300mbp": dict(genome=dict(chrom_lengths=[37_500_000] * 8, seed=11, meth_p=0.7, repeat_frac=0.08),
+                         pairs=dict(n_pairs=1_500_000, seed=13, inner=(20, 400), sub_rate=0.01, indel_rate=0.001)),
     # 24 chromosomes / 3.0 Gbp, 45% repeats, READLEN 150 uneven trimmed reads
     "se150_uneven_3gbp": dict(genome=dict(chrom_lengths=_mammal_lengths(), seed=21, meth_p=0.75,
                                           repeat_frac=0.45),

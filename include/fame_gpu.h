@@ -161,6 +161,12 @@ int fame_gpu_match_pairs(fame_gpu* g, const char* seqs1, const uint64_t* offs1, 
                          const uint64_t* offs2, uint32_t n, uint32_t flags, uint32_t maxpdist, uint64_t* mats1,
                          uint64_t* mats2, uint8_t* invalid1, uint8_t* invalid2, fame_pair_counters* cnt);
 
+/* The same with the mates already in device memory, concatenated: mate 1 of
+ * pair i is read i and mate 2 is read n + i of (seqs_dev, offs_dev[2n + 1]);
+ * mats_dev and invalid_dev hold 2n entries in that order. */
+int fame_gpu_match_pairs_dev(fame_gpu* g, const char* seqs_dev, const uint64_t* offs_dev, uint32_t n, uint32_t flags,
+                             uint32_t maxpdist, uint64_t* mats_dev, uint8_t* invalid_dev, fame_pair_counters* cnt);
+
 /* Copy out the methylation tallies as methLevels (ReadQueue.h:354-367): four
  * uint16 per CpG in cpgTable order {methFwd, unmethFwd, methRev, unmethRev}
  * with the reference's 16-bit wrap-around; reset != 0 zeroes them afterwards

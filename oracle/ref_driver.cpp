@@ -442,6 +442,38 @@ int fame_ref_match_pe(void* ref, const char* s1, const uint64_t* o1, const char*
     return 0;
 }
 
+// Seconds spent in matchPairedReads for already-stranded chunks (the steady
+// state of queryRoutinePaired after decideStrand); counters: [succ, nonunique,
+// unsucc, succPaired, tooShort].
+int fame_ref_time_pe(void* ref, const char* s1, const uint64_t* o1, const char* s2, const uint64_t* o2, uint32_t n,
+                     int both_strands, int match_r1_fwd, uint64_t* counters, double* seconds)
+{
+    RefGenome& r = *static_cast<RefGenome*>(ref);
+    ReadQueue* rq = in_tmp([&] { return new ReadQueue("/dev/null", "/dev/null", r, false, both_strands != 0); });
+    rq->matchR1Fwd = match_r1_fwd != 0;
+    uint64_t succ = 0, nonu = 0, unsucc = 0, paired = 0, tooShort = 0;
+    double secs = 0.0;
+    std::string id("r");
+    const uint32_t chunk = MyConst::CHUNKSIZE;
+    for (uint32_t c0 = 0; c0 < n; c0 += chunk) {
+        const uint32_t cn = std::min<uint32_t>(chunk, n - c0);
+        for (uint32_t j = 0; j < cn; ++j) {
+            std::string a(s1 + o1[c0 + j], s1 + o1[c0 + j + 1]);
+            std::string b(s2 + o2[c0 + j], s2 + o2[c0 + j + 1]);
+            rq->readBuffer[j] = Read(a, id);
+            rq->readBuffer2[j] = Read(b, id);
+        }
+        auto t0 = std::chrono::steady_clock::now();
+        rq->matchPairedReads(cn, succ, nonu, unsucc, paired, tooShort, false);
+        auto t1 = std::chrono::steady_clock::now();
+        secs += std::chrono::duration<double>(t1 - t0).count();
+    }
+    counters[0] = succ; counters[1] = nonu; counters[2] = unsucc; counters[3] = paired; counters[4] = tooShort;
+    *seconds = secs;
+    delete rq;
+    return 0;
+}
+
 // std::sort with the paired path's comparator (cmpMetaFirst, ReadQueue.h:340-346):
 // input in the given order, output the keys in sorted order (pins the tie order).
 int fame_ref_sort_desc(const uint32_t* keys, const uint8_t* counts, uint32_t n, uint32_t* out)

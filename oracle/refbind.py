@@ -38,6 +38,10 @@ class RefLib:
         L.fame_ref_shiftand.argtypes = [C.c_char_p, C.c_uint32, C.c_char_p, C.c_uint32, C.c_int, _P, _P, C.c_uint32]
         self.corenum = L.fame_ref_corenum()
         self.readlen = L.fame_ref_readlen()
+        self.maxpdist_value = L.fame_ref_maxpdist()
+
+    def maxpdist(self) -> int:
+        return int(self.maxpdist_value)
 
     # --- index -------------------------------------------------------------
     def build(self, fasta: str, noloss: bool = False):
@@ -143,6 +147,23 @@ class RefIndex:
         buf = np.frombuffer(seq_bytes, dtype=np.uint8)
         offs = np.ascontiguousarray(offs, dtype=np.uint64)
         f(self.h, _ptr(buf), _ptr(offs), n, int(both_strands), int(match_r1_fwd), _ptr(cnt), _ptr(secs))
+        return float(secs[0]), cnt
+
+    def time_pe(self, s1: bytes, o1, s2: bytes, o2, both_strands: bool = False, match_r1_fwd: bool = True):
+        """Seconds spent in matchPairedReads for already-stranded chunks, and
+        [succ, nonunique, unsucc, succPaired, tooShort]."""
+        import ctypes as C
+        f = self.L.lib.fame_ref_time_pe
+        f.argtypes = [_P, _P, _P, _P, _P, C.c_uint32, C.c_int, C.c_int, _P, _P]
+        n = len(o1) - 1
+        cnt = np.zeros(5, np.uint64)
+        secs = np.zeros(1, np.float64)
+        b1 = np.frombuffer(s1, np.uint8)
+        b2 = np.frombuffer(s2, np.uint8)
+        o1 = np.ascontiguousarray(o1, np.uint64)
+        o2 = np.ascontiguousarray(o2, np.uint64)
+        f(self.h, _ptr(b1), _ptr(o1), _ptr(b2), _ptr(o2), n, int(both_strands), int(match_r1_fwd), _ptr(cnt),
+          _ptr(secs))
         return float(secs[0]), cnt
 
     def match_pe(self, s1: bytes, o1, s2: bytes, o2, chunk: int = 0, both_strands: bool = False):
