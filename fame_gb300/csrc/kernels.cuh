@@ -907,14 +907,28 @@ namespace fame {
 constexpr uint32_t DP3_GROUPS = 3;                                     // reads per warp
 constexpr uint32_t DP3_MAXN = FAME_MAX_READ_LEN;
 constexpr uint32_t DP3_STEPS = 2 * DP3_MAXN + DP_BAND + 2;            // anti-diagonals, rounded up to even
+constexpr uint32_t DP3_WORDS = (DP3_STEPS + 15) / 16;                 // 16 two-bit choices per word and lane
 constexpr uint32_t DP3_REF = 288;                                      // reference bases, j in [-2, n + 10]
 constexpr uint32_t DP3_ALIGN = 2 * DP3_MAXN + 4 * DP_BAND + 10;       // alignment trace
-// row-n values, read, reference, trace; + 16 so that the groups' arrays start in different banks
+// row-n values, read masks, reference bits, trace; + 16 so that the groups'
+// arrays start in different banks
 constexpr uint32_t DP3_GROUP_BYTES = 48 + 256 + DP3_REF + DP3_ALIGN + 8 + 16;
-constexpr uint32_t DPW_BYTES = DP3_STEPS * 8 + DP3_GROUPS * DP3_GROUP_BYTES;   // per warp
+constexpr uint32_t DP3_CODE_BYTES = DP3_WORDS * 32 * 4;
+constexpr uint32_t DPW_BYTES = DP3_CODE_BYTES + DP3_GROUPS * DP3_GROUP_BYTES;   // per warp
 constexpr int DPW_REF0 = 2;
-static_assert(DP3_GROUP_BYTES % 16 == 0 && (DP3_STEPS * 8) % 16 == 0, "16-byte aligned shared-memory regions");
+static_assert(DP3_GROUP_BYTES % 16 == 0 && DP3_CODE_BYTES % 16 == 0, "16-byte aligned shared-memory regions");
 static_assert(DP3_MAXN + DP_BAND + 2 + DPW_REF0 < DP3_REF, "reference bases fit");
+
+// Reference bases as one bit each (A 1, C 2, G 4, T 8, N 16; 0 outside the
+// chromosome) and read characters as the set of reference bases they match
+// under CompiFwd / CompiRev (ReadQueue.h:295-338): a cell is a mismatch when
+// the two share no bit.
+__device__ __forceinline__ uint8_t ref_bit(int b) { return b < 5 ? (uint8_t)(1u << b) : (uint8_t)0; }
+__device__ __forceinline__ uint8_t read_mask(uint8_t r, int isFwd)
+{
+    if (isFwd) return r == 'A' ? 1 : r == 'C' ? 2 : r == 'G' ? 4 : r == 'T' ? (8 | 2) : r == 'N' ? 16 : 0;
+    return r == 'T' ? (1 | 4) : r == 'G' ? 2 : r == 'A' ? 8 : r == 'C' ? 4 : 0;
+}
 
 __global__ void k_dp_warp(DevIndex ix, ChunkBufs cb)
 {
@@ -924,12 +938,12 @@ __global__ void k_dp_warp(DevIndex ix, ChunkBufs cb)
     const int k = lane - 9 * grp;
     const bool in_grp = grp < (int)DP3_GROUPS;
     uint8_t* warp_p = smem + (threadIdx.x >> 5) * DPW_BYTES;
-    uint2* steps = (uint2*)warp_p;              // per anti-diagonal: ballots of the two choice bits
-    uint8_t* gbase_p = warp_p + DP3_STEPS * 8 + (in_grp ? grp : 0) * DP3_GROUP_BYTES;
+    uint32_t* codes = (uint32_t*)warp_p;        // [step / 16][lane]: 2-bit choices, step t % 16 at bits 2 (t % 16)
+    uint8_t* gbase_p = warp_p + DP3_CODE_BYTES + (in_grp ? grp : 0) * DP3_GROUP_BYTES;
     uint16_t* rown = (uint16_t*)gbase_p;        // row n, offsets -8..8
-    uint8_t* rowc = gbase_p + 48;
-    uint8_t* refc = rowc + 256;
-    uint8_t* al = refc + DP3_REF;
+    uint8_t* rowm = gbase_p + 48;               // read row masks
+    uint8_t* refb = rowm + 256;                 // reference column bits
+    uint8_t* al = refb + DP3_REF;
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     const uint32_t ndp = (uint32_t)cb.ctr[CTR_DP];
     const uint32_t RL = ix.readlen;
@@ -955,62 +969,68 @@ __global__ void k_dp_warp(DevIndex ix, ChunkBufs cb)
             chrom = ix.cpg_chrom[sind];
         }
         const char* raw = cb.seqs + off0;
-        const long n = (long)size;
+        const int n = (int)size;
         const int64_t gb0 = (int64_t)metaPos + offset;
         if (have) {
-            // row characters: row i (1..n) compares rowc[i - 1]; reference columns j in [-2, n + 10]
-            for (long q = k; q < n; q += 9)
-                rowc[q] = oriented_char(raw, size, orient, isFwd ? (uint32_t)(n - 1 - q) : (uint32_t)q);
-            for (long j = k - DPW_REF0; j <= n + DPB + 2; j += 9)
-                refc[j + DPW_REF0] = base_char(gbase(ix, chrom, gb0 + 1 - j));
+            // row i (1..n) compares rowm[i - 1]; reference columns j in [-2, n + 10]
+            for (int q = k; q < n; q += 9)
+                rowm[q] = read_mask(oriented_char(raw, size, orient, isFwd ? (uint32_t)(n - 1 - q) : (uint32_t)q), isFwd);
+            for (int j = k - DPW_REF0; j <= n + (int)DPB + 2; j += 9)
+                refb[j + DPW_REF0] = ref_bit(gbase(ix, chrom, gb0 + 1 - j));
         }
         __syncwarp();
-        // fill: steps t = 0 .. 2 * nmax + 8 over the group's anti-diagonals
-        long nmax = n;
+        // fill: steps t = 0 .. 2 * nmax + 9 over the group's anti-diagonals, two
+        // per iteration (even: lane k holds offset 2k - 8, odd: 2k - 7)
+        int nmax = n;
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) nmax = max(nmax, (long)__shfl_xor_sync(0xffffffffu, (int)nmax, d));
+        for (int d = 16; d > 0; d >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, d));
+        const int o_even = 2 * k - 8, o_odd = 2 * k - 7;
+        const bool act_even = have, act_odd = have && k < 8;
         int cur1 = 0xffff, cur2 = 0xffff;   // own values of steps t - 1 and t - 2
-        const int base_lane = 9 * (in_grp ? grp : 0);
-        for (long t = 0; t <= 2 * nmax + DPB; ++t) {
-            const int par = (int)(t & 1);
-            const long o = 2 * k - 8 + par;
-            // neighbour values of step t - 1: up (row - 1, o + 1), left (row, o - 1)
-            const int upl = par ? k + 1 : k;
-            const int lfl = par ? k : k - 1;
-            const int v_up = __shfl_sync(0xffffffffu, cur1, base_lane + min(max(upl, 0), 8));
-            const int v_lf = __shfl_sync(0xffffffffu, cur1, base_lane + min(max(lfl, 0), 8));
-            int val = 0xffff;
-            uint32_t mycode = 0;
-            if (have && o <= DPB && ((t - o) & 1) == 0) {
-                const long row = (t - o) >> 1;
-                const long j = row + o;
-                if (row == 0 && o >= 0) {
-                    val = (int)o;                                    // first row: 0..8
-                } else if (row >= 1 && row <= n && j == 0) {
-                    val = (int)row;                                  // first column, rows 1..8
-                } else if (row >= 1 && row <= n && j >= 1) {
-                    const int up = (o == DPB) ? 65535 - (int)(row - 1) - (int)DPB - 1 : v_up;
-                    const int lf = (o == -DPB) ? (row == DPB + 1 ? 65535 - DPB - (int)DPB - 1 : 65535 - (int)row) : v_lf;
-                    const int dg = cur2;
-                    const uint8_t rc = rowc[row - 1];
-                    const uint8_t g = refc[j + DPW_REF0];
-                    const int mm = isFwd ? cmp_fwd(rc, g) : cmp_rev(rc, g);
-                    int v = up + 1;
-                    if (lf + 1 < v) v = lf + 1;
-                    if (dg + mm < v) v = dg + mm;
-                    val = v & 0xffff;
-                    uint8_t code;
-                    if (up < lf) code = (up + 1 < dg + mm) ? 2 : (mm ? 1 : 0);
-                    else code = (lf + 1 < dg + mm) ? 3 : (mm ? 1 : 0);
-                    mycode = code;
-                    if (row == n) rown[o + DPB] = (uint16_t)val;
+        uint32_t acc = 0;
+        const int t_end = 2 * nmax + (int)DPB;
+        for (int t = 0; t <= t_end; t += 2) {
+#pragma unroll
+            for (int par = 0; par < 2; ++par) {
+                const int tt = t + par;
+                const int o = par ? o_odd : o_even;
+                // up input (row - 1, o + 1) and left input (row, o - 1) are step t - 1
+                // values: the own lane's and a neighbour's
+                const int nb = par ? __shfl_down_sync(0xffffffffu, cur1, 1) : __shfl_up_sync(0xffffffffu, cur1, 1);
+                const int v_up = par ? nb : cur1;
+                const int v_lf = par ? cur1 : nb;
+                const int row = (tt - o) >> 1;
+                const int j = row + o;
+                int val = 0xffff;
+                uint32_t code = 0;
+                if ((par ? act_odd : act_even) && row >= 0 && row <= n) {
+                    if (row == 0) {
+                        if (o >= 0) val = o;                                 // first row: 0..8
+                    } else if (j == 0) {
+                        val = row;                                           // first column, rows 1..8
+                    } else if (j > 0) {
+                        const int up = (o == (int)DPB) ? 65535 - (row - 1) - (int)DPB - 1 : v_up;
+                        const int lf = (o == -(int)DPB) ? (row == (int)DPB + 1 ? 65535 - 2 * (int)DPB - 1 : 65535 - row)
+                                                        : v_lf;
+                        const int mm = (rowm[row - 1] & refb[j + DPW_REF0]) ? 0 : 1;
+                        const int dg = cur2 + mm;
+                        int v = min(up + 1, lf + 1);
+                        v = min(v, dg);
+                        val = v & 0xffff;
+                        code = up < lf ? (up + 1 < dg ? 2u : (uint32_t)mm) : (lf + 1 < dg ? 3u : (uint32_t)mm);
+                        if (row == n) rown[o + DPB] = (uint16_t)val;
+                    }
                 }
+                acc = __funnelshift_r(acc, code, 2);
+                if ((tt & 15) == 15) codes[(tt >> 4) * 32 + lane] = acc;
+                cur2 = cur1;
+                cur1 = val;
             }
-            const uint32_t b0 = __ballot_sync(0xffffffffu, mycode & 1);
-            const uint32_t b1 = __ballot_sync(0xffffffffu, mycode & 2);
-            if (lane == 0) steps[t] = make_uint2(b0, b1);
-            cur2 = cur1;
-            cur1 = val;
+        }
+        {
+            const int last = t_end + 1;                  // the last step written into acc
+            const int rem = (last & 15) + 1;             // steps in its word
+            if (rem < 16) codes[(last >> 4) * 32 + lane] = acc >> (2 * (16 - rem));
         }
         __syncwarp();
         if (have && k == 0) {
@@ -1030,9 +1050,8 @@ __global__ void k_dp_warp(DevIndex ix, ChunkBufs cb)
                     const long oo = col - row;
                     if (oo < -DPB || oo > DPB || col < 1) { bad = true; break; }
                     const long tt = 2 * row + oo;
-                    const uint2 m = steps[tt];
-                    const int bit = 9 * grp + (int)((oo + DPB - (tt & 1)) >> 1);
-                    code = (uint8_t)(((m.x >> bit) & 1u) | (((m.y >> bit) & 1u) << 1));
+                    const int ln = 9 * grp + (int)((oo + DPB - (tt & 1)) >> 1);
+                    code = (uint8_t)((codes[(tt >> 4) * 32 + ln] >> (2 * (tt & 15))) & 3u);
                 }
                 if (alen >= DP3_ALIGN) { bad = true; break; }
                 al[alen++] = code;
