@@ -35,6 +35,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "aligned reads/s (single-end matching stage, bit-exact CpG report)"
+# DRAM bytes (read + write) of one steady-state k_seed launch of se100_300mbp, from
+# ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:'k_seed$' -s 2 -c 1
+SEED_TRAFFIC_PER_LAUNCH = 4.13e9 + 14.82e6
 
 
 def parse():
@@ -303,6 +306,36 @@ def run_gb300(args):
     torch.cuda.synchronize()
     t_e2e = allreduce_max(ev0.elapsed_time(ev1) / 1e3, world)
     gm.set_timing(False)
+    # ---- batched form: the same steps through the queue (CUDA-graph chunk
+    # slots on their own streams, copies of one chunk overlapping the kernels
+    # of another), from the same pinned host buffers; host clock between two
+    # device synchronisations (the work spans several streams)
+    from fame_gb300 import GpuQueue
+    nslots = 3
+    q = GpuQueue(gm, nslots, maxn, max(int(p[0].nbytes) for p in pinned.values()))
+    for w in range(nslots):
+        hs, ho, n = pinned[steady[w % len(steady)]]
+        q.collect(q.submit(hs, ho, flags))
+    launches_q0 = q.launches()
+    b_reads = 0
+    inflight = []
+    torch.cuda.synchronize()
+    tb0 = time.perf_counter()
+    for k in range(args.steps):
+        if len(inflight) == nslots:
+            s_, n_ = inflight.pop(0)
+            q.collect(s_, mats=h_mat[:n_], invalid=h_inv[:n_])
+        hs, ho, n = pinned[steady[k % len(steady)]]
+        inflight.append((q.submit(hs, ho, flags), n))
+        b_reads += n
+    for s_, n_ in inflight:
+        q.collect(s_, mats=h_mat[:n_], invalid=h_inv[:n_])
+    torch.cuda.synchronize()
+    t_b = allreduce_max(time.perf_counter() - tb0, world)
+    batched = {"value": b_reads * world / t_b, "unit": "reads/s", "slots": nslots,
+               "gpu_launches": q.launches() - launches_q0,
+               "timing": "host clock between device synchronisations; host buffers in and out"}
+    q.close()
     # ---- roofline of the index-gather (seeding) kernel and the Shift-And kernel
     hbm, src = peaks()
     names = ["read_prep", "seed_gather", "shift_and", "select_exact_cpg", "banded_dp", "seed_heavy"]
@@ -322,11 +355,15 @@ def run_gb300(args):
         "e2e": {"value": e_reads * world / t_e2e, "unit": "reads/s", "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps)},
         "gpu_launches": launches,
+        "batched": batched,
         "stage_seconds": st,
         "dominant_kernel": dominant,
         "roofline": {"kernel": "k_seed (index gathers)", "bound": "hbm", "achieved": gbps, "peak": hbm,
-                     "unit": "GB/s", "frac": gbps / hbm, "traffic": None,
-                     "note": "algorithmic bytes = 8 B bucket bounds + 4 B per bucket entry per k-mer; peak %s" % src},
+                     "unit": "GB/s", "frac": gbps / hbm, "traffic": SEED_TRAFFIC_PER_LAUNCH,
+                     "dram_achieved": SEED_TRAFFIC_PER_LAUNCH / (seed_s / args.steps) / 1e9 if seed_s > 0 else None,
+                     "note": "algorithmic bytes = 8 B bucket bounds + 4 B per bucket entry per k-mer; peak %s; "
+                             "traffic = dram read + write of one steady-state launch (ncu, 1 pass); "
+                             "dram_achieved = traffic / launch time" % src},
         "windows_scanned_per_read": scans / max(1, reads),
         "clocks": clk.summary(),
         "setup_seconds": {"generate": t_gen, "index_build": t_build, "upload": t_open},
@@ -339,6 +376,65 @@ def run_gb300(args):
     gm.close()
     if rank == 0:
         print(json.dumps(out))
+
+
+SERVING_METRIC = "aggregate reads/s of a single-cell job stream (serving form), with p50/p99 job latency"
+
+
+def run_gb300_serving(args):
+    """Serving form: single-cell jobs arrive as a Poisson stream; the serving
+    loop (fame_gb300/serving.py) admits them into the batched queue while
+    others run; the plain per-job path runs the same trace job after job."""
+    from fame_gb300 import GpuMatcher, HostIndex, synth
+    from fame_gb300.serving import Job, ServingLoop, latency_summary, plain_per_job
+    spec = synth.WORKLOADS[args.workload]
+    js = spec["jobs"]
+    rng = np.random.default_rng(js["seed"])
+    sizes = np.clip(np.round(js["median"] * np.exp(js["sigma"] * rng.standard_normal(js["n_jobs"]))),
+                    js["lo"], js["hi"]).astype(np.int64)
+    arrivals = np.cumsum(rng.exponential(1.0 / js["rate"], js["n_jobs"]))
+    t0 = time.time()
+    g = synth.make_genome(**spec["genome"])
+    rs = synth.make_reads(g, int(sizes.sum()), seed=js["seed"] + 1, sub_rate=js["sub_rate"],
+                          indel_rate=js["indel_rate"])
+    t_gen = time.time() - t0
+    seq, offs = rs.concat()
+    jobs, a = [], 0
+    for i, n in enumerate(sizes):
+        o = offs[a:a + n + 1]
+        jobs.append(Job("cell%d" % i, seq[int(o[0]):int(o[-1])], o - o[0], arrival=float(arrivals[i])))
+        a += int(n)
+    hi = HostIndex.build(g.seqs, readlen=100, threads=0)
+    gm = GpuMatcher(hi, 0)
+    loop = ServingLoop(gm, slots=4, max_active=16)
+    loop.run(jobs[:2], realtime=False)                       # warm-up (graphs, buffers)
+    plain_per_job(gm, jobs[:1], realtime=False)
+    with ClockSampler(0) as clk:
+        t1 = time.perf_counter()
+        served = loop.run(jobs, realtime=True)
+        t_serv = time.perf_counter() - t1
+        t1 = time.perf_counter()
+        plain = plain_per_job(gm, jobs, realtime=True)
+        t_plain = time.perf_counter() - t1
+    same = all(np.array_equal(a.meth, b.meth) and a.counters == b.counters
+               for a, b in zip(sorted(served, key=lambda r: r.job_id), sorted(plain, key=lambda r: r.job_id)))
+    loop.close()
+    gm.close()
+    total = int(sizes.sum())
+    out = {
+        "metric": SERVING_METRIC, "value": total / t_serv, "unit": "reads/s", "n_gpus": 1, "steps": 1,
+        "warmup": 1, "ms_per_step": 1e3 * t_serv, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8/u64 integer", "data": "synthetic (seeded jobs and arrival trace)",
+        "config": {"workload": args.workload, "jobs": len(jobs), "reads_total": total,
+                   "arrival_rate_per_s": js["rate"], "reads_per_job_median": js["median"],
+                   "reads_per_job_range": [int(sizes.min()), int(sizes.max())], "slots": 4},
+        "latency": {"serving": latency_summary(served), "plain_per_job": latency_summary(plain)},
+        "plain_per_job_reads_per_s": total / t_plain,
+        "results_identical_to_plain": bool(same),
+        "timing": "host clock over the whole trace (arrival-driven); per-job latency = completion - arrival",
+        "clocks": clk.summary(), "setup_seconds": {"generate": t_gen},
+    }
+    print(json.dumps(out))
 
 
 PE_METRIC = "aligned read pairs/s (paired-end matching stage, bit-exact CpG report)"
@@ -534,5 +630,7 @@ if __name__ == "__main__":
         run_reference(a)
     elif a.workload.startswith("pe"):
         run_gb300_pe(a)
+    elif a.workload.startswith("sc_serving"):
+        run_gb300_serving(a)
     else:
         run_gb300(a)

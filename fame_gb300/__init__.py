@@ -6,9 +6,9 @@ package holds its sources (``csrc/``), the in-tree build, a ctypes binding
 and a host-side mirror of FAME's ReadQueue interface.
 """
 from ._lib import (CHUNKSIZE, FAME_BOTH_STRANDS, FAME_GET_STRANDED, FAME_MATCH_R1_FWD, FAME_MAX_READ_LEN,
-                   Counters, FameError, GpuMatcher, HostIndex, PairCounters, lib)
+                   Counters, FameError, GpuMatcher, GpuQueue, HostIndex, PairCounters, lib)
 from .readqueue import PairedReadQueue, ReadQueue, SingleCellQueue, read_sc_meta, write_cpg_report
 from . import synth
 
 __all__ = ["CHUNKSIZE", "FAME_BOTH_STRANDS", "FAME_GET_STRANDED", "FAME_MATCH_R1_FWD", "FAME_MAX_READ_LEN",
-           "Counters", "FameError", "GpuMatcher", "HostIndex", "PairCounters", "lib", "PairedReadQueue", "ReadQueue", "SingleCellQueue", "read_sc_meta", "write_cpg_report"]
+           "Counters", "FameError", "GpuMatcher", "GpuQueue", "HostIndex", "PairCounters", "lib", "PairedReadQueue", "ReadQueue", "SingleCellQueue", "read_sc_meta", "write_cpg_report"]

@@ -63,7 +63,9 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_gpu_open", "fame_gpu_close", "fame_gpu_last_error", "fame_gpu_match_reads",
            "fame_gpu_match_reads_dev", "fame_gpu_tallies", "fame_gpu_alloc", "fame_gpu_free", "fame_gpu_memcpy",
            "fame_gpu_host_alloc", "fame_gpu_host_free", "fame_gpu_stream", "fame_gpu_set_timing",
-           "fame_gpu_stage_times", "fame_gpu_last_launches", "fame_gpu_match_pairs", "fame_gpu_match_pairs_dev"]
+           "fame_gpu_stage_times", "fame_gpu_last_launches", "fame_gpu_match_pairs", "fame_gpu_match_pairs_dev", "fame_queue_open",
+           "fame_queue_submit", "fame_queue_ready", "fame_queue_collect", "fame_queue_launches", "fame_queue_close",
+           "fame_gpu_tally_alloc", "fame_gpu_tally_read", "fame_gpu_tally_free", "fame_gpu_mem_info"]
 
 _lib = None
 
@@ -103,6 +105,17 @@ def lib(build_if_missing: bool = True):
     L.fame_gpu_last_launches.argtypes = [_P]
     L.fame_gpu_match_pairs.argtypes = [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]
     L.fame_gpu_match_pairs_dev.argtypes = [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P]
+    L.fame_queue_open.argtypes = [_P, C.c_uint32, C.c_uint32, C.c_uint64, _P]
+    L.fame_queue_submit.argtypes = [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P]
+    L.fame_queue_ready.argtypes = [_P, C.c_int]
+    L.fame_queue_collect.argtypes = [_P, C.c_int, _P, _P, _P]
+    L.fame_queue_launches.argtypes = [_P]
+    L.fame_queue_launches.restype = C.c_uint64
+    L.fame_queue_close.argtypes = [_P]
+    L.fame_gpu_tally_alloc.argtypes = [_P, _P]
+    L.fame_gpu_tally_read.argtypes = [_P, _P, _P, C.c_int]
+    L.fame_gpu_tally_free.argtypes = [_P, _P]
+    L.fame_gpu_mem_info.argtypes = [_P, _P, _P]
     _lib = L
     return L
 
@@ -320,3 +333,62 @@ class GpuMatcher:
 
     def host_free(self, arr: np.ndarray):
         _check(lib().fame_gpu_host_free(self.h, arr.ctypes.data), self.h)
+
+    # separate tally arrays (one per job of a serving loop)
+    def tally_alloc(self) -> int:
+        p = _P()
+        _check(lib().fame_gpu_tally_alloc(self.h, C.byref(p)), self.h)
+        return p.value
+
+    def tally_read(self, meth_dev: int, reset: bool = False) -> np.ndarray:
+        out = np.zeros(4 * self.n_cpg, np.uint16)
+        _check(lib().fame_gpu_tally_read(self.h, meth_dev, _ptr(out), int(reset)), self.h)
+        return out.reshape(-1, 4)
+
+    def tally_free(self, meth_dev: int):
+        _check(lib().fame_gpu_tally_free(self.h, meth_dev), self.h)
+
+    def mem_info(self):
+        f, t = C.c_uint64(), C.c_uint64()
+        _check(lib().fame_gpu_mem_info(self.h, C.byref(f), C.byref(t)), self.h)
+        return f.value, t.value
+
+
+class GpuQueue:
+    """The batched form (fame_queue_*): chunk slots on a GpuMatcher's context,
+    each running the chunk pipeline as a CUDA graph on its own stream."""
+
+    def __init__(self, gpu: GpuMatcher, slots: int, max_reads: int, max_bytes: int):
+        self.gpu = gpu
+        self.nslots = slots
+        self.h = _P()
+        _check(lib().fame_queue_open(gpu.h, slots, max_reads, max_bytes, C.byref(self.h)), gpu.h)
+        self.pending = {}
+
+    def submit(self, seq_bytes, offs, flags: int, meth_dev=None) -> int:
+        offs = np.ascontiguousarray(offs, dtype=np.uint64)
+        n = len(offs) - 1
+        buf = np.frombuffer(seq_bytes, dtype=np.uint8) if isinstance(seq_bytes, (bytes, bytearray)) else seq_bytes
+        slot = C.c_int()
+        _check(lib().fame_queue_submit(self.h, _ptr(buf), _ptr(offs), n, flags, meth_dev, C.byref(slot)), self.gpu.h)
+        self.pending[slot.value] = n
+        return slot.value
+
+    def ready(self, slot: int) -> bool:
+        return lib().fame_queue_ready(self.h, slot) == 1
+
+    def collect(self, slot: int, mats=None, invalid=None):
+        n = self.pending.pop(slot)
+        mats = np.zeros(n, np.uint64) if mats is None else mats
+        invalid = np.zeros(n, np.uint8) if invalid is None else invalid
+        cnt = Counters()
+        _check(lib().fame_queue_collect(self.h, slot, _ptr(mats), _ptr(invalid), C.byref(cnt)), self.gpu.h)
+        return mats, invalid, cnt
+
+    def launches(self) -> int:
+        return int(lib().fame_queue_launches(self.h))
+
+    def close(self):
+        if self.h and self.gpu.h:          # closing the context closes its queue
+            lib().fame_queue_close(self.h)
+        self.h = None

@@ -80,6 +80,14 @@ enum {
 
 constexpr int HIT_CAP = 6;
 
+// A count argument with this value is read from the chunk's device counters
+// instead (launches that run without a host round trip).
+constexpr uint32_t FROM_DEVICE = 0xffffffffu;
+
+// The candidate buffer overflowed: the chunk's later stages do nothing and the
+// host reruns it with a larger buffer.
+__device__ __forceinline__ bool cand_overflow(const ChunkBufs& cb) { return cb.ctr[CTR_CAND] > cb.cand_cap; }
+
 __device__ __forceinline__ uint64_t rotl64(uint64_t v, unsigned s)
 {
     s &= 63u;

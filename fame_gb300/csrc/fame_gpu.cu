@@ -52,7 +52,10 @@ struct fame_gpu {
     uint8_t* d_pe_heavy = nullptr;       // global scratch of k_pe_heavy
     uint64_t pe_heavy_warp_bytes = 0;
     uint32_t pe_heavy_warps = 0;
+    fame_queue* queue = nullptr;         // the batched form's slots, if open
 };
+
+void queue_quiesce(fame_queue* q);
 
 namespace {
 
@@ -134,6 +137,7 @@ extern "C" int fame_gpu_close(fame_gpu* g)
 {
     if (!g) return FAME_ERR_ARG;
     cudaSetDevice(g->device);
+    if (g->queue) fame_queue_close(g->queue);
     if (g->stream) cudaStreamSynchronize(g->stream);
     for (void* p : g->index_allocs) cudaFree(p);
     dev_free(g->d_seqs); dev_free(g->d_offs); dev_free(g->d_rflags); dev_free(g->d_task_cand);
@@ -329,7 +333,7 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dp_warp, 128, 4 * DPW_BYTES) != cudaSuccess || nb < 1)
             return fail(set_err(g, FAME_ERR_CUDA, "k_dp_warp does not fit an SM"));
         g->dp_grid = (uint32_t)(g->sm_count * nb);
-        uint64_t off[23];
+        uint64_t off[27];
         g->pe_warp_bytes = pe_layout(PE_LIGHT, off);
         const size_t pe_smem = 4 * g->pe_warp_bytes;
         void (*kp[5])(DevIndex, PeIndex, ChunkBufs, uint32_t) = {nullptr, k_pe<1>, k_pe<2>, k_pe<3>, k_pe<4>};
@@ -347,7 +351,7 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
 namespace {
 
 int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t n, uint32_t flags, uint64_t* d_mats,
-              uint8_t* d_invalid, fame_counters* cnt)
+              uint8_t* d_invalid, fame_counters* cnt, uint32_t* meth = nullptr)
 {
     const bool both = flags & FAME_BOTH_STRANDS, stranded = flags & FAME_GET_STRANDED;
     const uint32_t omask = (both || stranded) ? 3u : ((flags & FAME_MATCH_R1_FWD) ? 1u : 2u);
@@ -367,11 +371,12 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
     cb.dp_list = g->d_dp_list;
     cb.dp_mat = g->d_dp_mat;
     cb.dp_orient = g->d_dp_orient;
-    cb.meth = g->d_meth;
+    cb.meth = meth ? meth : g->d_meth;
     cb.ctr = g->d_ctr;
     cb.heavy = g->d_heavy;
     const int T = g->timing;
     g->launches = 0;
+    if (g->queue) queue_quiesce(g->queue);   // the queue's slots share the heavy-path scratch
     for (int attempt = 0; attempt < 4; ++attempt) {
         cb.cand = g->d_cand;
         cb.cand_task = g->d_cand_task;
@@ -499,7 +504,7 @@ namespace {
 
 // Heavy-pair caps: keys per map and phase, value-table slots, replayed buckets
 // (bucket_count = summed bucket sizes / 5 <= 224 k-mers x KMERCUTOFF / 5).
-constexpr PeCaps PE_HEAVY{16384, 65536, 131072 + NBHD - 1 + 64, 4096, 4096};
+constexpr PeCaps PE_HEAVY{16384, 65536, 131072 + NBHD - 1 + 64, 4096, 4096, 0};
 constexpr uint32_t PE_HEAVY_WARPS = 128;
 
 // Mates of pair r are reads r and n + r of (d_seqs, d_offs); mats and invalid
@@ -549,7 +554,7 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
     CK(cudaStreamSynchronize(g->stream));
     if (g->h_ctr[CTR_HEAVY]) {
         if (!g->d_pe_heavy) {
-            uint64_t off[23];
+            uint64_t off[27];
             g->pe_heavy_warp_bytes = pe_layout(PE_HEAVY, off);
             g->pe_heavy_warps = PE_HEAVY_WARPS;
             CK(cudaMalloc((void**)&g->d_pe_heavy, g->pe_heavy_warp_bytes * g->pe_heavy_warps));
@@ -801,4 +806,12 @@ extern "C" int fame_gpu_call_cpgs_noalloc(fame_gpu* g, const char* seqs_dev, con
     if (h[CTR_TOO_LONG]) return FAME_ERR_READ;
     if (h[CTR_ERRFLAG]) return FAME_ERR_ARG;
     return FAME_OK;
+}
+
+#include "queue.cuh"
+
+void queue_quiesce(fame_queue* q)
+{
+    for (auto& s : q->slots)
+        if (s.stream) cudaStreamSynchronize(s.stream);
 }

@@ -340,6 +340,10 @@ __device__ void shiftand_one(const DevIndex& ix, const ChunkBufs& cb, uint32_t c
 template <int W>
 __global__ void k_shiftand(DevIndex ix, ChunkBufs cb, uint32_t ncand)
 {
+    if (ncand == FROM_DEVICE) {
+        if (cand_overflow(cb) || !((cb.ctr[CTR_WMASK] >> W) & 1ull)) return;
+        ncand = (uint32_t)cb.ctr[CTR_CAND];
+    }
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncand; c += gridDim.x * blockDim.x) {
         const uint32_t task = cb.cand_task[c];
         const uint32_t r = task >> 1;
@@ -492,6 +496,7 @@ __device__ void meth_exact(const DevIndex& ix, const ChunkBufs& cb, uint32_t r, 
 
 __global__ void k_select(DevIndex ix, ChunkBufs cb)
 {
+    if (cand_overflow(cb)) return;
     __shared__ unsigned long long sc[8];
     if (threadIdx.x < 8) sc[threadIdx.x] = 0;
     __syncthreads();
@@ -859,6 +864,7 @@ __global__ void k_seed_heavy(DevIndex ix, ChunkBufs cb, HeavyScratch hs, uint32_
 {
     const uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (w >= hs.nwarps) return;
+    if (nheavy == FROM_DEVICE) nheavy = (uint32_t)cb.ctr[CTR_HEAVY];
     const SeedMem s = heavy_mem(hs, w);
     for (uint32_t i = w; i < nheavy; i += hs.nwarps) {
         const uint32_t task = cb.heavy[i];
@@ -932,6 +938,7 @@ __device__ __forceinline__ uint8_t read_mask(uint8_t r, int isFwd)
 
 __global__ void k_dp_warp(DevIndex ix, ChunkBufs cb)
 {
+    if (cand_overflow(cb)) return;
     extern __shared__ __align__(16) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int grp = lane / 9;                   // 3 groups of 9 lanes, lanes 27..31 idle

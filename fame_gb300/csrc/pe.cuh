@@ -52,6 +52,7 @@ struct PeCaps {
     uint32_t slot_cap;  // replayed bucket array
     uint32_t ovf_cap;
     uint32_t hcap;      // hits per mate and orientation
+    uint32_t ecap;      // bucket entries of one mate staged in working memory (0: read in place)
 };
 
 struct PeMem {
@@ -71,6 +72,10 @@ struct PeMem {
     uint32_t* ovf;
     uint2* list[2];       // (key, value) candidate lists
     uint64_t* hits[4];    // m1F, m2R, m1R, m2F
+    uint32_t* kpre;       // per k-mer: first staged entry (exclusive prefix of bucket sizes)
+    uint32_t* ge;         // staged entries (window | forward << 31) and their T masks
+    uint32_t* gt;
+    uint8_t* gk;          // k-mer of each staged entry
     PeCaps c;
 };
 
@@ -105,12 +110,16 @@ __host__ __device__ inline uint64_t pe_layout(PeCaps c, uint64_t* off)
     put(PE_KMAX);                           // 20 kfl
     put(256);                               // 21 rd[0]
     put(256);                               // 22 rd[1]
+    put(4ull * (PE_KMAX + 1));              // 23 kpre
+    put(4ull * c.ecap);                     // 24 ge
+    put(4ull * c.ecap);                     // 25 gt
+    put(c.ecap);                            // 26 gk
     return o;
 }
 
 __device__ inline PeMem pe_mem(uint8_t* base, PeCaps c)
 {
-    uint64_t off[23];
+    uint64_t off[27];
     pe_layout(c, off);
     PeMem s;
     s.c = c;
@@ -138,11 +147,15 @@ __device__ inline PeMem pe_mem(uint8_t* base, PeCaps c)
     s.kfl = base + off[20];
     s.rd[0] = base + off[21];
     s.rd[1] = base + off[22];
+    s.kpre = (uint32_t*)(base + off[23]);
+    s.ge = (uint32_t*)(base + off[24]);
+    s.gt = (uint32_t*)(base + off[25]);
+    s.gk = base + off[26];
     return s;
 }
 
 // shared-memory caps (one warp)
-constexpr PeCaps PE_LIGHT{96, 256, 512 + NBHD - 1, 64, 32};
+constexpr PeCaps PE_LIGHT{96, 256, 512 + NBHD - 1, 64, 32, 320};
 
 __device__ __forceinline__ uint32_t vt_hash(uint32_t k, uint32_t mask) { return (k * 0x9E3779B1u) >> 8 & mask; }
 
@@ -230,6 +243,46 @@ __device__ uint32_t pe_kmers(const DevIndex& ix, const PeIndex& px, const PeMem&
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) sigma += __shfl_xor_sync(0xffffffffu, sigma, d);
+    __syncwarp();
+    if (sigma > s.c.ecap) return sigma;     // entries are read in place
+    // stage the entries and T masks of all buckets (loads of a lane overlap)
+    {
+        const uint32_t per = (nk + 31) / 32;
+        const uint32_t b = min(nk, lane * per), e = min(nk, b + per);
+        uint32_t loc = 0;
+        for (uint32_t p = b; p < e; ++p) loc += s.kln[p];
+        uint32_t inc = loc;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, inc, d);
+            if (lane >= d) inc += v;
+        }
+        uint32_t run = inc - loc;
+        for (uint32_t p = b; p < e; ++p) {
+            s.kpre[p] = run;
+            for (uint32_t j = 0; j < s.kln[p]; ++j) s.gk[run + j] = (uint8_t)p;
+            run += s.kln[p];
+        }
+    }
+    __syncwarp();
+    for (uint32_t base = 0; base < sigma; base += 256) {
+        uint32_t ev[8], tv[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint32_t i = base + lane + 32 * j;
+            if (i < sigma) {
+                const uint32_t p = s.gk[i];
+                const uint32_t src = s.kst[p] + (i - s.kpre[p]);
+                ev[j] = __ldg(ix.entry + src);
+                tv[j] = __ldg(px.tmask + src);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint32_t i = base + lane + 32 * j;
+            if (i < sigma) { s.ge[i] = ev[j]; s.gt[i] = tv[j]; }
+        }
+    }
     __syncwarp();
     return sigma;
 }
@@ -423,18 +476,22 @@ __device__ inline void pe_sort(uint2* f, long n, PeCmp cmp)
 // ---------------------------------------------------------------------------
 // lane 0: map operations of one mate (getSeedRefsFirstRead / SecondRead)
 // ---------------------------------------------------------------------------
-__device__ void pe_count_first(const DevIndex& ix, const PeIndex& px, const PeMem& s, PeState& st, uint32_t len)
+__device__ void pe_count_first(const DevIndex& ix, const PeIndex& px, const PeMem& s, PeState& st, uint32_t len,
+                               bool staged)
 {
     const uint32_t nk = len - KMERLEN + 1;
     const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
     for (uint32_t p = 0; p < nk && !st.over; ++p) {
         if (s.kfl[p]) continue;
-        const uint32_t b0 = s.kst[p], n = s.kln[p], cm = s.kcm[p];
+        const uint32_t n = s.kln[p], cm = s.kcm[p];
+        const uint32_t b0 = staged ? s.kpre[p] : s.kst[p];
+        const uint32_t* E = staged ? s.ge : ix.entry;
+        const uint32_t* TM = staged ? s.gt : px.tmask;
         bool have = false;
         uint32_t lastId = 0, lastFwd = 0;
         for (uint32_t i = b0; i < b0 + n; ++i) {
-            if (cm & SEEDBITS & __ldg(px.tmask + i)) continue;
-            const uint32_t e = __ldg(ix.entry + i);
+            if (cm & SEEDBITS & TM[i]) continue;
+            const uint32_t e = E[i];
             const uint32_t id = e & 0x7fffffffu, fwd = e >> 31;
             if (have && id == lastId && fwd == lastFwd) continue;
             have = true; lastId = id; lastFwd = fwd;
@@ -453,19 +510,23 @@ __device__ void pe_count_first(const DevIndex& ix, const PeIndex& px, const PeMe
     }
 }
 
-__device__ void pe_count_second(const DevIndex& ix, const PeIndex& px, const PeMem& s, PeState& st, uint32_t len)
+__device__ void pe_count_second(const DevIndex& ix, const PeIndex& px, const PeMem& s, PeState& st, uint32_t len,
+                                bool staged)
 {
     const uint32_t nk = len - KMERLEN + 1;
     const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
     const int ctx = (int)px.ctx;
     for (uint32_t p = 0; p < nk && !st.over; ++p) {
         if (s.kfl[p]) continue;
-        const uint32_t b0 = s.kst[p], n = s.kln[p], cm = s.kcm[p];
+        const uint32_t n = s.kln[p], cm = s.kcm[p];
+        const uint32_t b0 = staged ? s.kpre[p] : s.kst[p];
+        const uint32_t* E = staged ? s.ge : ix.entry;
+        const uint32_t* TM = staged ? s.gt : px.tmask;
         bool have = false;
         uint32_t lastId = 0, lastFwd = 0;
         for (uint32_t i = b0; i < b0 + n; ++i) {
-            if (cm & SEEDBITS & __ldg(px.tmask + i)) continue;
-            const uint32_t e = __ldg(ix.entry + i);
+            if (cm & SEEDBITS & TM[i]) continue;
+            const uint32_t e = E[i];
             const uint32_t id = e & 0x7fffffffu, fwd = e >> 31;
             if (have && id == lastId && fwd == lastFwd) continue;
             have = true; lastId = id; lastFwd = fwd;
@@ -651,7 +712,7 @@ __device__ bool pe_pair(const DevIndex& ix, const PeIndex& px, const ChunkBufs& 
         const uint32_t sigma = pe_kmers(ix, px, s, s.rd[0], n1);
         PeState st{};
         if (lane == 0) {
-            pe_count_first(ix, px, s, st, n1);
+            pe_count_first(ix, px, s, st, n1, sigma <= s.c.ecap);
             // rebuild: keep count1 >= QTHRESH
             if (!st.over)
                 for (int dir = 0; dir < 2; ++dir)
@@ -671,10 +732,10 @@ __device__ bool pe_pair(const DevIndex& ix, const PeIndex& px, const ChunkBufs& 
         any = __shfl_sync(0xffffffffu, any, 0);
         if (!any) continue;
         __syncwarp();
-        pe_kmers(ix, px, s, s.rd[1], n2);
+        const uint32_t sigma2 = pe_kmers(ix, px, s, s.rd[1], n2);
         bool hasCpG = false;
         if (lane == 0) {
-            pe_count_second(ix, px, s, st, n2);
+            pe_count_second(ix, px, s, st, n2, sigma2 <= s.c.ecap);
             if (!st.over) {
                 // f2 flags (order-independent) and hasCpG
                 const int ctx = (int)px.ctx;

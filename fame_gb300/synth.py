@@ -249,6 +249,11 @@ WORKLOADS = {
     "se100_300mbp": dict(genome=dict(chrom_lengths=[37_500_000] * 8, seed=11, meth_p=0.7,
                                      repeat_frac=0.08),
                          reads=dict(n_reads=5_000_000, seed=12, sub_rate=0.01, indel_rate=0.001)),
+    # the 300 Mbp genome above; single-cell jobs: Poisson arrivals at 20 jobs/s, log-normal read counts
+    # (median 200k, clipped to [2k, 2M]), SE 100 bp
+    "sc_serving": dict(genome=dict(chrom_lengths=[37_500_000] * 8, seed=11, meth_p=0.7, repeat_frac=0.08),
+                       jobs=dict(n_jobs=24, rate=20.0, median=200_000, sigma=1.0, lo=2_000, hi=2_000_000, seed=14,
+                                 sub_rate=0.01, indel_rate=0.001)),
     # the 300 Mbp genome above, 1.5M pairs of 2 x 100 bp, inner distance U[20, 400]
     "pe100_300mbp": dict(genome=dict(chrom_lengths=[37_500_000] * 8, seed=11, meth_p=0.7, repeat_frac=0.08),
                          pairs=dict(n_pairs=1_500_000, seed=13, inner=(20, 400), sub_rate=0.01, indel_rate=0.001)),

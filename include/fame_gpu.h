@@ -173,6 +173,38 @@ int fame_gpu_match_pairs_dev(fame_gpu* g, const char* seqs_dev, const uint64_t* 
  * (printSCMethylationLevels, ReadQueue.cpp:1894-1921). */
 int fame_gpu_tallies(fame_gpu* g, uint16_t* meth, int reset);
 
+/* ---- Batched and serving form (no counterpart in the reference) ---------
+ * A queue of chunk slots on one context.  Each slot owns device buffers for
+ * one chunk of up to max_reads reads / max_bytes bases, page-locked staging
+ * and a CUDA stream, and runs the chunk pipeline as a captured CUDA graph
+ * with no host round trip inside; chunks in different slots overlap on the
+ * GPU.  One queue per context (at most 8 slots); its calls and the plain
+ * match calls come from one host thread.  Results equal those of
+ * fame_gpu_match_reads for the same chunk and flags. */
+typedef struct fame_queue fame_queue;
+int fame_queue_open(fame_gpu* g, uint32_t slots, uint32_t max_reads, uint64_t max_bytes, fame_queue** out);
+/* Copies one chunk into a free slot and starts it; returns the slot.
+ * meth_dev: the tally array the chunk adds to (from fame_gpu_tally_alloc,
+ * e.g. one job's), NULL for the context's own.  FAME_ERR_BUSY when every
+ * slot holds an uncollected chunk. */
+int fame_queue_submit(fame_queue* q, const char* seqs, const uint64_t* offs, uint32_t n, uint32_t flags,
+                      uint32_t* meth_dev, int* slot);
+/* 1 when the slot's chunk has finished, 0 while it runs. */
+int fame_queue_ready(fame_queue* q, int slot);
+/* Waits for the slot's chunk and copies out its results (NULL to skip). */
+int fame_queue_collect(fame_queue* q, int slot, uint64_t* mats, uint8_t* invalid, fame_counters* cnt);
+/* Kernels launched through the queue so far. */
+uint64_t fame_queue_launches(const fame_queue* q);
+int fame_queue_close(fame_queue* q);
+/* Separate tally arrays (4 x n_cpg uint32 in device memory, zeroed), e.g. one
+ * per single-cell job of a serving loop; read returns them as methLevels
+ * (uint16 wrap), reset zeroes them. */
+int fame_gpu_tally_alloc(fame_gpu* g, uint32_t** meth_dev);
+int fame_gpu_tally_read(fame_gpu* g, const uint32_t* meth_dev, uint16_t* meth, int reset);
+int fame_gpu_tally_free(fame_gpu* g, uint32_t* meth_dev);
+/* Free and total device memory (admission control of a serving loop). */
+int fame_gpu_mem_info(fame_gpu* g, uint64_t* free_bytes, uint64_t* total_bytes);
+
 /* Device memory helpers for the _dev entry points, and page-locked host
  * buffers (a host that parses its chunks straight into these gets the fast
  * host-to-device copy path). */
