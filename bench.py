@@ -37,7 +37,7 @@ sys.path.insert(0, ROOT)
 METRIC = "aligned reads/s (single-end matching stage, bit-exact CpG report)"
 # DRAM bytes (read + write) of one steady-state k_seed launch of se100_300mbp, from
 # ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:'k_seed$' -s 2 -c 1
-SEED_TRAFFIC_PER_LAUNCH = 4.13e9 + 14.82e6
+SEED_TRAFFIC_PER_LAUNCH = 3.17e9 + 20.89e6
 
 
 def parse():
@@ -341,6 +341,7 @@ def run_gb300(args):
     names = ["read_prep", "seed_gather", "shift_and", "select_exact_cpg", "banded_dp", "seed_heavy"]
     st = {names[i]: stage[i] / 1e3 for i in range(6)}
     dominant = max(names, key=lambda k: st[k])
+    traffic = SEED_TRAFFIC_PER_LAUNCH if args.workload == "se100_300mbp" and not args.reads else None
     seed_s = st["seed_gather"] + st["seed_heavy"]
     gbps = gather / seed_s / 1e9 if seed_s > 0 else 0.0
     out = {
@@ -359,8 +360,8 @@ def run_gb300(args):
         "stage_seconds": st,
         "dominant_kernel": dominant,
         "roofline": {"kernel": "k_seed (index gathers)", "bound": "hbm", "achieved": gbps, "peak": hbm,
-                     "unit": "GB/s", "frac": gbps / hbm, "traffic": SEED_TRAFFIC_PER_LAUNCH,
-                     "dram_achieved": SEED_TRAFFIC_PER_LAUNCH / (seed_s / args.steps) / 1e9 if seed_s > 0 else None,
+                     "unit": "GB/s", "frac": gbps / hbm, "traffic": traffic,
+                     "dram_achieved": traffic / (seed_s / args.steps) / 1e9 if (traffic and seed_s > 0) else None,
                      "note": "algorithmic bytes = 8 B bucket bounds + 4 B per bucket entry per k-mer; peak %s; "
                              "traffic = dram read + write of one steady-state launch (ncu, 1 pass); "
                              "dram_achieved = traffic / launch time" % src},

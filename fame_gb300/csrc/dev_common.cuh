@@ -8,7 +8,9 @@
 namespace fame {
 
 // The index as it lives in HBM (read-only for the whole context lifetime).
-//   tab    : bucket start offsets, HTABSIZE + 1 x uint32 (tabIndex)
+//   tab2   : per bucket {start offset (tabIndex), first entry of the bucket (0 if
+//            empty)}, HTABSIZE + 1 entries: one read gives a k-mer's bounds and,
+//            for the common one-entry bucket, its entry
 //   entry  : one uint32 per k-mer entry: window id | forward-strand << 31
 //            (kmerTableSmall.meta with strandTable folded into bit 31; the
 //            start-CpG bit the reference reserves there is never set by the
@@ -20,7 +22,7 @@ namespace fame {
 struct DevIndex {
     uint32_t readlen;
     uint32_t n_chrom;
-    const uint32_t* tab;
+    const uint2* tab2;
     const uint32_t* entry;
     const uint32_t* gpack;
     const uint32_t* gnmask;
@@ -55,6 +57,8 @@ struct ChunkBufs {
     uint32_t* meth;          // 4 x n_cpg counters (uint16 semantics after the fact)
     unsigned long long* ctr; // device counters, see CTR_*
     uint32_t* heavy;         // tasks handed to the heavy path
+    uint8_t* cand_flags;     // per candidate, bit 0: scan from startPos - 1 even at 0 (paired second mate); may be null
+    uint32_t cand_first;     // first candidate the Shift-And launch scans
 };
 
 enum {

@@ -29,6 +29,7 @@ struct fame_gpu {
     uint8_t* d_rflags = nullptr;
     uint4* d_task_cand = nullptr;
     uint32_t *d_cand = nullptr, *d_cand_task = nullptr, *d_hits = nullptr, *d_hit_n = nullptr;
+    uint8_t* d_cand_flags = nullptr;
     uint64_t* d_mats = nullptr;
     uint8_t* d_invalid = nullptr;
     uint32_t* d_dp_list = nullptr;
@@ -47,8 +48,10 @@ struct fame_gpu {
     uint32_t dp_grid = 0;   // resident blocks of k_dp_warp on the whole device
     // paired path
     PeIndex px{};
-    uint64_t pe_warp_bytes = 0;          // shared memory per warp of k_pe
-    uint32_t pe_grid[5]{};               // resident blocks of k_pe<W>
+    uint64_t pe_warp_bytes = 0;          // shared memory per warp of k_pe_seed
+    uint32_t pe_grid = 0;                // resident blocks of k_pe_seed
+    PeTaskRec* d_pe_recs = nullptr;      // per pair orientation
+    uint64_t cap_pe_recs = 0;
     uint8_t* d_pe_heavy = nullptr;       // global scratch of k_pe_heavy
     uint64_t pe_heavy_warp_bytes = 0;
     uint32_t pe_heavy_warps = 0;
@@ -114,8 +117,10 @@ int grow_chunk(fame_gpu* g, uint64_t n, uint64_t bytes, uint64_t cand)
     if (cand > g->cap_cand) {
         const uint64_t c = std::max<uint64_t>(cand, 1 << 16);
         dev_free(g->d_cand); dev_free(g->d_cand_task); dev_free(g->d_hits); dev_free(g->d_hit_n);
+        dev_free(g->d_cand_flags);
         if ((rc = dev_alloc(g, &g->d_cand, c)) || (rc = dev_alloc(g, &g->d_cand_task, c)) ||
-            (rc = dev_alloc(g, &g->d_hits, c * HIT_CAP)) || (rc = dev_alloc(g, &g->d_hit_n, c)))
+            (rc = dev_alloc(g, &g->d_hits, c * HIT_CAP)) || (rc = dev_alloc(g, &g->d_hit_n, c)) ||
+            (rc = dev_alloc(g, &g->d_cand_flags, c)))
             return rc;
         g->cap_cand = c;
     }
@@ -146,6 +151,8 @@ extern "C" int fame_gpu_close(fame_gpu* g)
     dev_free(g->d_dp_orient); dev_free(g->d_heavy); dev_free(g->d_ctr); dev_free(g->d_meth);
     dev_free(g->hs.base);
     dev_free(g->d_pe_heavy);
+    dev_free(g->d_pe_recs);
+    dev_free(g->d_cand_flags);
     if (g->h_ctr) cudaFreeHost(g->h_ctr);
     for (auto& e : g->ev) if (e) cudaEventDestroy(e);
     if (g->stream) cudaStreamDestroy(g->stream);
@@ -203,7 +210,7 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
                 return fail(set_err(g, FAME_ERR_CUDA, "tabIndex upload failed"));
         }
     }
-    g->ix.tab = d_tab;
+
     // ---- entries: window id | forward << 31
     uint32_t* d_entry;
     if ((rc = alloc_idx((void**)&d_entry, v->n_kmer * 4))) return fail(rc);
@@ -220,6 +227,14 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
             return fail(set_err(g, FAME_ERR_CUDA, "k-mer upload failed"));
     }
     g->ix.entry = d_entry;
+    // ---- bucket offsets with each bucket's first entry beside its start
+    {
+        uint2* d_tab2;
+        if ((rc = alloc_idx((void**)&d_tab2, (HTABSIZE + 1) * 8))) return fail(rc);
+        k_build_tab2<<<g->sm_count * 8, 256, 0, g->stream>>>(d_tab, d_entry, HTABSIZE, d_tab2);
+        if (cudaGetLastError() != cudaSuccess) return fail(set_err(g, FAME_ERR_CUDA, "tab2 build failed"));
+        g->ix.tab2 = d_tab2;
+    }
     // ---- paired path: tmask per entry (kmerTableSmall.tmask), filteredKmers sorted
     {
         uint32_t* d_tm;
@@ -308,6 +323,11 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         k_max_bucket<<<g->sm_count * 8, 256, 0, g->stream>>>(d_tab, HTABSIZE, d_mx);
         unsigned int mx = 0;
         cudaMemcpyAsync(&mx, d_mx, 4, cudaMemcpyDeviceToHost, g->stream);
+        cudaStreamSynchronize(g->stream);
+        // the plain offset table is not needed any more (tab2 holds the offsets)
+        cudaFree(d_tab);
+        g->index_allocs.erase(std::remove(g->index_allocs.begin(), g->index_allocs.end(), (void*)d_tab),
+                              g->index_allocs.end());
         if (cudaStreamSynchronize(g->stream) != cudaSuccess) { cudaFree(d_mx); return fail(set_err(g, FAME_ERR_CUDA, "bucket scan failed")); }
         cudaFree(d_mx);
         g->max_bucket = mx;
@@ -336,13 +356,10 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         uint64_t off[27];
         g->pe_warp_bytes = pe_layout(PE_LIGHT, off);
         const size_t pe_smem = 4 * g->pe_warp_bytes;
-        void (*kp[5])(DevIndex, PeIndex, ChunkBufs, uint32_t) = {nullptr, k_pe<1>, k_pe<2>, k_pe<3>, k_pe<4>};
-        for (int w = 1; w <= 4; ++w) {
-            if (cudaFuncSetAttribute(kp[w], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pe_smem) != cudaSuccess ||
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kp[w], 128, pe_smem) != cudaSuccess || nb < 1)
-                return fail(set_err(g, FAME_ERR_CUDA, "k_pe does not fit an SM"));
-            g->pe_grid[w] = (uint32_t)(g->sm_count * nb);
-        }
+        if (cudaFuncSetAttribute(k_pe_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pe_smem) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pe_seed, 128, pe_smem) != cudaSuccess || nb < 1)
+            return fail(set_err(g, FAME_ERR_CUDA, "k_pe_seed does not fit an SM"));
+        g->pe_grid = (uint32_t)(g->sm_count * nb);
     }
     *out = g;
     return FAME_OK;
@@ -515,7 +532,14 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
     const bool both = flags & FAME_BOTH_STRANDS, stranded = flags & FAME_GET_STRANDED;
     const uint32_t omask = (both || stranded) ? 3u : ((flags & FAME_MATCH_R1_FWD) ? 1u : 2u);
     int rc;
-    if ((rc = grow_chunk(g, 2ull * n, 0, 0))) return rc;
+    if ((rc = grow_chunk(g, 2ull * n, 0, 8ull * n + 4096))) return rc;
+    if (2ull * n > g->cap_pe_recs) {
+        dev_free(g->d_pe_recs);
+        const uint64_t c = std::max<uint64_t>(2ull * n, 2048);
+        if ((rc = dev_alloc(g, &g->d_pe_recs, c))) return rc;
+        g->cap_pe_recs = c;
+    }
+    if (g->queue) queue_quiesce(g->queue);
     ChunkBufs cb{};
     cb.seqs = d_seqs;
     cb.offs = d_offs;
@@ -535,54 +559,91 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
     px.ctx = (uint32_t)((double)maxpdist / WINLEN) + 1;
     px.maxdist = maxpdist + g->ix.readlen;
     g->launches = 0;
-    CK(cudaMemsetAsync(g->d_ctr, 0, CTR_N * sizeof(unsigned long long), g->stream));
-    k_pe_prep<<<(n + 255) / 256, 256, 0, g->stream>>>(cb, g->ix.readlen);
-    g->launches++;
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
-    CK(cudaStreamSynchronize(g->stream));
-    if (g->h_ctr[CTR_TOO_LONG]) return set_err(g, FAME_ERR_READ, "mate longer than FAME_MAX_READ_LEN");
-    const uint64_t wmask = g->h_ctr[CTR_WMASK];
-    const size_t smem = 4 * g->pe_warp_bytes;
-    const uint32_t wb = (uint32_t)g->pe_warp_bytes;
-    if (wmask & 2u) { k_pe<1><<<g->pe_grid[1], 128, smem, g->stream>>>(g->ix, px, cb, wb); g->launches++; }
-    if (wmask & 4u) { k_pe<2><<<g->pe_grid[2], 128, smem, g->stream>>>(g->ix, px, cb, wb); g->launches++; }
-    if (wmask & 8u) { k_pe<3><<<g->pe_grid[3], 128, smem, g->stream>>>(g->ix, px, cb, wb); g->launches++; }
-    if (wmask & 16u) { k_pe<4><<<g->pe_grid[4], 128, smem, g->stream>>>(g->ix, px, cb, wb); g->launches++; }
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
-    CK(cudaStreamSynchronize(g->stream));
-    if (g->h_ctr[CTR_HEAVY]) {
-        if (!g->d_pe_heavy) {
-            uint64_t off[27];
-            g->pe_heavy_warp_bytes = pe_layout(PE_HEAVY, off);
-            g->pe_heavy_warps = PE_HEAVY_WARPS;
-            CK(cudaMalloc((void**)&g->d_pe_heavy, g->pe_heavy_warp_bytes * g->pe_heavy_warps));
-        }
-        k_pe_heavy<<<g->pe_heavy_warps / 4, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_heavy,
-                                                                  g->pe_heavy_warp_bytes, PE_HEAVY);
-        g->launches++;
+    auto sync_ctr = [&]() -> int {
         CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
+        CK(cudaStreamSynchronize(g->stream));
+        return FAME_OK;
+    };
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        cb.cand = g->d_cand;
+        cb.cand_task = g->d_cand_task;
+        cb.cand_flags = g->d_cand_flags;
+        cb.cand_cap = (uint32_t)g->cap_cand;
+        cb.hits = g->d_hits;
+        cb.hit_n = g->d_hit_n;
+        cb.cand_first = 0;
+        CK(cudaMemsetAsync(g->d_ctr, 0, CTR_N * sizeof(unsigned long long), g->stream));
+        k_pe_prep<<<(n + 255) / 256, 256, 0, g->stream>>>(cb, g->ix.readlen);
+        g->launches++;
+        if ((rc = sync_ctr())) return rc;
+        if (g->h_ctr[CTR_TOO_LONG]) return set_err(g, FAME_ERR_READ, "mate longer than FAME_MAX_READ_LEN");
+        const uint64_t wmask = g->h_ctr[CTR_WMASK];
+        // A: maps, walk lists, first-walk candidates
+        k_pe_seed<<<g->pe_grid, 128, 4 * g->pe_warp_bytes, g->stream>>>(g->ix, px, cb, g->d_pe_recs,
+                                                                          (uint32_t)g->pe_warp_bytes);
+        g->launches++;
+        if ((rc = sync_ctr())) return rc;
+        const uint64_t nc1 = g->h_ctr[CTR_CAND];
+        if (nc1 > g->cap_cand) {
+            if ((rc = grow_chunk(g, 2ull * n, 0, nc1 * 2 + 4096))) return rc;
+            continue;
+        }
+        auto scans = [&](uint64_t first, uint64_t last) {
+            if (last <= first) return;
+            cb.cand_first = (uint32_t)first;
+            const uint32_t grid = (uint32_t)std::min<uint64_t>((last - first + 127) / 128, (uint64_t)g->sm_count * 32);
+            if (wmask & 2u) { k_shiftand<1><<<grid, 128, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
+            if (wmask & 4u) { k_shiftand<2><<<grid, 128, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
+            if (wmask & 8u) { k_shiftand<3><<<grid, 128, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
+            if (wmask & 16u) { k_shiftand<4><<<grid, 128, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
+            cb.cand_first = 0;
+        };
+        // B, C: first-walk scans, first walks, second-walk candidates
+        scans(0, nc1);
+        k_pe_walk1<<<(2 * n + 127) / 128, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_recs);
+        g->launches++;
+        if ((rc = sync_ctr())) return rc;
+        const uint64_t nc2 = g->h_ctr[CTR_CAND];
+        if (nc2 > g->cap_cand) {
+            if ((rc = grow_chunk(g, 2ull * n, 0, nc2 * 2 + 4096))) return rc;
+            continue;
+        }
+        // D, E: second-walk scans, second walks and the pair choice
+        scans(nc1, nc2);
+        k_pe_finish<<<(n + 127) / 128, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_recs);
+        g->launches++;
+        if ((rc = sync_ctr())) return rc;
+        if (g->h_ctr[CTR_HEAVY]) {
+            if (!g->d_pe_heavy) {
+                uint64_t off[27];
+                g->pe_heavy_warp_bytes = pe_layout(PE_HEAVY, off);
+                g->pe_heavy_warps = PE_HEAVY_WARPS;
+                CK(cudaMalloc((void**)&g->d_pe_heavy, g->pe_heavy_warp_bytes * g->pe_heavy_warps));
+            }
+            k_pe_heavy<<<g->pe_heavy_warps / 4, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_heavy,
+                                                                      g->pe_heavy_warp_bytes, PE_HEAVY);
+            g->launches++;
+        }
+        k_dp_warp<<<g->dp_grid, 128, 4 * DPW_BYTES, g->stream>>>(g->ix, cb);
+        g->launches++;
+        if ((rc = sync_ctr())) return rc;
+        if (g->h_ctr[CTR_ERRFLAG]) return set_err(g, FAME_ERR_INDEX, "a read pair exceeds the paired path's capacities");
+        if (cnt) {
+            const unsigned long long* h = g->h_ctr;
+            cnt->succ += h[CTR_SUCC];
+            cnt->nonunique += h[CTR_NONU];
+            cnt->unsucc += h[CTR_UNSUCC];
+            cnt->paired += h[CTR_PAIRED];
+            cnt->too_short += h[CTR_TOOSHORT];
+            cnt->r1_fwd += h[CTR_R1F];
+            cnt->r1_rev += h[CTR_R1R];
+            cnt->dp_reads += h[CTR_DP];
+            cnt->heavy_pairs += h[CTR_HEAVY];
+        }
+        return FAME_OK;
     }
-    k_dp_warp<<<g->dp_grid, 128, 4 * DPW_BYTES, g->stream>>>(g->ix, cb);
-    g->launches++;
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
-    CK(cudaStreamSynchronize(g->stream));
-    if (g->h_ctr[CTR_ERRFLAG]) return set_err(g, FAME_ERR_INDEX, "a read pair exceeds the paired path's capacities");
-    if (cnt) {
-        const unsigned long long* h = g->h_ctr;
-        cnt->succ += h[CTR_SUCC];
-        cnt->nonunique += h[CTR_NONU];
-        cnt->unsucc += h[CTR_UNSUCC];
-        cnt->paired += h[CTR_PAIRED];
-        cnt->too_short += h[CTR_TOOSHORT];
-        cnt->r1_fwd += h[CTR_R1F];
-        cnt->r1_rev += h[CTR_R1R];
-        cnt->dp_reads += h[CTR_DP];
-        cnt->heavy_pairs += h[CTR_HEAVY];
-    }
-    return FAME_OK;
+    return set_err(g, FAME_ERR_NOMEM, "candidate buffer kept overflowing");
 }
 
 }  // namespace

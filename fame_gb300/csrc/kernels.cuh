@@ -328,10 +328,11 @@ __device__ void shiftand_one(const DevIndex& ix, const ChunkBufs& cb, uint32_t c
     const uint32_t e = cb.cand[c];
     uint32_t n = 0;
     uint32_t* out = cb.hits + (uint64_t)c * HIT_CAP;
+    const bool unguarded = cb.cand_flags && (cb.cand_flags[c] & 1u);
     scan_window<W>(ix, sa, e & 0x7fffffffu, (int)(e >> 31), [&](uint32_t off, int err) {
         if (n < HIT_CAP) out[n] = (off << 8) | (uint32_t)err;
         ++n;
-    }, pk.key, pk.valid, pk.q, pk.start);
+    }, pk.key, pk.valid, pk.q, pk.start, unguarded);
     cb.hit_n[c] = n;
 }
 
@@ -344,7 +345,7 @@ __global__ void k_shiftand(DevIndex ix, ChunkBufs cb, uint32_t ncand)
         if (cand_overflow(cb) || !((cb.ctr[CTR_WMASK] >> W) & 1ull)) return;
         ncand = (uint32_t)cb.ctr[CTR_CAND];
     }
-    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncand; c += gridDim.x * blockDim.x) {
+    for (uint32_t c = cb.cand_first + blockIdx.x * blockDim.x + threadIdx.x; c < ncand; c += gridDim.x * blockDim.x) {
         const uint32_t task = cb.cand_task[c];
         const uint32_t r = task >> 1;
         const uint32_t len = (uint32_t)(cb.offs[r + 1] - cb.offs[r]);
@@ -751,7 +752,7 @@ __global__ void k_prep(ChunkBufs cb, uint32_t readlen)
 }
 
 // Light path: one warp per task, working memory in shared memory.
-constexpr uint32_t L_OPS = 256, L_DT = 512, L_SLOT = 512 + NBHD - 1, L_OVF = 32;
+constexpr uint32_t L_OPS = 128, L_DT = 256, L_SLOT = 512 + NBHD - 1, L_OVF = 32;
 struct LightLayout {
     // per warp, in bytes
     static constexpr uint32_t KST = 0;                          // 224 x u32
@@ -798,7 +799,7 @@ __device__ __forceinline__ SeedMem light_mem(uint8_t* base)
 }
 
 // tasks: all (read, orientation) pairs of the chunk in orientation-major order
-__global__ void k_seed(DevIndex ix, ChunkBufs cb, uint32_t ntask)
+__global__ void __launch_bounds__(128, 8) k_seed(DevIndex ix, ChunkBufs cb, uint32_t ntask)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const uint32_t wib = threadIdx.x >> 5;
@@ -874,6 +875,17 @@ __global__ void k_seed_heavy(DevIndex ix, ChunkBufs cb, HeavyScratch hs, uint32_
             cb.task_cand[task] = make_uint4(0, 0, 0, 0);
         }
         __syncwarp();
+    }
+}
+
+// tab2[k] = {tab[k], first entry of bucket k or 0}, k <= n (the bucket-offset
+// table with each bucket's first entry beside its start).
+__global__ void k_build_tab2(const uint32_t* tab, const uint32_t* entry, uint64_t n, uint2* tab2)
+{
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k <= n; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b0 = tab[k];
+        const uint32_t e = (k < n && tab[k + 1] > b0) ? entry[b0] : 0u;
+        tab2[k] = make_uint2(b0, e);
     }
 }
 

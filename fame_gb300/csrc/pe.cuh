@@ -234,7 +234,7 @@ __device__ uint32_t pe_kmers(const DevIndex& ix, const PeIndex& px, const PeMem&
             kq = (kq << 2) + ((c == 'C' || c == 'T') ? 3u : (c == 'G' ? 2u : 0u));
         }
         const uint32_t key = (uint32_t)(h & HTAB_MASK);
-        const uint32_t b0 = __ldg(ix.tab + key), b1 = __ldg(ix.tab + key + 1);
+        const uint32_t b0 = __ldg((const uint32_t*)(ix.tab2 + key)), b1 = __ldg((const uint32_t*)(ix.tab2 + key + 1));
         s.kst[p] = b0;
         s.kln[p] = b1 - b0;
         s.kcm[p] = cm;
@@ -685,6 +685,179 @@ __device__ __forceinline__ void pe_orient(uint8_t* rd, const char* raw, uint32_t
     for (uint32_t p = lane; p < len; p += 32) rd[p] = oriented_char(raw, len, orient, p);
 }
 
+// The pair choice of matchPairedReads (ReadQueue.cpp:1300-1638): the best
+// summed error count over the matches of both orientations within the pair
+// distance (extractPairedMatch), non-unique on a tie; CpG calls of a chosen
+// pair; counters; the mates' outputs.
+__device__ void pe_choose(const DevIndex& ix, const PeIndex& px, const ChunkBufs& cb, uint32_t i1, uint32_t i2,
+                          const uint64_t* m1F, uint32_t n1F, const uint64_t* m2R, uint32_t n2R, const uint64_t* m1R,
+                          uint32_t n1R, const uint64_t* m2F, uint32_t n2F)
+{
+    const uint32_t nh[4] = {n1F, n2R, n1R, n2F};
+    uint64_t mat1 = 0, mat2 = 0;
+    bool ok = false;
+    if ((nh[0] == 0 && nh[2] == 0) || (nh[1] == 0 && nh[3] == 0)) {
+        atomicAdd(cb.ctr + CTR_UNSUCC, 2ull);
+    } else {
+        const int WORST = 2 * (int)(MISCOUNT + ADDMIS) + 1;
+        int best = WORST;
+        bool nonUnique = false, orig = true;
+        uint64_t b1 = 0, b2 = 0;
+        if (cb.orient_mask & 1u)
+            for (uint32_t a = 0; a < nh[0]; ++a)
+                for (uint32_t b = 0; b < nh[1]; ++b) {
+                    const int e = pe_extract(ix, px, m1F[a], m2R[b]);
+                    if (e < 0) continue;
+                    if (e == best) nonUnique = true;
+                    else if (e < best) { best = e; b1 = m1F[a]; b2 = m2R[b]; nonUnique = false; }
+                }
+        if (cb.orient_mask & 2u)
+            for (uint32_t a = 0; a < nh[2]; ++a)
+                for (uint32_t b = 0; b < nh[3]; ++b) {
+                    const int e = pe_extract(ix, px, m1R[a], m2F[b]);
+                    if (e < 0) continue;
+                    if (e == best) nonUnique = true;
+                    else if (e < best) { best = e; b1 = m1R[a]; b2 = m2F[b]; orig = false; nonUnique = false; }
+                }
+        if (best == WORST) {
+            atomicAdd(cb.ctr + CTR_UNSUCC, 2ull);
+        } else if (nonUnique) {
+            atomicAdd(cb.ctr + CTR_NONU, 2ull);
+        } else {
+            ok = true;
+            mat1 = b1;
+            mat2 = b2;
+            if (cb.stranded) atomicAdd(cb.ctr + (orig ? CTR_R1F : CTR_R1R), 1ull);
+            pe_meth(ix, cb, i1, orig ? 0 : 1, b1);
+            pe_meth(ix, cb, i2, orig ? 1 : 0, b2);
+            const bool d1 = ix.win[(uint32_t)(b1 >> 32)].z == CPGDUMMY, d2 = ix.win[(uint32_t)(b2 >> 32)].z == CPGDUMMY;
+            if (d1 && d2) atomicAdd(cb.ctr + CTR_TOOSHORT, 2ull);
+            else if (d1 || d2) { atomicAdd(cb.ctr + CTR_TOOSHORT, 1ull); atomicAdd(cb.ctr + CTR_SUCC, 1ull); }
+            else { atomicAdd(cb.ctr + CTR_PAIRED, 1ull); atomicAdd(cb.ctr + CTR_SUCC, 2ull); }
+        }
+    }
+    cb.mats[i1] = ok ? mat1 : 0;
+    cb.mats[i2] = ok ? mat2 : 0;
+    cb.invalid[i1] = ok ? 0 : 1;
+    cb.invalid[i2] = ok ? 0 : 1;
+}
+
+// One orientation of a pair, all lanes: both maps, the f2 flags, hasCpG and
+// the final iteration orders (s.ord, st.nord).  Returns 1 when there is
+// something to walk, 0 when not, -1 when a capacity was exceeded.
+__device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& cb, const PeMem& s, uint32_t i1,
+                       uint32_t i2, uint32_t n1, uint32_t n2, int o, PeState& st)
+{
+    const int lane = threadIdx.x & 31;
+    st = PeState{};
+    // first = mate 1 (o = 0) or its reverse complement; second = the other strand of mate 2
+    pe_orient(s.rd[0], cb.seqs + cb.offs[i1], n1, o);
+    pe_orient(s.rd[1], cb.seqs + cb.offs[i2], n2, 1 - o);
+    for (uint32_t i = lane; i < s.c.vcap; i += 32) {
+        s.vk[0][i] = EMPTY_KEY;
+        s.vk[1][i] = EMPTY_KEY;
+        s.vv[0][i] = 0;
+        s.vv[1][i] = 0;
+    }
+    __syncwarp();
+    const uint32_t sigma = pe_kmers(ix, px, s, s.rd[0], n1);
+    if (lane == 0) {
+        pe_count_first(ix, px, s, st, n1, sigma <= s.c.ecap);
+        // rebuild: keep count1 >= QTHRESH
+        if (!st.over)
+            for (int dir = 0; dir < 2; ++dir)
+                for (uint32_t x = 0; x < st.n1[dir]; ++x) {
+                    const int h = pm_find(s, dir, s.ins1[dir][x]);
+                    if (pv_c1(s.vv[dir][h]) < QTHRESH) s.vv[dir][h] = 0;
+                    else s.vv[dir][h] = PV_PRESENT | pv_c1(s.vv[dir][h]);
+                }
+    }
+    if (__shfl_sync(0xffffffffu, st.over, 0)) return -1;
+    bool any = false;
+    if (lane == 0)
+        for (int dir = 0; dir < 2 && !any; ++dir)
+            for (uint32_t x = 0; x < st.n1[dir]; ++x)
+                if (pm_find(s, dir, s.ins1[dir][x]) >= 0) { any = true; break; }
+    if (!__shfl_sync(0xffffffffu, any, 0)) return 0;
+    __syncwarp();
+    const uint32_t sigma2 = pe_kmers(ix, px, s, s.rd[1], n2);
+    if (lane == 0) pe_count_second(ix, px, s, st, n2, sigma2 <= s.c.ecap);
+    if (__shfl_sync(0xffffffffu, st.over, 0)) return -1;
+    __syncwarp();
+    // f2 flags (order-independent: flags are only set) and hasCpG, lanes over the table slots
+    {
+        const int ctx = (int)px.ctx;
+        for (int dir = 0; dir < 2; ++dir)
+            for (uint32_t hh = lane; hh < s.c.vcap; hh += 32) {
+                const uint32_t v = s.vv[dir][hh];
+                const uint32_t key = s.vk[dir][hh];
+                if (key == EMPTY_KEY || !(v & PV_PRESENT) || pv_c2(v) < QTHRESH) continue;
+                atomicOr(&s.vv[dir][hh], PV_F2);
+                for (int c = 1; c <= ctx; ++c) {
+                    int h2 = pm_find(s, dir, key + (uint32_t)c);
+                    if (h2 >= 0) atomicOr(&s.vv[dir][h2], PV_F2);
+                    h2 = pm_find(s, dir, key - (uint32_t)c);
+                    if (h2 >= 0) atomicOr(&s.vv[dir][h2], PV_F2);
+                }
+            }
+    }
+    __syncwarp();
+    bool mine = false;
+    for (int dir = 0; dir < 2; ++dir)
+        for (uint32_t hh = lane; hh < s.c.vcap; hh += 32) {
+            const uint32_t v = s.vv[dir][hh];
+            const uint32_t key = s.vk[dir][hh];
+            mine |= key != EMPTY_KEY && (v & PV_PRESENT) && (v & PV_F2) && ix.win[key].z != CPGDUMMY;
+        }
+    if (!__any_sync(0xffffffffu, mine)) return 0;
+    if (lane == 0) {
+        // Final iteration orders: the replay of the first map, its kept keys, then the second
+        // mate's insertions.  The walks scan only keys with count >= QTHRESH (count1 in the
+        // first, count2 in the second), and a strand map with at most one such key in both
+        // counts puts it first after either sort whatever the order of the others, so then
+        // no replay is needed.
+        bool need = false;
+        for (int dir = 0; dir < 2; ++dir) {
+            uint32_t c1 = 0, c2 = 0;
+            for (uint32_t x = 0; x < st.n1[dir]; ++x) {
+                const int h = pm_find(s, dir, s.ins1[dir][x]);
+                if (h >= 0) { c1 += pv_c1(s.vv[dir][h]) >= QTHRESH; c2 += pv_c2(s.vv[dir][h]) >= QTHRESH; }
+            }
+            for (uint32_t x = 0; x < st.n2[dir]; ++x) {
+                const int h = pm_find(s, dir, s.ins2[dir][x]);
+                if (h >= 0) c2 += pv_c2(s.vv[dir][h]) >= QTHRESH;
+            }
+            need |= c1 > 1 || c2 > 1;
+        }
+        for (int dir = 0; dir < 2 && !need; ++dir) {
+            uint32_t ns = 0;
+            for (uint32_t x = 0; x < st.n1[dir]; ++x) {
+                const int h = pm_find(s, dir, s.ins1[dir][x]);
+                if (h >= 0 && pv_c1(s.vv[dir][h]) >= QTHRESH) s.ord[dir][ns++] = s.ins1[dir][x];
+            }
+            for (uint32_t x = 0; x < st.n2[dir]; ++x) s.ord[dir][ns++] = s.ins2[dir][x];
+            st.nord[dir] = ns;
+        }
+        for (int dir = 0; dir < 2 && need && !st.over; ++dir) {
+            uint32_t nt = 0;
+            if (!pe_replay(s, s.ins1[dir], st.n1[dir], sigma / 5, s.ord[dir], nt)) { st.over = true; break; }
+            uint32_t ns = 0;
+            for (uint32_t q = 0; q < nt; ++q) {
+                const uint32_t key = s.ord[dir][q];
+                const int h = pm_find(s, dir, key);
+                // kept keys are present with count1 >= QTHRESH; keys the second mate re-inserted
+                // after the rebuild dropped them come later, from ins2
+                if (h >= 0 && pv_c1(s.vv[dir][h]) >= QTHRESH) s.seq[ns++] = key;
+            }
+            for (uint32_t x = 0; x < st.n2[dir]; ++x) s.seq[ns++] = s.ins2[dir][x];
+            if (!pe_replay(s, s.seq, ns, 20, s.ord[dir], st.nord[dir])) { st.over = true; break; }
+        }
+    }
+    if (__shfl_sync(0xffffffffu, st.over, 0)) return -1;
+    __syncwarp();
+    return 1;
+}
+
 template <int WMAX>
 __device__ bool pe_pair(const DevIndex& ix, const PeIndex& px, const ChunkBufs& cb, const PeMem& s, uint32_t r)
 {
@@ -699,150 +872,21 @@ __device__ bool pe_pair(const DevIndex& ix, const PeIndex& px, const ChunkBufs& 
     if ((f1 | f2) & 3u) return true;     // counted and written by k_pe_prep
     for (int o = 0; o < 2; ++o) {
         if (!((cb.orient_mask >> o) & 1u)) continue;
-        // first = mate 1 (o = 0) or its reverse complement; second = the other strand of mate 2
-        pe_orient(s.rd[0], cb.seqs + cb.offs[i1], n1, o);
-        pe_orient(s.rd[1], cb.seqs + cb.offs[i2], n2, 1 - o);
-        for (uint32_t i = lane; i < s.c.vcap; i += 32) {
-            s.vk[0][i] = EMPTY_KEY;
-            s.vk[1][i] = EMPTY_KEY;
-            s.vv[0][i] = 0;
-            s.vv[1][i] = 0;
-        }
-        __syncwarp();
-        const uint32_t sigma = pe_kmers(ix, px, s, s.rd[0], n1);
-        PeState st{};
+        PeState st;
+        const int m = pe_maps(ix, px, cb, s, i1, i2, n1, n2, o, st);
+        if (m < 0) return false;
+        if (m == 0) continue;
         if (lane == 0) {
-            pe_count_first(ix, px, s, st, n1, sigma <= s.c.ecap);
-            // rebuild: keep count1 >= QTHRESH
-            if (!st.over)
-                for (int dir = 0; dir < 2; ++dir)
-                    for (uint32_t x = 0; x < st.n1[dir]; ++x) {
-                        const int h = pm_find(s, dir, s.ins1[dir][x]);
-                        if (pv_c1(s.vv[dir][h]) < QTHRESH) s.vv[dir][h] = 0;
-                        else s.vv[dir][h] = PV_PRESENT | pv_c1(s.vv[dir][h]);
-                    }
+            uint64_t* ha = s.hits[o == 0 ? 0 : 2];
+            uint64_t* hb = s.hits[o == 0 ? 1 : 3];
+            pe_walk_any<WMAX>(ix, px, s, st, cb, i1, o, 0, ha, nh[o == 0 ? 0 : 2]);
+            if (!st.over && nh[o == 0 ? 0 : 2] > 0)
+                pe_walk_any<WMAX>(ix, px, s, st, cb, i2, 1 - o, 1, hb, nh[o == 0 ? 1 : 3]);
         }
-        bool over = __shfl_sync(0xffffffffu, st.over, 0);
-        if (over) return false;
-        bool any = false;
-        if (lane == 0)
-            for (int dir = 0; dir < 2 && !any; ++dir)
-                for (uint32_t x = 0; x < st.n1[dir]; ++x)
-                    if (pm_find(s, dir, s.ins1[dir][x]) >= 0) { any = true; break; }
-        any = __shfl_sync(0xffffffffu, any, 0);
-        if (!any) continue;
-        __syncwarp();
-        const uint32_t sigma2 = pe_kmers(ix, px, s, s.rd[1], n2);
-        bool hasCpG = false;
-        if (lane == 0) {
-            pe_count_second(ix, px, s, st, n2, sigma2 <= s.c.ecap);
-            if (!st.over) {
-                // f2 flags (order-independent) and hasCpG
-                const int ctx = (int)px.ctx;
-                for (int dir = 0; dir < 2; ++dir)
-                    for (uint32_t hh = 0; hh < s.c.vcap; ++hh) {
-                        const uint32_t v = s.vv[dir][hh];
-                        const uint32_t key = s.vk[dir][hh];
-                        if (key == EMPTY_KEY || !(v & PV_PRESENT) || pv_c2(v) < QTHRESH) continue;
-                        s.vv[dir][hh] |= PV_F2;
-                        for (int c = 1; c <= ctx; ++c) {
-                            int h2 = pm_find(s, dir, key + (uint32_t)c);
-                            if (h2 >= 0) s.vv[dir][h2] |= PV_F2;
-                            h2 = pm_find(s, dir, key - (uint32_t)c);
-                            if (h2 >= 0) s.vv[dir][h2] |= PV_F2;
-                        }
-                    }
-                for (int dir = 0; dir < 2 && !hasCpG; ++dir)
-                    for (uint32_t hh = 0; hh < s.c.vcap; ++hh) {
-                        const uint32_t v = s.vv[dir][hh];
-                        const uint32_t key = s.vk[dir][hh];
-                        if (key != EMPTY_KEY && (v & PV_PRESENT) && (v & PV_F2) && ix.win[key].z != CPGDUMMY) {
-                            hasCpG = true;
-                            break;
-                        }
-                    }
-            }
-            if (hasCpG && !st.over) {
-                // final iteration orders: replay of the first map, kept keys, then the second mate's insertions
-                for (int dir = 0; dir < 2 && !st.over; ++dir) {
-                    uint32_t nt = 0;
-                    if (!pe_replay(s, s.ins1[dir], st.n1[dir], sigma / 5, s.ord[dir], nt)) { st.over = true; break; }
-                    uint32_t ns = 0;
-                    for (uint32_t q = 0; q < nt; ++q) {
-                        const uint32_t key = s.ord[dir][q];
-                        const int h = pm_find(s, dir, key);
-                        // kept keys are present with count1 >= QTHRESH; keys the second mate re-inserted
-                        // after the rebuild dropped them come later, from ins2
-                        if (h >= 0 && pv_c1(s.vv[dir][h]) >= QTHRESH) s.seq[ns++] = key;
-                    }
-                    for (uint32_t x = 0; x < st.n2[dir]; ++x) s.seq[ns++] = s.ins2[dir][x];
-                    if (!pe_replay(s, s.seq, ns, 20, s.ord[dir], st.nord[dir])) { st.over = true; break; }
-                }
-                if (!st.over) {
-                    uint64_t* ha = s.hits[o == 0 ? 0 : 2];
-                    uint64_t* hb = s.hits[o == 0 ? 1 : 3];
-                    pe_walk_any<WMAX>(ix, px, s, st, cb, i1, o, 0, ha, nh[o == 0 ? 0 : 2]);
-                    if (!st.over && nh[o == 0 ? 0 : 2] > 0)
-                        pe_walk_any<WMAX>(ix, px, s, st, cb, i2, 1 - o, 1, hb, nh[o == 0 ? 1 : 3]);
-                }
-            }
-        }
-        over = __shfl_sync(0xffffffffu, st.over, 0);
-        if (over) return false;
+        if (__shfl_sync(0xffffffffu, st.over, 0)) return false;
         __syncwarp();
     }
-    if (lane == 0) {
-        uint64_t* m1F = s.hits[0];
-        uint64_t* m2R = s.hits[1];
-        uint64_t* m1R = s.hits[2];
-        uint64_t* m2F = s.hits[3];
-        uint64_t mat1 = 0, mat2 = 0;
-        bool ok = false;
-        if ((nh[0] == 0 && nh[2] == 0) || (nh[1] == 0 && nh[3] == 0)) {
-            atomicAdd(cb.ctr + CTR_UNSUCC, 2ull);
-        } else {
-            const int WORST = 2 * (int)(MISCOUNT + ADDMIS) + 1;
-            int best = WORST;
-            bool nonUnique = false, orig = true;
-            uint64_t b1 = 0, b2 = 0;
-            if (cb.orient_mask & 1u)
-                for (uint32_t a = 0; a < nh[0]; ++a)
-                    for (uint32_t b = 0; b < nh[1]; ++b) {
-                        const int e = pe_extract(ix, px, m1F[a], m2R[b]);
-                        if (e < 0) continue;
-                        if (e == best) nonUnique = true;
-                        else if (e < best) { best = e; b1 = m1F[a]; b2 = m2R[b]; nonUnique = false; }
-                    }
-            if (cb.orient_mask & 2u)
-                for (uint32_t a = 0; a < nh[2]; ++a)
-                    for (uint32_t b = 0; b < nh[3]; ++b) {
-                        const int e = pe_extract(ix, px, m1R[a], m2F[b]);
-                        if (e < 0) continue;
-                        if (e == best) nonUnique = true;
-                        else if (e < best) { best = e; b1 = m1R[a]; b2 = m2F[b]; orig = false; nonUnique = false; }
-                    }
-            if (best == WORST) {
-                atomicAdd(cb.ctr + CTR_UNSUCC, 2ull);
-            } else if (nonUnique) {
-                atomicAdd(cb.ctr + CTR_NONU, 2ull);
-            } else {
-                ok = true;
-                mat1 = b1;
-                mat2 = b2;
-                if (cb.stranded) atomicAdd(cb.ctr + (orig ? CTR_R1F : CTR_R1R), 1ull);
-                pe_meth(ix, cb, i1, orig ? 0 : 1, b1);
-                pe_meth(ix, cb, i2, orig ? 1 : 0, b2);
-                const bool d1 = ix.win[(uint32_t)(b1 >> 32)].z == CPGDUMMY, d2 = ix.win[(uint32_t)(b2 >> 32)].z == CPGDUMMY;
-                if (d1 && d2) atomicAdd(cb.ctr + CTR_TOOSHORT, 2ull);
-                else if (d1 || d2) { atomicAdd(cb.ctr + CTR_TOOSHORT, 1ull); atomicAdd(cb.ctr + CTR_SUCC, 1ull); }
-                else { atomicAdd(cb.ctr + CTR_PAIRED, 1ull); atomicAdd(cb.ctr + CTR_SUCC, 2ull); }
-            }
-        }
-        cb.mats[i1] = ok ? mat1 : 0;
-        cb.mats[i2] = ok ? mat2 : 0;
-        cb.invalid[i1] = ok ? 0 : 1;
-        cb.invalid[i2] = ok ? 0 : 1;
-    }
+    if (lane == 0) pe_choose(ix, px, cb, i1, i2, s.hits[0], nh[0], s.hits[1], nh[1], s.hits[2], nh[2], s.hits[3], nh[3]);
     __syncwarp();
     return true;
 }
@@ -891,32 +935,8 @@ __global__ void k_pe_prep(ChunkBufs cb, uint32_t readlen)
     atomicOr(cb.ctr + CTR_WMASK, 1ull << wmax);
 }
 
-// Pairs whose widest mate needs WMAX words; warp per pair, working memory in
-// shared memory, pairs over the caps go to the heavy list.
-template <int WMAX>
-__global__ void k_pe(DevIndex ix, PeIndex px, ChunkBufs cb, uint32_t warp_bytes)
-{
-    extern __shared__ __align__(16) uint8_t smem[];
-    const int lane = threadIdx.x & 31;
-    const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const uint32_t nw = gridDim.x * (blockDim.x >> 5);
-    const PeMem s = pe_mem(smem + (threadIdx.x >> 5) * warp_bytes, PE_LIGHT);
-    for (uint32_t r = wid; r < cb.n; r += nw) {
-        const uint32_t l1 = (uint32_t)(cb.offs[r + 1] - cb.offs[r]);
-        const uint32_t l2 = (uint32_t)(cb.offs[cb.n + r + 1] - cb.offs[cb.n + r]);
-        if ((cb.rflags[r] | cb.rflags[cb.n + r]) & 7u) continue;
-        if ((int)(max(l1, l2) / 64 + 1) != WMAX) continue;
-        if (!pe_pair<WMAX>(ix, px, cb, s, r)) {
-            if (lane == 0) {
-                const uint32_t k = (uint32_t)atomicAdd(cb.ctr + CTR_HEAVY, 1ull);
-                cb.heavy[k] = r;
-            }
-        }
-        __syncwarp();
-    }
-}
-
-// Heavy pairs: same code with large caps in global scratch.
+// Pairs the pipelined path hands over: the whole per-pair path (pe_pair) with
+// large capacities in global scratch.
 __global__ void k_pe_heavy(DevIndex ix, PeIndex px, ChunkBufs cb, uint8_t* scratch, uint64_t warp_bytes, PeCaps caps)
 {
     const int lane = threadIdx.x & 31;
@@ -930,6 +950,282 @@ __global__ void k_pe_heavy(DevIndex ix, PeIndex px, ChunkBufs cb, uint8_t* scrat
             if (lane == 0) atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull);
         }
         __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined paired path.  The walks' window scans leave the pair's warp and
+// run like the single-end scans, one thread per candidate window:
+//   A  k_pe_seed   warp per pair: both orientations' maps (pe_maps), the walk
+//                  lists sorted as the walks sort them and cut to the keys whose
+//                  count reaches QTHRESH, and the first walk's candidates
+//                  (f2-flagged keys; the walk's dynamic threshold
+//                  max(bmCount - KMERDIST, QTHRESH) only removes keys, so these
+//                  are a superset of what it scans)
+//   B  k_shiftand  the first walk's candidates (pattern: the first mate)
+//   C  k_pe_walk1  thread per pair orientation: the first walk over the scan
+//                  results, its matches, the f3 flags (windows within
+//                  contextWLen of a window with hits) and the second walk's
+//                  candidates (f3-flagged keys)
+//   D  k_shiftand  the second walk's candidates (the second mate, reverse
+//                  windows from startPos - 1)
+//   E  k_pe_finish thread per pair: the second walks, the pair choice, CpG calls
+// A pair that exceeds a list or match capacity, or whose window has more hit
+// runs than the scan keeps, is handed whole to k_pe_heavy (the full per-pair
+// path above); nothing of it is written before that.
+// ---------------------------------------------------------------------------
+constexpr int PE_CAPL = 8;    // keys of one walk list and strand
+constexpr int PE_HCAP = 32;   // matches of one mate and orientation
+constexpr uint32_t PT_NONE = 0, PT_WALK = 1, PT_FALLBACK = 2;
+constexpr uint32_t NO_CAND = 0xffffffffu;
+
+struct PeTaskRec {            // one pair orientation
+    uint32_t state;
+    uint32_t m1n;             // matches of the first walk
+    uint8_t n1[2], n2[2];     // keys of the walk lists per strand
+    uint32_t pad;
+    uint4 w1[2][PE_CAPL];     // {key, count1 | count2 << 8 | f2 << 16, candidate, -}
+    uint4 w2[2][PE_CAPL];     // {key, count1 | count2 << 8, candidate, f3}
+    uint64_t m1[PE_HCAP];
+};
+
+// Stage A, lane 0: the walk lists of one orientation and its first-walk candidates.
+__device__ bool pe_lists(const PeMem& s, const PeState& st, const ChunkBufs& cb, PeTaskRec& t, uint32_t i1, int o)
+{
+    for (int second = 0; second < 2; ++second) {
+        const PeCmp cmp{second};
+        for (int dir = 0; dir < 2; ++dir) {
+            const uint32_t nl = st.nord[dir];
+            for (uint32_t q = 0; q < nl; ++q) {
+                const uint32_t key = s.ord[dir][q];
+                const int h = pm_find(s, dir, key);
+                s.list[dir][q] = make_uint2(key, h >= 0 ? s.vv[dir][h] : 0u);
+            }
+            pe_sort(s.list[dir], (long)nl, cmp);
+            uint32_t k = 0;
+            for (uint32_t q = 0; q < nl; ++q) {
+                const uint32_t v = s.list[dir][q].y;
+                if ((second ? pv_c2(v) : pv_c1(v)) < QTHRESH) break;   // counts sorted descending
+                if (k >= (uint32_t)PE_CAPL) return false;
+                const uint32_t cnts = pv_c1(v) | (pv_c2(v) << 8);
+                if (second) t.w2[dir][k] = make_uint4(s.list[dir][q].x, cnts, NO_CAND, 0);
+                else t.w1[dir][k] = make_uint4(s.list[dir][q].x, cnts | ((v & PV_F2) ? 1u << 16 : 0u), NO_CAND, 0);
+                ++k;
+            }
+            if (second) t.n2[dir] = (uint8_t)k;
+            else t.n1[dir] = (uint8_t)k;
+        }
+    }
+    for (int dir = 0; dir < 2; ++dir)
+        for (uint32_t k = 0; k < t.n1[dir]; ++k) {
+            if (!((t.w1[dir][k].y >> 16) & 1u)) continue;
+            const uint32_t ci = (uint32_t)atomicAdd(cb.ctr + CTR_CAND, 1ull);
+            if (ci < cb.cand_cap) {
+                cb.cand[ci] = t.w1[dir][k].x | ((uint32_t)dir << 31);
+                cb.cand_task[ci] = (i1 << 1) | (uint32_t)o;
+                cb.cand_flags[ci] = 0;
+            }
+            t.w1[dir][k].z = ci;
+        }
+    return true;
+}
+
+__global__ void k_pe_seed(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs, uint32_t warp_bytes)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int lane = threadIdx.x & 31;
+    const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+    const PeMem s = pe_mem(smem + (threadIdx.x >> 5) * warp_bytes, PE_LIGHT);
+    const uint32_t n = cb.n;
+    for (uint32_t r = wid; r < n; r += nw) {
+        if (lane == 0)
+            for (int o = 0; o < 2; ++o) {
+                recs[2 * r + o].state = PT_NONE;
+                recs[2 * r + o].m1n = 0;
+                recs[2 * r + o].n1[0] = recs[2 * r + o].n1[1] = 0;
+                recs[2 * r + o].n2[0] = recs[2 * r + o].n2[1] = 0;
+            }
+        if ((cb.rflags[r] | cb.rflags[n + r]) & 7u) continue;   // k_pe_prep finished the pair
+        const uint32_t i1 = r, i2 = n + r;
+        const uint32_t n1 = (uint32_t)(cb.offs[i1 + 1] - cb.offs[i1]);
+        const uint32_t n2 = (uint32_t)(cb.offs[i2 + 1] - cb.offs[i2]);
+        bool fb = false;
+        for (int o = 0; o < 2 && !fb; ++o) {
+            if (!((cb.orient_mask >> o) & 1u)) continue;
+            PeState st;
+            const int m = pe_maps(ix, px, cb, s, i1, i2, n1, n2, o, st);
+            if (m < 0) { fb = true; break; }
+            if (m == 0) continue;
+            bool ok = true;
+            if (lane == 0) {
+                PeTaskRec& t = recs[2 * r + o];
+                ok = pe_lists(s, st, cb, t, i1, o);
+                t.state = ok ? PT_WALK : PT_FALLBACK;
+            }
+            fb = !__shfl_sync(0xffffffffu, ok, 0);
+            __syncwarp();
+        }
+        if (fb && lane == 0) {
+            recs[2 * r].state = PT_FALLBACK;
+            recs[2 * r + 1].state = PT_FALLBACK;
+        }
+        __syncwarp();
+    }
+}
+
+// Walk order of two strand lists: the heads' count1 decide when both have keys
+// to scan (ReadQueue.cpp:2185, 2265); with one list empty the order changes nothing.
+__device__ __forceinline__ void pe_walk_order(uint32_t n0, uint32_t n1, uint32_t head0_c1, uint32_t head1_c1, int* order)
+{
+    order[0] = 0;
+    order[1] = 1;
+    if (n0 > 0 && n1 > 0 && head1_c1 > head0_c1) { order[0] = 1; order[1] = 0; }
+}
+
+// Stage C: the first walk of one pair orientation.
+__global__ void k_pe_walk1(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * cb.n) return;
+    PeTaskRec& rec = recs[t];
+    if (rec.state != PT_WALK) return;
+    const uint32_t r = t >> 1;
+    const int o = (int)(t & 1);
+    int order[2];
+    pe_walk_order(rec.n1[0], rec.n1[1], rec.w1[0][0].y & 0xffu, rec.w1[1][0].y & 0xffu, order);
+    int32_t bmCount = 0;
+    uint32_t prevChr = 0;
+    uint64_t prevOff = 0xffffffffffffffffull;
+    uint32_t m1n = 0;
+    uint32_t hitwin[2][PE_CAPL];
+    uint32_t nhw[2] = {0, 0};
+    for (int wk = 0; wk < 2; ++wk) {
+        const int dir = order[wk];
+        if (wk == 1) { prevChr = 0; prevOff = 0xffffffffffffffffull; }
+        for (uint32_t k = 0; k < rec.n1[dir]; ++k) {
+            const uint4 e = rec.w1[dir][k];
+            const int32_t cnt = (int32_t)(e.y & 0xffu);
+            const int32_t thr = bmCount - (int32_t)KMERDIST > (int32_t)QTHRESH ? bmCount - (int32_t)KMERDIST : (int32_t)QTHRESH;
+            if (cnt < thr) break;
+            if (!((e.y >> 16) & 1u)) continue;
+            const uint32_t c = e.z, w = e.x;
+            const uint32_t nh = cb.hit_n[c];
+            if (nh > (uint32_t)HIT_CAP) { rec.state = PT_FALLBACK; return; }
+            const uint4 wi = ix.win[w];
+            const uint32_t sp = wi.x, ch = wi.y;
+            uint32_t last = 0;
+            for (uint32_t i = 0; i < nh; ++i) {
+                const uint32_t h = cb.hits[(uint64_t)c * HIT_CAP + i];
+                const uint32_t off = h >> 8, err = h & 0xffu;
+                if (!(i == 0 && (uint64_t)off + sp == prevOff && ch == prevChr)) {
+                    if (m1n >= (uint32_t)PE_HCAP) { rec.state = PT_FALLBACK; return; }
+                    rec.m1[m1n++] = mk_match(off, err, (uint64_t)dir, w);
+                }
+                last = off;
+            }
+            if (nh > 0) {
+                if (cnt > bmCount) bmCount = cnt;
+                hitwin[dir][nhw[dir]++] = w;
+                prevChr = ch;
+                prevOff = (uint64_t)sp + last;
+            } else {
+                prevChr = 0;
+                prevOff = 0xffffffffffffffffull;
+            }
+        }
+    }
+    rec.m1n = m1n;
+    if (m1n == 0) return;
+    // f3: the first walk flags each window with hits and its neighbours within contextWLen
+    const uint32_t ctx = px.ctx;
+    for (int dir = 0; dir < 2; ++dir)
+        for (uint32_t k = 0; k < rec.n2[dir]; ++k) {
+            const uint32_t key = rec.w2[dir][k].x;
+            bool f3 = false;
+            for (uint32_t h = 0; h < nhw[dir] && !f3; ++h)
+                for (uint32_t c = 0; c <= ctx && !f3; ++c)
+                    f3 = key == hitwin[dir][h] + c || key == hitwin[dir][h] - c;
+            rec.w2[dir][k].w = f3 ? 1u : 0u;
+            if (!f3) continue;
+            const uint32_t ci = (uint32_t)atomicAdd(cb.ctr + CTR_CAND, 1ull);
+            if (ci < cb.cand_cap) {
+                cb.cand[ci] = key | ((uint32_t)dir << 31);
+                cb.cand_task[ci] = ((cb.n + r) << 1) | (uint32_t)(1 - o);
+                cb.cand_flags[ci] = dir == 0 ? 1 : 0;                        // matchRevSecond's unguarded start
+            }
+            rec.w2[dir][k].z = ci;
+        }
+}
+
+// Stage E: the second walks of both orientations and the pair choice.
+__global__ void k_pe_finish(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs)
+{
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = cb.n;
+    if (r >= n) return;
+    if ((cb.rflags[r] | cb.rflags[n + r]) & 7u) return;       // k_pe_prep finished the pair
+    if (recs[2 * r].state == PT_FALLBACK || recs[2 * r + 1].state == PT_FALLBACK) {
+        const uint32_t k = (uint32_t)atomicAdd(cb.ctr + CTR_HEAVY, 1ull);
+        cb.heavy[k] = r;
+        return;
+    }
+    uint64_t m2[2][PE_HCAP];
+    uint32_t n2c[2] = {0, 0};
+    for (int o = 0; o < 2; ++o) {
+        const PeTaskRec& rec = recs[2 * r + o];
+        if (rec.state != PT_WALK || rec.m1n == 0) continue;
+        int order[2];
+        pe_walk_order(rec.n2[0], rec.n2[1], rec.w2[0][0].y & 0xffu, rec.w2[1][0].y & 0xffu, order);
+        int32_t bmCount = 0;
+        uint32_t prevChr = 0;
+        uint64_t prevOff = 0xffffffffffffffffull;
+        for (int wk = 0; wk < 2; ++wk) {
+            const int dir = order[wk];
+            if (wk == 1) { prevChr = 0; prevOff = 0xffffffffffffffffull; }
+            for (uint32_t k = 0; k < rec.n2[dir]; ++k) {
+                const uint4 e = rec.w2[dir][k];
+                const int32_t cnt = (int32_t)((e.y >> 8) & 0xffu);
+                const int32_t thr = bmCount - (int32_t)KMERDIST > (int32_t)QTHRESH ? bmCount - (int32_t)KMERDIST : (int32_t)QTHRESH;
+                if (cnt < thr) break;
+                if (!e.w) continue;
+                const uint32_t c = e.z, w = e.x;
+                const uint32_t nh = cb.hit_n[c];
+                const uint4 wi = ix.win[w];
+                const uint32_t sp = wi.x, ch = wi.y;
+                if (nh > (uint32_t)HIT_CAP) goto fallback;
+                uint32_t last = 0;
+                for (uint32_t i = 0; i < nh; ++i) {
+                    const uint32_t h = cb.hits[(uint64_t)c * HIT_CAP + i];
+                    const uint32_t off = h >> 8, err = h & 0xffu;
+                    if (!(i == 0 && (uint64_t)off + sp == prevOff && ch == prevChr)) {
+                        if (n2c[o] >= (uint32_t)PE_HCAP) goto fallback;
+                        m2[o][n2c[o]++] = mk_match(off, err, (uint64_t)dir, w);
+                    }
+                    last = off;
+                }
+                if (nh > 0) {
+                    if (cnt > bmCount) bmCount = cnt;
+                    prevChr = ch;
+                    prevOff = (uint64_t)sp + last;
+                } else {
+                    prevChr = 0;
+                    prevOff = 0xffffffffffffffffull;
+                }
+            }
+        }
+    }
+    {
+        const PeTaskRec& a = recs[2 * r];
+        const PeTaskRec& b = recs[2 * r + 1];
+        pe_choose(ix, px, cb, r, n + r, a.m1, a.state == PT_WALK ? a.m1n : 0, m2[0], n2c[0], b.m1,
+                  b.state == PT_WALK ? b.m1n : 0, m2[1], n2c[1]);
+    }
+    return;
+fallback:
+    {
+        const uint32_t k = (uint32_t)atomicAdd(cb.ctr + CTR_HEAVY, 1ull);
+        cb.heavy[k] = r;
     }
 }
 

@@ -186,16 +186,19 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
             if ((SEEDBITS >> (31 - i)) & 1u) h ^= rotl64(nt_val(s.seq[p + i]), 31 - i);
         s.kst[p] = (uint32_t)(h & HTAB_MASK);
     }
+    constexpr int KPL = (FAME_MAX_READ_LEN - KMERLEN + 1 + 31) / 32;   // k-mers per lane, at most
+    uint32_t e0[KPL];                                                    // first entry of each bucket
     {
-        constexpr int KPL = (FAME_MAX_READ_LEN - KMERLEN + 1 + 31) / 32;   // k-mers per lane, at most
         uint32_t b0[KPL], b1[KPL];
 #pragma unroll
         for (int j = 0; j < KPL; ++j) {
             const uint32_t p = lane + 32 * j;
             if (p < nk) {
                 const uint32_t key = s.kst[p];
-                b0[j] = __ldg(ix.tab + key);
-                b1[j] = __ldg(ix.tab + key + 1);
+                const uint2 t = __ldg(ix.tab2 + key);
+                b0[j] = t.x;
+                e0[j] = t.y;
+                b1[j] = __ldg((const uint32_t*)(ix.tab2 + key + 1));
             }
         }
 #pragma unroll
@@ -237,7 +240,13 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
     if (T > s.ops_cap) return 1;
     if (lane == 0) atomicAdd(gather_bytes_acc, gb);
     // 2. gather entries (getSeedRefs pass 2, ReadQueue.cpp:2361-2460): the
-    //    k-mer of every op first, then the entry reads, up to 8 per lane in flight
+    //    first entry of each bucket came with its bounds; the k-mer of every
+    //    op, then the other entries, up to 8 reads per lane in flight
+#pragma unroll
+    for (int j = 0; j < KPL; ++j) {
+        const uint32_t p = lane + 32 * j;
+        if (p < nk && s.kpre[p + 1] > s.kpre[p]) s.ops[s.kpre[p]] = e0[j];
+    }
     for (uint32_t p = lane; p < nk; p += 32) {
         const uint32_t b = s.kpre[p], n = s.kpre[p + 1] - b;
         for (uint32_t j = 0; j < n; ++j) s.opk[b + j] = (uint8_t)p;
@@ -245,18 +254,24 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
     __syncwarp();
     for (uint32_t base = 0; base < T; base += 256) {
         uint32_t e[8];
+        bool ld[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const uint32_t i = base + lane + 32 * j;
+            ld[j] = false;
             if (i < T) {
                 const uint32_t p = s.opk[i];
-                e[j] = __ldg(ix.entry + s.kst[p] + (i - s.kpre[p]));
+                const uint32_t k = i - s.kpre[p];
+                if (k > 0) {
+                    e[j] = __ldg(ix.entry + s.kst[p] + k);
+                    ld[j] = true;
+                }
             }
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const uint32_t i = base + lane + 32 * j;
-            if (i < T) s.ops[i] = e[j];
+            if (ld[j]) s.ops[i] = e[j];
         }
     }
     // 3. distinct keys with counts and first op (consecutive duplicates within a
