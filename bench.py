@@ -12,8 +12,9 @@ orientation, as FAME's queryRoutine runs them.
 value: reads/s with reads resident in HBM (fame_gpu_match_reads_dev).
 e2e:   reads/s through fame_gpu_match_reads from pinned host buffers, host to
        device copy of the chunk and device to host copy of the results timed.
-Both: per-step inputs are new reads, and each step gathers from a 5.2 GB index
-(4.3 GB bucket offsets + 1.2 GB entries), far larger than the 129 MB L2.
+Both: per-step inputs are new reads, and each step gathers from a 9.8 GB index
+(8.6 GB bucket offsets with first entries + 1.2 GB entries), far larger than
+the 129 MB L2.
 
 --impl reference: the reference's own OpenMP matchReads (compiled from its
 sources by oracle/build_ref.sh) on the machine's host cores, on bounded samples of
@@ -352,7 +353,7 @@ def run_gb300(args):
         "config": {"workload": args.workload, "genome_bp": int(g.total_len), "chromosomes": len(g.seqs),
                    "reads_total": len(rs), "read_len": readlen, "chunk_reads": CHUNKSIZE,
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2: each step gathers from a 5.2 GB index and new reads"},
+                   "l2": "inputs larger than L2: each step gathers from a 9.8 GB index and new reads"},
         "e2e": {"value": e_reads * world / t_e2e, "unit": "reads/s", "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps)},
         "gpu_launches": launches,
@@ -525,7 +526,7 @@ def run_gb300_pe(args):
         "data": "synthetic (seeded; genome and bisulfite read pairs per the workload definition)",
         "config": {"workload": args.workload, "genome_bp": int(g.total_len), "pairs_total": n, "read_len": 100,
                    "chunk_pairs": CHUNKSIZE, "maxpdist": PE_MAXPDIST, "parallelism": "single GPU",
-                   "l2": "inputs larger than L2: each step gathers from a 6.5 GB index and new pairs"},
+                   "l2": "inputs larger than L2: each step gathers from an 11 GB index and new pairs"},
         "e2e": {"value": e_pairs / t_e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps)},
         "gpu_launches": launches, "heavy_pairs": heavy, "clocks": clk.summary(),

@@ -65,7 +65,8 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_gpu_host_alloc", "fame_gpu_host_free", "fame_gpu_stream", "fame_gpu_set_timing",
            "fame_gpu_stage_times", "fame_gpu_last_launches", "fame_gpu_match_pairs", "fame_gpu_match_pairs_dev", "fame_queue_open",
            "fame_queue_submit", "fame_queue_ready", "fame_queue_collect", "fame_queue_launches", "fame_queue_close",
-           "fame_gpu_tally_alloc", "fame_gpu_tally_read", "fame_gpu_tally_free", "fame_gpu_mem_info"]
+           "fame_gpu_tally_alloc", "fame_gpu_tally_read", "fame_gpu_tally_free", "fame_gpu_mem_info",
+           "fame_report_cpg", "fame_report_sc_header", "fame_report_sc_rows"]
 
 _lib = None
 
@@ -116,6 +117,9 @@ def lib(build_if_missing: bool = True):
     L.fame_gpu_tally_read.argtypes = [_P, _P, _P, C.c_int]
     L.fame_gpu_tally_free.argtypes = [_P, _P]
     L.fame_gpu_mem_info.argtypes = [_P, _P, _P]
+    L.fame_report_cpg.argtypes = [_P, _P, C.c_char_p, C.c_int]
+    L.fame_report_sc_header.argtypes = [_P, C.c_char_p]
+    L.fame_report_sc_rows.argtypes = [_P, C.c_char_p, _P, C.c_char_p, C.c_int]
     _lib = L
     return L
 

@@ -187,15 +187,12 @@ class PairedReadQueue:
         return tot
 
 
-def write_cpg_report(path: str, index: HostIndex, meth: np.ndarray):
-    """printMethylationLevels (ReadQueue.cpp:1860-1893)."""
-    t = index.tables()
-    names = np.array(index.chrom_names(), dtype=object)
-    pos = t["cpg_pos"].astype(np.int64) + index.readlen - 2
-    with open(path, "w") as f:
-        for i in range(len(pos)):
-            m = meth[i]
-            f.write("%s\t%d\t%d\t%d\t%d\t%d\n" % (names[t["cpg_chrom"][i]], pos[i], m[0], m[1], m[2], m[3]))
+def write_cpg_report(path: str, index: HostIndex, meth: np.ndarray, n_threads: int = 0):
+    """printMethylationLevels (ReadQueue.cpp:1860-1893), by the native writer."""
+    import ctypes as C
+    from ._lib import _check, _ptr, lib
+    m = np.ascontiguousarray(meth, dtype=np.uint16)
+    _check(lib().fame_report_cpg(C.byref(index.view), _ptr(m), path.encode(), n_threads))
 
 
 class SingleCellQueue:
@@ -210,17 +207,14 @@ class SingleCellQueue:
 
     def __init__(self, out_path: str, index: HostIndex, gpu: GpuMatcher, both_strands: bool = False,
                  chunk_size: int = CHUNKSIZE):
+        import ctypes as C
+        from ._lib import _check, lib
         self.index = index
         self.gpu = gpu
         self.both = both_strands
         self.chunk_size = chunk_size
-        self.out = open(out_path, "w")
-        t = index.tables(sparse=False)
-        names = index.chrom_names()
-        self.out.write("\nSC_ID\tCount_Type\t")
-        self.out.write("".join("%s\t" % names[c] for c in t["cpg_chrom"]))
-        self.out.write("\nSC_ID\tCount_Type\t")
-        self.out.write("".join("%d\t" % (p + index.readlen - 2) for p in t["cpg_pos"].astype(np.int64)))
+        self.path = out_path
+        _check(lib().fame_report_sc_header(C.byref(index.view), out_path.encode()))
 
     def match_sc_batch(self, reads, sc_id: str):
         rq = ReadQueue(reads, self.index, self.gpu, both_strands=self.both, chunk_size=self.chunk_size)
@@ -229,13 +223,13 @@ class SingleCellQueue:
         return tot
 
     def print_sc_methylation_levels(self, sc_id: str):
-        meth = self.gpu.tallies(reset=True)
-        for col, label in ((0, "methFwd"), (1, "unmethFwd"), (2, "methRev"), (3, "unmethFwd")):
-            self.out.write("\n%s\t%s\t" % (sc_id, label))
-            self.out.write("".join("%d\t" % v for v in meth[:, col]))
+        import ctypes as C
+        from ._lib import _check, _ptr, lib
+        meth = np.ascontiguousarray(self.gpu.tallies(reset=True), dtype=np.uint16)
+        _check(lib().fame_report_sc_rows(C.byref(self.index.view), sc_id.encode(), _ptr(meth), self.path.encode(), 0))
 
     def close(self):
-        self.out.close()
+        pass
 
 
 def read_sc_meta(path: str):

@@ -173,6 +173,20 @@ int fame_gpu_match_pairs_dev(fame_gpu* g, const char* seqs_dev, const uint64_t* 
  * (printSCMethylationLevels, ReadQueue.cpp:1894-1921). */
 int fame_gpu_tallies(fame_gpu* g, uint16_t* meth, int reset);
 
+/* ---- Report writers (host; byte-identical to the reference's output) ------
+ * fame_report_cpg writes <path> as printMethylationLevels writes
+ * <basename>_cpg.tsv (ReadQueue.cpp:1860-1893): per CpG in cpgTable order
+ * "chrom\tpos+READLEN-2\tmethFwd\tunmethFwd\tmethRev\tunmethRev\n";
+ * meth holds 4 uint16 per CpG (fame_gpu_tallies).  n_threads <= 0: all cores.
+ * fame_report_sc_header starts a single-cell matrix file (the two header rows
+ * of the single-cell ReadQueue); fame_report_sc_rows appends one cell's four
+ * rows (printSCMethylationLevels, ReadQueue.cpp:1894-1921, including its
+ * fourth row label "unmethFwd"). */
+int fame_report_cpg(const fame_index_view* v, const uint16_t* meth, const char* path, int n_threads);
+int fame_report_sc_header(const fame_index_view* v, const char* path);
+int fame_report_sc_rows(const fame_index_view* v, const char* sc_id, const uint16_t* meth, const char* path,
+                        int n_threads);
+
 /* ---- Batched and serving form (no counterpart in the reference) ---------
  * A queue of chunk slots on one context.  Each slot owns device buffers for
  * one chunk of up to max_reads reads / max_bytes bases, page-locked staging

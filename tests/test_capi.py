@@ -34,6 +34,16 @@ def test_argument_errors_without_gpu():
     assert L.fame_gpu_match_reads(None, None, None, 0, 0, None, None, None) == -1
     assert L.fame_gpu_tallies(None, None, 0) == -1
     assert L.fame_index_read(None, None) == -1
+    assert L.fame_gpu_match_pairs(None, None, None, None, None, 0, 0, 550, None, None, None, None, None) == -1
+    assert L.fame_gpu_match_pairs_dev(None, None, None, 0, 0, 550, None, None, None) == -1
+    assert L.fame_queue_open(None, 2, 10, 1000, None) == -1
+    assert L.fame_queue_submit(None, None, None, 0, 0, None, None) == -1
+    assert L.fame_queue_collect(None, 0, None, None, None) == -1
+    assert L.fame_queue_ready(None, 0) == -1
+    assert L.fame_queue_close(None) == -1
+    assert L.fame_gpu_tally_alloc(None, None) == -1
+    assert L.fame_gpu_tally_read(None, None, None, 0) == -1
+    assert L.fame_gpu_mem_info(None, None, None) == -1
 
 
 def test_index_read_errors(tmp_path):

@@ -1,0 +1,55 @@
+"""The native report writers (fame_report_*) against the reference's output
+format, written here with plain Python formatting: printMethylationLevels
+(ReadQueue.cpp:1860-1893) and the single-cell matrix (header of the
+single-cell ReadQueue, printSCMethylationLevels, ReadQueue.cpp:1894-1921)."""
+import numpy as np
+
+from fame_gb300 import SingleCellQueue, write_cpg_report
+
+
+def expected_cpg(index, meth):
+    t = index.tables()
+    names = index.chrom_names()
+    lines = []
+    for i, (c, p) in enumerate(zip(t["cpg_chrom"], t["cpg_pos"].astype(np.int64))):
+        m = meth[i]
+        lines.append("%s\t%d\t%d\t%d\t%d\t%d\n" % (names[c], (p + index.readlen - 2) & 0xFFFFFFFF, m[0], m[1], m[2], m[3]))
+    return "".join(lines)
+
+
+def test_cpg_report_matches_reference_format(product_index, tmp_path):
+    rng = np.random.default_rng(9)
+    meth = rng.integers(0, 65536, size=(product_index.n_cpg, 4)).astype(np.uint16)
+    meth[: product_index.n_cpg // 3] = 0
+    out = tmp_path / "r_cpg.tsv"
+    write_cpg_report(str(out), product_index, meth, n_threads=3)
+    assert out.read_text() == expected_cpg(product_index, meth)
+
+
+class _FakeGpu:
+    def __init__(self, rows):
+        self.rows = list(rows)
+
+    def tallies(self, reset=False):
+        return self.rows.pop(0)
+
+
+def test_single_cell_matrix_matches_reference_format(product_index, tmp_path):
+    rng = np.random.default_rng(10)
+    n = product_index.n_cpg
+    cells = [("cellA", rng.integers(0, 900, size=(n, 4)).astype(np.uint16)),
+             ("cellB", rng.integers(0, 3, size=(n, 4)).astype(np.uint16))]
+    out = tmp_path / "sc.tsv"
+    sc = SingleCellQueue(str(out), product_index, _FakeGpu([m for _, m in cells]))
+    for cid, _ in cells:
+        sc.print_sc_methylation_levels(cid)
+    sc.close()
+    t = product_index.tables(sparse=False)
+    names = product_index.chrom_names()
+    exp = "\nSC_ID\tCount_Type\t" + "".join("%s\t" % names[c] for c in t["cpg_chrom"])
+    exp += "\nSC_ID\tCount_Type\t" + "".join("%d\t" % (p + product_index.readlen - 2)
+                                            for p in t["cpg_pos"].astype(np.int64))
+    for cid, m in cells:
+        for col, label in ((0, "methFwd"), (1, "unmethFwd"), (2, "methRev"), (3, "unmethFwd")):
+            exp += "\n%s\t%s\t" % (cid, label) + "".join("%d\t" % v for v in m[:, col])
+    assert out.read_text() == exp
