@@ -66,7 +66,8 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_gpu_stage_times", "fame_gpu_last_launches", "fame_gpu_match_pairs", "fame_gpu_match_pairs_dev", "fame_queue_open",
            "fame_queue_submit", "fame_queue_ready", "fame_queue_collect", "fame_queue_launches", "fame_queue_close",
            "fame_gpu_tally_alloc", "fame_gpu_tally_read", "fame_gpu_tally_free", "fame_gpu_mem_info",
-           "fame_report_cpg", "fame_report_sc_header", "fame_report_sc_rows"]
+           "fame_report_cpg", "fame_report_sc_header", "fame_report_sc_rows", "fame_fastq_open", "fame_fastq_read",
+           "fame_fastq_close"]
 
 _lib = None
 
@@ -120,6 +121,9 @@ def lib(build_if_missing: bool = True):
     L.fame_report_cpg.argtypes = [_P, _P, C.c_char_p, C.c_int]
     L.fame_report_sc_header.argtypes = [_P, C.c_char_p]
     L.fame_report_sc_rows.argtypes = [_P, C.c_char_p, _P, C.c_char_p, C.c_int]
+    L.fame_fastq_open.argtypes = [C.c_char_p, C.c_int, C.c_int, _P]
+    L.fame_fastq_read.argtypes = [_P, C.c_uint32, _P, C.c_uint64, _P, _P]
+    L.fame_fastq_close.argtypes = [_P]
     _lib = L
     return L
 
@@ -356,6 +360,32 @@ class GpuMatcher:
         f, t = C.c_uint64(), C.c_uint64()
         _check(lib().fame_gpu_mem_info(self.h, C.byref(f), C.byref(t)), self.h)
         return f.value, t.value
+
+
+class FastqReader:
+    """Native FASTQ chunk reader (fame_fastq_*): parseChunk's records, the
+    sequences packed with offsets, into page-locked buffers when given."""
+
+    def __init__(self, path: str, is_gz: bool = False, n_threads: int = 0, max_reads: int = 300000,
+                 max_len: int = 256, seqs: np.ndarray = None, offs: np.ndarray = None):
+        self.h = _P()
+        _check(lib().fame_fastq_open(path.encode(), int(is_gz), n_threads, C.byref(self.h)))
+        self.max_reads = max_reads
+        self.seqs = np.zeros(max_reads * max_len, np.uint8) if seqs is None else seqs
+        self.offs = np.zeros(max_reads + 1, np.uint64) if offs is None else offs
+
+    def read(self):
+        """Next chunk: (sequence bytes view, offsets view) of n records (n == 0 at the end)."""
+        n = C.c_uint32()
+        _check(lib().fame_fastq_read(self.h, self.max_reads, _ptr(self.seqs), self.seqs.nbytes, _ptr(self.offs),
+                                     C.byref(n)))
+        k = n.value
+        return self.seqs[: int(self.offs[k])], self.offs[: k + 1]
+
+    def close(self):
+        if self.h:
+            lib().fame_fastq_close(self.h)
+            self.h = None
 
 
 class GpuQueue:

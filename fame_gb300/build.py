@@ -71,7 +71,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(run, [c for c, _ in jobs]))
     tmp = LIB + ".tmp"
-    run([nvcc] + ARCH + ["-shared", "-o", tmp] + [o for _, o in jobs] + ["-lpthread"])
+    run([nvcc] + ARCH + ["-shared", "-o", tmp] + [o for _, o in jobs] + ["-lpthread", "-lz"])
     os.replace(tmp, LIB)
     return LIB
 

@@ -13,23 +13,17 @@ from ._lib import CHUNKSIZE, FAME_BOTH_STRANDS, FAME_GET_STRANDED, FAME_MATCH_R1
 
 
 class _FastqSource:
-    """parseChunk's reading: four getline calls per record, sequence = line 2."""
+    """parseChunk's reading through the native reader (fame_fastq_*): four
+    lines per record, sequence = line 2."""
 
-    def __init__(self, path: str, is_gz: bool = False):
-        import gzip
-        self.f = gzip.open(path, "rb") if is_gz else open(path, "rb")
+    def __init__(self, path: str, is_gz: bool = False, chunk: int = CHUNKSIZE):
+        from ._lib import FastqReader
+        self.r = FastqReader(path, is_gz, max_reads=chunk)
 
     def take(self, n):
-        seqs = []
-        while len(seqs) < n:
-            hdr = self.f.readline()
-            if not hdr:
-                break
-            seq = self.f.readline().rstrip(b"\n")
-            self.f.readline()
-            self.f.readline()
-            seqs.append(seq)
-        return seqs
+        assert n <= self.r.max_reads
+        seq, offs = self.r.read()
+        return seq.copy(), offs.copy()
 
 
 class _ListSource:
@@ -40,14 +34,16 @@ class _ListSource:
     def take(self, n):
         out = self.seqs[self.i:self.i + n]
         self.i += len(out)
-        return out
+        offs = np.zeros(len(out) + 1, dtype=np.uint64)
+        np.cumsum([len(x) for x in out], out=offs[1:])
+        return np.frombuffer(b"".join(out), dtype=np.uint8), offs
 
 
 class ReadQueue:
     def __init__(self, reads, index: HostIndex, gpu: GpuMatcher, is_gz: bool = False, both_strands: bool = False,
                  chunk_size: int = CHUNKSIZE):
         if isinstance(reads, str):
-            self.src = _FastqSource(reads, is_gz)
+            self.src = _FastqSource(reads, is_gz, chunk_size)
         else:
             self.src = _ListSource(list(reads))
         self.index = index
@@ -57,24 +53,23 @@ class ReadQueue:
         self.r1_fwd_matches = 0
         self.r1_rev_matches = 0
         self.match_r1_fwd = True
-        self.buffer = []
+        self.buffer = (np.zeros(0, np.uint8), np.zeros(1, np.uint64))   # packed sequences, offsets
         self.mats = np.zeros(0, np.uint64)
         self.invalid = np.zeros(0, np.uint8)
 
     def parse_chunk(self):
         """Returns (procReads, more): more is True iff a full chunk was read."""
         self.buffer = self.src.take(self.chunk_size)
-        n = len(self.buffer)
+        n = len(self.buffer[1]) - 1
         return n, n >= self.chunk_size
 
     def match_reads(self, proc_reads: int, get_stranded: bool):
-        """Match buffer[:proc_reads]; returns (succ, nonunique, unsucc) of this call."""
-        seqs = self.buffer[:proc_reads]
-        offs = np.zeros(len(seqs) + 1, dtype=np.uint64)
-        np.cumsum([len(s) for s in seqs], out=offs[1:])
+        """Match the first proc_reads reads of the buffer; returns this call's Counters."""
+        seq, offs = self.buffer
+        offs = offs[:proc_reads + 1]
         flags = (FAME_GET_STRANDED if get_stranded else 0) | (FAME_BOTH_STRANDS if self.both_strands_flag else 0) | \
             (FAME_MATCH_R1_FWD if self.match_r1_fwd else 0)
-        mats, inval, cnt = self.gpu.match_reads(b"".join(seqs), offs, flags)
+        mats, inval, cnt = self.gpu.match_reads(seq[: int(offs[-1])], offs, flags)
         self.mats, self.invalid = mats, inval
         self.r1_fwd_matches += cnt.r1_fwd
         self.r1_rev_matches += cnt.r1_rev
@@ -120,7 +115,8 @@ class PairedReadQueue:
 
     def __init__(self, reads1, reads2, index: HostIndex, gpu: GpuMatcher, maxpdist: int, is_gz: bool = False,
                  both_strands: bool = False, chunk_size: int = CHUNKSIZE):
-        self.src = [(_FastqSource(r, is_gz) if isinstance(r, str) else _ListSource(list(r))) for r in (reads1, reads2)]
+        self.src = [(_FastqSource(r, is_gz, chunk_size) if isinstance(r, str) else _ListSource(list(r)))
+                    for r in (reads1, reads2)]
         self.index = index
         self.gpu = gpu
         self.maxpdist = maxpdist
@@ -129,27 +125,26 @@ class PairedReadQueue:
         self.r1_fwd_matches = 0
         self.r1_rev_matches = 0
         self.match_r1_fwd = True
-        self.buffer = ([], [])
+        self.buffer = ((np.zeros(0, np.uint8), np.zeros(1, np.uint64)),) * 2
         self.mats = (np.zeros(0, np.uint64), np.zeros(0, np.uint64))
         self.invalid = (np.zeros(0, np.uint8), np.zeros(0, np.uint8))
 
     def parse_chunk(self):
         """Returns (procReads, more): the pairs read, more iff a full chunk was read."""
         b1 = self.src[0].take(self.chunk_size)
-        b2 = self.src[1].take(len(b1))
-        if len(b2) != len(b1):
+        b2 = self.src[1].take(self.chunk_size)
+        n = len(b1[1]) - 1
+        if len(b2[1]) - 1 != n:
             raise ValueError("mate files hold different numbers of reads")
         self.buffer = (b1, b2)
-        return len(b1), len(b1) >= self.chunk_size
+        return n, n >= self.chunk_size
 
     def match_paired_reads(self, proc_reads: int, get_stranded: bool):
         """Match pairs buffer[:proc_reads]; returns this call's PairCounters."""
         packed = []
-        for mates in self.buffer:
-            seqs = mates[:proc_reads]
-            offs = np.zeros(len(seqs) + 1, dtype=np.uint64)
-            np.cumsum([len(x) for x in seqs], out=offs[1:])
-            packed.append((b"".join(seqs), offs))
+        for seq, offs in self.buffer:
+            offs = offs[:proc_reads + 1]
+            packed.append((seq[: int(offs[-1])], offs))
         flags = (FAME_GET_STRANDED if get_stranded else 0) | (FAME_BOTH_STRANDS if self.both_strands_flag else 0) | \
             (FAME_MATCH_R1_FWD if self.match_r1_fwd else 0)
         m1, m2, i1, i2, cnt = self.gpu.match_pairs(packed[0][0], packed[0][1], packed[1][0], packed[1][1], flags,

@@ -173,6 +173,18 @@ int fame_gpu_match_pairs_dev(fame_gpu* g, const char* seqs_dev, const uint64_t* 
  * (printSCMethylationLevels, ReadQueue.cpp:1894-1921). */
 int fame_gpu_tallies(fame_gpu* g, uint16_t* meth, int reset);
 
+/* ---- FASTQ chunks (host) ---------------------------------------------------
+ * parseChunk / parseChunkGZ (ReadQueue.cpp:218-373): four lines per record,
+ * the sequence is the second, nothing validated.  fame_fastq_read packs the
+ * sequences of up to max_reads records back to back into seqs (seq_cap bytes;
+ * FAME_ERR_ARG when they do not fit) with offsets offs[n + 1], and returns the
+ * record count in *n (0 at the end of the input); parsing is spread over
+ * n_threads host threads (<= 0: up to 16). */
+typedef struct fame_fastq fame_fastq;
+int fame_fastq_open(const char* path, int is_gz, int n_threads, fame_fastq** out);
+int fame_fastq_read(fame_fastq* f, uint32_t max_reads, char* seqs, uint64_t seq_cap, uint64_t* offs, uint32_t* n);
+int fame_fastq_close(fame_fastq* f);
+
 /* ---- Report writers (host; byte-identical to the reference's output) ------
  * fame_report_cpg writes <path> as printMethylationLevels writes
  * <basename>_cpg.tsv (ReadQueue.cpp:1860-1893): per CpG in cpgTable order

@@ -84,6 +84,37 @@ def test_readqueue_mirror(golden, product_index, gpu):
     gpu.tallies(reset=True)
 
 
+@pytest.mark.parametrize("gz", [False, True], ids=["fastq", "fastq.gz"])
+def test_readqueue_from_fastq_file(golden, product_index, gpu, tmp_path, gz):
+    """The whole host flow from a FASTQ file (native chunk reader, GPU chunks,
+    native report writer) gives the reference's counters and CpG report."""
+    import gzip
+    from fame_gb300 import write_cpg_report
+    seq = golden["read_seq"].tobytes()
+    offs = golden["read_offs"]
+    lines = []
+    for i in range(len(offs) - 1):
+        r = seq[int(offs[i]):int(offs[i + 1])]
+        lines += [b"@read%d" % i, r, b"+", b"I" * len(r)]
+    path = tmp_path / ("reads.fq.gz" if gz else "reads.fq")
+    with (gzip.open if gz else open)(path, "wb") as f:
+        f.write(b"\n".join(lines) + b"\n")
+    gpu.tallies(reset=True)
+    rq = ReadQueue(str(path), product_index, gpu, is_gz=gz, chunk_size=1000)
+    tot = rq.query_routine()
+    c = golden["chunk1000_counters"]
+    assert (tot["succ"], tot["nonunique"], tot["unsucc"]) == (c[0], c[1], c[2])
+    report = tmp_path / "out"
+    rq.print_methylation_levels(str(report))
+    t = product_index.tables()
+    names = product_index.chrom_names()
+    m = golden["chunk1000_meth"]
+    exp = "".join("%s\t%d\t%d\t%d\t%d\t%d\n" % (names[ch], p + 98, *m[i])
+                  for i, (ch, p) in enumerate(zip(t["cpg_chrom"], t["cpg_pos"].astype(np.int64))))
+    assert (tmp_path / "out_cpg.tsv").read_text() == exp
+    gpu.tallies(reset=True)
+
+
 def _oracle_run(oi, seq, offs, chunk=0, both=False):
     o = oi.match_se(seq, offs, chunk=chunk, both_strands=both)
     return dict(mat=o["mat"], invalid=o["invalid"], meth=o["meth"], counters=o["counters"])
