@@ -353,7 +353,7 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dp_warp, 128, 4 * DPW_BYTES) != cudaSuccess || nb < 1)
             return fail(set_err(g, FAME_ERR_CUDA, "k_dp_warp does not fit an SM"));
         g->dp_grid = (uint32_t)(g->sm_count * nb);
-        uint64_t off[27];
+        uint64_t off[28];
         g->pe_warp_bytes = pe_layout(PE_LIGHT, off);
         const size_t pe_smem = 4 * g->pe_warp_bytes;
         if (cudaFuncSetAttribute(k_pe_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pe_smem) != cudaSuccess ||
@@ -616,7 +616,7 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         if ((rc = sync_ctr())) return rc;
         if (g->h_ctr[CTR_HEAVY]) {
             if (!g->d_pe_heavy) {
-                uint64_t off[27];
+                uint64_t off[28];
                 g->pe_heavy_warp_bytes = pe_layout(PE_HEAVY, off);
                 g->pe_heavy_warps = PE_HEAVY_WARPS;
                 CK(cudaMalloc((void**)&g->d_pe_heavy, g->pe_heavy_warp_bytes * g->pe_heavy_warps));

@@ -1,97 +1,11 @@
 // Matching kernels after seeding: Shift-And window scans, candidate
 // selection with the exact-match CpG calls, and the banded DP CpG calls.
 #pragma once
+#include "editscan.h"
 #include "qgram.h"
 #include "seed.cuh"
 
 namespace fame {
-
-// ---------------------------------------------------------------------------
-// ShiftAnd<6> (ShiftAnd.h:121-432).  State bit s of layer e: a prefix of s
-// pattern characters aligns with <= e edits ending at the current text base.
-// A read T also sets the mask of a reference C (bisulfite asymmetry,
-// ShiftAnd.h:399-402).  W = pLen / 64 + 1 words; only bits <= pLen matter.
-// ---------------------------------------------------------------------------
-template <int W>
-struct ShiftAndState {
-    uint64_t m[4][W];
-    uint64_t acc;          // accepted bit of word W - 1
-    uint64_t a[NERR + 1][W];
-    uint32_t plen;
-
-    __device__ __forceinline__ void load(const char* raw, uint32_t len, int orient)
-    {
-        plen = len;
-        acc = 1ull << (len % 64);
-        uint64_t mA = ~0ull, mC = ~0ull, mG = ~0ull, mT = ~0ull;
-#pragma unroll
-        for (int w = 0; w < W; ++w) { m[0][w] = m[1][w] = m[2][w] = m[3][w] = 0; }
-        for (uint32_t i = len; i > 0;) {
-            mA <<= 1; mC <<= 1; mG <<= 1; mT <<= 1;
-            const uint8_t c = orient ? rc_byte((uint8_t)raw[len - i]) : (uint8_t)raw[i - 1];
-            switch (c) {
-                case 'A': mA |= 1; break;
-                case 'C': mC |= 1; break;
-                case 'G': mG |= 1; break;
-                case 'T': mT |= 1; mC |= 1; break;
-                default: break;
-            }
-            if (i % 64 == 0) {
-                const int w = (int)(i / 64);
-#pragma unroll
-                for (int q = 0; q < W; ++q)
-                    if (q == w) { m[0][q] = mA; m[1][q] = mC; m[2][q] = mG; m[3][q] = mT; }
-                mA = mC = mG = mT = ~0ull;
-            }
-            --i;
-        }
-        m[0][0] = (mA << 1) | 1; m[1][0] = (mC << 1) | 1; m[2][0] = (mG << 1) | 1; m[3][0] = (mT << 1) | 1;
-    }
-
-    __device__ __forceinline__ void reset()
-    {
-#pragma unroll
-        for (int i = 0; i <= (int)NERR; ++i) {
-#pragma unroll
-            for (int j = 1; j < W; ++j) a[i][j] = 0;
-            a[i][0] = (1ull << (i + 1)) - 1;
-        }
-    }
-
-    // queryLetter (ShiftAnd.h:276-318)
-    __device__ __forceinline__ void letter(int b)
-    {
-        uint64_t mk[W];
-#pragma unroll
-        for (int j = 0; j < W; ++j) mk[j] = b == 0 ? m[0][j] : b == 1 ? m[1][j] : b == 2 ? m[2][j] : m[3][j];
-#pragma unroll
-        for (int i = NERR; i > 0; --i) {
-#pragma unroll
-            for (int j = W - 1; j > 0; --j)
-                a[i][j] = (((a[i][j] << 1) | (a[i][j - 1] >> 63)) & mk[j]) | a[i - 1][j] |
-                          ((a[i - 1][j] << 1) | (a[i - 1][j - 1] >> 63));
-            a[i][0] = (((a[i][0] << 1) | 1) & mk[0]) | a[i - 1][0] | (a[i - 1][0] << 1);
-        }
-#pragma unroll
-        for (int j = W - 1; j > 0; --j) a[0][j] = ((a[0][j] << 1) | (a[0][j - 1] >> 63)) & mk[j];
-        a[0][0] = ((a[0][0] << 1) | 1) & mk[0];
-#pragma unroll
-        for (int i = 1; i <= (int)NERR; ++i) {
-#pragma unroll
-            for (int j = W - 1; j > 0; --j) a[i][j] |= (a[i - 1][j] << 1) | (a[i - 1][j - 1] >> 63);
-            a[i][0] |= a[i - 1][0] << 1;
-        }
-    }
-
-    // isMatch (ShiftAnd.h:323-341): smallest layer with the accepting state
-    __device__ __forceinline__ int match() const
-    {
-#pragma unroll
-        for (int i = 0; i <= (int)NERR; ++i)
-            if (a[i][W - 1] & acc) return i;
-        return -1;
-    }
-};
 
 // Full scan of one candidate window (querySeq / queryRevSeq, ShiftAnd.h:130-255,
 // on the text spans of saQuerySeedSetRef, ReadQueue.cpp:1953-1962, 2048-2058).
@@ -100,7 +14,7 @@ struct ShiftAndState {
 // unguarded: the reverse scan starts at startPos - 1 even for a window at
 // position 0 (matchRevSecond, ReadQueue.cpp:4736), i.e. it includes base 0.
 template <int W, class Emit>
-__device__ void scan_window_full(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t wid, int fwd, Emit emit,
+__device__ void scan_window_full(const DevIndex& ix, EditScan<W>& sa, uint32_t wid, int fwd, Emit emit,
                                  bool unguarded = false)
 {
     const uint4 wi = ix.win[wid];
@@ -194,7 +108,7 @@ struct ScanText {
 // N bases reset the automaton exactly as in the full scan.  Too many spans
 // (repetitive windows) fall back to the full scan.
 template <int W, class Emit>
-__device__ void scan_window(const DevIndex& ix, ShiftAndState<W>& sa, uint32_t wid, int fwd, Emit emit,
+__device__ void scan_window(const DevIndex& ix, EditScan<W>& sa, uint32_t wid, int fwd, Emit emit,
                             const uint32_t* pkey, uint32_t pvalid, uint32_t q, const uint32_t* pstart,
                             bool unguarded = false)
 {
@@ -321,7 +235,7 @@ __device__ void shiftand_one(const DevIndex& ix, const ChunkBufs& cb, uint32_t c
     const uint32_t r = task >> 1, o = task & 1;
     const uint64_t off0 = cb.offs[r];
     const uint32_t len = (uint32_t)(cb.offs[r + 1] - off0);
-    ShiftAndState<W> sa;
+    EditScan<W> sa;
     sa.load(cb.seqs + off0, len, (int)o);
     PieceKeys pk;
     pk.load(cb.seqs + off0, len, (int)o);
@@ -396,7 +310,7 @@ __device__ __noinline__ void rescan_into(const DevIndex& ix, const ChunkBufs& cb
     const uint32_t r = task >> 1, o = task & 1;
     const uint64_t off0 = cb.offs[r];
     const uint32_t len = (uint32_t)(cb.offs[r + 1] - off0);
-    ShiftAndState<W> sa;
+    EditScan<W> sa;
     sa.load(cb.seqs + off0, len, (int)o);
     scan_window_full<W>(ix, sa, w, dir, [&](uint32_t off, int err) {
         if (u.abort) return;
@@ -733,22 +647,44 @@ __device__ void meth_dp(const DevIndex& ix, const ChunkBufs& cb, const DpScratch
 // ---------------------------------------------------------------------------
 // read checks (ReadQueue.cpp:428-490)
 // ---------------------------------------------------------------------------
+// True when one of the bytes [a, a + len) of the read buffer is 'N'.  Reads
+// the 8-byte aligned words (by address) that hold those bytes, so no load
+// leaves a word that holds a byte of the range; bytes outside the range are
+// made non-zero, then a zero-byte test on the word XOR "NNNNNNNN".
+__device__ __forceinline__ bool has_n(const char* seqs, uint64_t a, uint32_t len)
+{
+    if (len == 0) return false;
+    const uintptr_t p = (uintptr_t)(seqs + a), e = p + len;
+    for (uintptr_t w = p & ~(uintptr_t)7; w < e; w += 8) {
+        uint64_t x = *(const uint64_t*)w ^ 0x4E4E4E4E4E4E4E4Eull;
+        if (w < p) x |= (1ull << (8 * (p - w))) - 1;
+        if (w + 8 > e) x |= ~0ull << (8 * (e - w));
+        if ((x - 0x0101010101010101ull) & ~x & 0x8080808080808080ull) return true;
+    }
+    return false;
+}
+
 __global__ void k_prep(ChunkBufs cb, uint32_t readlen)
 {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= cb.n) return;
-    const uint64_t o0 = cb.offs[r];
-    const uint32_t len = (uint32_t)(cb.offs[r + 1] - o0);
-    uint8_t f = 0;
-    if (len < readlen - 20) f = 1;
-    else {
-        for (uint32_t i = 0; i < len; ++i) if (cb.seqs[o0 + i] == 'N') { f = 2; break; }
-        if (!f && len > FAME_MAX_READ_LEN) { f = 4; atomicAdd(cb.ctr + CTR_TOO_LONG, 1ull); }
-        if (!f) atomicOr(cb.ctr + CTR_WMASK, 1ull << min(4u, len / 64 + 1));
+    uint32_t wbit = 0;
+    if (r < cb.n) {
+        const uint64_t o0 = cb.offs[r];
+        const uint32_t len = (uint32_t)(cb.offs[r + 1] - o0);
+        uint8_t f = 0;
+        if (len < readlen - 20) f = 1;
+        else {
+            if (has_n(cb.seqs, o0, len)) f = 2;
+            if (!f && len > FAME_MAX_READ_LEN) { f = 4; atomicAdd(cb.ctr + CTR_TOO_LONG, 1ull); }
+            if (!f) wbit = 1u << min(4u, len / 64 + 1);
+        }
+        cb.rflags[r] = f;
+        cb.task_cand[2 * r] = make_uint4(0, 0, 0, 0);
+        cb.task_cand[2 * r + 1] = make_uint4(0, 0, 0, 0);
     }
-    cb.rflags[r] = f;
-    cb.task_cand[2 * r] = make_uint4(0, 0, 0, 0);
-    cb.task_cand[2 * r + 1] = make_uint4(0, 0, 0, 0);
+    // one atomic per warp for the automaton widths present
+    wbit = __reduce_or_sync(0xffffffffu, wbit);
+    if ((threadIdx.x & 31) == 0 && wbit) atomicOr(cb.ctr + CTR_WMASK, (unsigned long long)wbit);
 }
 
 // Light path: one warp per task, working memory in shared memory.

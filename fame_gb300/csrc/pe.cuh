@@ -76,6 +76,7 @@ struct PeMem {
     uint32_t* ge;         // staged entries (window | forward << 31) and their T masks
     uint32_t* gt;
     uint8_t* gk;          // k-mer of each staged entry
+    uint8_t* sv;          // staged entry survives the T-mask filter and the dedup
     PeCaps c;
 };
 
@@ -114,12 +115,13 @@ __host__ __device__ inline uint64_t pe_layout(PeCaps c, uint64_t* off)
     put(4ull * c.ecap);                     // 24 ge
     put(4ull * c.ecap);                     // 25 gt
     put(c.ecap);                            // 26 gk
+    put(c.ecap);                            // 27 sv
     return o;
 }
 
 __device__ inline PeMem pe_mem(uint8_t* base, PeCaps c)
 {
-    uint64_t off[27];
+    uint64_t off[28];
     pe_layout(c, off);
     PeMem s;
     s.c = c;
@@ -151,11 +153,12 @@ __device__ inline PeMem pe_mem(uint8_t* base, PeCaps c)
     s.ge = (uint32_t*)(base + off[24]);
     s.gt = (uint32_t*)(base + off[25]);
     s.gk = base + off[26];
+    s.sv = base + off[27];
     return s;
 }
 
-// shared-memory caps (one warp)
-constexpr PeCaps PE_LIGHT{96, 256, 512 + NBHD - 1, 64, 32, 320};
+// shared-memory caps of k_pe_seed (one warp; it keeps no matches)
+constexpr PeCaps PE_LIGHT{64, 256, 256 + NBHD - 1, 64, 0, 320};
 
 __device__ __forceinline__ uint32_t vt_hash(uint32_t k, uint32_t mask) { return (k * 0x9E3779B1u) >> 8 & mask; }
 
@@ -474,6 +477,142 @@ __device__ inline void pe_sort(uint2* f, long n, PeCmp cmp)
 }
 
 // ---------------------------------------------------------------------------
+// Lane-parallel map counting of one mate from the staged bucket entries.
+//
+// A bucket entry survives when the T-mask filter keeps it and it is not a
+// repeat of the previous surviving entry of its bucket.  An op may insert its
+// key when its k-mer index p has p == 0 or p - 1 < maxQPos, a prefix of the
+// ops (they come in k-mer order), so a key's first surviving op decides:
+// the key is inserted there when that op may insert (or, for the second mate,
+// when the key is already in the map), and then every one of its ops counts;
+// otherwise none does.  Counts commute, so only the first-touch order needs
+// the ops in order: chunks of 32 ops in order, equal keys of a chunk grouped
+// with __match_any_sync, new keys appended with ballots.  For the second
+// mate an insert also needs a map key within contextWLen windows; the
+// parallel form applies when every op that may insert finds one among the
+// keys kept from the first mate (the map before the second mate touches it),
+// and returns false otherwise, leaving the map untouched for the ordered
+// lane-0 loop.  Scratch bits of a value during the passes: bit 30 the key
+// was seen, bits 18-29 its op count.
+// ---------------------------------------------------------------------------
+constexpr uint32_t PV_SEEN = 1u << 30;
+constexpr uint32_t PV_RAW_SHIFT = 18;
+constexpr uint32_t PV_RAW_MASK = 0xfffu << PV_RAW_SHIFT;
+
+__device__ void pe_survivors(const PeMem& s, uint32_t nk)
+{
+    const int lane = threadIdx.x & 31;
+    for (uint32_t p = lane; p < nk; p += 32) {
+        const uint32_t b0 = s.kpre[p], n = s.kln[p], cm = s.kcm[p];
+        const bool filt = s.kfl[p] != 0;
+        bool have = false;
+        uint32_t last = 0;
+        for (uint32_t i = b0; i < b0 + n; ++i) {
+            uint8_t keep = 0;
+            if (!filt && !(cm & SEEDBITS & s.gt[i])) {
+                const uint32_t e = s.ge[i];           // window | forward << 31: equal iff same window and strand
+                if (!(have && e == last)) keep = 1;
+                have = true;
+                last = e;
+            }
+            s.sv[i] = keep;
+        }
+    }
+    __syncwarp();
+}
+
+// All lanes.  Returns 1 done, 0 not applicable (second mate, a neighbour
+// created by the mate itself would be needed), -1 over the table capacity.
+__device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint32_t len, uint32_t sigma, int phase)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nk = len - KMERLEN + 1;
+    const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
+    pe_survivors(s, nk);
+    if (phase == 2) {
+        const int ctx = (int)px.ctx;
+        bool dyn = false;
+        for (uint32_t i = lane; i < sigma; i += 32) {
+            if (!s.sv[i]) continue;
+            const uint32_t p = s.gk[i];
+            if (!(p == 0 || p - 1 < maxQPos)) continue;
+            const uint32_t e = s.ge[i];
+            bool ok = false;
+            for (int c = -ctx; c <= ctx && !ok; ++c) ok = pm_find(s, (int)(e >> 31), (e & 0x7fffffffu) + (uint32_t)c) >= 0;
+            dyn |= !ok;
+        }
+        if (__any_sync(0xffffffffu, dyn)) return 0;
+    }
+    uint32_t nkeys[2] = {__shfl_sync(0xffffffffu, st.nkeys[0], 0), __shfl_sync(0xffffffffu, st.nkeys[1], 0)};
+    uint32_t nins[2] = {0, 0};
+    uint32_t* ins[2] = {phase == 1 ? s.ins1[0] : s.ins2[0], phase == 1 ? s.ins1[1] : s.ins2[1]};
+    const uint32_t mask = s.c.vcap - 1;
+    bool over = false;
+    for (uint32_t base = 0; base < sigma && !over; base += 32) {
+        if (4 * (nkeys[0] + 32) > 3 * s.c.vcap || 4 * (nkeys[1] + 32) > 3 * s.c.vcap) { over = true; break; }
+        const uint32_t i = base + lane;
+        const bool live = i < sigma && s.sv[i];
+        const uint32_t e = live ? s.ge[i] : 0u;
+        const int dir = (int)(e >> 31);
+        const uint32_t id = e & 0x7fffffffu;
+        const uint32_t p = live ? s.gk[i] : 0u;
+        const bool may = live && (p == 0 || p - 1 < maxQPos);
+        const unsigned vm = __ballot_sync(0xffffffffu, live);
+        const unsigned grp = __match_any_sync(0xffffffffu, live ? e : EMPTY_KEY) & vm;
+        const bool leader = live && (__ffs(grp) - 1) == lane;
+        bool fresh = false, added = false;
+        if (leader) {
+            uint32_t h = vt_hash(id, mask);
+            for (;; h = (h + 1) & mask) {
+                const uint32_t k = s.vk[dir][h];
+                if (k == id) break;
+                if (k == EMPTY_KEY) {
+                    const uint32_t old = atomicCAS(&s.vk[dir][h], EMPTY_KEY, id);
+                    if (old == EMPTY_KEY) { added = true; break; }
+                    if (old == id) break;
+                }
+            }
+            uint32_t v = s.vv[dir][h];
+            if (!(v & PV_SEEN)) {
+                v |= PV_SEEN;
+                if (!(v & PV_PRESENT) && may) { v |= PV_PRESENT; fresh = true; }
+            }
+            if (v & PV_PRESENT) v += (uint32_t)__popc(grp) << PV_RAW_SHIFT;
+            s.vv[dir][h] = v;
+        }
+        for (int d = 0; d < 2; ++d) {
+            const unsigned na = __ballot_sync(0xffffffffu, added && dir == d);
+            nkeys[d] += __popc(na);
+            const unsigned bm = __ballot_sync(0xffffffffu, fresh && dir == d);
+            if (fresh && dir == d) {
+                const uint32_t at = nins[d] + __popc(bm & ((1u << lane) - 1));
+                if (at < s.c.icap) ins[d][at] = id;
+            }
+            nins[d] += __popc(bm);
+        }
+        if (nins[0] > s.c.icap || nins[1] > s.c.icap) over = true;
+        __syncwarp();
+    }
+    if (over) return -1;
+    // fold the op counts into count1 / count2 (8-bit wrap) and clear the scratch bits
+    for (int dir = 0; dir < 2; ++dir)
+        for (uint32_t h = lane; h < s.c.vcap; h += 32) {
+            const uint32_t v = s.vv[dir][h];
+            const uint32_t raw = ((v & PV_RAW_MASK) >> PV_RAW_SHIFT) & 0xffu;
+            const uint32_t base_v = v & ~(PV_RAW_MASK | PV_SEEN);
+            if (!(v & PV_PRESENT)) s.vv[dir][h] = base_v;
+            else s.vv[dir][h] = phase == 1 ? ((base_v & ~0xffu) | raw) : ((base_v & ~0xff00u) | (raw << 8));
+        }
+    __syncwarp();
+    for (int d = 0; d < 2; ++d) {
+        st.nkeys[d] = nkeys[d];
+        if (phase == 1) st.n1[d] = nins[d];
+        else st.n2[d] = nins[d];
+    }
+    return 1;
+}
+
+// ---------------------------------------------------------------------------
 // lane 0: map operations of one mate (getSeedRefsFirstRead / SecondRead)
 // ---------------------------------------------------------------------------
 __device__ void pe_count_first(const DevIndex& ix, const PeIndex& px, const PeMem& s, PeState& st, uint32_t len,
@@ -561,7 +700,7 @@ __device__ __noinline__ void pe_walk(const DevIndex& ix, const PeIndex& px, cons
     const uint64_t off0 = cb.offs[r_idx];
     const uint32_t len = (uint32_t)(cb.offs[r_idx + 1] - off0);
     const char* raw = cb.seqs + off0;
-    ShiftAndState<W> sa;
+    EditScan<W> sa;
     sa.load(raw, len, orient);
     PieceKeys pk;
     pk.load(raw, len, orient);
@@ -761,18 +900,20 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
     }
     __syncwarp();
     const uint32_t sigma = pe_kmers(ix, px, s, s.rd[0], n1);
-    if (lane == 0) {
-        pe_count_first(ix, px, s, st, n1, sigma <= s.c.ecap);
-        // rebuild: keep count1 >= QTHRESH
-        if (!st.over)
-            for (int dir = 0; dir < 2; ++dir)
-                for (uint32_t x = 0; x < st.n1[dir]; ++x) {
-                    const int h = pm_find(s, dir, s.ins1[dir][x]);
-                    if (pv_c1(s.vv[dir][h]) < QTHRESH) s.vv[dir][h] = 0;
-                    else s.vv[dir][h] = PV_PRESENT | pv_c1(s.vv[dir][h]);
-                }
+    if (sigma <= s.c.ecap) {
+        if (pe_count_par(px, s, st, n1, sigma, 1) < 0) return -1;
+    } else if (lane == 0) {
+        pe_count_first(ix, px, s, st, n1, false);
     }
     if (__shfl_sync(0xffffffffu, st.over, 0)) return -1;
+    // rebuild: keep count1 >= QTHRESH (order-independent)
+    for (int dir = 0; dir < 2; ++dir)
+        for (uint32_t h = lane; h < s.c.vcap; h += 32) {
+            const uint32_t v = s.vv[dir][h];
+            if (!(v & PV_PRESENT)) continue;
+            s.vv[dir][h] = pv_c1(v) < QTHRESH ? 0u : (PV_PRESENT | pv_c1(v));
+        }
+    __syncwarp();
     bool any = false;
     if (lane == 0)
         for (int dir = 0; dir < 2 && !any; ++dir)
@@ -781,7 +922,10 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
     if (!__shfl_sync(0xffffffffu, any, 0)) return 0;
     __syncwarp();
     const uint32_t sigma2 = pe_kmers(ix, px, s, s.rd[1], n2);
-    if (lane == 0) pe_count_second(ix, px, s, st, n2, sigma2 <= s.c.ecap);
+    int par2 = 0;
+    if (sigma2 <= s.c.ecap) par2 = pe_count_par(px, s, st, n2, sigma2, 2);
+    if (par2 < 0) return -1;
+    if (par2 == 0 && lane == 0) pe_count_second(ix, px, s, st, n2, sigma2 <= s.c.ecap);
     if (__shfl_sync(0xffffffffu, st.over, 0)) return -1;
     __syncwarp();
     // f2 flags (order-independent: flags are only set) and hasCpG, lanes over the table slots

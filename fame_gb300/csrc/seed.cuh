@@ -80,7 +80,7 @@ __device__ __forceinline__ uint32_t sim_key(const SeedMem& s, uint32_t x) { retu
 // rehash_impl (hopscotch_hash.h:1243-1300): the bucket elements are re-inserted
 // in array order into a table of max(count, ceil(size / 0.9)) buckets; here they
 // are pushed on the pending stack (lowest bucket on top), overflow stays.
-__device__ __noinline__ bool sim_rehash(MapSim& m, const SeedMem& s, uint32_t count)
+__device__ bool sim_rehash(MapSim& m, const SeedMem& s, uint32_t count)
 {
     const uint32_t need = (uint32_t)ceilf((float)m.nb / 0.9f);
     if (need > count) count = need;
@@ -99,7 +99,7 @@ __device__ __noinline__ bool sim_rehash(MapSim& m, const SeedMem& s, uint32_t co
 }
 
 // insert_impl (hopscotch_hash.h:1410-1460) for the element on top of the stack.
-__device__ __noinline__ bool sim_step(MapSim& m, const SeedMem& s)
+__device__ bool sim_step(MapSim& m, const SeedMem& s)
 {
     const uint32_t x = s.stk[m.sp - 1];
     const uint32_t k = sim_key(s, x);
