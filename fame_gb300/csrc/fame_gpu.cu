@@ -443,10 +443,10 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
             const uint32_t tb = 128;
             const uint32_t grid = (uint32_t)std::min<uint64_t>((ncand + tb - 1) / tb, (uint64_t)g->sm_count * 32);
             const uint64_t wmask = g->h_ctr[CTR_WMASK];
-            if (wmask & 2u) { k_shiftand<1><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
-            if (wmask & 4u) { k_shiftand<2><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
-            if (wmask & 8u) { k_shiftand<3><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
-            if (wmask & 16u) { k_shiftand<4><<<grid, tb, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+            if (wmask & 2u) { k_shiftand<1><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+            if (wmask & 4u) { k_shiftand<2><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+            if (wmask & 8u) { k_shiftand<3><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
+            if (wmask & 16u) { k_shiftand<4><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
         }
         if (T) cudaEventRecord(g->ev[3], g->stream);
         k_select<<<(n + 255) / 256, 256, 0, g->stream>>>(g->ix, cb);
@@ -593,10 +593,10 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
             if (last <= first) return;
             cb.cand_first = (uint32_t)first;
             const uint32_t grid = (uint32_t)std::min<uint64_t>((last - first + 127) / 128, (uint64_t)g->sm_count * 32);
-            if (wmask & 2u) { k_shiftand<1><<<grid, 128, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
-            if (wmask & 4u) { k_shiftand<2><<<grid, 128, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
-            if (wmask & 8u) { k_shiftand<3><<<grid, 128, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
-            if (wmask & 16u) { k_shiftand<4><<<grid, 128, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
+            if (wmask & 2u) { k_shiftand<1><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
+            if (wmask & 4u) { k_shiftand<2><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
+            if (wmask & 8u) { k_shiftand<3><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
+            if (wmask & 16u) { k_shiftand<4><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)last); g->launches++; }
             cb.cand_first = 0;
         };
         // B, C: first-walk scans, first walks, second-walk candidates

@@ -84,35 +84,16 @@ struct ScanText {
     uint32_t len;     // scan positions
     uint32_t off_a;   // reported offset = off_a + dir_sign * u (see off())
     int fwd;
-    __device__ __forceinline__ int base(uint32_t u, bool& isN) const
-    {
-        const uint64_t g = dir > 0 ? g0 + u : g0 - u;
-        isN = (__ldg(ix->gnmask + (g >> 5)) >> (g & 31)) & 1u;
-        const int b = (int)((__ldg(ix->gpack + (g >> 4)) >> (2 * (g & 15))) & 3u);
-        return fwd ? b : 3 - b;
-    }
     __device__ __forceinline__ uint32_t off(uint32_t u) const { return fwd ? u + MISCOUNT : off_a - u; }
+    // genome range [G0, G1) of the text
+    __device__ __forceinline__ uint64_t G0() const { return fwd ? g0 : g0 + 1 - len; }
 };
 
-// Scan of one candidate window with the same hits as scan_window_full.
-//
-// Any alignment of the read with <= 6 edits leaves one of 7 disjoint read
-// pieces without an edit, so that piece's first q bases occur in the text
-// (equal in the reduced alphabet A / G / C=T, which the asymmetric match
-// implies).  A cheap pass finds those q-gram occurrences and turns each into
-// the span of scan positions where the alignment can end; the automaton then
-// runs only over those spans, each entered at least m + 7 positions early
-// (the state at a position depends on the last m + 6 bases only, and a reset
-// state never accepts where the full scan would not) or continued from the
-// previous span, and each extended until its run of accepting positions ends.
-// N bases reset the automaton exactly as in the full scan.  Too many spans
-// (repetitive windows) fall back to the full scan.
-template <int W, class Emit>
-__device__ void scan_window(const DevIndex& ix, EditScan<W>& sa, uint32_t wid, int fwd, Emit emit,
-                            const uint32_t* pkey, uint32_t pvalid, uint32_t q, const uint32_t* pstart,
-                            bool unguarded = false)
+// The text querySeq / queryRevSeq scan for window wid (saQuerySeedSetRef,
+// ReadQueue.cpp:1953-1962, 2048-2058) for a read of m bases.
+__device__ __forceinline__ ScanText window_text(const DevIndex& ix, uint32_t wid, int fwd, bool unguarded,
+                                                uint32_t m)
 {
-    constexpr int CAP = 32;
     const uint4 wi = ix.win[wid];
     const uint32_t sp = wi.x, ch = wi.y;
     const int64_t L = (int64_t)ix.chrom_len[ch];
@@ -134,12 +115,88 @@ __device__ void scan_window(const DevIndex& ix, EditScan<W>& sa, uint32_t wid, i
         tx.g0 = gch + (uint64_t)hi;
         tx.dir = -1;
         tx.len = (uint32_t)(hi - lo);
-        tx.off_a = (uint32_t)(hi - lo) + sa.plen - 1 + MISCOUNT;
+        tx.off_a = (uint32_t)(hi - lo) + m - 1 + MISCOUNT;
     }
+    return tx;
+}
+
+// The automaton over nm merged spans (ascending, disjoint; span(i) returns
+// lo | hi << 16 in scan positions).  Each span is entered at least m + 7
+// positions early (the state at a position depends on the last m + 6 bases
+// only, and a reset state never accepts where the full scan would not) or
+// continued from the previous span, and extended until its run of accepting
+// positions ends.  N bases reset the automaton exactly as in the full scan.
+template <int W, class Span, class Emit>
+__device__ void run_spans(EditScan<W>& sa, const ScanText& tx, int nm, Span span, Emit emit)
+{
+    const DevIndex& ix = *tx.ix;
+    const uint32_t m = sa.plen;
+    const uint32_t gate = m - NERR;
+    bool was = false;
+    uint32_t cur_off = 0;
+    int cur_err = 0;
+    uint32_t ncl = 0;
+    int64_t cursor = -1;
+    uint64_t cw = ~0ull, cwn = ~0ull;   // genome words held in wpack / wn
+    uint32_t wpack = 0, wn = 0;
+    sa.reset();
+    for (int i = 0; i < nm; ++i) {
+        const uint32_t sv = span(i);
+        const int64_t lo = (int64_t)(sv & 0xffffu), hi = (int64_t)(sv >> 16);
+        int64_t start = lo - (int64_t)(m + NERR + 1);
+        if (start < 0) start = 0;
+        if (start <= cursor + 1) {
+            start = cursor + 1;
+        } else {
+            sa.reset();
+            ncl = 0;
+        }
+        int64_t u = start;
+        for (; u < (int64_t)tx.len && (u <= hi || was); ++u) {
+            const uint64_t g = tx.dir > 0 ? tx.g0 + (uint64_t)u : tx.g0 - (uint64_t)u;
+            if ((g >> 4) != cw) { cw = g >> 4; wpack = __ldg(ix.gpack + cw); }
+            if ((g >> 5) != cwn) { cwn = g >> 5; wn = __ldg(ix.gnmask + cwn); }
+            if ((wn >> (g & 31)) & 1u) { sa.reset(); continue; }
+            const int b = (int)((wpack >> (2 * (g & 15))) & 3u);
+            sa.letter(tx.fwd ? b : 3 - b);
+            if (++ncl < gate) continue;
+            const int er = sa.match();
+            if (er >= 0) {
+                const uint32_t off = tx.off((uint32_t)u);
+                if (was) { if (er <= cur_err) { cur_off = off; cur_err = er; } }
+                else { was = true; cur_off = off; cur_err = er; }
+            } else if (was) {
+                emit(cur_off, cur_err);
+                was = false;
+            }
+        }
+        cursor = u - 1;
+        if (u >= (int64_t)tx.len) break;
+    }
+    if (was) emit(cur_off, cur_err);
+}
+
+// Scan of one candidate window by one thread, with the same hits as
+// scan_window_full.
+//
+// Any alignment of the read with <= 6 edits leaves one of 7 disjoint read
+// pieces without an edit, so that piece's first q bases occur in the text
+// (equal in the reduced alphabet A / G / C=T, which the asymmetric match
+// implies).  A cheap pass finds those q-gram occurrences and turns each into
+// the span of scan positions where the alignment can end; the automaton then
+// runs only over the merged spans (run_spans).  Too many spans (repetitive
+// windows) fall back to the full scan.
+template <int W, class Emit>
+__device__ void scan_window(const DevIndex& ix, EditScan<W>& sa, uint32_t wid, int fwd, Emit emit,
+                            const uint32_t* pkey, uint32_t pvalid, uint32_t q, const uint32_t* pstart,
+                            bool unguarded = false)
+{
+    constexpr int CAP = 32;
+    const ScanText tx = window_text(ix, wid, fwd, unguarded, sa.plen);
     const uint32_t m = sa.plen;
     // ---- q-gram pass
     int32_t ilo[CAP], ihi[CAP];
-    const uint64_t G0 = fwd ? tx.g0 : tx.g0 + 1 - tx.len, G1 = G0 + tx.len;
+    const uint64_t G0 = tx.G0(), G1 = G0 + tx.len;
     const int nint = qgram_spans<CAP>(ix.gpack, ix.gnmask, G0, G1, fwd, m, q, pkey, pvalid, pstart, ilo, ihi);
     if (nint < 0) { scan_window_full<W>(ix, sa, wid, fwd, emit, unguarded); return; }
     if (nint == 0) return;
@@ -156,44 +213,146 @@ __device__ void scan_window(const DevIndex& ix, EditScan<W>& sa, uint32_t wid, i
         if (nm > 0 && ilo[i] <= ihi[nm - 1] + 1) { if (ihi[i] > ihi[nm - 1]) ihi[nm - 1] = ihi[i]; }
         else { ilo[nm] = ilo[i]; ihi[nm] = ihi[i]; ++nm; }
     }
-    // ---- automaton over the spans (state at scan position 0 = the full scan's reset)
-    const uint32_t gate = m - NERR;
-    bool was = false;
-    uint32_t cur_off = 0;
-    int cur_err = 0;
-    uint32_t ncl = 0;
-    int64_t cursor = -1;
-    sa.reset();
-    for (int i = 0; i < nm; ++i) {
-        int64_t start = (int64_t)ilo[i] - (int64_t)(m + NERR + 1);
-        if (start < 0) start = 0;
-        if (start <= cursor + 1) {
-            start = cursor + 1;
-        } else {
-            sa.reset();
-            ncl = 0;
+    run_spans<W>(sa, tx, nm, [&](int i) { return (uint32_t)ilo[i] | ((uint32_t)ihi[i] << 16); }, emit);
+}
+
+// The q-gram pass of one candidate window run by a whole warp (every lane
+// calls it with the same arguments): lane k < 7 builds piece k's key, lanes
+// own consecutive packed words of the text (coalesced loads, each word's
+// predecessor by shuffle), hits append raw spans to a per-warp list, and the
+// list is sorted and merged with warp scans.  Writes the merged spans
+// (lo | hi << 16, ascending) to pool[0..) and returns their number, or -1 when
+// the window has more than 32 raw spans or more than pool_cap merged ones
+// (the caller then scans the whole window).  Same spans as qgram_spans plus
+// scan_window's merge.
+__device__ int qgram_spans_warp(const DevIndex& ix, const char* raw, uint32_t m, int orient, const ScanText& tx,
+                                uint32_t* pool, int pool_cap, int32_t* rlo, int32_t* rhi, uint32_t* rn,
+                                uint32_t lane)
+{
+    constexpr uint32_t FULL = 0xffffffffu;
+    const uint32_t q = min(16u, m / 7);
+    if (q == 0 || tx.len == 0) return 0;
+    const int fwd = tx.fwd;
+    // ---- piece keys (scan order, first symbol most significant), compared in genome order
+    uint32_t key = 0;
+    bool ok = lane < (uint32_t)QG_PIECES;
+    if (ok) {
+        const uint32_t st = (lane * m) / 7;
+        for (uint32_t i = 0; i < q; ++i) {
+            const uint32_t p = st + i;
+            const uint8_t c = orient ? rc_byte((uint8_t)raw[m - 1 - p]) : (uint8_t)raw[p];
+            uint32_t sym;
+            switch (c) {
+                case 'A': sym = 0; break;
+                case 'G': sym = 1; break;
+                case 'C': case 'T': sym = 2; break;
+                default: sym = 3; ok = false; break;
+            }
+            key = (key << 2) | sym;
         }
-        int64_t u = start;
-        for (; u < (int64_t)tx.len && (u <= ihi[i] || was); ++u) {
-            bool isN;
-            const int b = tx.base((uint32_t)u, isN);
-            if (isN) { sa.reset(); continue; }
-            sa.letter(b);
-            if (++ncl < gate) continue;
-            const int er = sa.match();
-            if (er >= 0) {
-                const uint32_t off = tx.off((uint32_t)u);
-                if (was) { if (er <= cur_err) { cur_off = off; cur_err = er; } }
-                else { was = true; cur_off = off; cur_err = er; }
-            } else if (was) {
-                emit(cur_off, cur_err);
-                was = false;
+        if (fwd) key = qg_symrev(key, q);
+    }
+    const uint32_t pvalid = __ballot_sync(FULL, ok) & ((1u << QG_PIECES) - 1);
+    if (!pvalid) return 0;
+    const uint32_t kfill = __shfl_sync(FULL, key, __ffs(pvalid) - 1);
+    if (!ok) key = kfill;
+    uint32_t ckey[QG_PIECES];
+#pragma unroll
+    for (int k = 0; k < QG_PIECES; ++k) ckey[k] = __shfl_sync(FULL, key, k);
+    const uint32_t qmask = q >= 16 ? 0xffffffffu : ((1u << (2 * q)) - 1);
+    const uint32_t nq = (1u << q) - 1;
+    const uint64_t G0 = tx.G0(), G1 = G0 + tx.len;
+    const int32_t len = (int32_t)tx.len;
+    const uint64_t w0 = G0 >> 4, w1 = (G1 - 1) >> 4;
+    const uint32_t nw = (uint32_t)(w1 - w0 + 1);
+    __syncwarp();   // every lane is done with the previous window's list
+    if (lane == 0) *rn = 0;
+    __syncwarp();
+    uint32_t carryS = 0, carryN = 0xffffu;   // word before the first: all bases excluded
+    for (uint32_t base = 0; base < nw; base += 32) {
+        const uint64_t wi = w0 + base + lane;
+        const bool act = base + lane < nw;
+        uint32_t cur = 0, nb = 0xffffu;
+        if (act) {
+            cur = qg_reduce(__ldg(ix.gpack + wi), fwd);
+            nb = (__ldg(ix.gnmask + (wi >> 1)) >> (16 * (uint32_t)(wi & 1))) & 0xffffu;
+            if (wi == w0) nb |= (1u << (G0 & 15)) - 1;
+            if (wi == w1) nb |= (0xffffu << (((G1 - 1) & 15) + 1)) & 0xffffu;
+        }
+        uint32_t prevS = __shfl_up_sync(FULL, cur, 1), prevN = __shfl_up_sync(FULL, nb, 1);
+        if (lane == 0) { prevS = carryS; prevN = carryN; }
+        carryS = __shfl_sync(FULL, cur, 31);
+        carryN = __shfl_sync(FULL, nb, 31);
+        const uint64_t catS = (uint64_t)prevS | ((uint64_t)cur << 32);
+        const uint32_t catN = prevN | (nb << 16);
+        // q-gram ending at base i of this word starts at bit 17 + i - q
+        const uint64_t sS = catS >> (2 * (17 - q));
+        const uint32_t sN = catN >> (17 - q);
+        uint32_t hm = 0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const uint32_t k2 = (uint32_t)(sS >> (2 * i)) & qmask;
+            bool eq = false;
+#pragma unroll
+            for (int k = 0; k < QG_PIECES; ++k) eq |= k2 == ckey[k];
+            hm |= (eq ? 1u : 0u) << i;
+        }
+        if (!act) hm = 0;
+        if (__ballot_sync(FULL, hm != 0) == 0) continue;
+        while (hm) {
+            const int i = __ffs(hm) - 1;
+            hm &= hm - 1;
+            if ((sN >> i) & nq) continue;
+            const uint32_t k2 = (uint32_t)(sS >> (2 * i)) & qmask;
+            const int64_t A = (int64_t)(16 * wi + (uint64_t)i) - (int64_t)q + 1;   // genome start of the q-gram
+            const int32_t x = fwd ? (int32_t)(A - (int64_t)G0) : (int32_t)((int64_t)G1 - A - (int64_t)q);
+#pragma unroll
+            for (int k = 0; k < QG_PIECES; ++k) {
+                if (!((pvalid >> k) & 1u) || k2 != ckey[k]) continue;
+                const int32_t end0 = x - 1 + (int32_t)(m - ((uint32_t)k * m) / 7);
+                int32_t a = end0 - (int32_t)NERR, b = end0 + (int32_t)NERR;
+                if (b < 0 || a > len - 1) continue;
+                if (a < 0) a = 0;
+                if (b > len - 1) b = len - 1;
+                const uint32_t slot = atomicAdd(rn, 1u);
+                if (slot < 32) { rlo[slot] = a; rhi[slot] = b; }
             }
         }
-        cursor = u - 1;
-        if (u >= (int64_t)tx.len) break;
     }
-    if (was) emit(cur_off, cur_err);
+    __syncwarp();
+    const uint32_t n = *rn;
+    if (n > 32) return -1;
+    if (n == 0) return 0;
+    // ---- sort by start (rank of each raw span), then merge with a prefix maximum of the ends
+    int32_t lo = lane < n ? rlo[lane] : 0x7fffffff, hi = lane < n ? rhi[lane] : 0;
+    uint32_t rank = 0;
+    for (uint32_t j = 0; j < n; ++j) {
+        const int32_t lj = __shfl_sync(FULL, lo, j);
+        rank += (lj < lo || (lj == lo && j < lane)) ? 1u : 0u;
+    }
+    __syncwarp();
+    if (lane < n) { rlo[rank] = lo; rhi[rank] = hi; }
+    __syncwarp();
+    lo = lane < n ? rlo[lane] : 0x7fffffff;
+    hi = lane < n ? rhi[lane] : 0;
+    int32_t incl = hi;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int32_t t = __shfl_up_sync(FULL, incl, d);
+        if (lane >= (uint32_t)d && t > incl) incl = t;
+    }
+    const int32_t excl = __shfl_up_sync(FULL, incl, 1);
+    const bool start = lane < n && (lane == 0 || lo > excl + 1);
+    const uint32_t sb = __ballot_sync(FULL, start);
+    const int nm = __popc(sb);
+    if (nm > pool_cap) return -1;
+    const int gid = __popc(sb & (0xffffffffu >> (31 - lane))) - 1;
+    const bool last = lane < n && (lane == n - 1 || ((sb >> (lane + 1)) & 1u));
+    uint16_t* ph = (uint16_t*)pool;
+    if (start) ph[2 * gid] = (uint16_t)lo;
+    if (last) ph[2 * gid + 1] = (uint16_t)incl;
+    __syncwarp();
+    return nm;
 }
 
 // Reduced-alphabet keys of the first q bases of the 7 read pieces.
@@ -228,42 +387,91 @@ struct PieceKeys {
     }
 };
 
-template <int W>
-__device__ void shiftand_one(const DevIndex& ix, const ChunkBufs& cb, uint32_t c)
-{
-    const uint32_t task = cb.cand_task[c];
-    const uint32_t r = task >> 1, o = task & 1;
-    const uint64_t off0 = cb.offs[r];
-    const uint32_t len = (uint32_t)(cb.offs[r + 1] - off0);
-    EditScan<W> sa;
-    sa.load(cb.seqs + off0, len, (int)o);
-    PieceKeys pk;
-    pk.load(cb.seqs + off0, len, (int)o);
-    const uint32_t e = cb.cand[c];
-    uint32_t n = 0;
-    uint32_t* out = cb.hits + (uint64_t)c * HIT_CAP;
-    const bool unguarded = cb.cand_flags && (cb.cand_flags[c] & 1u);
-    scan_window<W>(ix, sa, e & 0x7fffffffu, (int)(e >> 31), [&](uint32_t off, int err) {
-        if (n < HIT_CAP) out[n] = (off << 8) | (uint32_t)err;
-        ++n;
-    }, pk.key, pk.valid, pk.q, pk.start, unguarded);
-    cb.hit_n[c] = n;
-}
+// Window scans of the candidates whose read length needs W pattern words (one
+// launch per W, so the register file is sized for that W only).  Blocks of
+// SA_WARPS warps (launched with 32 * SA_WARPS threads); a warp takes 32
+// consecutive candidates, runs the q-gram pass of each with all its lanes
+// (qgram_spans_warp, spans into a per-warp pool), then each lane runs the
+// automaton over the spans of one candidate.  hits / hit_n as scan_window.
+constexpr int SA_WARPS = 4;
+constexpr int SA_POOL = 256;   // merged spans per warp for its 32 candidates
+struct SaWarp {
+    uint32_t pool[SA_POOL];
+    int32_t rlo[32], rhi[32];
+    uint32_t rn;
+    int16_t nsp[32];           // merged spans of each candidate, -1: scan the whole window
+    uint16_t off[32];          // first pool entry of each candidate
+};
 
-// One launch per pattern word count W: each handles the candidates whose read
-// length needs W words, so the register file is sized for that W only.
 template <int W>
-__global__ void k_shiftand(DevIndex ix, ChunkBufs cb, uint32_t ncand)
+__global__ void __launch_bounds__(32 * SA_WARPS) k_shiftand(DevIndex ix, ChunkBufs cb, uint32_t ncand)
 {
+    constexpr uint32_t FULL = 0xffffffffu;
     if (ncand == FROM_DEVICE) {
         if (cand_overflow(cb) || !((cb.ctr[CTR_WMASK] >> W) & 1ull)) return;
         ncand = (uint32_t)cb.ctr[CTR_CAND];
     }
-    for (uint32_t c = cb.cand_first + blockIdx.x * blockDim.x + threadIdx.x; c < ncand; c += gridDim.x * blockDim.x) {
-        const uint32_t task = cb.cand_task[c];
-        const uint32_t r = task >> 1;
-        const uint32_t len = (uint32_t)(cb.offs[r + 1] - cb.offs[r]);
-        if ((int)(len / 64 + 1) == W) shiftand_one<W>(ix, cb, c);
+    __shared__ SaWarp smem[SA_WARPS];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    SaWarp& S = smem[wib];
+    const uint64_t nwarps = (uint64_t)gridDim.x * SA_WARPS;
+    for (uint64_t c0 = cb.cand_first + ((uint64_t)blockIdx.x * SA_WARPS + wib) * 32; c0 < ncand; c0 += nwarps * 32) {
+        const uint32_t c = (uint32_t)c0 + lane;
+        bool mine = c < ncand;
+        uint32_t o = 0, len = 0, e = 0;
+        uint64_t off0 = 0;
+        bool ung = false;
+        if (mine) {
+            const uint32_t task = cb.cand_task[c];
+            const uint32_t r = task >> 1;
+            o = task & 1;
+            off0 = cb.offs[r];
+            len = (uint32_t)(cb.offs[r + 1] - off0);
+            e = cb.cand[c];
+            ung = cb.cand_flags && (cb.cand_flags[c] & 1u);
+            mine = (int)(len / 64 + 1) == W;
+        }
+        // ---- q-gram pass of each candidate, whole warp
+        uint32_t todo = __ballot_sync(FULL, mine);
+        int used = 0;
+        while (todo) {
+            const int i = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const uint32_t mi = __shfl_sync(FULL, len, i), oi = __shfl_sync(FULL, o, i), ei = __shfl_sync(FULL, e, i);
+            const bool ui = __shfl_sync(FULL, ung ? 1u : 0u, i) != 0;
+            const uint64_t offi = ((uint64_t)__shfl_sync(FULL, (uint32_t)(off0 >> 32), i) << 32) |
+                                  __shfl_sync(FULL, (uint32_t)off0, i);
+            const ScanText tx = window_text(ix, ei & 0x7fffffffu, (int)(ei >> 31), ui, mi);
+            const int nm = qgram_spans_warp(ix, cb.seqs + offi, mi, (int)oi, tx, S.pool + used, SA_POOL - used,
+                                            S.rlo, S.rhi, &S.rn, lane);
+            if (lane == 0) {
+                S.nsp[i] = (int16_t)nm;
+                S.off[i] = (uint16_t)used;
+            }
+            if (nm > 0) used += nm;
+        }
+        __syncwarp();
+        // ---- automaton, one candidate per lane
+        if (mine) {
+            EditScan<W> sa;
+            sa.load(cb.seqs + off0, len, (int)o);
+            const int nm = S.nsp[lane];
+            uint32_t n = 0;
+            uint32_t* out = cb.hits + (uint64_t)c * HIT_CAP;
+            auto emit = [&](uint32_t off, int err) {
+                if (n < HIT_CAP) out[n] = (off << 8) | (uint32_t)err;
+                ++n;
+            };
+            if (nm < 0) {
+                scan_window_full<W>(ix, sa, e & 0x7fffffffu, (int)(e >> 31), emit, ung);
+            } else if (nm > 0) {
+                const ScanText tx = window_text(ix, e & 0x7fffffffu, (int)(e >> 31), ung, len);
+                const uint32_t* sp = S.pool + S.off[lane];
+                run_spans<W>(sa, tx, nm, [&](int k) { return sp[k]; }, emit);
+            }
+            cb.hit_n[c] = n;
+        }
+        __syncwarp();
     }
 }
 

@@ -132,10 +132,10 @@ void qslot_enqueue(fame_gpu* g, QSlot& s, uint32_t n, uint32_t flags, uint32_t* 
     k_seed<<<std::max(1u, blocks), 128, 4 * LightLayout::BYTES, s.stream>>>(g->ix, cb, ntask);
     k_seed_heavy<<<(s.hs.nwarps + 3) / 4, 128, 0, s.stream>>>(g->ix, cb, s.hs, FROM_DEVICE);
     const uint32_t grid = (uint32_t)g->sm_count * 32;
-    k_shiftand<1><<<grid, 128, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
-    k_shiftand<2><<<grid, 128, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
-    k_shiftand<3><<<grid, 128, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
-    k_shiftand<4><<<grid, 128, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
+    k_shiftand<1><<<grid, 32 * SA_WARPS, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
+    k_shiftand<2><<<grid, 32 * SA_WARPS, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
+    k_shiftand<3><<<grid, 32 * SA_WARPS, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
+    k_shiftand<4><<<grid, 32 * SA_WARPS, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
     k_select<<<(n + 255) / 256, 256, 0, s.stream>>>(g->ix, cb);
     k_dp_warp<<<g->dp_grid, 128, 4 * DPW_BYTES, s.stream>>>(g->ix, cb);
     cudaMemcpyAsync(s.h_mats, s.d_mats, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, s.stream);
