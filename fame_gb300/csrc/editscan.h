@@ -95,30 +95,39 @@ struct EditScan {
     {
         plen = len;
         const int d = 32 * NW - (int)len;
-        uint32_t tA = 0, tC = 0, tG = 0, tT = 0;
-        for (int row = 32 * NW - 1; row >= 0; --row) {
-            tA <<= 1; tC <<= 1; tG <<= 1; tT <<= 1;
-            if (row >= d) {
-                const uint32_t p = (uint32_t)(row - d);
-                uint8_t c = (uint8_t)(orient ? raw[len - 1 - p] : raw[p]);
-                if (orient) c = c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : c == 'T' ? 'A' : c;
-                switch (c) {
-                    case 'A': tA |= 1; break;
-                    case 'C': tC |= 1; break;
-                    case 'G': tG |= 1; break;
-                    case 'T': tT |= 1; tC |= 1; break;
-                    default: break;
-                }
-            } else {
-                tA |= 1; tC |= 1; tG |= 1; tT |= 1;
-            }
-            if ((row & 31) == 0) {
+        // word j holds rows 32j .. 32j + 31, built from its top row down
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
-                for (int j = 0; j < NW; ++j)
-                    if (j == (row >> 5)) { peq[0][j] = tA; peq[1][j] = tC; peq[2][j] = tG; peq[3][j] = tT; }
+        for (int j = 0; j < NW; ++j) {
+            uint32_t tA = 0, tC = 0, tG = 0, tT = 0;
+            for (int row = 32 * j + 31; row >= 32 * j; --row) {
+                tA <<= 1; tC <<= 1; tG <<= 1; tT <<= 1;
+                if (row >= d) {
+                    const uint32_t p = (uint32_t)(row - d);
+                    uint8_t c = (uint8_t)(orient ? raw[len - 1 - p] : raw[p]);
+                    if (orient) c = c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : c == 'T' ? 'A' : c;
+                    tA |= c == 'A' ? 1u : 0u;
+                    tC |= (c == 'C' || c == 'T') ? 1u : 0u;
+                    tG |= c == 'G' ? 1u : 0u;
+                    tT |= c == 'T' ? 1u : 0u;
+                } else {
+                    tA |= 1; tC |= 1; tG |= 1; tT |= 1;
+                }
             }
+            peq[0][j] = tA; peq[1][j] = tC; peq[2][j] = tG; peq[3][j] = tT;
+        }
+    }
+
+    // The rows of load() from bit masks already built (row 32j + l of word j).
+    FAME_HD void set(const uint32_t* m4, uint32_t len)
+    {
+        plen = len;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+        for (int j = 0; j < NW; ++j) {
+            peq[0][j] = m4[j]; peq[1][j] = m4[NW + j]; peq[2][j] = m4[2 * NW + j]; peq[3][j] = m4[3 * NW + j];
         }
     }
 

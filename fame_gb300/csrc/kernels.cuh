@@ -14,7 +14,7 @@ namespace fame {
 // unguarded: the reverse scan starts at startPos - 1 even for a window at
 // position 0 (matchRevSecond, ReadQueue.cpp:4736), i.e. it includes base 0.
 template <int W, class Emit>
-__device__ void scan_window_full(const DevIndex& ix, EditScan<W>& sa, uint32_t wid, int fwd, Emit emit,
+__device__ __forceinline__ void scan_window_full(const DevIndex& ix, EditScan<W>& sa, uint32_t wid, int fwd, Emit emit,
                                  bool unguarded = false)
 {
     const uint4 wi = ix.win[wid];
@@ -127,7 +127,7 @@ __device__ __forceinline__ ScanText window_text(const DevIndex& ix, uint32_t wid
 // continued from the previous span, and extended until its run of accepting
 // positions ends.  N bases reset the automaton exactly as in the full scan.
 template <int W, class Span, class Emit>
-__device__ void run_spans(EditScan<W>& sa, const ScanText& tx, int nm, Span span, Emit emit)
+__device__ __forceinline__ void run_spans(EditScan<W>& sa, const ScanText& tx, int nm, Span span, Emit emit)
 {
     const DevIndex& ix = *tx.ix;
     const uint32_t m = sa.plen;
@@ -225,9 +225,15 @@ __device__ void scan_window(const DevIndex& ix, EditScan<W>& sa, uint32_t wid, i
 // the window has more than 32 raw spans or more than pool_cap merged ones
 // (the caller then scans the whole window).  Same spans as qgram_spans plus
 // scan_window's merge.
+//
+// Key test: when some bit offset s gives the distinct piece keys distinct
+// 5-bit fields (key >> s) & 31, the keys sit in a 32-slot table at their
+// fields (tab; tabp[slot] = the pieces with that key) and a text position is
+// tested with one table read and one compare; otherwise with 7 compares.  The
+// N and window-edge masks are only built for a word with a key hit.
 __device__ int qgram_spans_warp(const DevIndex& ix, const char* raw, uint32_t m, int orient, const ScanText& tx,
                                 uint32_t* pool, int pool_cap, int32_t* rlo, int32_t* rhi, uint32_t* rn,
-                                uint32_t lane)
+                                uint32_t* tab, uint32_t* tabp, uint32_t lane)
 {
     constexpr uint32_t FULL = 0xffffffffu;
     const uint32_t q = min(16u, m / 7);
@@ -261,55 +267,97 @@ __device__ int qgram_spans_warp(const DevIndex& ix, const char* raw, uint32_t m,
     for (int k = 0; k < QG_PIECES; ++k) ckey[k] = __shfl_sync(FULL, key, k);
     const uint32_t qmask = q >= 16 ? 0xffffffffu : ((1u << (2 * q)) - 1);
     const uint32_t nq = (1u << q) - 1;
+    // ---- the key table: lane s tests bit offset s
+    bool good = lane + 5 <= 2 * q;
+#pragma unroll
+    for (int a = 0; a < QG_PIECES; ++a)
+#pragma unroll
+        for (int b = a + 1; b < QG_PIECES; ++b)
+            if (((ckey[a] >> lane) & 31u) == ((ckey[b] >> lane) & 31u) && ckey[a] != ckey[b]) good = false;
+    const uint32_t gm = __ballot_sync(FULL, good);
+    const int ts = gm ? __ffs(gm) - 1 : -1;
+    __syncwarp();   // every lane is done with the previous window's table and list
+    if (ts >= 0) {
+        tab[lane] = 0xffffffffu;   // no text key: reduced symbols are 0..2
+        tabp[lane] = 0;
+        __syncwarp();
+        if (lane < (uint32_t)QG_PIECES) {
+            tab[(key >> ts) & 31u] = key;
+            if ((pvalid >> lane) & 1u) atomicOr(tabp + ((key >> ts) & 31u), 1u << lane);
+        }
+    }
+    const uint32_t tb = (uint32_t)__cvta_generic_to_shared(tab);
     const uint64_t G0 = tx.G0(), G1 = G0 + tx.len;
     const int32_t len = (int32_t)tx.len;
     const uint64_t w0 = G0 >> 4, w1 = (G1 - 1) >> 4;
     const uint32_t nw = (uint32_t)(w1 - w0 + 1);
-    __syncwarp();   // every lane is done with the previous window's list
     if (lane == 0) *rn = 0;
     __syncwarp();
-    uint32_t carryS = 0, carryN = 0xffffu;   // word before the first: all bases excluded
+    // excluded bases (N or outside the window) of packed word w, one bit per base
+    auto nbits = [&](uint64_t w) -> uint32_t {
+        if (w < w0 || w > w1) return 0xffffu;
+        uint32_t bb = (__ldg(ix.gnmask + (w >> 1)) >> (16 * (uint32_t)(w & 1))) & 0xffffu;
+        if (w == w0) bb |= (1u << (G0 & 15)) - 1;
+        if (w == w1) bb |= (0xffffu << (((G1 - 1) & 15) + 1)) & 0xffffu;
+        return bb;
+    };
+    uint32_t carryS = 0;   // reduced symbols of the word before this iteration's first
     for (uint32_t base = 0; base < nw; base += 32) {
         const uint64_t wi = w0 + base + lane;
         const bool act = base + lane < nw;
-        uint32_t cur = 0, nb = 0xffffu;
-        if (act) {
-            cur = qg_reduce(__ldg(ix.gpack + wi), fwd);
-            nb = (__ldg(ix.gnmask + (wi >> 1)) >> (16 * (uint32_t)(wi & 1))) & 0xffffu;
-            if (wi == w0) nb |= (1u << (G0 & 15)) - 1;
-            if (wi == w1) nb |= (0xffffu << (((G1 - 1) & 15) + 1)) & 0xffffu;
-        }
-        uint32_t prevS = __shfl_up_sync(FULL, cur, 1), prevN = __shfl_up_sync(FULL, nb, 1);
-        if (lane == 0) { prevS = carryS; prevN = carryN; }
+        const uint32_t cur = act ? qg_reduce(__ldg(ix.gpack + wi), fwd) : 0u;
+        uint32_t prevS = __shfl_up_sync(FULL, cur, 1);
+        if (lane == 0) prevS = carryS;
         carryS = __shfl_sync(FULL, cur, 31);
-        carryN = __shfl_sync(FULL, nb, 31);
-        const uint64_t catS = (uint64_t)prevS | ((uint64_t)cur << 32);
-        const uint32_t catN = prevN | (nb << 16);
         // q-gram ending at base i of this word starts at bit 17 + i - q
-        const uint64_t sS = catS >> (2 * (17 - q));
-        const uint32_t sN = catN >> (17 - q);
-        uint32_t hm = 0;
+        const uint64_t sS = (((uint64_t)cur << 32) | prevS) >> (2 * (17 - q));
+        bool anyh = false;
+        if (ts >= 0) {
+            const uint64_t sF = sS >> ts;
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            const uint32_t k2 = (uint32_t)(sS >> (2 * i)) & qmask;
-            bool eq = false;
+            for (int i = 0; i < 16; ++i) {
+                const uint32_t k2 = (uint32_t)(sS >> (2 * i)) & qmask;
+                const uint32_t off = (((uint32_t)(sF >> (2 * i)) & 31u) << 2) + tb;
+                uint32_t t;
+                asm volatile("ld.shared.u32 %0, [%1];" : "=r"(t) : "r"(off));
+                anyh |= t == k2;
+            }
+        } else {
 #pragma unroll
-            for (int k = 0; k < QG_PIECES; ++k) eq |= k2 == ckey[k];
-            hm |= (eq ? 1u : 0u) << i;
+            for (int i = 0; i < 16; ++i) {
+                const uint32_t k2 = (uint32_t)(sS >> (2 * i)) & qmask;
+#pragma unroll
+                for (int k = 0; k < QG_PIECES; ++k) anyh |= k2 == ckey[k];
+            }
         }
-        if (!act) hm = 0;
-        if (__ballot_sync(FULL, hm != 0) == 0) continue;
-        while (hm) {
-            const int i = __ffs(hm) - 1;
-            hm &= hm - 1;
+        anyh = anyh && act;
+        if (__ballot_sync(FULL, anyh) == 0) continue;
+        // ---- a word with a key hit: exclusion masks, then the spans of its hits
+        const uint32_t nb = act ? nbits(wi) : 0xffffu;
+        uint32_t prevN = __shfl_up_sync(FULL, nb, 1);
+        if (lane == 0) prevN = wi == w0 ? 0xffffu : nbits(wi - 1);
+        const uint32_t sN = (prevN | (nb << 16)) >> (17 - q);
+        if (!anyh) continue;
+        for (int i = 0; i < 16; ++i) {
             if ((sN >> i) & nq) continue;
             const uint32_t k2 = (uint32_t)(sS >> (2 * i)) & qmask;
+            uint32_t pieces = 0;
+            if (ts >= 0) {
+                const uint32_t f = (k2 >> ts) & 31u;
+                if (tab[f] == k2) pieces = tabp[f];
+            } else {
+#pragma unroll
+                for (int k = 0; k < QG_PIECES; ++k)
+                    if (k2 == ckey[k]) pieces |= 1u << k;
+                pieces &= pvalid;
+            }
+            if (!pieces) continue;
             const int64_t A = (int64_t)(16 * wi + (uint64_t)i) - (int64_t)q + 1;   // genome start of the q-gram
             const int32_t x = fwd ? (int32_t)(A - (int64_t)G0) : (int32_t)((int64_t)G1 - A - (int64_t)q);
-#pragma unroll
-            for (int k = 0; k < QG_PIECES; ++k) {
-                if (!((pvalid >> k) & 1u) || k2 != ckey[k]) continue;
-                const int32_t end0 = x - 1 + (int32_t)(m - ((uint32_t)k * m) / 7);
+            while (pieces) {
+                const uint32_t k = (uint32_t)(__ffs(pieces) - 1);
+                pieces &= pieces - 1;
+                const int32_t end0 = x - 1 + (int32_t)(m - (k * m) / 7);
                 int32_t a = end0 - (int32_t)NERR, b = end0 + (int32_t)NERR;
                 if (b < 0 || a > len - 1) continue;
                 if (a < 0) a = 0;
@@ -401,6 +449,7 @@ struct SaWarp {
     uint32_t rn;
     int16_t nsp[32];           // merged spans of each candidate, -1: scan the whole window
     uint16_t off[32];          // first pool entry of each candidate
+    uint32_t tab[32], tabp[32]; // key table of the window being filtered
 };
 
 template <int W>
@@ -443,7 +492,7 @@ __global__ void __launch_bounds__(32 * SA_WARPS) k_shiftand(DevIndex ix, ChunkBu
                                   __shfl_sync(FULL, (uint32_t)off0, i);
             const ScanText tx = window_text(ix, ei & 0x7fffffffu, (int)(ei >> 31), ui, mi);
             const int nm = qgram_spans_warp(ix, cb.seqs + offi, mi, (int)oi, tx, S.pool + used, SA_POOL - used,
-                                            S.rlo, S.rhi, &S.rn, lane);
+                                            S.rlo, S.rhi, &S.rn, S.tab, S.tabp, lane);
             if (lane == 0) {
                 S.nsp[i] = (int16_t)nm;
                 S.off[i] = (uint16_t)used;
