@@ -87,21 +87,25 @@ def allreduce_max(x, world):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+    """nvidia-smi clocks and throttle reasons, sampled every 50 ms from before
+    the warm-up (so the tool's start-up overlaps no timed loop) until stop();
+    the summary keeps the samples taken inside the marked timed windows."""
 
     FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown," \
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
              "clocks_event_reasons.sw_power_cap"
 
-    def __init__(self, device):
+    def __init__(self, device, interval_ms=50):
         self.device = device
-        self.samples = []
+        self.interval_ms = interval_ms
+        self.samples = []   # (host time, fields)
+        self.windows = []
         self.proc = None
 
-    def __enter__(self):
+    def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.interval_ms)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -111,26 +115,39 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.samples.append([x.strip() for x in line.split(",")])
+            self.samples.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
 
-    def __exit__(self, *a):
+    def mark(self, t0, t1):
+        self.windows.append((t0, t1))
+
+    def stop(self):
         if self.proc:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+            self.proc = None
+
+    def __enter__(self):
+        return self.start()
+
+    def __exit__(self, *a):
+        self.stop()
 
     def summary(self):
-        if not self.samples:
+        inside = [f for t, f in self.samples if any(a <= t <= b for a, b in self.windows)]
+        rows = inside or [f for _, f in self.samples]
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        sm = [float(s[0]) for s in rows if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in rows if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4)
+        reasons = sorted({names[i] for s in rows for i in range(4)
                           if len(s) > 3 + i and s[3 + i].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(rows),
+                "samples_from": "timed loops" if inside else "whole run (no sample inside a timed loop)"}
 
 
 # ---------------------------------------------------------------------------
@@ -254,6 +271,7 @@ def run_gb300(args):
     from fame_gb300._lib import lib as _L
     _L().fame_gpu_stream(gm.h, __import__("ctypes").byref(p_stream))
     stream = torch.cuda.ExternalStream(p_stream.value, device=local)
+    clk = ClockSampler(local).start()
     # warm-up: chunk 0 with the strand vote (getStranded), then decided orientation
     first = mine[0]
     d_s, d_o, n = dev[first]
@@ -273,20 +291,20 @@ def run_gb300(args):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
-        tw0 = time.perf_counter()
-        for k in range(args.steps):
-            d_s, d_o, n = dev[steady[k % len(steady)]]
-            c = gm.match_reads_dev(d_s, d_o, n, flags, d_mat, d_inv)
-            stage += gm.stage_times()
-            reads += n
-            gather += c.gather_bytes
-            scans += c.windows_scanned
-            launches += gm.last_launches()
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        tw1 = time.perf_counter()
+    ev0.record(stream)
+    tw0 = time.perf_counter()
+    for k in range(args.steps):
+        d_s, d_o, n = dev[steady[k % len(steady)]]
+        c = gm.match_reads_dev(d_s, d_o, n, flags, d_mat, d_inv)
+        stage += gm.stage_times()
+        reads += n
+        gather += c.gather_bytes
+        scans += c.windows_scanned
+        launches += gm.last_launches()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    tw1 = time.perf_counter()
+    clk.mark(tw0, tw1)
     barrier(world)
     t_dev = ev0.elapsed_time(ev1) / 1e3
     t_max = allreduce_max(t_dev, world)
@@ -296,6 +314,7 @@ def run_gb300(args):
     h2d = d2h = 0
     barrier(world)
     torch.cuda.synchronize()
+    te0 = time.perf_counter()
     ev0.record(stream)
     for k in range(args.steps):
         hs, ho, n = pinned[steady[k % len(steady)]]
@@ -305,6 +324,7 @@ def run_gb300(args):
         d2h += 9 * n
     ev1.record(stream)
     torch.cuda.synchronize()
+    clk.mark(te0, time.perf_counter())
     t_e2e = allreduce_max(ev0.elapsed_time(ev1) / 1e3, world)
     gm.set_timing(False)
     # ---- batched form: the same steps through the queue (CUDA-graph chunk
@@ -332,7 +352,10 @@ def run_gb300(args):
     for s_, n_ in inflight:
         q.collect(s_, mats=h_mat[:n_], invalid=h_inv[:n_])
     torch.cuda.synchronize()
-    t_b = allreduce_max(time.perf_counter() - tb0, world)
+    tb1 = time.perf_counter()
+    clk.mark(tb0, tb1)
+    clk.stop()
+    t_b = allreduce_max(tb1 - tb0, world)
     batched = {"value": b_reads * world / t_b, "unit": "reads/s", "slots": nslots,
                "gpu_launches": q.launches() - launches_q0,
                "timing": "host clock between device synchronisations; host buffers in and out"}
@@ -415,6 +438,7 @@ def run_gb300_serving(args):
         t1 = time.perf_counter()
         served = loop.run(jobs, realtime=True)
         t_serv = time.perf_counter() - t1
+        clk.mark(t1, t1 + t_serv)
         t1 = time.perf_counter()
         plain = plain_per_job(gm, jobs, realtime=True)
         t_plain = time.perf_counter() - t1
@@ -484,6 +508,7 @@ def run_gb300_pe(args):
     p_stream = ctypes.c_void_p()
     _L().fame_gpu_stream(gm.h, ctypes.byref(p_stream))
     stream = torch.cuda.ExternalStream(p_stream.value, device=0)
+    clk = ClockSampler(0).start()
     d_s, d_o, nn = dev[0]
     c = gm.match_pairs_dev(d_s, d_o, nn, FAME_GET_STRANDED, PE_MAXPDIST, d_mat, d_inv)
     flags = FAME_MATCH_R1_FWD if c.r1_fwd > c.r1_rev else 0
@@ -496,18 +521,20 @@ def run_gb300_pe(args):
     launches = 0
     heavy = 0
     torch.cuda.synchronize()
-    with ClockSampler(0) as clk:
-        ev0.record(stream)
-        for k in range(args.steps):
-            d_s, d_o, nn = dev[steady[k % len(steady)]]
-            c = gm.match_pairs_dev(d_s, d_o, nn, flags, PE_MAXPDIST, d_mat, d_inv)
-            pairs += nn
-            heavy += c.heavy_pairs
-            launches += gm.last_launches()
-        ev1.record(stream)
-        torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    for k in range(args.steps):
+        d_s, d_o, nn = dev[steady[k % len(steady)]]
+        c = gm.match_pairs_dev(d_s, d_o, nn, flags, PE_MAXPDIST, d_mat, d_inv)
+        pairs += nn
+        heavy += c.heavy_pairs
+        launches += gm.last_launches()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk.mark(t0, time.perf_counter())
     t_dev = ev0.elapsed_time(ev1) / 1e3
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
     ev0.record(stream)
     e_pairs = h2d = d2h = 0
     for k in range(args.steps):
@@ -518,6 +545,8 @@ def run_gb300_pe(args):
         d2h += 18 * nn
     ev1.record(stream)
     torch.cuda.synchronize()
+    clk.mark(t0, time.perf_counter())
+    clk.stop()
     t_e2e = ev0.elapsed_time(ev1) / 1e3
     out = {
         "metric": PE_METRIC, "value": pairs / t_dev, "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,

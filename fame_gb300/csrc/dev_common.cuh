@@ -79,6 +79,7 @@ enum {
     CTR_WMASK,          // bit W set when a valid read needs a W-word automaton
     CTR_PAIRED,         // pairs with both mates in CpG windows
     CTR_TOOSHORT,       // the paired path's tooShort count
+    CTR_CAND_USED,      // candidate slots holding a candidate (CTR_CAND counts reserved ones)
     CTR_N
 };
 
@@ -87,6 +88,8 @@ constexpr int HIT_CAP = 6;
 // A count argument with this value is read from the chunk's device counters
 // instead (launches that run without a host round trip).
 constexpr uint32_t FROM_DEVICE = 0xffffffffu;
+// cand_task value of a reserved candidate slot that holds no candidate
+constexpr uint32_t CAND_HOLE = 0xffffffffu;
 
 // The candidate buffer overflowed: the chunk's later stages do nothing and the
 // host reruns it with a larger buffer.

@@ -92,6 +92,10 @@ void dev_free(T*& p)
     p = nullptr;
 }
 
+// Heavy-pair caps: keys per map and phase, value-table slots, replayed buckets
+// (bucket_count = summed bucket sizes / 5 <= 224 k-mers x KMERCUTOFF / 5).
+constexpr PeCaps PE_HEAVY{16384, 65536, 131072 + NBHD - 1 + 64, 4096, 4096, 0};
+
 int grow_chunk(fame_gpu* g, uint64_t n, uint64_t bytes, uint64_t cand)
 {
     int rc;
@@ -353,8 +357,12 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dp_warp, 128, 4 * DPW_BYTES) != cudaSuccess || nb < 1)
             return fail(set_err(g, FAME_ERR_CUDA, "k_dp_warp does not fit an SM"));
         g->dp_grid = (uint32_t)(g->sm_count * nb);
-        uint64_t off[28];
+        uint64_t off[28], hoff[28];
         g->pe_warp_bytes = pe_layout(PE_LIGHT, off);
+        pe_layout(PE_HEAVY, hoff);
+        // pe_kmers keeps its per-read arrays (8 * 256 + 96 bytes) in layout regions 11 .. 16
+        if (off[17] - off[11] < PE_KMER_AREA || hoff[17] - hoff[11] < PE_KMER_AREA)
+            return fail(set_err(g, FAME_ERR_CUDA, "paired layout: k-mer area too small"));
         const size_t pe_smem = 4 * g->pe_warp_bytes;
         if (cudaFuncSetAttribute(k_pe_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pe_smem) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pe_seed, 128, pe_smem) != cudaSuccess || nb < 1)
@@ -473,7 +481,7 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
             cnt->invalid_len += h[CTR_INV_LEN];
             cnt->invalid_n += h[CTR_INV_N];
             cnt->gather_bytes += h[CTR_GATHER_BYTES];
-            cnt->windows_scanned += ncand;
+            cnt->windows_scanned += h[CTR_CAND_USED];
             cnt->dp_reads += h[CTR_DP];
         }
         return FAME_OK;
@@ -519,9 +527,6 @@ extern "C" int fame_gpu_match_reads(fame_gpu* g, const char* seqs, const uint64_
 
 namespace {
 
-// Heavy-pair caps: keys per map and phase, value-table slots, replayed buckets
-// (bucket_count = summed bucket sizes / 5 <= 224 k-mers x KMERCUTOFF / 5).
-constexpr PeCaps PE_HEAVY{16384, 65536, 131072 + NBHD - 1 + 64, 4096, 4096, 0};
 constexpr uint32_t PE_HEAVY_WARPS = 128;
 
 // Mates of pair r are reads r and n + r of (d_seqs, d_offs); mats and invalid

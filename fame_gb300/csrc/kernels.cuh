@@ -472,6 +472,10 @@ __global__ void __launch_bounds__(32 * SA_WARPS) k_shiftand(DevIndex ix, ChunkBu
         bool ung = false;
         if (mine) {
             const uint32_t task = cb.cand_task[c];
+            mine = task != CAND_HOLE;
+        }
+        if (mine) {
+            const uint32_t task = cb.cand_task[c];
             const uint32_t r = task >> 1;
             o = task & 1;
             off0 = cb.offs[r];
@@ -968,6 +972,8 @@ struct LightLayout {
     static constexpr uint32_t STAGE = OVF + L_OVF * 4;
     static constexpr uint32_t END_B = STAGE + L_OPS * 4;
     static constexpr uint32_t BYTES = ((END_A > END_B ? END_A : END_B) + 15) / 16 * 16;
+    // the hash pass keeps its prefix array (8 bytes per read base + 1) in ops .. count
+    static_assert(END_A - OPS >= 8 * (FAME_MAX_READ_LEN + 1) && OPS % 8 == 0, "prefix array does not fit");
 };
 
 __device__ __forceinline__ SeedMem light_mem(uint8_t* base)
@@ -1000,18 +1006,20 @@ __global__ void __launch_bounds__(128, 8) k_seed(DevIndex ix, ChunkBufs cb, uint
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     const int norient = __popc(cb.orient_mask);
     const uint32_t first_o = (cb.orient_mask & 1u) ? 0 : 1;
+    CandRes res;
     for (uint32_t t = blockIdx.x * (blockDim.x >> 5) + wib; t < ntask; t += nwarps) {
         const uint32_t r = norient == 2 ? (t >> 1) : t;
         const uint32_t o = norient == 2 ? (t & 1) : first_o;
         if (cb.rflags[r]) continue;
         const uint32_t task = 2 * r + o;
-        const int heavy = seed_task(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES);
+        const int heavy = seed_task(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES, res);
         if (heavy && (threadIdx.x & 31) == 0) {
             const uint32_t h = (uint32_t)atomicAdd(cb.ctr + CTR_HEAVY, 1ull);
             cb.heavy[h] = task;
         }
         __syncwarp();
     }
+    cand_res_finish(cb, res);
 }
 
 // Heavy path: one warp per task with its working memory in global scratch.
@@ -1060,15 +1068,17 @@ __global__ void k_seed_heavy(DevIndex ix, ChunkBufs cb, HeavyScratch hs, uint32_
     if (w >= hs.nwarps) return;
     if (nheavy == FROM_DEVICE) nheavy = (uint32_t)cb.ctr[CTR_HEAVY];
     const SeedMem s = heavy_mem(hs, w);
+    CandRes res;
     for (uint32_t i = w; i < nheavy; i += hs.nwarps) {
         const uint32_t task = cb.heavy[i];
-        const int bad = seed_task(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES);
+        const int bad = seed_task(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES, res);
         if (bad && (threadIdx.x & 31) == 0) {
             atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull);
             cb.task_cand[task] = make_uint4(0, 0, 0, 0);
         }
         __syncwarp();
     }
+    cand_res_finish(cb, res);
 }
 
 // tab2[k] = {tab[k], first entry of bucket k or 0}, k <= n (the bucket-offset

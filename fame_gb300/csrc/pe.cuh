@@ -22,6 +22,7 @@
 // exceeds the shared-memory caps are handed to a launch with global scratch.
 #pragma once
 #include "kernels.cuh"
+#include "seedhash.h"
 
 namespace fame {
 
@@ -44,6 +45,7 @@ __device__ __forceinline__ uint32_t pv_c1(uint32_t v) { return v & 0xffu; }
 __device__ __forceinline__ uint32_t pv_c2(uint32_t v) { return (v >> 8) & 0xffu; }
 
 constexpr uint32_t PE_KMAX = FAME_MAX_READ_LEN - KMERLEN + 1;   // k-mers of the longest read
+constexpr uint64_t PE_KMER_AREA = 8 * 256 + 96;                  // pe_kmers' per-read arrays
 
 // Capacities of one warp's working memory.
 struct PeCaps {
@@ -223,26 +225,74 @@ __device__ __forceinline__ bool filtered_has(const PeIndex& px, uint64_t k)
 // rd; returns the summed bucket sizes (the maps' bucket_count * 5).
 __device__ uint32_t pe_kmers(const DevIndex& ix, const PeIndex& px, const PeMem& s, const uint8_t* rd, uint32_t len)
 {
+    constexpr uint32_t FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t nk = len - KMERLEN + 1;
     uint32_t sigma = 0;
-    for (uint32_t p = lane; p < nk; p += 32) {
-        uint64_t h = 0;
-        uint32_t cm = 0, kq = 0;
+    // per-read arrays in the replay area (dead until both mates' maps are
+    // built): the hash prefix P[0..len] of seedhash.h, a C bitmap (bit j of
+    // Cw: base j is C) and the filteredKmers codes, 16 per word (base j at
+    // bits 2(j mod 16) of Kw[j / 16])
+    uint64_t* P = (uint64_t*)s.seq;
+    uint32_t* Cw = (uint32_t*)(P + 256);
+    uint32_t* Kw = Cw + 8;
+    {
+        uint64_t carry = 0;
+        for (uint32_t b = 0; b <= len; b += 32) {
+            const uint32_t j = b + lane;
+            const uint8_t c = j < len ? rd[j] : (uint8_t)0;
+            const uint64_t u = j < len ? sh_u(c, j) : 0ull;
+            uint64_t inc = u;
 #pragma unroll
-        for (uint32_t i = 0; i < KMERLEN; ++i) {
-            const uint8_t c = rd[p + i];
-            if ((SEEDBITS >> (31 - i)) & 1u) h ^= rotl64(nt_val(c), 31 - i);
-            cm = (cm << 1) | (c == 'C' ? 1u : 0u);
-            kq = (kq << 2) + ((c == 'C' || c == 'T') ? 3u : (c == 'G' ? 2u : 0u));
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint64_t t = __shfl_up_sync(FULL, inc, d);
+                if (lane >= d) inc ^= t;
+            }
+            if (j <= len) P[j] = carry ^ inc ^ u;
+            carry ^= __shfl_sync(FULL, inc, 31);
+            const uint32_t cbits = __ballot_sync(FULL, c == 'C');
+            uint32_t kw = ((c == 'C' || c == 'T') ? 3u : (c == 'G' ? 2u : 0u)) << (2 * (lane & 15));
+#pragma unroll
+            for (int d = 1; d < 16; d <<= 1) kw |= __shfl_xor_sync(FULL, kw, d);
+            if (b < 256) {
+                if (lane == 0) Cw[b >> 5] = cbits;
+                if ((lane & 15) == 0) Kw[(b >> 4) + (lane >> 4)] = kw;
+            }
         }
-        const uint32_t key = (uint32_t)(h & HTAB_MASK);
-        const uint32_t b0 = __ldg((const uint32_t*)(ix.tab2 + key)), b1 = __ldg((const uint32_t*)(ix.tab2 + key + 1));
-        s.kst[p] = b0;
-        s.kln[p] = b1 - b0;
-        s.kcm[p] = cm;
-        s.kfl[p] = (p > 0 && filtered_has(px, kq)) ? 1 : 0;
-        sigma += b1 - b0;
+    }
+    __syncwarp();
+    // per k-mer: table index, bucket bounds (all loads of a lane issued before
+    // any is used), C mask (base p at bit 31) and the filteredKmers key (the
+    // 2-bit codes of bases p + 16 .. p + 31, the first at the top)
+    constexpr int KPL = (PE_KMAX + 31) / 32;
+    uint32_t b0[KPL], b1[KPL];
+#pragma unroll
+    for (int jj = 0; jj < KPL; ++jj) {
+        const uint32_t p = lane + 32 * jj;
+        if (p < nk) {
+            const uint32_t key = sh_prefix_hash([&](uint32_t j) { return P[j]; }, p, HTAB_MASK);
+            b0[jj] = __ldg((const uint32_t*)(ix.tab2 + key));
+            b1[jj] = __ldg((const uint32_t*)(ix.tab2 + key + 1));
+        }
+    }
+#pragma unroll
+    for (int jj = 0; jj < KPL; ++jj) {
+        const uint32_t p = lane + 32 * jj;
+        if (p < nk) {
+            const uint32_t w = p >> 5;
+            s.kcm[p] = __brev(__funnelshift_r(Cw[w], Cw[w + 1], p & 31));
+            uint8_t fl = 0;
+            if (p > 0 && px.n_filtered) {
+                const uint32_t bit = 2 * (p + 16);
+                const uint32_t y = __brev(__funnelshift_r(Kw[bit >> 5], Kw[(bit >> 5) + 1], bit & 31));
+                const uint32_t kq = ((y >> 1) & 0x55555555u) | ((y << 1) & 0xAAAAAAAAu);
+                fl = filtered_has(px, kq) ? 1 : 0;
+            }
+            s.kfl[p] = fl;
+            s.kst[p] = b0[jj];
+            s.kln[p] = b1[jj] - b0[jj];
+            sigma += b1[jj] - b0[jj];
+        }
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) sigma += __shfl_xor_sync(0xffffffffu, sigma, d);

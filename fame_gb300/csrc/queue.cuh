@@ -306,7 +306,7 @@ extern "C" int fame_queue_collect(fame_queue* q, int slot, uint64_t* mats, uint8
         cnt->invalid_len += h[CTR_INV_LEN];
         cnt->invalid_n += h[CTR_INV_N];
         cnt->gather_bytes += h[CTR_GATHER_BYTES];
-        cnt->windows_scanned += h[CTR_CAND];
+        cnt->windows_scanned += h[CTR_CAND_USED];
         cnt->dp_reads += h[CTR_DP];
     }
     return FAME_OK;

@@ -19,6 +19,7 @@
 //      windows with count >= QTHRESH in bucket order (forward map first)
 #pragma once
 #include "dev_common.cuh"
+#include "seedhash.h"
 
 namespace fame {
 
@@ -156,11 +157,37 @@ __device__ bool sim_step(MapSim& m, const SeedMem& s)
     return sim_rehash(m, s, next);
 }
 
+// A warp's reservation of candidate slots: tasks take contiguous runs from
+// it, so the candidate counter sees one atomic per CAND_RES_CHUNK slots
+// instead of one per task.  Slots a warp reserves and leaves unused are
+// marked CAND_HOLE (the window scans skip them).
+constexpr uint32_t CAND_RES_CHUNK = 8;
+struct CandRes {
+    uint32_t base = 0, left = 0;
+    uint32_t used = 0;   // slots filled since the last flush
+};
+
+__device__ __forceinline__ void cand_res_release(const ChunkBufs& cb, CandRes& res)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t j = lane; j < res.left; j += 32)
+        if ((uint64_t)res.base + j < cb.cand_cap) cb.cand_task[res.base + j] = CAND_HOLE;
+    res.left = 0;
+}
+
+// End of a warp's tasks: unused slots become holes, the filled count is added.
+__device__ __forceinline__ void cand_res_finish(const ChunkBufs& cb, CandRes& res)
+{
+    cand_res_release(cb, res);
+    if ((threadIdx.x & 31) == 0 && res.used) atomicAdd(cb.ctr + CTR_CAND_USED, (unsigned long long)res.used);
+    res.used = 0;
+}
+
 // Warp-cooperative seeding of one task.  Returns 0 on success, 1 when the task
 // does not fit the memory caps (the caller hands it to the heavy path).
 // All lanes of the warp must call it.
 __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem& s, uint32_t task,
-                         unsigned long long* gather_bytes_acc)
+                         unsigned long long* gather_bytes_acc, CandRes& res)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t r = task >> 1, o = task & 1;
@@ -175,17 +202,30 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
     __syncwarp();
     // 1. hashes and bucket bounds (getSeedRefs pass 1, ReadQueue.cpp:2331-2354):
     //    every lane first hashes its k-mers, then issues all of its bucket
-    //    reads before using any, so their DRAM latencies overlap
+    //    reads before using any, so their DRAM latencies overlap.  Hashes by
+    //    the prefix form of seedhash.h: P[j] (j <= len, 8 bytes each) in the
+    //    ops / count area, which is dead until the gather.
     const uint32_t nk = len - KMERLEN + 1;
     uint32_t sigma = 0;
     unsigned long long gb = 0;
-    for (uint32_t p = lane; p < nk; p += 32) {
-        uint64_t h = 0;
+    uint64_t* P = (uint64_t*)s.ops;
+    {
+        uint64_t carry = 0;   // P[b]
+        for (uint32_t b = 0; b <= len; b += 32) {
+            const uint32_t j = b + lane;
+            const uint64_t u = j < len ? sh_u(s.seq[j], j) : 0ull;
+            uint64_t inc = u;   // u[b] ^ ... ^ u[j]
 #pragma unroll
-        for (uint32_t i = 0; i < KMERLEN; ++i)
-            if ((SEEDBITS >> (31 - i)) & 1u) h ^= rotl64(nt_val(s.seq[p + i]), 31 - i);
-        s.kst[p] = (uint32_t)(h & HTAB_MASK);
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint64_t t = __shfl_up_sync(0xffffffffu, inc, d);
+                if (lane >= (uint32_t)d) inc ^= t;
+            }
+            if (j <= len) P[j] = carry ^ inc ^ u;
+            carry ^= __shfl_sync(0xffffffffu, inc, 31);
+        }
     }
+    __syncwarp();
+    for (uint32_t p = lane; p < nk; p += 32) s.kst[p] = sh_prefix_hash([&](uint32_t j) { return P[j]; }, p, HTAB_MASK);
     constexpr int KPL = (FAME_MAX_READ_LEN - KMERLEN + 1 + 31) / 32;   // k-mers per lane, at most
     uint32_t e0[KPL];                                                    // first entry of each bucket
     {
@@ -396,11 +436,22 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
         if (dir == 1) nf = nstage;
     }
     if (fail) return 1;
-    // 6. publish the candidates
+    // 6. publish the candidates, contiguous, from the warp's reservation
     uint32_t base = 0;
-    if (lane == 0 && nstage) base = (uint32_t)atomicAdd(cb.ctr + CTR_CAND, (unsigned long long)nstage);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base + nstage <= cb.cand_cap) {
+    if (nstage) {
+        if (nstage > res.left) {
+            cand_res_release(cb, res);
+            const uint32_t want = max(nstage, CAND_RES_CHUNK);
+            if (lane == 0) res.base = (uint32_t)atomicAdd(cb.ctr + CTR_CAND, (unsigned long long)want);
+            res.base = __shfl_sync(0xffffffffu, res.base, 0);
+            res.left = want;
+        }
+        base = res.base;
+        res.base += nstage;
+        res.left -= nstage;
+        res.used += nstage;
+    }
+    if ((uint64_t)base + nstage <= cb.cand_cap) {
         for (uint32_t j = lane; j < nstage; j += 32) {
             cb.cand[base + j] = s.stage[j];
             cb.cand_task[base + j] = task;
