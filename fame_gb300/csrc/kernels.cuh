@@ -1193,6 +1193,24 @@ __global__ void k_dp_warp(DevIndex ix, ChunkBufs cb)
         const char* raw = cb.seqs + off0;
         const int n = (int)size;
         const int64_t gb0 = (int64_t)metaPos + offset;
+        // the read's CpG range [minIndex, maxIndex] of the window (the loop of
+        // ReadQueue.cpp:3651-3664 over its CpGs, which are in position order):
+        // counts over the window's CpGs, split over the group's lanes
+        uint32_t nlt = 0, nle = 0;
+        if (have) {
+            const uint32_t minPos = (uint32_t)(metaPos + offset - (size - 1)), maxPos = metaPos + offset;
+            for (uint32_t id = sind + (uint32_t)k; id <= eind; id += 9) {
+                const uint32_t cp = __ldg(ix.cpg_pos + id) + RL - 2;
+                nlt += cp < minPos ? 1u : 0u;
+                nle += cp <= maxPos ? 1u : 0u;
+            }
+        }
+        uint32_t cnt_lt = 0, cnt_le = 0;
+#pragma unroll
+        for (int kk = 0; kk < 9; ++kk) {
+            cnt_lt += __shfl_sync(0xffffffffu, nlt, 9 * (in_grp ? grp : 0) + kk);
+            cnt_le += __shfl_sync(0xffffffffu, nle, 9 * (in_grp ? grp : 0) + kk);
+        }
         if (have) {
             // row i (1..n) compares rowm[i - 1]; reference columns j in [-2, n + 10]
             for (int q = k; q < n; q += 9)
@@ -1289,14 +1307,7 @@ __global__ void k_dp_warp(DevIndex ix, ChunkBufs cb)
             if (bad) {
                 atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull);
             } else {
-                const uint32_t minPos = (uint32_t)(metaPos + offset - (size - 1));
-                const uint32_t maxPos = metaPos + offset;
-                int32_t minIndex = (int32_t)sind, maxIndex = (int32_t)eind;
-                for (int32_t id = (int32_t)sind; (uint32_t)id <= eind; ++id) {
-                    const uint32_t pos = ix.cpg_pos[id];
-                    if (pos + RL - 2 < minPos) ++minIndex;
-                    else if (pos + RL - 2 > maxPos) { maxIndex = id - 1; break; }
-                }
+                const int32_t minIndex = (int32_t)(sind + cnt_lt), maxIndex = (int32_t)(sind + cnt_le) - 1;
                 uint32_t refSeqPos = metaPos + offset;
                 int32_t readSeqPos = (int32_t)size - 1;
                 int32_t alignPos = (int32_t)alen - 1;

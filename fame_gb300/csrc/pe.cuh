@@ -46,6 +46,7 @@ __device__ __forceinline__ uint32_t pv_c2(uint32_t v) { return (v >> 8) & 0xffu;
 
 constexpr uint32_t PE_KMAX = FAME_MAX_READ_LEN - KMERLEN + 1;   // k-mers of the longest read
 constexpr uint64_t PE_KMER_AREA = 8 * 256 + 96;                  // pe_kmers' per-read arrays
+constexpr uint32_t PE_CSET = 512;                                // second-mate candidate key set (in the same area)
 
 // Capacities of one warp's working memory.
 struct PeCaps {
@@ -580,18 +581,53 @@ __device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint
     const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
     pe_survivors(s, nk);
     if (phase == 2) {
+        // An op may insert its absent key only with a map key within ctx windows
+        // (bit 1 of sv: one among the keys kept from the first mate).  Without
+        // one, it can still get one from an earlier second-mate insert, so the
+        // order matters exactly when another absent key of an op that may
+        // insert lies within ctx windows of it: then the lane-0 path runs.
+        // Absent keys of such ops go to a set in the k-mer area (dead between
+        // pe_kmers and the replay).
         const int ctx = (int)px.ctx;
-        bool dyn = false;
+        if (2 * sigma > PE_CSET) return 0;
+        uint32_t* cset = s.seq;
+        for (uint32_t i = lane; i < PE_CSET; i += 32) cset[i] = EMPTY_KEY;
+        __syncwarp();
         for (uint32_t i = lane; i < sigma; i += 32) {
             if (!s.sv[i]) continue;
             const uint32_t p = s.gk[i];
             if (!(p == 0 || p - 1 < maxQPos)) continue;
             const uint32_t e = s.ge[i];
+            const int dir = (int)(e >> 31);
+            const uint32_t id = e & 0x7fffffffu;
             bool ok = false;
-            for (int c = -ctx; c <= ctx && !ok; ++c) ok = pm_find(s, (int)(e >> 31), (e & 0x7fffffffu) + (uint32_t)c) >= 0;
-            dyn |= !ok;
+            for (int c = -ctx; c <= ctx && !ok; ++c) ok = pm_find(s, dir, id + (uint32_t)c) >= 0;
+            if (ok) s.sv[i] |= 2;
+            if (pm_find(s, dir, id) < 0) {
+                for (uint32_t h = (e * 0x9E3779B1u) >> 23;; h = (h + 1) & (PE_CSET - 1)) {
+                    const uint32_t old = atomicCAS(&cset[h], EMPTY_KEY, e);
+                    if (old == EMPTY_KEY || old == e) break;
+                }
+            }
         }
-        if (__any_sync(0xffffffffu, dyn)) return 0;
+        __syncwarp();
+        bool amb = false;
+        for (uint32_t i = lane; i < sigma && !amb; i += 32) {
+            if (!(s.sv[i] & 1) || (s.sv[i] & 2)) continue;
+            const uint32_t p = s.gk[i];
+            if (!(p == 0 || p - 1 < maxQPos)) continue;
+            const uint32_t e = s.ge[i];
+            for (int c = -ctx; c <= ctx && !amb; ++c) {
+                if (c == 0) continue;
+                const uint32_t f = e + (uint32_t)c;   // same strand bit: window ids stay below 2^31 - ctx
+                for (uint32_t h = (f * 0x9E3779B1u) >> 23;; h = (h + 1) & (PE_CSET - 1)) {
+                    const uint32_t k = cset[h];
+                    if (k == f) { amb = true; break; }
+                    if (k == EMPTY_KEY) break;
+                }
+            }
+        }
+        if (__any_sync(0xffffffffu, amb)) return 0;
     }
     uint32_t nkeys[2] = {__shfl_sync(0xffffffffu, st.nkeys[0], 0), __shfl_sync(0xffffffffu, st.nkeys[1], 0)};
     uint32_t nins[2] = {0, 0};
@@ -606,7 +642,7 @@ __device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint
         const int dir = (int)(e >> 31);
         const uint32_t id = e & 0x7fffffffu;
         const uint32_t p = live ? s.gk[i] : 0u;
-        const bool may = live && (p == 0 || p - 1 < maxQPos);
+        const bool may = live && (p == 0 || p - 1 < maxQPos) && (phase == 1 || (s.sv[i] & 2));
         const unsigned vm = __ballot_sync(0xffffffffu, live);
         const unsigned grp = __match_any_sync(0xffffffffu, live ? e : EMPTY_KEY) & vm;
         const bool leader = live && (__ffs(grp) - 1) == lane;
