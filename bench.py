@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 METRIC = "aligned reads/s (single-end matching stage, bit-exact CpG report)"
 # DRAM bytes (read + write) of one steady-state k_seed launch of se100_300mbp, from
 # ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:'k_seed$' -s 2 -c 1
-SEED_TRAFFIC_PER_LAUNCH = 3.17e9 + 20.89e6
+SEED_TRAFFIC_PER_LAUNCH = 3.173e9 + 21.32e6
 
 
 def parse():

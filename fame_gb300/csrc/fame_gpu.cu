@@ -1,11 +1,17 @@
 // C ABI implementation: index upload, per-chunk matching pipeline, tallies.
 #include <cuda_runtime.h>
 
+#include <sys/mman.h>
+#include <sys/syscall.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/fame_gpu.h"
@@ -17,6 +23,8 @@ using namespace fame;
 struct fame_gpu {
     int device = 0;
     cudaStream_t stream = nullptr;
+    std::mutex host_mu;
+    std::unordered_map<void*, size_t> host_mapped;   // page-locked blocks placed by host_alloc_near
     std::string err;
     DevIndex ix{};
     std::vector<void*> index_allocs;
@@ -95,6 +103,59 @@ void dev_free(T*& p)
 // Heavy-pair caps: keys per map and phase, value-table slots, replayed buckets
 // (bucket_count = summed bucket sizes / 5 <= 224 k-mers x KMERCUTOFF / 5).
 constexpr PeCaps PE_HEAVY{16384, 65536, 131072 + NBHD - 1 + 64, 4096, 4096, 0};
+
+// Page-locked host memory on the host NUMA node nearest the device (anonymous
+// pages bound there with mbind, touched, then registered with CUDA), so
+// host-device copies do not cross to another socket's memory; cudaMallocHost
+// when the node is unknown or the placement is refused.
+void* host_alloc_near(fame_gpu* g, size_t bytes)
+{
+    bytes = std::max<size_t>(bytes, 16);
+    int node = -1;
+    if (cudaDeviceGetAttribute(&node, cudaDevAttrHostNumaId, g->device) != cudaSuccess) node = -1;
+    if (node >= 0 && node < 64) {
+        const size_t pg = (size_t)sysconf(_SC_PAGESIZE);
+        const size_t len = (bytes + pg - 1) / pg * pg;
+        void* m = mmap(nullptr, len, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+        if (m != MAP_FAILED) {
+            unsigned long mask = 1ul << node;
+            const long MPOL_PREFERRED_ = 1;
+            if (syscall(SYS_mbind, m, len, MPOL_PREFERRED_, &mask, 65ul, 0u) == 0) {
+                std::memset(m, 0, len);
+                if (cudaHostRegister(m, len, cudaHostRegisterDefault) == cudaSuccess) {
+                    std::lock_guard<std::mutex> lk(g->host_mu);
+                    g->host_mapped[m] = len;
+                    return m;
+                }
+                cudaGetLastError();
+            }
+            munmap(m, len);
+        }
+    }
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void host_free_near(fame_gpu* g, void* p)
+{
+    if (!p) return;
+    size_t len = 0;
+    {
+        std::lock_guard<std::mutex> lk(g->host_mu);
+        auto it = g->host_mapped.find(p);
+        if (it != g->host_mapped.end()) {
+            len = it->second;
+            g->host_mapped.erase(it);
+        }
+    }
+    if (len) {
+        cudaHostUnregister(p);
+        munmap(p, len);
+    } else {
+        cudaFreeHost(p);
+    }
+}
 
 int grow_chunk(fame_gpu* g, uint64_t n, uint64_t bytes, uint64_t cand)
 {
@@ -735,14 +796,16 @@ extern "C" int fame_gpu_memcpy(fame_gpu* g, void* dst, const void* src, size_t b
 extern "C" int fame_gpu_host_alloc(fame_gpu* g, size_t bytes, void** p)
 {
     if (!g || !p) return FAME_ERR_ARG;
-    CK(cudaMallocHost(p, std::max<size_t>(bytes, 16)));
+    CK(cudaSetDevice(g->device));
+    *p = host_alloc_near(g, bytes);
+    if (!*p) return set_err(g, FAME_ERR_NOMEM, "page-locked host allocation");
     return FAME_OK;
 }
 
 extern "C" int fame_gpu_host_free(fame_gpu* g, void* p)
 {
     if (!g) return FAME_ERR_ARG;
-    if (p) CK(cudaFreeHost(p));
+    host_free_near(g, p);
     return FAME_OK;
 }
 

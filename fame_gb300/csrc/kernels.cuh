@@ -1,6 +1,8 @@
 // Matching kernels after seeding: Shift-And window scans, candidate
 // selection with the exact-match CpG calls, and the banded DP CpG calls.
 #pragma once
+#include <type_traits>
+
 #include "editscan.h"
 #include "qgram.h"
 #include "seed.cuh"
@@ -267,8 +269,9 @@ __device__ int qgram_spans_warp(const DevIndex& ix, const char* raw, uint32_t m,
     for (int k = 0; k < QG_PIECES; ++k) ckey[k] = __shfl_sync(FULL, key, k);
     const uint32_t qmask = q >= 16 ? 0xffffffffu : ((1u << (2 * q)) - 1);
     const uint32_t nq = (1u << q) - 1;
-    // ---- the key table: lane s tests bit offset s
-    bool good = lane + 5 <= 2 * q;
+    // ---- the key table: lane s tests bit offset s (s >= 2: the lookup below
+    // takes the slot's byte offset straight from the text bits)
+    bool good = lane >= 2 && lane + 5 <= 2 * q;
 #pragma unroll
     for (int a = 0; a < QG_PIECES; ++a)
 #pragma unroll
@@ -313,11 +316,13 @@ __device__ int qgram_spans_warp(const DevIndex& ix, const char* raw, uint32_t m,
         const uint64_t sS = (((uint64_t)cur << 32) | prevS) >> (2 * (17 - q));
         bool anyh = false;
         if (ts >= 0) {
-            const uint64_t sF = sS >> ts;
+            // bits 2..6 of (sS >> (ts - 2 + 2i)) are position i's key field; the
+            // table sits at a 128-byte boundary, so field * 4 | tb is its slot
+            const uint64_t sF = sS >> (ts - 2);
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
                 const uint32_t k2 = (uint32_t)(sS >> (2 * i)) & qmask;
-                const uint32_t off = (((uint32_t)(sF >> (2 * i)) & 31u) << 2) + tb;
+                const uint32_t off = ((uint32_t)(sF >> (2 * i)) & 0x7cu) | tb;
                 uint32_t t;
                 asm volatile("ld.shared.u32 %0, [%1];" : "=r"(t) : "r"(off));
                 anyh |= t == k2;
@@ -443,14 +448,16 @@ struct PieceKeys {
 // automaton over the spans of one candidate.  hits / hit_n as scan_window.
 constexpr int SA_WARPS = 4;
 constexpr int SA_POOL = 256;   // merged spans per warp for its 32 candidates
-struct SaWarp {
+struct __align__(128) SaWarp {
+    uint32_t tab[32];          // key table of the window being filtered (128-byte aligned)
+    uint32_t tabp[32];
     uint32_t pool[SA_POOL];
     int32_t rlo[32], rhi[32];
     uint32_t rn;
     int16_t nsp[32];           // merged spans of each candidate, -1: scan the whole window
     uint16_t off[32];          // first pool entry of each candidate
-    uint32_t tab[32], tabp[32]; // key table of the window being filtered
 };
+static_assert(sizeof(SaWarp) % 128 == 0, "key tables of the warps must stay 128-byte aligned");
 
 template <int W>
 __global__ void __launch_bounds__(32 * SA_WARPS) k_shiftand(DevIndex ix, ChunkBufs cb, uint32_t ncand)
@@ -1229,43 +1236,52 @@ __global__ void k_dp_warp(DevIndex ix, ChunkBufs cb)
         int cur1 = 0xffff, cur2 = 0xffff;   // own values of steps t - 1 and t - 2
         uint32_t acc = 0;
         const int t_end = 2 * nmax + (int)DPB;
-        for (int t = 0; t <= t_end; t += 2) {
-#pragma unroll
-            for (int par = 0; par < 2; ++par) {
-                const int tt = t + par;
-                const int o = par ? o_odd : o_even;
-                // up input (row - 1, o + 1) and left input (row, o - 1) are step t - 1
-                // values: the own lane's and a neighbour's
-                const int nb = par ? __shfl_down_sync(0xffffffffu, cur1, 1) : __shfl_up_sync(0xffffffffu, cur1, 1);
-                const int v_up = par ? nb : cur1;
-                const int v_lf = par ? cur1 : nb;
-                const int row = (tt - o) >> 1;
-                const int j = row + o;
-                int val = 0xffff;
-                uint32_t code = 0;
-                if ((par ? act_odd : act_even) && row >= 0 && row <= n) {
-                    if (row == 0) {
-                        if (o >= 0) val = o;                                 // first row: 0..8
-                    } else if (j == 0) {
-                        val = row;                                           // first column, rows 1..8
-                    } else if (j > 0) {
-                        const int up = (o == (int)DPB) ? 65535 - (row - 1) - (int)DPB - 1 : v_up;
-                        const int lf = (o == -(int)DPB) ? (row == (int)DPB + 1 ? 65535 - 2 * (int)DPB - 1 : 65535 - row)
-                                                        : v_lf;
-                        const int mm = (rowm[row - 1] & refb[j + DPW_REF0]) ? 0 : 1;
-                        const int dg = cur2 + mm;
-                        int v = min(up + 1, lf + 1);
-                        v = min(v, dg);
-                        val = v & 0xffff;
-                        code = up < lf ? (up + 1 < dg ? 2u : (uint32_t)mm) : (lf + 1 < dg ? 3u : (uint32_t)mm);
-                        if (row == n) rown[o + DPB] = (uint16_t)val;
-                    }
+        // one anti-diagonal step; from step 10 on every cell is interior (row >= 1,
+        // column >= 1) and the first-row / first-column cases drop out
+        auto step = [&](const int tt, const int par, auto interior) {
+            const int o = par ? o_odd : o_even;
+            // up input (row - 1, o + 1) and left input (row, o - 1) are step t - 1
+            // values: the own lane's and a neighbour's
+            const int nb = par ? __shfl_down_sync(0xffffffffu, cur1, 1) : __shfl_up_sync(0xffffffffu, cur1, 1);
+            const int v_up = par ? nb : cur1;
+            const int v_lf = par ? cur1 : nb;
+            const int row = (tt - o) >> 1;
+            const int j = row + o;
+            int val = 0xffff;
+            uint32_t code = 0;
+            const bool act = par ? act_odd : act_even;
+            if (decltype(interior)::value ? (act && row <= n) : (act && row >= 0 && row <= n)) {
+                if (!decltype(interior)::value && row == 0) {
+                    if (o >= 0) val = o;                                     // first row: 0..8
+                } else if (!decltype(interior)::value && j == 0) {
+                    val = row;                                               // first column, rows 1..8
+                } else if (decltype(interior)::value || j > 0) {
+                    const int up = (o == (int)DPB) ? 65535 - (row - 1) - (int)DPB - 1 : v_up;
+                    const int lf = (o == -(int)DPB) ? (row == (int)DPB + 1 ? 65535 - 2 * (int)DPB - 1 : 65535 - row)
+                                                    : v_lf;
+                    const int mm = (rowm[row - 1] & refb[j + DPW_REF0]) ? 0 : 1;
+                    const int dg = cur2 + mm;
+                    int v = min(up + 1, lf + 1);
+                    v = min(v, dg);
+                    val = v & 0xffff;
+                    code = up < lf ? (up + 1 < dg ? 2u : (uint32_t)mm) : (lf + 1 < dg ? 3u : (uint32_t)mm);
+                    if (row == n) rown[o + DPB] = (uint16_t)val;
                 }
-                acc = __funnelshift_r(acc, code, 2);
-                if ((tt & 15) == 15) codes[(tt >> 4) * 32 + lane] = acc;
-                cur2 = cur1;
-                cur1 = val;
             }
+            acc = __funnelshift_r(acc, code, 2);
+            if ((tt & 15) == 15) codes[(tt >> 4) * 32 + lane] = acc;
+            cur2 = cur1;
+            cur1 = val;
+        };
+        static_assert(DPB + 2 <= 10, "every cell is interior from step DPB + 2 on");
+        int t = 0;
+        for (; t < 10 && t <= t_end; t += 2) {
+            step(t, 0, std::false_type{});
+            step(t + 1, 1, std::false_type{});
+        }
+        for (; t <= t_end; t += 2) {
+            step(t, 0, std::true_type{});
+            step(t + 1, 1, std::true_type{});
         }
         {
             const int last = t_end + 1;                  // the last step written into acc

@@ -74,17 +74,17 @@ struct fame_queue {
 
 namespace {
 
-void qslot_free(QSlot& s)
+void qslot_free(fame_gpu* g, QSlot& s)
 {
     for (auto& gr : s.graphs) cudaGraphExecDestroy(gr.exec);
     s.graphs.clear();
     dev_free(s.d_seqs); dev_free(s.d_offs); dev_free(s.d_rflags); dev_free(s.d_task_cand); dev_free(s.d_cand);
     dev_free(s.d_cand_task); dev_free(s.d_hits); dev_free(s.d_hit_n); dev_free(s.d_mats); dev_free(s.d_invalid);
     dev_free(s.d_dp_list); dev_free(s.d_dp_mat); dev_free(s.d_dp_orient); dev_free(s.d_heavy); dev_free(s.d_ctr);
-    if (s.h_seqs) cudaFreeHost(s.h_seqs);
-    if (s.h_offs) cudaFreeHost(s.h_offs);
-    if (s.h_mats) cudaFreeHost(s.h_mats);
-    if (s.h_invalid) cudaFreeHost(s.h_invalid);
+    host_free_near(g, s.h_seqs);
+    host_free_near(g, s.h_offs);
+    host_free_near(g, s.h_mats);
+    host_free_near(g, s.h_invalid);
     if (s.h_ctr) cudaFreeHost(s.h_ctr);
     s.h_seqs = nullptr; s.h_offs = nullptr; s.h_mats = nullptr; s.h_invalid = nullptr; s.h_ctr = nullptr;
     if (s.done) cudaEventDestroy(s.done);
@@ -192,7 +192,7 @@ extern "C" int fame_queue_open(fame_gpu* g, uint32_t nslots, uint32_t max_reads,
     const uint64_t cand = 2ull * max_reads * 4 + 4096;
     const uint32_t hw = std::max(1u, g->hs.nwarps / nslots);
     auto fail = [&](int rc) {
-        for (auto& s : q->slots) qslot_free(s);
+        for (auto& s : q->slots) qslot_free(g, s);
         delete q;
         return rc;
     };
@@ -211,10 +211,11 @@ extern "C" int fame_queue_open(fame_gpu* g, uint32_t nslots, uint32_t max_reads,
             (rc = dev_alloc(g, &s.d_dp_orient, max_reads)) || (rc = dev_alloc(g, &s.d_heavy, 2ull * max_reads)) ||
             (rc = dev_alloc(g, &s.d_ctr, CTR_N)))
             return fail(rc);
-        if (cudaMallocHost((void**)&s.h_seqs, max_bytes) != cudaSuccess ||
-            cudaMallocHost((void**)&s.h_offs, (max_reads + 1ull) * 8) != cudaSuccess ||
-            cudaMallocHost((void**)&s.h_mats, max_reads * 8ull) != cudaSuccess ||
-            cudaMallocHost((void**)&s.h_invalid, max_reads) != cudaSuccess ||
+        s.h_seqs = (char*)host_alloc_near(g, max_bytes);
+        s.h_offs = (uint64_t*)host_alloc_near(g, (max_reads + 1ull) * 8);
+        s.h_mats = (uint64_t*)host_alloc_near(g, max_reads * 8ull);
+        s.h_invalid = (uint8_t*)host_alloc_near(g, max_reads);
+        if (!s.h_seqs || !s.h_offs || !s.h_mats || !s.h_invalid ||
             cudaMallocHost((void**)&s.h_ctr, CTR_N * sizeof(unsigned long long)) != cudaSuccess)
             return fail(set_err(g, FAME_ERR_NOMEM, "queue page-locked staging"));
         s.cap_cand = cand;
@@ -320,7 +321,7 @@ extern "C" int fame_queue_close(fame_queue* q)
     cudaSetDevice(q->g->device);
     for (auto& s : q->slots) {
         if (s.stream) cudaStreamSynchronize(s.stream);
-        qslot_free(s);
+        qslot_free(q->g, s);
     }
     q->g->queue = nullptr;
     delete q;
