@@ -46,7 +46,6 @@ __device__ __forceinline__ uint32_t pv_c2(uint32_t v) { return (v >> 8) & 0xffu;
 
 constexpr uint32_t PE_KMAX = FAME_MAX_READ_LEN - KMERLEN + 1;   // k-mers of the longest read
 constexpr uint64_t PE_KMER_AREA = 8 * 256 + 96;                  // pe_kmers' per-read arrays
-constexpr uint32_t PE_CSET = 512;                                // second-mate candidate key set (in the same area)
 
 // Capacities of one warp's working memory.
 struct PeCaps {
@@ -580,55 +579,6 @@ __device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint
     const uint32_t nk = len - KMERLEN + 1;
     const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
     pe_survivors(s, nk);
-    if (phase == 2) {
-        // An op may insert its absent key only with a map key within ctx windows
-        // (bit 1 of sv: one among the keys kept from the first mate).  Without
-        // one, it can still get one from an earlier second-mate insert, so the
-        // order matters exactly when another absent key of an op that may
-        // insert lies within ctx windows of it: then the lane-0 path runs.
-        // Absent keys of such ops go to a set in the k-mer area (dead between
-        // pe_kmers and the replay).
-        const int ctx = (int)px.ctx;
-        if (2 * sigma > PE_CSET) return 0;
-        uint32_t* cset = s.seq;
-        for (uint32_t i = lane; i < PE_CSET; i += 32) cset[i] = EMPTY_KEY;
-        __syncwarp();
-        for (uint32_t i = lane; i < sigma; i += 32) {
-            if (!s.sv[i]) continue;
-            const uint32_t p = s.gk[i];
-            if (!(p == 0 || p - 1 < maxQPos)) continue;
-            const uint32_t e = s.ge[i];
-            const int dir = (int)(e >> 31);
-            const uint32_t id = e & 0x7fffffffu;
-            bool ok = false;
-            for (int c = -ctx; c <= ctx && !ok; ++c) ok = pm_find(s, dir, id + (uint32_t)c) >= 0;
-            if (ok) s.sv[i] |= 2;
-            if (pm_find(s, dir, id) < 0) {
-                for (uint32_t h = (e * 0x9E3779B1u) >> 23;; h = (h + 1) & (PE_CSET - 1)) {
-                    const uint32_t old = atomicCAS(&cset[h], EMPTY_KEY, e);
-                    if (old == EMPTY_KEY || old == e) break;
-                }
-            }
-        }
-        __syncwarp();
-        bool amb = false;
-        for (uint32_t i = lane; i < sigma && !amb; i += 32) {
-            if (!(s.sv[i] & 1) || (s.sv[i] & 2)) continue;
-            const uint32_t p = s.gk[i];
-            if (!(p == 0 || p - 1 < maxQPos)) continue;
-            const uint32_t e = s.ge[i];
-            for (int c = -ctx; c <= ctx && !amb; ++c) {
-                if (c == 0) continue;
-                const uint32_t f = e + (uint32_t)c;   // same strand bit: window ids stay below 2^31 - ctx
-                for (uint32_t h = (f * 0x9E3779B1u) >> 23;; h = (h + 1) & (PE_CSET - 1)) {
-                    const uint32_t k = cset[h];
-                    if (k == f) { amb = true; break; }
-                    if (k == EMPTY_KEY) break;
-                }
-            }
-        }
-        if (__any_sync(0xffffffffu, amb)) return 0;
-    }
     uint32_t nkeys[2] = {__shfl_sync(0xffffffffu, st.nkeys[0], 0), __shfl_sync(0xffffffffu, st.nkeys[1], 0)};
     uint32_t nins[2] = {0, 0};
     uint32_t* ins[2] = {phase == 1 ? s.ins1[0] : s.ins2[0], phase == 1 ? s.ins1[1] : s.ins2[1]};
@@ -642,7 +592,7 @@ __device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint
         const int dir = (int)(e >> 31);
         const uint32_t id = e & 0x7fffffffu;
         const uint32_t p = live ? s.gk[i] : 0u;
-        const bool may = live && (p == 0 || p - 1 < maxQPos) && (phase == 1 || (s.sv[i] & 2));
+        const bool may = live && (p == 0 || p - 1 < maxQPos);
         const unsigned vm = __ballot_sync(0xffffffffu, live);
         const unsigned grp = __match_any_sync(0xffffffffu, live ? e : EMPTY_KEY) & vm;
         const bool leader = live && (__ffs(grp) - 1) == lane;
@@ -694,6 +644,163 @@ __device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint
         st.nkeys[d] = nkeys[d];
         if (phase == 1) st.n1[d] = nins[d];
         else st.n2[d] = nins[d];
+    }
+    return 1;
+}
+
+// Lane-parallel counting of the second mate, exact for any op order
+// (getSeedRefsSecondRead).  An op may insert its absent key K when its k-mer
+// index allows it (p == 0 or p - 1 < maxQPos) and a key within ctx windows is
+// in the map at that moment: one kept from the first mate, or one the second
+// mate inserted at an earlier op.  So the op at which K is inserted is the
+// least solution of
+//     at(K) = min { i : op i has key K and may insert, and K has a kept key
+//                   within ctx windows or some K' within ctx has at(K') < i },
+// found by atomicMin passes over the ops until none changes (the chains of
+// keys that give each other context are short).  K then counts its ops from
+// at(K) on, a kept key all of its ops, and the inserted keys enter ins2 in
+// the order of at().  at[] lives in the k-mer area (dead between pe_kmers and
+// the replay), one word per value-table slot.  Returns 1, or -1 when a
+// capacity is exceeded.
+__device__ __forceinline__ int pm_slot(const PeMem& s, int dir, uint32_t key)
+{
+    const uint32_t mask = s.c.vcap - 1;
+    for (uint32_t h = vt_hash(key, mask);; h = (h + 1) & mask) {
+        const uint32_t k = s.vk[dir][h];
+        if (k == key) return (int)h;
+        if (k == EMPTY_KEY) return -1;
+    }
+}
+
+__device__ int pe_count_par2(const PeIndex& px, const PeMem& s, PeState& st, uint32_t len, uint32_t sigma)
+{
+    constexpr uint32_t FULL = 0xffffffffu, INF = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t nk = len - KMERLEN + 1;
+    const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
+    const int ctx = (int)px.ctx;
+    const uint32_t mask = s.c.vcap - 1;
+    pe_survivors(s, nk);
+    uint32_t* at[2] = {s.seq, s.seq + s.c.vcap};
+    for (uint32_t h = lane; h < s.c.vcap; h += 32) at[0][h] = at[1][h] = INF;
+    uint32_t nkeys[2] = {__shfl_sync(FULL, st.nkeys[0], 0), __shfl_sync(FULL, st.nkeys[1], 0)};
+    __syncwarp();
+    // A: table slots for the keys of ops that may insert; an absent key with a
+    //    kept key within ctx windows is inserted by its first such op
+    for (uint32_t base = 0; base < sigma; base += 32) {
+        if (4 * (nkeys[0] + 32) > 3 * s.c.vcap || 4 * (nkeys[1] + 32) > 3 * s.c.vcap) return -1;
+        const uint32_t i = base + lane;
+        const bool live = i < sigma && (s.sv[i] & 1);
+        const uint32_t p = live ? s.gk[i] : 0u;
+        const bool may = live && (p == 0 || p - 1 < maxQPos);
+        const uint32_t e = may ? s.ge[i] : 0u;
+        const int dir = (int)(e >> 31);
+        const uint32_t id = e & 0x7fffffffu;
+        bool added = false;
+        if (may) {
+            uint32_t h = vt_hash(id, mask);
+            for (;; h = (h + 1) & mask) {
+                const uint32_t k = s.vk[dir][h];
+                if (k == id) break;
+                if (k == EMPTY_KEY) {
+                    const uint32_t old = atomicCAS(&s.vk[dir][h], EMPTY_KEY, id);
+                    if (old == EMPTY_KEY) { added = true; break; }
+                    if (old == id) break;
+                }
+            }
+            if (!(s.vv[dir][h] & PV_PRESENT)) {
+                bool kept = false;
+                for (int c = -ctx; c <= ctx && !kept; ++c)
+                    if (c != 0) kept = pm_find(s, dir, id + (uint32_t)c) >= 0;
+                if (kept) atomicMin(&at[dir][h], i);
+            }
+        }
+        for (int d = 0; d < 2; ++d) nkeys[d] += __popc(__ballot_sync(FULL, added && dir == d));
+        __syncwarp();
+    }
+    // B: context from keys the second mate inserts earlier, to the fixed point
+    // (without one after 64 passes the pair goes to the per-pair path)
+    bool settled = false;
+    for (int round = 0; round < 64 && !settled; ++round) {
+        bool changed = false;
+        for (uint32_t i = lane; i < sigma; i += 32) {
+            if (!(s.sv[i] & 1)) continue;
+            const uint32_t p = s.gk[i];
+            if (!(p == 0 || p - 1 < maxQPos)) continue;
+            const uint32_t e = s.ge[i];
+            const int dir = (int)(e >> 31);
+            const uint32_t id = e & 0x7fffffffu;
+            const int h = pm_slot(s, dir, id);
+            if (h < 0 || (s.vv[dir][h] & PV_PRESENT) || at[dir][h] <= i) continue;
+            for (int c = -ctx; c <= ctx; ++c) {
+                if (c == 0) continue;
+                const int h2 = pm_slot(s, dir, id + (uint32_t)c);
+                if (h2 >= 0 && at[dir][h2] < i) {
+                    if (atomicMin(&at[dir][h], i) > i) changed = true;
+                    break;
+                }
+            }
+        }
+        __syncwarp();
+        settled = !__any_sync(FULL, changed);
+    }
+    if (!settled) return -1;
+    // C: counts (raw, folded below), then the inserts in op order
+    for (uint32_t i = lane; i < sigma; i += 32) {
+        if (!(s.sv[i] & 1)) continue;
+        const uint32_t e = s.ge[i];
+        const int dir = (int)(e >> 31);
+        const int h = pm_slot(s, dir, e & 0x7fffffffu);
+        if (h < 0) continue;
+        if ((s.vv[dir][h] & PV_PRESENT) || at[dir][h] <= i) atomicAdd(&s.vv[dir][h], 1u << PV_RAW_SHIFT);
+    }
+    __syncwarp();
+    uint32_t nins[2] = {0, 0};
+    bool over = false;
+    for (uint32_t base = 0; base < sigma; base += 32) {
+        const uint32_t i = base + lane;
+        bool fresh = false;
+        int dir = 0;
+        uint32_t id = 0;
+        if (i < sigma && (s.sv[i] & 1)) {
+            const uint32_t e = s.ge[i];
+            dir = (int)(e >> 31);
+            id = e & 0x7fffffffu;
+            const int h = pm_slot(s, dir, id);
+            fresh = h >= 0 && at[dir][h] == i;
+        }
+        for (int d = 0; d < 2; ++d) {
+            const unsigned bm = __ballot_sync(FULL, fresh && dir == d);
+            if (fresh && dir == d) {
+                const uint32_t a = nins[d] + __popc(bm & ((1u << lane) - 1));
+                if (a < s.c.icap) s.ins2[d][a] = id;
+            }
+            nins[d] += __popc(bm);
+        }
+        if (nins[0] > s.c.icap || nins[1] > s.c.icap) over = true;
+    }
+    __syncwarp();
+    if (over) return -1;
+    for (uint32_t i = lane; i < sigma; i += 32) {   // the inserted keys become present
+        if (!(s.sv[i] & 1)) continue;
+        const uint32_t e = s.ge[i];
+        const int dir = (int)(e >> 31);
+        const int h = pm_slot(s, dir, e & 0x7fffffffu);
+        if (h >= 0 && at[dir][h] == i) atomicOr(&s.vv[dir][h], PV_PRESENT);
+    }
+    __syncwarp();
+    // fold the op counts into count2 (8-bit wrap) and clear the scratch bits
+    for (int dir = 0; dir < 2; ++dir)
+        for (uint32_t h = lane; h < s.c.vcap; h += 32) {
+            const uint32_t v = s.vv[dir][h];
+            const uint32_t raw = ((v & PV_RAW_MASK) >> PV_RAW_SHIFT) & 0xffu;
+            const uint32_t base_v = v & ~(PV_RAW_MASK | PV_SEEN);
+            s.vv[dir][h] = (base_v & PV_PRESENT) ? ((base_v & ~0xff00u) | (raw << 8)) : base_v;
+        }
+    __syncwarp();
+    for (int d = 0; d < 2; ++d) {
+        st.nkeys[d] = nkeys[d];
+        st.n2[d] = nins[d];
     }
     return 1;
 }
@@ -1009,7 +1116,7 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
     __syncwarp();
     const uint32_t sigma2 = pe_kmers(ix, px, s, s.rd[1], n2);
     int par2 = 0;
-    if (sigma2 <= s.c.ecap) par2 = pe_count_par(px, s, st, n2, sigma2, 2);
+    if (sigma2 <= s.c.ecap && 2 * s.c.vcap * 4 <= PE_KMER_AREA) par2 = pe_count_par2(px, s, st, n2, sigma2);
     if (par2 < 0) return -1;
     if (par2 == 0 && lane == 0) pe_count_second(ix, px, s, st, n2, sigma2 <= s.c.ecap);
     if (__shfl_sync(0xffffffffu, st.over, 0)) return -1;
