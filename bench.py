@@ -86,6 +86,31 @@ def allreduce_max(x, world):
     return float(t.item())
 
 
+def host_placement(device):
+    """Host facts that bound the end-to-end copies: the GPU's nearest host NUMA
+    node (sysfs, by PCI bus id) and the memory nodes / CPUs this process may use.
+    Page-locked buffers go to the GPU's node when the process may use it."""
+    out = {}
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(device), "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=30).stdout.strip()
+        dom, rest = bus.split(":", 1)
+        with open("/sys/bus/pci/devices/%04x:%s/numa_node" % (int(dom, 16), rest.lower())) as f:
+            out["gpu_host_numa_node"] = int(f.read().strip())
+    except Exception:
+        out["gpu_host_numa_node"] = None
+    try:
+        with open("/proc/self/status") as f:
+            for line in f:
+                if line.startswith("Mems_allowed_list:"):
+                    out["mems_allowed"] = line.split(":", 1)[1].strip()
+                if line.startswith("Cpus_allowed_list:"):
+                    out["cpus_allowed"] = line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons, sampled every 50 ms from before
     the warm-up (so the tool's start-up overlaps no timed loop) until stop();
@@ -390,6 +415,7 @@ def run_gb300(args):
                              "traffic = dram read + write of one steady-state launch (ncu, 1 pass); "
                              "dram_achieved = traffic / launch time" % src},
         "windows_scanned_per_read": scans / max(1, reads),
+        "host": host_placement(local),
         "clocks": clk.summary(),
         "setup_seconds": {"generate": t_gen, "index_build": t_build, "upload": t_open},
     }

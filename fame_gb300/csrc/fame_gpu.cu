@@ -102,7 +102,7 @@ void dev_free(T*& p)
 
 // Heavy-pair caps: keys per map and phase, value-table slots, replayed buckets
 // (bucket_count = summed bucket sizes / 5 <= 224 k-mers x KMERCUTOFF / 5).
-constexpr PeCaps PE_HEAVY{16384, 65536, 131072 + NBHD - 1 + 64, 4096, 4096, 0};
+constexpr PeCaps PE_HEAVY{16384, 65536, 131072 + NBHD - 1 + 64, 4096, 4096, 0, PE_KMAX};
 
 // Page-locked host memory on the host NUMA node nearest the device (anonymous
 // pages bound there with mbind, touched, then registered with CUDA), so
@@ -424,9 +424,9 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         // pe_kmers keeps its per-read arrays (8 * 256 + 96 bytes) in layout regions 11 .. 16
         if (off[17] - off[11] < PE_KMER_AREA || hoff[17] - hoff[11] < PE_KMER_AREA)
             return fail(set_err(g, FAME_ERR_CUDA, "paired layout: k-mer area too small"));
-        const size_t pe_smem = 4 * g->pe_warp_bytes;
+        const size_t pe_smem = PE_SEED_WARPS * g->pe_warp_bytes;   // the largest layout (mates up to 255 bases)
         if (cudaFuncSetAttribute(k_pe_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pe_smem) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pe_seed, 128, pe_smem) != cudaSuccess || nb < 1)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pe_seed, 32 * PE_SEED_WARPS, pe_smem) != cudaSuccess || nb < 1)
             return fail(set_err(g, FAME_ERR_CUDA, "k_pe_seed does not fit an SM"));
         g->pe_grid = (uint32_t)(g->sm_count * nb);
     }
@@ -645,9 +645,26 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         if ((rc = sync_ctr())) return rc;
         if (g->h_ctr[CTR_TOO_LONG]) return set_err(g, FAME_ERR_READ, "mate longer than FAME_MAX_READ_LEN");
         const uint64_t wmask = g->h_ctr[CTR_WMASK];
-        // A: maps, walk lists, first-walk candidates
-        k_pe_seed<<<g->pe_grid, 128, 4 * g->pe_warp_bytes, g->stream>>>(g->ix, px, cb, g->d_pe_recs,
-                                                                          (uint32_t)g->pe_warp_bytes);
+        // A: maps, walk lists, first-walk candidates; the per-k-mer arrays are
+        // sized for the longest valid mate (widths W present: < 64 W bases)
+        PeCaps caps = PE_LIGHT;
+        {
+            uint32_t wmax = 1;
+            for (uint32_t w = 1; w <= 4; ++w)
+                if ((wmask >> w) & 1u) wmax = w;
+            caps.kmax = std::min<uint32_t>(PE_KMAX, 64 * wmax - KMERLEN);
+        }
+        uint64_t coff[28];
+        const uint64_t wbytes = pe_layout(caps, coff);
+        uint32_t grid = g->pe_grid;
+        {
+            int nb = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pe_seed, 32 * PE_SEED_WARPS,
+                                                              PE_SEED_WARPS * wbytes) == cudaSuccess && nb > 0)
+                grid = (uint32_t)(g->sm_count * nb);
+        }
+        k_pe_seed<<<grid, 32 * PE_SEED_WARPS, PE_SEED_WARPS * wbytes, g->stream>>>(g->ix, px, cb, g->d_pe_recs,
+                                                                                  (uint32_t)wbytes, caps);
         g->launches++;
         if ((rc = sync_ctr())) return rc;
         const uint64_t nc1 = g->h_ctr[CTR_CAND];

@@ -46,6 +46,7 @@ __device__ __forceinline__ uint32_t pv_c2(uint32_t v) { return (v >> 8) & 0xffu;
 
 constexpr uint32_t PE_KMAX = FAME_MAX_READ_LEN - KMERLEN + 1;   // k-mers of the longest read
 constexpr uint64_t PE_KMER_AREA = 8 * 256 + 96;                  // pe_kmers' per-read arrays
+constexpr uint32_t PE_SEED_WARPS = 2;                            // warps per block of k_pe_seed
 
 // Capacities of one warp's working memory.
 struct PeCaps {
@@ -55,6 +56,7 @@ struct PeCaps {
     uint32_t ovf_cap;
     uint32_t hcap;      // hits per mate and orientation
     uint32_t ecap;      // bucket entries of one mate staged in working memory (0: read in place)
+    uint32_t kmax;      // k-mers of the longest mate (per-k-mer arrays)
 };
 
 struct PeMem {
@@ -107,13 +109,13 @@ __host__ __device__ inline uint64_t pe_layout(PeCaps c, uint64_t* off)
     put(4ull * c.slot_cap);                 // 14 slot
     put(4ull * c.icap * 2);                 // 15 stk
     put(4ull * c.ovf_cap);                  // 16 ovf
-    put(4ull * PE_KMAX);                    // 17 kst
-    put(4ull * PE_KMAX);                    // 18 kln
-    put(4ull * PE_KMAX);                    // 19 kcm
-    put(PE_KMAX);                           // 20 kfl
+    put(4ull * c.kmax);                     // 17 kst
+    put(4ull * c.kmax);                     // 18 kln
+    put(4ull * c.kmax);                     // 19 kcm
+    put(c.kmax);                            // 20 kfl
     put(256);                               // 21 rd[0]
     put(256);                               // 22 rd[1]
-    put(4ull * (PE_KMAX + 1));              // 23 kpre
+    put(4ull * (c.kmax + 1));               // 23 kpre
     put(4ull * c.ecap);                     // 24 ge
     put(4ull * c.ecap);                     // 25 gt
     put(c.ecap);                            // 26 gk
@@ -160,7 +162,7 @@ __device__ inline PeMem pe_mem(uint8_t* base, PeCaps c)
 }
 
 // shared-memory caps of k_pe_seed (one warp; it keeps no matches)
-constexpr PeCaps PE_LIGHT{64, 256, 256 + NBHD - 1, 64, 0, 320};
+constexpr PeCaps PE_LIGHT{64, 256, 256 + NBHD - 1, 64, 0, 320, PE_KMAX};
 
 __device__ __forceinline__ uint32_t vt_hash(uint32_t k, uint32_t mask) { return (k * 0x9E3779B1u) >> 8 & mask; }
 
@@ -1367,13 +1369,13 @@ __device__ bool pe_lists(const PeMem& s, const PeState& st, const ChunkBufs& cb,
     return true;
 }
 
-__global__ void k_pe_seed(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs, uint32_t warp_bytes)
+__global__ void k_pe_seed(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs, uint32_t warp_bytes, PeCaps caps)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const uint32_t nw = gridDim.x * (blockDim.x >> 5);
-    const PeMem s = pe_mem(smem + (threadIdx.x >> 5) * warp_bytes, PE_LIGHT);
+    const PeMem s = pe_mem(smem + (threadIdx.x >> 5) * warp_bytes, caps);
     const uint32_t n = cb.n;
     for (uint32_t r = wid; r < n; r += nw) {
         if (lane == 0)
@@ -1387,7 +1389,7 @@ __global__ void k_pe_seed(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs
         const uint32_t i1 = r, i2 = n + r;
         const uint32_t n1 = (uint32_t)(cb.offs[i1 + 1] - cb.offs[i1]);
         const uint32_t n2 = (uint32_t)(cb.offs[i2 + 1] - cb.offs[i2]);
-        bool fb = false;
+        bool fb = n1 > caps.kmax + KMERLEN - 1 || n2 > caps.kmax + KMERLEN - 1;   // over the k-mer arrays
         for (int o = 0; o < 2 && !fb; ++o) {
             if (!((cb.orient_mask >> o) & 1u)) continue;
             PeState st;

@@ -233,7 +233,9 @@ int fame_gpu_mem_info(fame_gpu* g, uint64_t* free_bytes, uint64_t* total_bytes);
 
 /* Device memory helpers for the _dev entry points, and page-locked host
  * buffers (a host that parses its chunks straight into these gets the fast
- * host-to-device copy path). */
+ * host-to-device copy path).  Host buffers are placed on the host NUMA node
+ * nearest the device when the process may use it (else ordinary page-locked
+ * memory); free them with fame_gpu_host_free on the same context. */
 int fame_gpu_alloc(fame_gpu* g, size_t bytes, void** ptr_dev);
 int fame_gpu_free(fame_gpu* g, void* ptr_dev);
 int fame_gpu_memcpy(fame_gpu* g, void* dst, const void* src, size_t bytes, int kind /* 1 H2D, 2 D2H, 3 D2D */);
