@@ -201,6 +201,50 @@ def test_edge_cases(gpu):
     gpu.tallies(reset=True)
 
 
+def test_n_bases_at_word_edges(gpu, golden, oracle_index):
+    """One N at the first, second, 8-byte-word-edge, middle and last bases of
+    reads laid back to back at every byte alignment (the N check reads whole
+    aligned words), mixed with clean reads; and the same chunk through the
+    device entry point from a base address that is not word aligned."""
+    seq = golden["read_seq"].tobytes()
+    offs = golden["read_offs"].astype(np.int64)
+    reads = []
+    for i in range(600):
+        r = bytearray(seq[offs[i]:offs[i + 1]])
+        L = len(r)
+        pos = [0, 1, 7, 8, L // 2, L - 9, L - 8, L - 2, L - 1, -1][i % 10]
+        if pos >= 0:
+            r[pos] = ord("N")
+        reads.append(bytes(r))
+    o = np.zeros(len(reads) + 1, np.uint64)
+    np.cumsum([len(r) for r in reads], out=o[1:])
+    cat = b"".join(reads)
+    got = run_mode(gpu, cat, o, 0, True)
+    assert_same(got, _oracle_run(oracle_index, cat, o, 0, True), "N positions")
+    assert int(got["invalid"].sum()) == sum(1 for r in reads if len(r) < 80 or b"N" in r)
+    # device entry point, reads starting 3 bytes into an allocation
+    n = len(reads)
+    d_buf = gpu.alloc(len(cat) + 16)
+    d_offs = gpu.alloc(8 * (n + 1))
+    d_mat = gpu.alloc(8 * n)
+    d_inv = gpu.alloc(n)
+    try:
+        gpu.memcpy(d_buf + 3, np.frombuffer(cat, np.uint8).ctypes.data, len(cat), 1)
+        gpu.memcpy(d_offs, o.ctypes.data, 8 * (n + 1), 1)
+        gpu.tallies(reset=True)
+        gpu.match_reads_dev(d_buf + 3, d_offs, n, FAME_BOTH_STRANDS, d_mat, d_inv)
+        mats = np.zeros(n, np.uint64)
+        inv = np.zeros(n, np.uint8)
+        gpu.memcpy(mats.ctypes.data, d_mat, 8 * n, 2)
+        gpu.memcpy(inv.ctypes.data, d_inv, n, 2)
+        meth = gpu.tallies(reset=True)
+    finally:
+        for p_ in (d_buf, d_offs, d_mat, d_inv):
+            gpu.free(p_)
+    assert np.array_equal(mats, got["mat"]) and np.array_equal(inv, got["invalid"])
+    assert np.array_equal(meth, got["meth"])
+
+
 def test_determinism_and_order(gpu, golden):
     seq = golden["read_seq"].tobytes()
     offs = golden["read_offs"]
