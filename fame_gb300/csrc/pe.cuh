@@ -529,23 +529,20 @@ __device__ inline void pe_sort(uint2* f, long n, PeCmp cmp)
 }
 
 // ---------------------------------------------------------------------------
-// Lane-parallel map counting of one mate from the staged bucket entries.
+// Lane-parallel map counting of the first mate from the staged bucket entries
+// (getSeedRefsFirstRead).
 //
 // A bucket entry survives when the T-mask filter keeps it and it is not a
 // repeat of the previous surviving entry of its bucket.  An op may insert its
 // key when its k-mer index p has p == 0 or p - 1 < maxQPos, a prefix of the
 // ops (they come in k-mer order), so a key's first surviving op decides:
-// the key is inserted there when that op may insert (or, for the second mate,
-// when the key is already in the map), and then every one of its ops counts;
-// otherwise none does.  Counts commute, so only the first-touch order needs
-// the ops in order: chunks of 32 ops in order, equal keys of a chunk grouped
-// with __match_any_sync, new keys appended with ballots.  For the second
-// mate an insert also needs a map key within contextWLen windows; the
-// parallel form applies when every op that may insert finds one among the
-// keys kept from the first mate (the map before the second mate touches it),
-// and returns false otherwise, leaving the map untouched for the ordered
-// lane-0 loop.  Scratch bits of a value during the passes: bit 30 the key
-// was seen, bits 18-29 its op count.
+// the key is inserted there when that op may insert, and then every one of
+// its ops counts; otherwise none does.  Counts commute, so only the
+// first-touch order needs the ops in order: chunks of 32 ops in order, equal
+// keys of a chunk grouped with __match_any_sync, new keys appended with
+// ballots.  The second mate, whose inserts also need a map key within
+// contextWLen windows, is pe_count_par2.  Scratch bits of a value during the
+// passes: bit 30 the key was seen, bits 18-29 its op count.
 // ---------------------------------------------------------------------------
 constexpr uint32_t PV_SEEN = 1u << 30;
 constexpr uint32_t PV_RAW_SHIFT = 18;
@@ -575,7 +572,7 @@ __device__ void pe_survivors(const PeMem& s, uint32_t nk)
 
 // All lanes.  Returns 1 done, 0 not applicable (second mate, a neighbour
 // created by the mate itself would be needed), -1 over the table capacity.
-__device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint32_t len, uint32_t sigma, int phase)
+__device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint32_t len, uint32_t sigma)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t nk = len - KMERLEN + 1;
@@ -583,7 +580,7 @@ __device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint
     pe_survivors(s, nk);
     uint32_t nkeys[2] = {__shfl_sync(0xffffffffu, st.nkeys[0], 0), __shfl_sync(0xffffffffu, st.nkeys[1], 0)};
     uint32_t nins[2] = {0, 0};
-    uint32_t* ins[2] = {phase == 1 ? s.ins1[0] : s.ins2[0], phase == 1 ? s.ins1[1] : s.ins2[1]};
+    uint32_t* ins[2] = {s.ins1[0], s.ins1[1]};
     const uint32_t mask = s.c.vcap - 1;
     bool over = false;
     for (uint32_t base = 0; base < sigma && !over; base += 32) {
@@ -638,14 +635,12 @@ __device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint
             const uint32_t v = s.vv[dir][h];
             const uint32_t raw = ((v & PV_RAW_MASK) >> PV_RAW_SHIFT) & 0xffu;
             const uint32_t base_v = v & ~(PV_RAW_MASK | PV_SEEN);
-            if (!(v & PV_PRESENT)) s.vv[dir][h] = base_v;
-            else s.vv[dir][h] = phase == 1 ? ((base_v & ~0xffu) | raw) : ((base_v & ~0xff00u) | (raw << 8));
+            s.vv[dir][h] = (v & PV_PRESENT) ? ((base_v & ~0xffu) | raw) : base_v;
         }
     __syncwarp();
     for (int d = 0; d < 2; ++d) {
         st.nkeys[d] = nkeys[d];
-        if (phase == 1) st.n1[d] = nins[d];
-        else st.n2[d] = nins[d];
+        st.n1[d] = nins[d];
     }
     return 1;
 }
@@ -1096,7 +1091,7 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
     __syncwarp();
     const uint32_t sigma = pe_kmers(ix, px, s, s.rd[0], n1);
     if (sigma <= s.c.ecap) {
-        if (pe_count_par(px, s, st, n1, sigma, 1) < 0) return -1;
+        if (pe_count_par(px, s, st, n1, sigma) < 0) return -1;
     } else if (lane == 0) {
         pe_count_first(ix, px, s, st, n1, false);
     }
