@@ -94,19 +94,22 @@ def test_paired_read_queue_mirror(gpu, pe_golden, product_index):
 
 @pytest.mark.parametrize("seed,maxpdist", [(301, 550), (302, 400), (303, 2100)])
 def test_oracle_random_pairs(gpu, oracle_index, golden_genome, seed, maxpdist):
-    """Seeded pairs with 100 and 150 bp mates at several MAXPDIST values
+    """Seeded pairs with 100, 150 and 230 bp mates (automaton widths 2, 3 and
+    4; per-chunk k-mer arrays of 96, 160 and 224) at several MAXPDIST values
     (contextWLen 1 and 2) against the oracle."""
     g = genome_of(golden_genome)
     r1, r2 = synth.make_pairs(g, 1500, seed=seed, sub_rate=0.02, indel_rate=0.004,
                               inner=(20, maxpdist - 50))
     q1, q2 = synth.make_pairs(g, 300, seed=seed + 1000, read_len=150, inner=(20, 200))
-    s1a, o1a = r1.concat()
-    s2a, o2a = r2.concat()
-    s1b, o1b = q1.concat()
-    s2b, o2b = q2.concat()
-    s1, s2 = s1a + s1b, s2a + s2b
-    o1 = np.concatenate([o1a, o1b[1:] + o1a[-1]])
-    o2 = np.concatenate([o2a, o2b[1:] + o2a[-1]])
+    w1, w2 = synth.make_pairs(g, 80, seed=seed + 2000, read_len=230, inner=(20, 200))   # 4-word automaton
+    s1, s2 = b"", b""
+    o1 = o2 = np.zeros(1, np.uint64)
+    for a, b in ((r1, r2), (q1, q2), (w1, w2)):
+        sa, oa = a.concat()
+        sb, ob = b.concat()
+        s1, s2 = s1 + sa, s2 + sb
+        o1 = np.concatenate([o1, oa[1:].astype(np.uint64) + o1[-1]])
+        o2 = np.concatenate([o2, ob[1:].astype(np.uint64) + o2[-1]])
     for chunk, both in ((0, False), (600, False), (0, True)):
         got = run_pairs(gpu, s1, o1, s2, o2, chunk, both, maxpdist)
         ref = oracle_index.match_pe(s1, o1, s2, o2, chunk=chunk, both_strands=both, maxpdist=maxpdist)
