@@ -414,6 +414,14 @@ def run_gb300(args):
                      "note": "algorithmic bytes = 8 B bucket bounds + 4 B per bucket entry per k-mer; peak %s; "
                              "traffic = dram read + write of one steady-state launch (ncu, 1 pass); "
                              "dram_achieved = traffic / launch time" % src},
+        "alu_bound_kernels": {
+            "note": "stages bound by the integer/logic pipe, not by HBM or tensor cores: ALU-pipe utilisation "
+                    "from the committed ncu captures of the 20 Mbp workload (not measured by this run)",
+            "k_shiftand": {"stage_ms": 1e3 * st["shift_and"] / args.steps, "alu_pipe_of_peak": 0.647,
+                           "profile": "profiles/k_shiftand_se100_20mbp.md"},
+            "k_dp_warp": {"stage_ms": 1e3 * st["banded_dp"] / args.steps, "alu_pipe_of_peak": 0.684,
+                          "profile": "profiles/k_dp_warp_se100_20mbp.md"},
+        },
         "windows_scanned_per_read": scans / max(1, reads),
         "host": host_placement(local),
         "clocks": clk.summary(),
