@@ -1144,35 +1144,59 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
             mine |= key != EMPTY_KEY && (v & PV_PRESENT) && (v & PV_F2) && ix.win[key].z != CPGDUMMY;
         }
     if (!__any_sync(0xffffffffu, mine)) return 0;
-    if (lane == 0) {
-        // Final iteration orders: the replay of the first map, its kept keys, then the second
-        // mate's insertions.  The walks scan only keys with count >= QTHRESH (count1 in the
-        // first, count2 in the second), and a strand map with at most one such key in both
-        // counts puts it first after either sort whatever the order of the others, so then
-        // no replay is needed.
-        bool need = false;
+    // Final iteration orders: the replay of the first map, its kept keys, then the second
+    // mate's insertions.  The walks scan only keys with count >= QTHRESH (count1 in the
+    // first, count2 in the second), and a strand map with at most one such key in both
+    // counts puts it first after either sort whatever the order of the others, so then
+    // no replay is needed: the kept keys in first-touch order, then the second mate's
+    // insertions, taken lane-parallel with ballots.  (The insertion counts of lane 0,
+    // which ran any ordered counting, hold for the warp.)
+    constexpr uint32_t FULL = 0xffffffffu;
+    uint32_t n1d[2], n2d[2];
+    for (int dir = 0; dir < 2; ++dir) {
+        n1d[dir] = __shfl_sync(FULL, st.n1[dir], 0);
+        n2d[dir] = __shfl_sync(FULL, st.n2[dir], 0);
+    }
+    bool need = false;
+    for (int dir = 0; dir < 2; ++dir) {
+        uint32_t c1 = 0, c2 = 0;
+        for (uint32_t x = lane; x < n1d[dir]; x += 32) {
+            const int h = pm_find(s, dir, s.ins1[dir][x]);
+            if (h >= 0) { c1 += pv_c1(s.vv[dir][h]) >= QTHRESH; c2 += pv_c2(s.vv[dir][h]) >= QTHRESH; }
+        }
+        for (uint32_t x = lane; x < n2d[dir]; x += 32) {
+            const int h = pm_find(s, dir, s.ins2[dir][x]);
+            if (h >= 0) c2 += pv_c2(s.vv[dir][h]) >= QTHRESH;
+        }
+        c1 = __reduce_add_sync(FULL, c1);
+        c2 = __reduce_add_sync(FULL, c2);
+        need |= c1 > 1 || c2 > 1;
+    }
+    if (!need) {
         for (int dir = 0; dir < 2; ++dir) {
-            uint32_t c1 = 0, c2 = 0;
-            for (uint32_t x = 0; x < st.n1[dir]; ++x) {
-                const int h = pm_find(s, dir, s.ins1[dir][x]);
-                if (h >= 0) { c1 += pv_c1(s.vv[dir][h]) >= QTHRESH; c2 += pv_c2(s.vv[dir][h]) >= QTHRESH; }
-            }
-            for (uint32_t x = 0; x < st.n2[dir]; ++x) {
-                const int h = pm_find(s, dir, s.ins2[dir][x]);
-                if (h >= 0) c2 += pv_c2(s.vv[dir][h]) >= QTHRESH;
-            }
-            need |= c1 > 1 || c2 > 1;
-        }
-        for (int dir = 0; dir < 2 && !need; ++dir) {
             uint32_t ns = 0;
-            for (uint32_t x = 0; x < st.n1[dir]; ++x) {
-                const int h = pm_find(s, dir, s.ins1[dir][x]);
-                if (h >= 0 && pv_c1(s.vv[dir][h]) >= QTHRESH) s.ord[dir][ns++] = s.ins1[dir][x];
+            for (uint32_t b0 = 0; b0 < n1d[dir]; b0 += 32) {
+                const uint32_t x = b0 + lane;
+                bool keep = false;
+                uint32_t key = 0;
+                if (x < n1d[dir]) {
+                    key = s.ins1[dir][x];
+                    const int h = pm_find(s, dir, key);
+                    keep = h >= 0 && pv_c1(s.vv[dir][h]) >= QTHRESH;
+                }
+                const uint32_t bm = __ballot_sync(FULL, keep);
+                if (keep) s.ord[dir][ns + __popc(bm & ((1u << lane) - 1))] = key;
+                ns += __popc(bm);
             }
-            for (uint32_t x = 0; x < st.n2[dir]; ++x) s.ord[dir][ns++] = s.ins2[dir][x];
-            st.nord[dir] = ns;
+            for (uint32_t x = lane; x < n2d[dir]; x += 32) s.ord[dir][ns + x] = s.ins2[dir][x];
+            st.nord[dir] = ns + n2d[dir];
         }
-        for (int dir = 0; dir < 2 && need && !st.over; ++dir) {
+        __syncwarp();
+        return 1;
+    }
+    if (lane == 0) {
+        // a strand map with two or more keys to scan: replay its insertions
+        for (int dir = 0; dir < 2 && !st.over; ++dir) {
             uint32_t nt = 0;
             if (!pe_replay(s, s.ins1[dir], st.n1[dir], sigma / 5, s.ord[dir], nt)) { st.over = true; break; }
             uint32_t ns = 0;
