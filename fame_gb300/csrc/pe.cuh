@@ -1105,11 +1105,11 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
         }
     __syncwarp();
     bool any = false;
-    if (lane == 0)
-        for (int dir = 0; dir < 2 && !any; ++dir)
-            for (uint32_t x = 0; x < st.n1[dir]; ++x)
-                if (pm_find(s, dir, s.ins1[dir][x]) >= 0) { any = true; break; }
-    if (!__shfl_sync(0xffffffffu, any, 0)) return 0;
+    for (int dir = 0; dir < 2; ++dir) {
+        const uint32_t n1d = __shfl_sync(0xffffffffu, st.n1[dir], 0);   // lane 0's, after any ordered counting
+        for (uint32_t x = lane; x < n1d && !any; x += 32) any = pm_find(s, dir, s.ins1[dir][x]) >= 0;
+    }
+    if (!__any_sync(0xffffffffu, any)) return 0;
     __syncwarp();
     const uint32_t sigma2 = pe_kmers(ix, px, s, s.rd[1], n2);
     int par2 = 0;
@@ -1348,32 +1348,28 @@ struct PeTaskRec {            // one pair orientation
 };
 
 // Stage A, lane 0: the walk lists of one orientation and its first-walk candidates.
-__device__ bool pe_lists(const PeMem& s, const PeState& st, const ChunkBufs& cb, PeTaskRec& t, uint32_t i1, int o)
+// lane 0: sort one strand list and keep its keys with count >= QTHRESH
+__device__ bool pe_list_cut(const PeMem& s, PeTaskRec& t, int dir, uint32_t nl, int second, const PeCmp& cmp)
 {
-    for (int second = 0; second < 2; ++second) {
-        const PeCmp cmp{second};
-        for (int dir = 0; dir < 2; ++dir) {
-            const uint32_t nl = st.nord[dir];
-            for (uint32_t q = 0; q < nl; ++q) {
-                const uint32_t key = s.ord[dir][q];
-                const int h = pm_find(s, dir, key);
-                s.list[dir][q] = make_uint2(key, h >= 0 ? s.vv[dir][h] : 0u);
-            }
-            pe_sort(s.list[dir], (long)nl, cmp);
-            uint32_t k = 0;
-            for (uint32_t q = 0; q < nl; ++q) {
-                const uint32_t v = s.list[dir][q].y;
-                if ((second ? pv_c2(v) : pv_c1(v)) < QTHRESH) break;   // counts sorted descending
-                if (k >= (uint32_t)PE_CAPL) return false;
-                const uint32_t cnts = pv_c1(v) | (pv_c2(v) << 8);
-                if (second) t.w2[dir][k] = make_uint4(s.list[dir][q].x, cnts, NO_CAND, 0);
-                else t.w1[dir][k] = make_uint4(s.list[dir][q].x, cnts | ((v & PV_F2) ? 1u << 16 : 0u), NO_CAND, 0);
-                ++k;
-            }
-            if (second) t.n2[dir] = (uint8_t)k;
-            else t.n1[dir] = (uint8_t)k;
-        }
+    pe_sort(s.list[dir], (long)nl, cmp);
+    uint32_t k = 0;
+    for (uint32_t q = 0; q < nl; ++q) {
+        const uint32_t v = s.list[dir][q].y;
+        if ((second ? pv_c2(v) : pv_c1(v)) < QTHRESH) break;   // counts sorted descending
+        if (k >= (uint32_t)PE_CAPL) return false;
+        const uint32_t cnts = pv_c1(v) | (pv_c2(v) << 8);
+        if (second) t.w2[dir][k] = make_uint4(s.list[dir][q].x, cnts, NO_CAND, 0);
+        else t.w1[dir][k] = make_uint4(s.list[dir][q].x, cnts | ((v & PV_F2) ? 1u << 16 : 0u), NO_CAND, 0);
+        ++k;
     }
+    if (second) t.n2[dir] = (uint8_t)k;
+    else t.n1[dir] = (uint8_t)k;
+    return true;
+}
+
+// lane 0: the first walk's f2-flagged keys become scan candidates
+__device__ void pe_first_candidates(const ChunkBufs& cb, PeTaskRec& t, uint32_t i1, int o)
+{
     for (int dir = 0; dir < 2; ++dir)
         for (uint32_t k = 0; k < t.n1[dir]; ++k) {
             if (!((t.w1[dir][k].y >> 16) & 1u)) continue;
@@ -1385,6 +1381,33 @@ __device__ bool pe_lists(const PeMem& s, const PeState& st, const ChunkBufs& cb,
             }
             t.w1[dir][k].z = ci;
         }
+}
+
+// The walk lists of one pair orientation (all lanes call it; lane 0's result):
+// each strand's keys in iteration order with their values, sorted by count1
+// (first walk) or count2 (second walk) with the libstdc++ introsort on lane 0,
+// cut at QTHRESH.
+__device__ bool pe_lists(const PeMem& s, const PeState& st, const ChunkBufs& cb, PeTaskRec& t, uint32_t i1, int o)
+{
+    const int lane = threadIdx.x & 31;
+    bool ok = true;
+    for (int second = 0; second < 2; ++second) {
+        const PeCmp cmp{second};
+        for (int dir = 0; dir < 2; ++dir) {
+            const uint32_t nl = __shfl_sync(0xffffffffu, st.nord[dir], 0);
+            for (uint32_t q = lane; q < nl; q += 32) {
+                const uint32_t key = s.ord[dir][q];
+                const int h = pm_find(s, dir, key);
+                s.list[dir][q] = make_uint2(key, h >= 0 ? s.vv[dir][h] : 0u);
+            }
+            __syncwarp();
+            if (lane == 0 && ok) ok = pe_list_cut(s, t, dir, nl, second, cmp);
+            __syncwarp();
+        }
+    }
+    if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) return false;
+    if (lane == 0) pe_first_candidates(cb, t, i1, o);
+    __syncwarp();
     return true;
 }
 
@@ -1415,13 +1438,10 @@ __global__ void k_pe_seed(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs
             const int m = pe_maps(ix, px, cb, s, i1, i2, n1, n2, o, st);
             if (m < 0) { fb = true; break; }
             if (m == 0) continue;
-            bool ok = true;
-            if (lane == 0) {
-                PeTaskRec& t = recs[2 * r + o];
-                ok = pe_lists(s, st, cb, t, i1, o);
-                t.state = ok ? PT_WALK : PT_FALLBACK;
-            }
-            fb = !__shfl_sync(0xffffffffu, ok, 0);
+            PeTaskRec& t = recs[2 * r + o];
+            const bool ok = pe_lists(s, st, cb, t, i1, o);
+            if (lane == 0) t.state = ok ? PT_WALK : PT_FALLBACK;
+            fb = !ok;
             __syncwarp();
         }
         if (fb && lane == 0) {
