@@ -23,6 +23,7 @@ the same chunks.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -84,6 +85,31 @@ def allreduce_max(x, world):
     t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+_REAL_STDOUT = None
+
+
+def stdout_to_stderr():
+    """The bench's only stdout is its JSON line: everything else written to
+    file descriptor 1 (the reference library's C++ output included) goes to
+    stderr."""
+    global _REAL_STDOUT
+    sys.stdout.flush()
+    _REAL_STDOUT = os.fdopen(os.dup(1), "w")
+    os.dup2(2, 1)
+
+
+def emit(obj):
+    """Write the JSON line to the real stdout, after flushing C stdio."""
+    try:
+        ctypes.CDLL(None).fflush(None)
+    except Exception:
+        pass
+    sys.stdout.flush()
+    out = _REAL_STDOUT or sys.stdout
+    out.write(json.dumps(obj) + "\n")
+    out.flush()
 
 
 def host_placement(device):
@@ -434,7 +460,7 @@ def run_gb300(args):
         gm.free(dev[i][1])
     gm.close()
     if rank == 0:
-        print(json.dumps(out))
+        emit(out)
 
 
 SERVING_METRIC = "aggregate reads/s of a single-cell job stream (serving form), with p50/p99 job latency"
@@ -494,7 +520,7 @@ def run_gb300_serving(args):
         "timing": "host clock over the whole trace (arrival-driven); per-job latency = completion - arrival",
         "clocks": clk.summary(), "setup_seconds": {"generate": t_gen},
     }
-    print(json.dumps(out))
+    emit(out)
 
 
 PE_METRIC = "aligned read pairs/s (paired-end matching stage, bit-exact CpG report)"
@@ -601,7 +627,7 @@ def run_gb300_pe(args):
         gm.free(d_s)
         gm.free(d_o)
     gm.close()
-    print(json.dumps(out))
+    emit(out)
 
 
 def cpu_baseline_pe(hi, s1, o1, s2, o2, chunks, sample):
@@ -657,7 +683,7 @@ def run_reference(args):
         ri = L.build(fasta)  # the reference's own readReference + RefGenome constructor
         kind = "reference"
     except Exception as e:
-        print(json.dumps({"impl": "reference", "unavailable": "reference build failed: %s" % e}))
+        emit({"impl": "reference", "unavailable": "reference build failed: %s" % e})
         return
     seq, chunks = chunk_list(rs, CHUNKSIZE)
     sample = min(args.cpu_sample, CHUNKSIZE)
@@ -677,7 +703,7 @@ def run_reference(args):
         secs += s
         reads += n
     v = reads / secs
-    print(json.dumps({
+    emit({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "reads/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 integer",
@@ -685,11 +711,12 @@ def run_reference(args):
         "cpu_baseline": {"value": v, "unit": "reads/s", "cores": L.corenum, "kind": kind,
                          "sample": "%d reads per step from consecutive 300k-read chunks, decided orientation"
                                    % sample},
-        "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
     ri.close()
 
 
 if __name__ == "__main__":
+    stdout_to_stderr()
     a = parse()
     if a.impl == "reference":
         run_reference(a)
