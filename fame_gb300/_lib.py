@@ -67,7 +67,7 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_queue_submit", "fame_queue_ready", "fame_queue_collect", "fame_queue_launches", "fame_queue_close",
            "fame_gpu_tally_alloc", "fame_gpu_tally_read", "fame_gpu_tally_free", "fame_gpu_mem_info",
            "fame_report_cpg", "fame_report_sc_header", "fame_report_sc_rows", "fame_fastq_open", "fame_fastq_read",
-           "fame_fastq_close"]
+           "fame_fastq_close", "fame_queue_stage", "fame_queue_submit_staged", "fame_match_fastq"]
 
 _lib = None
 
@@ -124,6 +124,9 @@ def lib(build_if_missing: bool = True):
     L.fame_fastq_open.argtypes = [C.c_char_p, C.c_int, C.c_int, _P]
     L.fame_fastq_read.argtypes = [_P, C.c_uint32, _P, C.c_uint64, _P, _P]
     L.fame_fastq_close.argtypes = [_P]
+    L.fame_queue_stage.argtypes = [_P, _P, _P, _P, _P, _P]
+    L.fame_queue_submit_staged.argtypes = [_P, C.c_int, C.c_uint32, C.c_uint32, _P]
+    L.fame_match_fastq.argtypes = [_P, C.c_char_p, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, _P, _P, _P]
     _lib = L
     return L
 
@@ -303,6 +306,18 @@ class GpuMatcher:
         _check(lib().fame_gpu_match_reads_dev(self.h, seqs_dev, offs_dev, n, flags, mats_dev, invalid_dev,
                                               C.byref(cnt)), self.h)
         return cnt
+
+    def match_fastq(self, path: str, is_gz: bool, flags: int, chunk: int = 0, slots: int = 3, threads: int = 0,
+                    meth_dev=None):
+        """A whole single-end FASTQ file (fame_match_fastq): parse and match
+        overlapped, strand vote on the first chunk unless FAME_BOTH_STRANDS;
+        tallies accumulate in the context (or meth_dev).  Returns
+        (Counters, reads)."""
+        cnt = Counters()
+        n = C.c_uint64(0)
+        _check(lib().fame_match_fastq(self.h, path.encode(), int(is_gz), flags, chunk, slots, threads, meth_dev,
+                                      C.byref(cnt), C.byref(n)), self.h)
+        return cnt, int(n.value)
 
     def tallies(self, reset: bool = False) -> np.ndarray:
         out = np.zeros(4 * self.n_cpg, np.uint16)

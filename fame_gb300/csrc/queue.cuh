@@ -51,6 +51,7 @@ struct QSlot {
     uint32_t n = 0;
     uint32_t flags = 0;
     uint32_t* meth = nullptr;
+    bool staged = false;       // handed to the caller by fame_queue_stage, not yet submitted
     // graph cache
     struct Graph {
         uint32_t n, flags;
@@ -229,23 +230,22 @@ extern "C" int fame_queue_open(fame_gpu* g, uint32_t nslots, uint32_t max_reads,
     return FAME_OK;
 }
 
-extern "C" int fame_queue_submit(fame_queue* q, const char* seqs, const uint64_t* offs, uint32_t n, uint32_t flags,
-                                 uint32_t* meth_dev, int* slot)
+namespace {
+
+int qslot_free_index(fame_queue* q)
 {
-    if (!q || !slot || (n && (!seqs || !offs))) return FAME_ERR_ARG;
-    fame_gpu* g = q->g;
-    if (n > q->max_reads || (n && offs[n] - offs[0] > q->max_bytes))
-        return set_err(g, FAME_ERR_ARG, "chunk exceeds the queue's slot size");
-    CK(cudaSetDevice(g->device));
-    // a free slot, else wait for the oldest busy one to finish (its result stays until collected)
-    int pick = -1;
     for (size_t i = 0; i < q->slots.size(); ++i)
-        if (!q->slots[i].busy) { pick = (int)i; break; }
-    if (pick < 0) return set_err(g, FAME_ERR_BUSY, "every queue slot holds an uncollected chunk");
+        if (!q->slots[i].busy && !q->slots[i].staged) return (int)i;
+    return -1;
+}
+
+// The chunk in slot pick's staging (s.h_seqs / s.h_offs, offsets from 0):
+// copies, the cached graph, the completion event.
+int qslot_launch(fame_queue* q, int pick, uint32_t n, uint32_t flags, uint32_t* meth_dev, int* slot)
+{
+    fame_gpu* g = q->g;
     QSlot& s = q->slots[pick];
-    const uint64_t base = n ? offs[0] : 0, bytes = n ? offs[n] - offs[0] : 0;
-    std::memcpy(s.h_seqs, seqs + base, bytes);
-    for (uint32_t i = 0; i <= n; ++i) s.h_offs[i] = n ? offs[i] - base : 0;
+    const uint64_t bytes = n ? s.h_offs[n] : 0;
     s.n = n;
     s.flags = flags;
     s.meth = meth_dev;
@@ -266,6 +266,55 @@ extern "C" int fame_queue_submit(fame_queue* q, const char* seqs, const uint64_t
     q->launches += QUEUE_KERNELS_PER_CHUNK;
     *slot = pick;
     return FAME_OK;
+}
+
+}  // namespace
+
+extern "C" int fame_queue_submit(fame_queue* q, const char* seqs, const uint64_t* offs, uint32_t n, uint32_t flags,
+                                 uint32_t* meth_dev, int* slot)
+{
+    if (!q || !slot || (n && (!seqs || !offs))) return FAME_ERR_ARG;
+    fame_gpu* g = q->g;
+    if (n > q->max_reads || (n && offs[n] - offs[0] > q->max_bytes))
+        return set_err(g, FAME_ERR_ARG, "chunk exceeds the queue's slot size");
+    CK(cudaSetDevice(g->device));
+    const int pick = qslot_free_index(q);
+    if (pick < 0) return set_err(g, FAME_ERR_BUSY, "every queue slot holds an uncollected chunk");
+    QSlot& s = q->slots[pick];
+    const uint64_t base = n ? offs[0] : 0, bytes = n ? offs[n] - offs[0] : 0;
+    std::memcpy(s.h_seqs, seqs + base, bytes);
+    for (uint32_t i = 0; i <= n; ++i) s.h_offs[i] = n ? offs[i] - base : 0;
+    return qslot_launch(q, pick, n, flags, meth_dev, slot);
+}
+
+extern "C" int fame_queue_stage(fame_queue* q, int* slot, char** seqs, uint64_t** offs, uint32_t* max_reads,
+                                uint64_t* max_bytes)
+{
+    if (!q || !slot || !seqs || !offs) return FAME_ERR_ARG;
+    const int pick = qslot_free_index(q);
+    if (pick < 0) return set_err(q->g, FAME_ERR_BUSY, "every queue slot holds an uncollected chunk");
+    QSlot& s = q->slots[pick];
+    s.staged = true;
+    *slot = pick;
+    *seqs = s.h_seqs;
+    *offs = s.h_offs;
+    if (max_reads) *max_reads = q->max_reads;
+    if (max_bytes) *max_bytes = q->max_bytes;
+    return FAME_OK;
+}
+
+extern "C" int fame_queue_submit_staged(fame_queue* q, int slot, uint32_t n, uint32_t flags, uint32_t* meth_dev)
+{
+    if (!q || slot < 0 || slot >= (int)q->slots.size()) return FAME_ERR_ARG;
+    fame_gpu* g = q->g;
+    QSlot& s = q->slots[slot];
+    if (!s.staged) return set_err(g, FAME_ERR_ARG, "queue slot was not staged");
+    s.staged = false;
+    if (n > q->max_reads || (n && (s.h_offs[0] != 0 || s.h_offs[n] > q->max_bytes)))
+        return set_err(g, FAME_ERR_ARG, "staged chunk exceeds the queue's slot size");
+    CK(cudaSetDevice(g->device));
+    int out = 0;
+    return qslot_launch(q, slot, n, flags, meth_dev, &out);
 }
 
 extern "C" int fame_queue_ready(fame_queue* q, int slot)

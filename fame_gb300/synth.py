@@ -73,7 +73,23 @@ class ReadSet:
     def subset(self, idx) -> "ReadSet":
         return ReadSet(self.seqs[idx], self.lens[idx], self.chrom[idx], self.start[idx], self.fwd[idx])
 
-    def write_fastq(self, path: str) -> None:
+    def write_fastq(self, path: str, block: int = 500_000) -> None:
+        """Records "@r<i>" / sequence / "+" / all-'I' qualities; reads of one
+        length are written as fixed-width blocks (names "@r"), others one by one."""
+        lens = self.lens
+        if len(self) and (lens == lens[0]).all():
+            L = int(lens[0])
+            with open(path, "wb") as f:
+                for b0 in range(0, len(self), block):
+                    s = self.seqs[b0:b0 + block, :L]
+                    rec = np.empty((len(s), 2 * L + 7), np.uint8)
+                    rec[:, :3] = np.frombuffer(b"@r\n", np.uint8)
+                    rec[:, 3:3 + L] = s
+                    rec[:, 3 + L:6 + L] = np.frombuffer(b"\n+\n", np.uint8)
+                    rec[:, 6 + L:6 + 2 * L] = ord("I")
+                    rec[:, -1] = ord("\n")
+                    f.write(rec.tobytes())
+            return
         with open(path, "wb") as f:
             for i in range(len(self)):
                 s = self.seqs[i, : self.lens[i]].tobytes()

@@ -222,6 +222,26 @@ int fame_queue_collect(fame_queue* q, int slot, uint64_t* mats, uint8_t* invalid
 /* Kernels launched through the queue so far. */
 uint64_t fame_queue_launches(const fame_queue* q);
 int fame_queue_close(fame_queue* q);
+/* Zero-copy submission: stage reserves a free slot and returns its
+ * page-locked staging (room for max_reads reads, offs[0..n] from 0, and
+ * max_bytes bases); the caller writes a chunk there (e.g. with
+ * fame_fastq_read) and starts it with submit_staged (n = 0 returns the slot
+ * unused).  FAME_ERR_BUSY when no slot is free. */
+int fame_queue_stage(fame_queue* q, int* slot, char** seqs, uint64_t** offs, uint32_t* max_reads, uint64_t* max_bytes);
+int fame_queue_submit_staged(fame_queue* q, int slot, uint32_t n, uint32_t flags, uint32_t* meth_dev);
+
+/* ---- FASTQ file to tallies: queryRoutine (main.cpp:363-399) -------------
+ * parseChunk / parseChunkGZ (ReadQueue.cpp:218-373) and matchReads over a
+ * whole file, chunks of `chunk` records (0: CHUNKSIZE, 300,000): the first matched alone
+ * with the strand vote unless flags has FAME_BOTH_STRANDS, then the others
+ * with the decided orientation (decideStrand, ReadQueue.cpp:376-400), parsed
+ * by n_threads host threads straight into the staging of a queue of `slots`
+ * (2..8) chunk slots while earlier chunks run on the GPU.  Tallies add to
+ * meth_dev (NULL: the context's array); cnt receives the summed counters and
+ * n_reads the records read.  Opens its own queue: FAME_ERR_BUSY when the
+ * context already has one. */
+int fame_match_fastq(fame_gpu* g, const char* path, int is_gz, uint32_t flags, uint32_t chunk, uint32_t slots,
+                     int n_threads, uint32_t* meth_dev, fame_counters* cnt, uint64_t* n_reads);
 /* Separate tally arrays (4 x n_cpg uint32 in device memory, zeroed), e.g. one
  * per single-cell job of a serving loop; read returns them as methLevels
  * (uint16 wrap), reset zeroes them. */
