@@ -75,3 +75,38 @@ def test_reader_large_file(tmp_path):
             break
     r.close()
     assert total == n
+
+
+@pytest.mark.parametrize("chunk,threads", [(1, 1), (999, 4)])
+def test_reader_pipe(tmp_path, chunk, threads):
+    """A named pipe cannot be mapped: the buffered path, same records."""
+    import os
+    import threading
+    rng = np.random.default_rng(7 + chunk)
+    recs = records(rng, 2500)
+    data_path = tmp_path / "src.fq"
+    write(data_path, recs, final_newline=False)
+    fifo = tmp_path / "pipe.fq"
+    os.mkfifo(fifo)
+
+    def feed():
+        with open(fifo, "wb") as f:
+            f.write(data_path.read_bytes())
+
+    th = threading.Thread(target=feed)
+    th.start()
+    got = read_all(fifo, False, chunk, threads)
+    th.join()
+    assert got == [s for _, s, _, _ in recs]
+
+
+def test_reader_empty_and_tiny(tmp_path):
+    empty = tmp_path / "e.fq"
+    empty.write_bytes(b"")
+    assert read_all(empty, False, 10, 4) == []
+    one = tmp_path / "one.fq"
+    one.write_bytes(b"@a\nACGT")          # a record cut after its sequence line
+    assert read_all(one, False, 10, 4) == [b"ACGT"]
+    blank = tmp_path / "blank.fq"
+    blank.write_bytes(b"\n\n\n\n\n\n")     # empty lines are lines: two records of empty sequences
+    assert read_all(blank, False, 10, 2) == [b"", b""]
