@@ -67,7 +67,8 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_queue_submit", "fame_queue_ready", "fame_queue_collect", "fame_queue_launches", "fame_queue_close",
            "fame_gpu_tally_alloc", "fame_gpu_tally_read", "fame_gpu_tally_free", "fame_gpu_mem_info",
            "fame_report_cpg", "fame_report_sc_header", "fame_report_sc_rows", "fame_fastq_open", "fame_fastq_read",
-           "fame_fastq_close", "fame_queue_stage", "fame_queue_submit_staged", "fame_match_fastq"]
+           "fame_fastq_close", "fame_queue_stage", "fame_queue_submit_staged", "fame_match_fastq",
+           "fame_match_fastq_paired"]
 
 _lib = None
 
@@ -127,6 +128,8 @@ def lib(build_if_missing: bool = True):
     L.fame_queue_stage.argtypes = [_P, _P, _P, _P, _P, _P]
     L.fame_queue_submit_staged.argtypes = [_P, C.c_int, C.c_uint32, C.c_uint32, _P]
     L.fame_match_fastq.argtypes = [_P, C.c_char_p, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, _P, _P, _P]
+    L.fame_match_fastq_paired.argtypes = [_P, C.c_char_p, C.c_char_p, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32,
+                                          C.c_int, _P, _P]
     _lib = L
     return L
 
@@ -317,6 +320,18 @@ class GpuMatcher:
         n = C.c_uint64(0)
         _check(lib().fame_match_fastq(self.h, path.encode(), int(is_gz), flags, chunk, slots, threads, meth_dev,
                                       C.byref(cnt), C.byref(n)), self.h)
+        return cnt, int(n.value)
+
+    def match_fastq_paired(self, path1: str, path2: str, is_gz: bool, flags: int, maxpdist: int, chunk: int = 0,
+                           threads: int = 0):
+        """Two mate FASTQ files (fame_match_fastq_paired): parse of the next
+        chunk overlapped with the matching, strand vote on the first chunk
+        unless FAME_BOTH_STRANDS; tallies accumulate in the context.  Returns
+        (PairCounters, pairs)."""
+        cnt = PairCounters()
+        n = C.c_uint64(0)
+        _check(lib().fame_match_fastq_paired(self.h, path1.encode(), path2.encode(), int(is_gz), flags, maxpdist,
+                                             chunk, threads, C.byref(cnt), C.byref(n)), self.h)
         return cnt, int(n.value)
 
     def tallies(self, reset: bool = False) -> np.ndarray:

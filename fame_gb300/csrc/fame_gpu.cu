@@ -16,6 +16,7 @@
 
 #include "../../include/fame_gpu.h"
 #include "index_host.h"
+#include "internal.h"
 #include "pe.cuh"
 
 using namespace fame;
@@ -202,6 +203,8 @@ uint32_t pow2_ceil_host(uint64_t v)
 }  // namespace
 
 extern "C" const char* fame_gpu_last_error(const fame_gpu* g) { return g ? g->err.c_str() : "null context"; }
+
+int fame_gpu_fail(fame_gpu* g, int code, const char* msg) { return set_err(g, code, msg ? msg : ""); }
 
 extern "C" int fame_gpu_close(fame_gpu* g)
 {

@@ -1,0 +1,8 @@
+// Library-internal declarations shared by the host-side sources (not part of
+// the C ABI).
+#pragma once
+
+#include "../../include/fame_gpu.h"
+
+// Records msg as the context's last error and returns code.
+int fame_gpu_fail(fame_gpu* g, int code, const char* msg);

@@ -242,6 +242,17 @@ int fame_queue_submit_staged(fame_queue* q, int slot, uint32_t n, uint32_t flags
  * context already has one. */
 int fame_match_fastq(fame_gpu* g, const char* path, int is_gz, uint32_t flags, uint32_t chunk, uint32_t slots,
                      int n_threads, uint32_t* meth_dev, fame_counters* cnt, uint64_t* n_reads);
+/* queryRoutinePaired (main.cpp:400-441) over two mate FASTQ files: chunks of
+ * `chunk` pairs (0: CHUNKSIZE) read from both files (FAME_ERR_IO when they
+ * hold different numbers of records), the first matched with the strand vote
+ * unless flags has FAME_BOTH_STRANDS, each through fame_gpu_match_pairs while
+ * a host thread parses the next chunk of both files into page-locked
+ * buffers.  maxpdist as for fame_gpu_match_pairs; tallies add to the
+ * context's array; cnt receives the summed counters and n_pairs the pairs
+ * read. */
+int fame_match_fastq_paired(fame_gpu* g, const char* path1, const char* path2, int is_gz, uint32_t flags,
+                            uint32_t maxpdist, uint32_t chunk, int n_threads, fame_pair_counters* cnt,
+                            uint64_t* n_pairs);
 /* Separate tally arrays (4 x n_cpg uint32 in device memory, zeroed), e.g. one
  * per single-cell job of a serving loop; read returns them as methLevels
  * (uint16 wrap), reset zeroes them. */
