@@ -68,7 +68,7 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_gpu_tally_alloc", "fame_gpu_tally_read", "fame_gpu_tally_free", "fame_gpu_mem_info",
            "fame_report_cpg", "fame_report_sc_header", "fame_report_sc_rows", "fame_fastq_open", "fame_fastq_read",
            "fame_fastq_close", "fame_queue_stage", "fame_queue_submit_staged", "fame_match_fastq",
-           "fame_match_fastq_paired"]
+           "fame_match_fastq_paired", "fame_index_write"]
 
 _lib = None
 
@@ -84,6 +84,7 @@ def lib(build_if_missing: bool = True):
         _build.build()
     L = C.CDLL(_build.LIB)
     L.fame_index_read.argtypes = [C.c_char_p, _P]
+    L.fame_index_write.argtypes = [_P, C.c_char_p]
     L.fame_index_build.argtypes = [C.c_uint32, C.c_uint32, _P, _P, _P, C.c_int, C.c_int, _P]
     L.fame_index_view_of.argtypes = [_P, _P]
     L.fame_index_free.argtypes = [_P]
@@ -158,6 +159,10 @@ class HostIndex:
         h = _P()
         _check(lib().fame_index_read(path.encode(), C.byref(h)))
         return cls(h)
+
+    def write(self, path: str):
+        """The --load_index format (RefGenome::save): <path> and <path>_strands."""
+        _check(lib().fame_index_write(self.h, path.encode()))
 
     @classmethod
     def build(cls, chrom_seqs, readlen: int = 100, names=None, noloss: bool = False, threads: int = 0) -> "HostIndex":

@@ -17,6 +17,8 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/fame_gpu.h"
@@ -287,7 +289,7 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
             std::vector<uint64_t> tmp_o;
             std::vector<uint32_t> tmp_off;
             std::vector<uint8_t> tmp_s;
-            std::vector<uint64_t> ks, sorted;
+            std::vector<uint64_t> ks, sorted, seen;
             std::vector<uint32_t> masks;
             std::vector<uint32_t> idx;
             for (uint64_t key = b; key < e; ++key) {
@@ -308,9 +310,17 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
                     for (uint32_t i = 0; i < n; ++i)
                         ks[i] = sorted[i] = kmer_seq(*ix, (uint32_t)(ord[s0 + i] >> 32), eoff[s0 + i], estr[s0 + i]);
                     std::sort(sorted.begin(), sorted.end());
+                    seen.clear();
                     for (uint32_t i = 0; i < n; ++i) {
                         auto r = std::equal_range(sorted.begin(), sorted.end(), ks[i]);
-                        if ((uint64_t)(r.second - r.first) >= KMERCUTOFF) { keep[s0 + i] = 0; filt[t].push_back(ks[i]); }
+                        if ((uint64_t)(r.second - r.first) >= KMERCUTOFF) {
+                            keep[s0 + i] = 0;
+                            // the set's insertion order (RefGenome.cpp:2330): first occurrence in bucket order
+                            if (std::find(seen.begin(), seen.end(), ks[i]) == seen.end()) {
+                                seen.push_back(ks[i]);
+                                filt[t].push_back(ks[i]);
+                            }
+                        }
                     }
                 }
                 // filterRedundancyInHashTable (RefGenome.cpp:2191-2264)
@@ -393,9 +403,13 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
                 }
             });
         }
-        for (auto& f : filt) ix->filtered.insert(ix->filtered.end(), f.begin(), f.end());
+        // threads hold consecutive bucket ranges: their lists in thread order are the scan order
+        for (auto& f : filt) ix->filtered_order.insert(ix->filtered_order.end(), f.begin(), f.end());
+        ix->filtered = ix->filtered_order;
         std::sort(ix->filtered.begin(), ix->filtered.end());
         ix->filtered.erase(std::unique(ix->filtered.begin(), ix->filtered.end()), ix->filtered.end());
+        ix->name_order.resize(n_chrom);
+        for (uint32_t c = 0; c < n_chrom; ++c) ix->name_order[c] = (uint8_t)c;   // readReference inserts in order
     } catch (const std::bad_alloc&) {
         delete ix;
         return FAME_ERR_NOMEM;
@@ -455,7 +469,8 @@ extern "C" int fame_index_read(const char* path, fame_host_index** out)
             n = r.get<uint64_t>();
             ix->win.resize(n); r.bytes(ix->win.data(), n * sizeof(fame_window));
             n = r.get<uint64_t>();
-            ix->filtered.resize(n); r.bytes(ix->filtered.data(), n * 8);
+            ix->filtered_order.resize(n); r.bytes(ix->filtered_order.data(), n * 8);
+            ix->filtered = ix->filtered_order;
             std::sort(ix->filtered.begin(), ix->filtered.end());
             n = r.get<uint64_t>();
             ix->names.assign(ix->seq.size(), std::string());
@@ -465,6 +480,7 @@ extern "C" int fame_index_read(const char* path, fame_host_index** out)
                 std::string s(l, '\0');
                 r.bytes(&s[0], l);
                 if (id < ix->names.size()) ix->names[id] = s;
+                ix->name_order.push_back(id);
             }
             if (!r.ok || ix->tab64.size() != HTABSIZE + 1 || ix->tab64.back() != ix->kmer.size()) rc = FAME_ERR_IO;
         }
@@ -488,6 +504,134 @@ extern "C" int fame_index_read(const char* path, fame_host_index** out)
     if (rc != FAME_OK) { delete ix; return rc; }
     *out = ix;
     return FAME_OK;
+}
+
+// ---------------------------------------------------------------------------
+// --load_index writer (RefGenome::save, RefGenome.cpp:83-228; write_strands
+// 392-413; write_filteredKmers 434-443)
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Writer {
+    FILE* f;
+    bool ok = true;
+    template <class T> void put(T v) { if (fwrite(&v, sizeof(T), 1, f) != 1) ok = false; }
+    void bytes(const void* p, uint64_t n) { if (n && fwrite(p, 1, n, f) != n) ok = false; }
+};
+
+// The reference's KmerHash (RefGenome.h:215-222): the k-mer itself.
+struct KmerIdentity {
+    size_t operator()(const uint64_t& k) const { return static_cast<size_t>(k); }
+};
+
+// Structs written as the reference writes them (raw, 8 and 16 bytes); the
+// padding bytes, uninitialised there, are zero here.
+void put_cpgs(Writer& w, const std::vector<fame_cpg>& v)
+{
+    w.put<uint64_t>(v.size());
+    std::vector<uint8_t> blk;
+    for (size_t i = 0; i < v.size(); i += 65536) {
+        const size_t n = std::min<size_t>(65536, v.size() - i);
+        blk.assign(n * 8, 0);
+        for (size_t j = 0; j < n; ++j) {
+            blk[8 * j] = v[i + j].chrom;
+            std::memcpy(&blk[8 * j + 4], &v[i + j].pos, 4);
+        }
+        w.bytes(blk.data(), blk.size());
+    }
+}
+
+}  // namespace
+
+extern "C" int fame_index_write(const fame_host_index* ix, const char* path)
+{
+    if (!ix || !path || (ix->tab32.empty() && ix->tab64.empty())) return FAME_ERR_ARG;
+    FILE* f = fopen(path, "wb");
+    if (!f) return FAME_ERR_IO;
+    std::vector<char> vbuf(8u << 20);
+    setvbuf(f, vbuf.data(), _IOFBF, vbuf.size());
+    Writer w{f};
+    try {
+        w.put<uint64_t>(HTABSIZE);
+        w.put<uint32_t>(ix->readlen);
+        w.put<uint32_t>(WINLEN);
+        w.put<uint32_t>(KMERLEN);
+        w.put<uint64_t>(KMERCUTOFF);
+        w.put<uint32_t>(SEEDBITS);
+        put_cpgs(w, ix->cpg);
+        put_cpgs(w, ix->cpg_start);
+        w.put<uint64_t>(ix->seq.size());
+        for (const auto& s : ix->seq) {
+            w.put<uint64_t>(s.size());
+            w.bytes(s.data(), s.size());
+        }
+        // tabIndex as uint64
+        w.put<uint64_t>(HTABSIZE + 1);
+        if (!ix->tab64.empty()) {
+            w.bytes(ix->tab64.data(), (HTABSIZE + 1) * 8);
+        } else {
+            std::vector<uint64_t> blk(1u << 20);
+            for (uint64_t i = 0; i <= HTABSIZE; i += blk.size()) {
+                const uint64_t n = std::min<uint64_t>(blk.size(), HTABSIZE + 1 - i);
+                for (uint64_t j = 0; j < n; ++j) blk[j] = ix->tab32[i + j];
+                w.bytes(blk.data(), n * 8);
+            }
+        }
+        // k-mers: KMER::getCore and the T mask of each (the loaded layout)
+        w.put<uint64_t>(ix->kmer.size());
+        w.bytes(ix->kmer.data(), ix->kmer.size() * sizeof(fame_kmer));
+        w.put<uint64_t>(0);   // metaCpGs: empty in the window index
+        w.put<uint64_t>(0);   // metaStartCpGs
+        w.put<uint64_t>(ix->win.size());
+        {
+            std::vector<uint8_t> blk;
+            for (size_t i = 0; i < ix->win.size(); i += 65536) {
+                const size_t n = std::min<size_t>(65536, ix->win.size() - i);
+                blk.assign(n * 16, 0);
+                for (size_t j = 0; j < n; ++j) {
+                    const fame_window& x = ix->win[i + j];
+                    std::memcpy(&blk[16 * j], &x.start_pos, 4);
+                    blk[16 * j + 4] = x.chrom;
+                    std::memcpy(&blk[16 * j + 8], &x.start_ind, 4);
+                    std::memcpy(&blk[16 * j + 12], &x.end_ind, 4);
+                }
+                w.bytes(blk.data(), blk.size());
+            }
+        }
+        // filteredKmers and chrMap in the iteration order of the reference's
+        // unordered containers: the same container types receiving the same
+        // keys in the same order iterate the same way
+        {
+            std::unordered_set<uint64_t, KmerIdentity> fk;
+            for (uint64_t k : ix->filtered_order) fk.emplace(k);
+            w.put<uint64_t>(fk.size());
+            for (uint64_t k : fk) w.put<uint64_t>(k);
+        }
+        {
+            std::unordered_map<uint8_t, std::string> cm;
+            for (uint8_t id : ix->name_order)
+                if (id < ix->names.size()) cm.insert(std::pair<uint8_t, std::string>(id, ix->names[id]));
+            w.put<uint64_t>(cm.size());
+            for (const auto& e : cm) {
+                w.put<uint8_t>(e.first);
+                w.put<uint64_t>(e.second.size());
+                w.bytes(e.second.data(), e.second.size());
+            }
+        }
+    } catch (const std::bad_alloc&) {
+        fclose(f);
+        return FAME_ERR_NOMEM;
+    }
+    if (fclose(f) != 0) w.ok = false;
+    if (!w.ok) return FAME_ERR_IO;
+    // <path>_strands: k-mer count, then the strand bits LSB first
+    FILE* g = fopen((std::string(path) + "_strands").c_str(), "wb");
+    if (!g) return FAME_ERR_IO;
+    Writer ws{g};
+    ws.put<uint64_t>(ix->kmer.size());
+    ws.bytes(ix->strand_bits.data(), (ix->kmer.size() + 7) / 8);
+    if (fclose(g) != 0) ws.ok = false;
+    return ws.ok ? FAME_OK : FAME_ERR_IO;
 }
 
 extern "C" int fame_index_view_of(const fame_host_index* cix, fame_index_view* v)

@@ -18,6 +18,8 @@ struct fame_host_index {
     std::vector<uint8_t> strand_bits;    // strandTable, LSB first
     std::vector<fame_window> win;        // metaWindows
     std::vector<uint64_t> filtered;      // filteredKmers (sorted)
+    std::vector<uint64_t> filtered_order;  // the same k-mers in the order the reference's set received them
+    std::vector<uint8_t> name_order;     // chrMap ids in the order the reference's map received them
     std::vector<const char*> seq_ptrs;   // for views
     std::vector<uint64_t> seq_lens;
     std::vector<const char*> name_ptrs;

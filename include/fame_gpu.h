@@ -105,6 +105,15 @@ int fame_index_read(const char* path, fame_host_index** out);
 int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* const* seq, const uint64_t* len,
                      const char* const* names, int noloss, int n_threads, fame_host_index** out);
 
+/* Write the index in the --load_index format to <path> and <path>_strands
+ * (RefGenome::save, RefGenome.cpp:83-228): the reference's file for the same
+ * index byte for byte, except the struct padding bytes (uninitialised there,
+ * zero here).  The filtered k-mers and the chromosome names come in the
+ * iteration order of the reference's unordered containers (libstdc++), i.e.
+ * as received from the build or from the file read.  The tabIndex section
+ * alone is 8 GiB (HTABSIZE + 1 offsets). */
+int fame_index_write(const fame_host_index* ix, const char* path);
+
 /* Borrow a view of a host index (valid until fame_index_free). */
 int fame_index_view_of(const fame_host_index* ix, fame_index_view* view);
 void fame_index_free(fame_host_index* ix);

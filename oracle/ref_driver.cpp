@@ -107,6 +107,19 @@ void* fame_ref_build(const char* fasta, int noloss)
     return r;
 }
 
+// Build the index as main.cpp does and write it with the reference's own
+// RefGenome::save (main.cpp:325-343, RefGenome.cpp:83-228).
+int fame_ref_build_save(const char* fasta, int noloss, const char* path)
+{
+    std::vector<struct CpG> cpgTab, cpgStartTab;
+    std::vector<std::vector<char>> genSeq;
+    std::unordered_map<uint8_t, std::string> chrMap;
+    readReference(fasta, cpgTab, cpgStartTab, genSeq, chrMap, false);
+    RefGenome r(std::move(cpgTab), std::move(cpgStartTab), genSeq, noloss != 0, chrMap);
+    r.save(path);
+    return 0;
+}
+
 // Load an index written by RefGenome::save (--load_index path, RefGenome.cpp:230-387).
 void* fame_ref_load(const char* path)
 {
