@@ -715,7 +715,9 @@ def run_reference(args):
         L = refbind.RefLib()
         fasta = "/tmp/fame_bench_%s.fa" % args.workload
         g.write_fasta(fasta)
+        t0 = time.time()
         ri = L.build(fasta)  # the reference's own readReference + RefGenome constructor
+        t_build = time.time() - t0
         kind = "reference"
     except Exception as e:
         emit({"impl": "reference", "unavailable": "reference build failed: %s" % e})
@@ -746,7 +748,8 @@ def run_reference(args):
         "cpu_baseline": {"value": v, "unit": "reads/s", "cores": L.corenum, "kind": kind,
                          "sample": "%d reads per step from consecutive 300k-read chunks, decided orientation"
                                    % sample},
-        "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "setup_seconds": {"index_build": t_build, "index_build_cores": L.corenum}})
     ri.close()
 
 
