@@ -11,10 +11,13 @@
 // with atomic bucket counters and restores that order with a per-bucket sort.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
+#include <memory>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -123,6 +126,12 @@ inline uint8_t base_at(const fame_host_index& ix, uint32_t c, uint64_t p)
     return p < ix.seq[c].size() ? (uint8_t)ix.seq[c][p] : 'N';  // past the chromosome end: no base
 }
 
+// Fields of the builder's 64-bit bucket entries (window 63-32, insertion
+// index 31-16, offset in the window 15-1, strand 0).
+inline uint32_t ent_win(uint64_t e) { return (uint32_t)(e >> 32); }
+inline uint32_t ent_off(uint64_t e) { return (uint32_t)(e >> 1) & 0x7fffu; }
+inline int ent_fwd(uint64_t e) { return (int)(e & 1u); }
+
 // reproduceKmerSeq (RefGenome.cpp:2028-2132)
 uint64_t kmer_seq(const fame_host_index& ix, uint32_t w, uint32_t off, int fwd)
 {
@@ -143,18 +152,60 @@ uint64_t kmer_seq(const fame_host_index& ix, uint32_t w, uint32_t off, int fwd)
     return k;
 }
 
-// reproduceTMask (RefGenome.cpp:2135-2189)
-uint32_t tmask_repro(const fame_host_index& ix, uint32_t w, uint32_t off, int fwd)
+// Per chromosome, one bit per base: 'T' most significant bit first in each
+// 64-bit word, 'A' least significant bit first; positions past the end
+// (and N) are 0, as base_at reads them.  The padding covers windows that
+// reach WINLEN past a chromosome's end.
+struct BaseBits {
+    std::vector<std::vector<uint64_t>> t_msb, a_lsb;
+
+    BaseBits(const fame_host_index& ix, int T) : t_msb(ix.seq.size()), a_lsb(ix.seq.size())
+    {
+        for (size_t c = 0; c < ix.seq.size(); ++c) {
+            const uint64_t words = (ix.seq[c].size() + 2 * WINLEN) / 64 + 2;
+            t_msb[c].assign(words, 0);
+            a_lsb[c].assign(words, 0);
+            const std::string& g = ix.seq[c];
+            const uint64_t full = g.size() / 64 + 1;
+            parallel_for(full, T, [&](uint64_t b, uint64_t e, int) {
+                for (uint64_t wd = b; wd < e; ++wd) {
+                    uint64_t t = 0, a = 0;
+                    const uint64_t p0 = wd * 64, p1 = std::min<uint64_t>(p0 + 64, g.size());
+                    for (uint64_t p = p0; p < p1; ++p) {
+                        if (g[p] == 'T') t |= 1ull << (63 - (p - p0));
+                        else if (g[p] == 'A') a |= 1ull << (p - p0);
+                    }
+                    t_msb[c][wd] = t;
+                    a_lsb[c][wd] = a;
+                }
+            });
+        }
+    }
+    // bit 31 - i: 'T' at s + i, i < 32
+    uint32_t t_fwd(uint32_t c, uint64_t s) const
+    {
+        const std::vector<uint64_t>& b = t_msb[c];
+        const uint64_t w = s >> 6, r = s & 63;
+        const uint64_t x = r ? (b[w] << r) | (b[w + 1] >> (64 - r)) : b[w];
+        return (uint32_t)(x >> 32);
+    }
+    // bit j: 'A' at s + j, j < 32
+    uint32_t a_lo(uint32_t c, uint64_t s) const
+    {
+        const std::vector<uint64_t>& b = a_lsb[c];
+        const uint64_t w = s >> 6, r = s & 63;
+        const uint64_t x = r ? (b[w] >> r) | (b[w + 1] << (64 - r)) : b[w];
+        return (uint32_t)x;
+    }
+};
+
+// reproduceTMask (RefGenome.cpp:2135-2189): forward, bit 31 - i is 'T' at
+// s0 + i; reverse, bit 31 - i is 'A' at s0 + 31 - i, i.e. bit j is 'A' at s0 + j.
+uint32_t tmask_repro(const fame_host_index& ix, const BaseBits& bb, uint32_t w, uint32_t off, int fwd)
 {
     const uint32_t c = ix.win[w].chrom;
     const uint64_t s0 = (uint64_t)ix.win[w].start_pos + off;
-    uint32_t t = 0;
-    for (unsigned i = 0; i < KMERLEN; ++i) {
-        t <<= 1;
-        if (fwd) { if (base_at(ix, c, s0 + i) == 'T') t |= 1; }
-        else { if (base_at(ix, c, s0 + KMERLEN - 1 - i) == 'A') t |= 1; }
-    }
-    return t;
+    return fwd ? bb.t_fwd(c, s0) : bb.a_lo(c, s0);
 }
 
 }  // namespace
@@ -170,6 +221,16 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
     int T = n_threads > 0 ? n_threads : (int)std::max(1u, std::thread::hardware_concurrency());
     fame_host_index* ix = new (std::nothrow) fame_host_index();
     if (!ix) return FAME_ERR_NOMEM;
+    // FAME_INDEX_TIMING set: the wall time of each phase on stderr
+    const bool timing = std::getenv("FAME_INDEX_TIMING") != nullptr;
+    auto t_last = std::chrono::steady_clock::now();
+    auto phase = [&](const char* name) {
+        if (!timing) return;
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "fame_index_build: %-22s %8.2f s\n", name,
+                     std::chrono::duration<double>(now - t_last).count());
+        t_last = now;
+    };
     try {
         ix->readlen = readlen;
         ix->seq.resize(n_chrom);
@@ -206,6 +267,7 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
             ix->cpg.insert(ix->cpg.end(), cpg[c].begin(), cpg[c].end());
             ix->cpg_start.insert(ix->cpg_start.end(), cpgs[c].begin(), cpgs[c].end());
         }
+        phase("sequences, CpGs");
         // generateWindows (RefGenome.cpp:532-567); cpgTable[ci] is read even at
         // ci == size there, which this treats as "no CpG".
         {
@@ -227,8 +289,11 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
             }
         }
         const uint64_t nwin = ix->win.size();
+        const BaseBits bb(*ix, T);
+        phase("windows");
         // pass 1: bucket sizes (estimateTablesizes) and per-window entry counts
-        std::vector<uint32_t> cnt(HTABSIZE + 1, 0);
+        std::unique_ptr<uint32_t[]> cnt(new uint32_t[HTABSIZE + 1]);
+        parallel_for(HTABSIZE + 1, T, [&](uint64_t b, uint64_t e, int) { std::memset(&cnt[b], 0, (e - b) * 4); });
         std::vector<uint32_t> wcount(nwin, 0);
         parallel_for(nwin, T, [&](uint64_t b, uint64_t e, int) {
             std::vector<uint8_t> red(WINLEN), redr(WINLEN);
@@ -242,6 +307,7 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
                 wcount[w] = k;
             }
         });
+        phase("pass 1 (count)");
         // bucket starts
         uint64_t total = 0;
         {
@@ -254,17 +320,19 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
             for (int t = 0; t < T; ++t) part[t + 1] += part[t];
             total = part[T];
             if (total >= 0xffffffffull) { delete ix; return FAME_ERR_INDEX; }
-            ix->tab32.assign(HTABSIZE + 1, 0);
+            ix->tab32.resize(HTABSIZE + 1);   // no zero fill: every entry is written below
             parallel_for(HTABSIZE, T, [&](uint64_t b, uint64_t e, int t) {
                 uint64_t s = part[t];
                 for (uint64_t i = b; i < e; ++i) { ix->tab32[i] = (uint32_t)s; s += cnt[i]; cnt[i] = (uint32_t)(s - cnt[i]); }
             });
             ix->tab32[HTABSIZE] = (uint32_t)total;
         }
-        // pass 2: fill with atomic cursors; order key = (window, position in window)
-        std::vector<uint64_t> ord(total);
-        std::vector<uint32_t> eoff(total);
-        std::vector<uint8_t> estr(total);
+        phase("bucket starts");
+        // pass 2: fill with atomic cursors.  One 64-bit entry per k-mer:
+        // window (bits 63-32) and its index in the window's insertion order
+        // (31-16), which order the bucket, then the offset in the window
+        // (15-1) and the strand (0).
+        std::unique_ptr<uint64_t[]> ent(new uint64_t[total]);
         parallel_for(nwin, T, [&](uint64_t b, uint64_t e, int) {
             std::vector<uint8_t> red(WINLEN), redr(WINLEN);
             std::vector<uint32_t> iv(2 * (WINLEN + 2));
@@ -272,43 +340,34 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
                 uint32_t k = 0;
                 window_kmers(*ix, w, red.data(), redr.data(), iv.data(), [&](uint32_t key, uint32_t off, int strand) {
                     const uint32_t slot = __atomic_fetch_add(&cnt[key], 1u, __ATOMIC_RELAXED);
-                    ord[slot] = (w << 32) | k;
-                    eoff[slot] = off;
-                    estr[slot] = (uint8_t)strand;
-                    ++k;
+                    ent[slot] = (w << 32) | ((uint64_t)k << 16) | ((uint64_t)off << 1) | (uint64_t)strand;
+                    ++k;   // at most 2 * WINLEN k-mers per window: 16 bits
                 });
             }
         });
-        std::vector<uint32_t>().swap(cnt);
+        cnt.reset();
+        phase("pass 2 (fill)");
         // per bucket: reverse insertion order, then the two filters.  keep[i]
         // marks survivors; filtered k-mer sequences are collected per thread.
-        std::vector<uint8_t> keep(total, 1);
+        std::unique_ptr<uint8_t[]> keep(new uint8_t[total]);
         std::vector<std::vector<uint64_t>> filt(T);
-        std::vector<uint32_t> newlen(HTABSIZE, 0);
+        std::unique_ptr<uint32_t[]> newlen(new uint32_t[HTABSIZE]);
         parallel_for(HTABSIZE, T, [&](uint64_t b, uint64_t e, int t) {
-            std::vector<uint64_t> tmp_o;
-            std::vector<uint32_t> tmp_off;
-            std::vector<uint8_t> tmp_s;
             std::vector<uint64_t> ks, sorted, seen;
             std::vector<uint32_t> masks;
-            std::vector<uint32_t> idx;
             for (uint64_t key = b; key < e; ++key) {
                 const uint32_t s0 = ix->tab32[key], s1 = ix->tab32[key + 1];
                 const uint32_t n = s1 - s0;
+                newlen[key] = 0;
                 if (n == 0) continue;
-                if (n > 1) {
-                    idx.resize(n);
-                    for (uint32_t i = 0; i < n; ++i) idx[i] = i;
-                    std::sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) { return ord[s0 + x] > ord[s0 + y]; });
-                    tmp_o.resize(n); tmp_off.resize(n); tmp_s.resize(n);
-                    for (uint32_t i = 0; i < n; ++i) { tmp_o[i] = ord[s0 + idx[i]]; tmp_off[i] = eoff[s0 + idx[i]]; tmp_s[i] = estr[s0 + idx[i]]; }
-                    for (uint32_t i = 0; i < n; ++i) { ord[s0 + i] = tmp_o[i]; eoff[s0 + i] = tmp_off[i]; estr[s0 + i] = tmp_s[i]; }
-                }
+                uint64_t* E = &ent[s0];
+                if (n > 1) std::sort(E, E + n, std::greater<uint64_t>());   // reverse insertion order
+                std::memset(&keep[s0], 1, n);
                 // filterHashTable (RefGenome.cpp:2267-2352)
                 if (!noloss && n >= KMERCUTOFF) {
                     ks.resize(n); sorted.resize(n);
                     for (uint32_t i = 0; i < n; ++i)
-                        ks[i] = sorted[i] = kmer_seq(*ix, (uint32_t)(ord[s0 + i] >> 32), eoff[s0 + i], estr[s0 + i]);
+                        ks[i] = sorted[i] = kmer_seq(*ix, ent_win(E[i]), ent_off(E[i]), ent_fwd(E[i]));
                     std::sort(sorted.begin(), sorted.end());
                     seen.clear();
                     for (uint32_t i = 0; i < n; ++i) {
@@ -330,9 +389,9 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
                 uint32_t kept = 0;
                 for (uint32_t i = 0; i < n; ++i) {
                     if (!keep[s0 + i]) continue;
-                    const uint32_t w = (uint32_t)(ord[s0 + i] >> 32);
-                    const int fwd = estr[s0 + i];
-                    const uint32_t tm = tmask_repro(*ix, w, eoff[s0 + i], fwd);
+                    const uint32_t w = ent_win(E[i]);
+                    const int fwd = ent_fwd(E[i]);
+                    const uint32_t tm = tmask_repro(*ix, bb, w, ent_off(E[i]), fwd);
                     if (w != prevMeta || fwd != prevFwd) {
                         masks.clear();
                         masks.push_back(tm);
@@ -349,6 +408,7 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
                 newlen[key] = kept;
             }
         });
+        phase("bucket order, filters");
         // compaction
         uint64_t nk = 0;
         {
@@ -377,17 +437,19 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
                     ix->tab32[key] = (uint32_t)o;
                     for (uint32_t i = s0; i < s1; ++i) {
                         if (!keep[i]) continue;
-                        ix->kmer[o].meta = (uint32_t)(ord[i] >> 32);
-                        kstr[o] = estr[i];
-                        koff[o] = eoff[i];
+                        ix->kmer[o].meta = ent_win(ent[i]);
+                        kstr[o] = (uint8_t)ent_fwd(ent[i]);
+                        koff[o] = ent_off(ent[i]);
                         ++o;
                     }
                 }
             });
             ix->tab32[HTABSIZE] = (uint32_t)nk;
+            phase("compaction");
             // strandTable
             ix->strand_bits.assign((nk + 7) / 8, 0);
             for (uint64_t i = 0; i < nk; ++i) if (kstr[i]) ix->strand_bits[i >> 3] |= (uint8_t)(1u << (i & 7));
+            phase("strand bits");
             // getTMask at save time (RefGenome.h:62-100): strand taken at
             // strandTable[window id]; the reverse loop skips base 0.
             parallel_for(nk, T, [&](uint64_t b, uint64_t e, int) {
@@ -396,13 +458,14 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
                     const uint32_t c = ix->win[w].chrom;
                     const uint64_t s0 = (uint64_t)ix->win[w].start_pos + koff[k];
                     const int fwd = w < nk ? kstr[w] : 0;
-                    uint32_t tm = 0;
-                    if (fwd) { for (unsigned i = 0; i < KMERLEN; ++i) { tm <<= 1; if (base_at(*ix, c, s0 + i) == 'T') tm |= 1; } }
-                    else { for (unsigned i = KMERLEN - 1; i > 0; --i) { tm <<= 1; if (base_at(*ix, c, s0 + i) == 'A') tm |= 1; } }
+                    // forward: bit 31 - i is 'T' at s0 + i; reverse (i = 31 .. 1):
+                    // bit i - 1 is 'A' at s0 + i, bit 31 stays 0
+                    const uint32_t tm = fwd ? bb.t_fwd(c, s0) : (bb.a_lo(c, s0 + 1) & 0x7fffffffu);
                     ix->kmer[k].tmask = tm;
                 }
             });
         }
+        phase("T masks");
         // threads hold consecutive bucket ranges: their lists in thread order are the scan order
         for (auto& f : filt) ix->filtered_order.insert(ix->filtered_order.end(), f.begin(), f.end());
         ix->filtered = ix->filtered_order;
@@ -410,6 +473,7 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
         ix->filtered.erase(std::unique(ix->filtered.begin(), ix->filtered.end()), ix->filtered.end());
         ix->name_order.resize(n_chrom);
         for (uint32_t c = 0; c < n_chrom; ++c) ix->name_order[c] = (uint8_t)c;   // readReference inserts in order
+        phase("filtered set");
     } catch (const std::bad_alloc&) {
         delete ix;
         return FAME_ERR_NOMEM;
