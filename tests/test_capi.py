@@ -44,6 +44,11 @@ def test_argument_errors_without_gpu():
     assert L.fame_gpu_tally_alloc(None, None) == -1
     assert L.fame_gpu_tally_read(None, None, None, 0) == -1
     assert L.fame_gpu_mem_info(None, None, None) == -1
+    assert L.fame_queue_stage(None, None, None, None, None, None) == -1
+    assert L.fame_queue_submit_staged(None, 0, 0, 0, None) == -1
+    assert L.fame_match_fastq(None, b"x.fq", 0, 0, 0, 2, 0, None, None, None) == -1
+    assert L.fame_match_fastq_paired(None, b"1.fq", b"2.fq", 0, 0, 550, 0, 0, None, None) == -1
+    assert L.fame_index_write(None, b"x.idx") == -1
 
 
 def test_index_read_errors(tmp_path):
