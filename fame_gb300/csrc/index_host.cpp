@@ -421,8 +421,8 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
             for (int t = 0; t < T; ++t) part[t + 1] += part[t];
             nk = part[T];
             ix->kmer.resize(nk);
-            std::vector<uint8_t> kstr(nk);
-            std::vector<uint32_t> koff(nk);
+            std::vector<uint8_t, NoInitAlloc<uint8_t>> kstr(nk);     // every entry written below
+            std::vector<uint32_t, NoInitAlloc<uint32_t>> koff(nk);
             // the old start of each thread's first key after its range, read
             // before any thread rewrites tab32 (same partition as parallel_for)
             std::vector<uint32_t> bound(T, 0);
@@ -447,8 +447,15 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
             ix->tab32[HTABSIZE] = (uint32_t)nk;
             phase("compaction");
             // strandTable
-            ix->strand_bits.assign((nk + 7) / 8, 0);
-            for (uint64_t i = 0; i < nk; ++i) if (kstr[i]) ix->strand_bits[i >> 3] |= (uint8_t)(1u << (i & 7));
+            ix->strand_bits.resize((nk + 7) / 8);
+            parallel_for((nk + 7) / 8, T, [&](uint64_t b, uint64_t e, int) {
+                for (uint64_t j = b; j < e; ++j) {
+                    uint8_t v = 0;
+                    for (uint64_t i = 8 * j; i < std::min<uint64_t>(8 * j + 8, nk); ++i)
+                        if (kstr[i]) v |= (uint8_t)(1u << (i & 7));
+                    ix->strand_bits[j] = v;
+                }
+            });
             phase("strand bits");
             // getTMask at save time (RefGenome.h:62-100): strand taken at
             // strandTable[window id]; the reverse loop skips base 0.
