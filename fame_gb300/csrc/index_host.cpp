@@ -292,7 +292,7 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
         const BaseBits bb(*ix, T);
         phase("windows");
         // pass 1: bucket sizes (estimateTablesizes) and per-window entry counts
-        std::unique_ptr<uint32_t[]> cnt(new uint32_t[HTABSIZE + 1]);
+        BigVec<uint32_t> cnt(HTABSIZE + 1);
         parallel_for(HTABSIZE + 1, T, [&](uint64_t b, uint64_t e, int) { std::memset(&cnt[b], 0, (e - b) * 4); });
         std::vector<uint32_t> wcount(nwin, 0);
         parallel_for(nwin, T, [&](uint64_t b, uint64_t e, int) {
@@ -332,7 +332,7 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
         // window (bits 63-32) and its index in the window's insertion order
         // (31-16), which order the bucket, then the offset in the window
         // (15-1) and the strand (0).
-        std::unique_ptr<uint64_t[]> ent(new uint64_t[total]);
+        BigVec<uint64_t> ent(total);
         parallel_for(nwin, T, [&](uint64_t b, uint64_t e, int) {
             std::vector<uint8_t> red(WINLEN), redr(WINLEN);
             std::vector<uint32_t> iv(2 * (WINLEN + 2));
@@ -345,13 +345,13 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
                 });
             }
         });
-        cnt.reset();
+        BigVec<uint32_t>().swap(cnt);
         phase("pass 2 (fill)");
         // per bucket: reverse insertion order, then the two filters.  keep[i]
         // marks survivors; filtered k-mer sequences are collected per thread.
-        std::unique_ptr<uint8_t[]> keep(new uint8_t[total]);
+        BigVec<uint8_t> keep(total);
         std::vector<std::vector<uint64_t>> filt(T);
-        std::unique_ptr<uint32_t[]> newlen(new uint32_t[HTABSIZE]);
+        BigVec<uint32_t> newlen(HTABSIZE);
         parallel_for(HTABSIZE, T, [&](uint64_t b, uint64_t e, int t) {
             std::vector<uint64_t> ks, sorted, seen;
             std::vector<uint32_t> masks;
@@ -421,8 +421,8 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
             for (int t = 0; t < T; ++t) part[t + 1] += part[t];
             nk = part[T];
             ix->kmer.resize(nk);
-            std::vector<uint8_t, NoInitAlloc<uint8_t>> kstr(nk);     // every entry written below
-            std::vector<uint32_t, NoInitAlloc<uint32_t>> koff(nk);
+            BigVec<uint8_t> kstr(nk);     // every entry written below
+            BigVec<uint32_t> koff(nk);
             // the old start of each thread's first key after its range, read
             // before any thread rewrites tab32 (same partition as parallel_for)
             std::vector<uint32_t> bound(T, 0);
