@@ -18,6 +18,7 @@
 #include <cstring>
 #include <functional>
 #include <memory>
+#include <stdexcept>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -530,6 +531,7 @@ extern "C" int fame_index_read(const char* path, fame_host_index** out)
             ix->seq.resize(n);
             for (auto& s : ix->seq) { uint64_t l = r.get<uint64_t>(); s.resize(l); r.bytes(&s[0], l); }
             n = r.get<uint64_t>();
+            if (n != HTABSIZE + 1) throw std::length_error("tabIndex size");
             ix->tab64.resize(n); r.bytes(ix->tab64.data(), n * 8);
             n = r.get<uint64_t>();
             ix->kmer.resize(n); r.bytes(ix->kmer.data(), n * sizeof(fame_kmer));
@@ -557,6 +559,8 @@ extern "C" int fame_index_read(const char* path, fame_host_index** out)
         }
     } catch (const std::bad_alloc&) {
         rc = FAME_ERR_NOMEM;
+    } catch (const std::exception&) {   // a size field no index file can hold
+        rc = FAME_ERR_IO;
     }
     fclose(f);
     if (rc == FAME_OK) {

@@ -50,7 +50,7 @@ struct fame_host_index {
     std::vector<fame_cpg> cpg;           // cpgTable
     std::vector<fame_cpg> cpg_start;     // cpgStartTable
     BigVec<uint32_t> tab32;              // tabIndex as uint32 (HTABSIZE + 1)
-    std::vector<uint64_t> tab64;         // or as read from a file (uint64)
+    BigVec<uint64_t> tab64;              // or as read from a file (uint64)
     BigVec<fame_kmer> kmer;              // kmerTableSmall
     std::vector<uint8_t> strand_bits;    // strandTable, LSB first
     std::vector<fame_window> win;        // metaWindows

@@ -63,6 +63,9 @@ def test_index_read_errors(tmp_path):
     trunc = tmp_path / "trunc.idx"
     trunc.write_bytes(hdr + struct.pack("<Q", 5))   # announces 5 CpGs, ends there
     assert L.fame_index_read(str(trunc).encode(), C.byref(h)) == -6
+    huge = tmp_path / "huge.idx"
+    huge.write_bytes(hdr + struct.pack("<Q", 1 << 62))   # a CpG count no file can hold
+    assert L.fame_index_read(str(huge).encode(), C.byref(h)) in (-3, -6)
     wrongseed = tmp_path / "seed.idx"
     wrongseed.write_bytes(struct.pack("<QIIIQI", 1 << 30, 100, 2048, 32, 1500, 0x12345678))
     assert L.fame_index_read(str(wrongseed).encode(), C.byref(h)) == -6
