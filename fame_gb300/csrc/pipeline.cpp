@@ -14,8 +14,8 @@
 // batched queue (its page-locked staging), so the host parses chunk i + 1
 // while the GPU matches chunks i, i - 1, ...
 // Paired-end: two page-locked chunk buffers per mate file; a host thread
-// parses the next chunk of both files into one while fame_gpu_match_pairs
-// runs on the other.
+// parses the next chunk of both files (one reader thread each) into one
+// while fame_gpu_match_pairs runs on the other.
 #include <cstdint>
 #include <deque>
 #include <thread>
@@ -153,14 +153,19 @@ struct PairChunk {
     uint32_t n = 0;
 };
 
-// The next chunk of both mate files (parseChunk of the two-file ReadQueue).
-// Returns a FAME code and, on failure, the reason in *why (the caller's
-// thread records it in the context).
+// The next chunk of both mate files (parseChunk of the two-file ReadQueue),
+// the two files read at the same time (each reader has its own threads; for
+// gzip input each file is inflated on its own thread).  Returns a FAME code
+// and, on failure, the reason in *why (the caller's thread records it in the
+// context).
 int parse_pairs(PairFiles& pf, PairChunk& c, uint32_t chunk, uint64_t cap, const char** why)
 {
     uint32_t n[2] = {0, 0};
-    for (int m = 0; m < 2; ++m) {
-        const int rc = fame_fastq_read(pf.f[m], chunk, c.s[m], cap, c.o[m], &n[m]);
+    int rcm[2] = {FAME_OK, FAME_OK};
+    std::thread second([&] { rcm[1] = fame_fastq_read(pf.f[1], chunk, c.s[1], cap, c.o[1], &n[1]); });
+    rcm[0] = fame_fastq_read(pf.f[0], chunk, c.s[0], cap, c.o[0], &n[0]);
+    second.join();
+    for (int rc : rcm) {
         if (rc) {
             *why = rc == FAME_ERR_ARG ? "FASTQ chunk larger than the buffer (reads over 255 bases)" : "FASTQ read failed";
             return rc;

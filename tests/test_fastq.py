@@ -110,3 +110,26 @@ def test_reader_empty_and_tiny(tmp_path):
     blank = tmp_path / "blank.fq"
     blank.write_bytes(b"\n\n\n\n\n\n")     # empty lines are lines: two records of empty sequences
     assert read_all(blank, False, 10, 2) == [b"", b""]
+
+
+@pytest.mark.parametrize("gz", [False, True])
+def test_two_readers_at_once(tmp_path, gz):
+    """Two readers used from two threads at the same time (the paired
+    pipeline reads both mate files so) give each file's records."""
+    import threading
+    rng = np.random.default_rng(11)
+    recs = [records(rng, 1500), records(rng, 1500)]
+    paths = [tmp_path / ("m%d.fq%s" % (m, ".gz" if gz else "")) for m in (1, 2)]
+    for p, r in zip(paths, recs):
+        write(p, r, gz=gz)
+    got = [None, None]
+
+    def run(m):
+        got[m] = read_all(paths[m], gz, 400, 3)
+
+    th = [threading.Thread(target=run, args=(m,)) for m in (0, 1)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert got == [[s for _, s, _, _ in r] for r in recs]
