@@ -699,11 +699,73 @@ def cpu_baseline_pe(hi, s1, o1, s2, o2, chunks, sample):
         return {"value": None, "unit": "pairs/s", "cores": 1, "kind": "port", "sample": "reference unavailable (%s)" % e}
 
 
+def run_reference_pe(args, L):
+    """The paired workload through the reference's matchPairedReads (bounded
+    samples of consecutive chunks, decided orientation), pairs/s."""
+    from fame_gb300 import CHUNKSIZE
+    g, r1, r2 = make_pair_workload(args.workload, args.reads)
+    fasta = "/tmp/fame_bench_%s.fa" % args.workload
+    g.write_fasta(fasta)
+    t0 = time.time()
+    ri = L.build(fasta)
+    t_build = time.time() - t0
+    s1, o1 = r1.concat()
+    s2, o2 = r2.concat()
+    n = len(o1) - 1
+    sample = min(args.cpu_sample, CHUNKSIZE)
+    starts = list(range(CHUNKSIZE, n, CHUNKSIZE)) or [0]
+
+    def step(k):
+        c0 = starts[k % len(starts)]
+        nn = min(sample, n - c0)
+        p1 = o1[c0:c0 + nn + 1]
+        p2 = o2[c0:c0 + nn + 1]
+        secs, _ = ri.time_pe(s1[int(p1[0]):int(p1[-1])], p1 - p1[0], s2[int(p2[0]):int(p2[-1])], p2 - p2[0],
+                             both_strands=False, match_r1_fwd=True)
+        return secs, nn
+
+    for k in range(args.warmup):
+        step(k)
+    secs = 0.0
+    pairs = 0
+    for k in range(args.steps):
+        s_, nn = step(k)
+        secs += s_
+        pairs += nn
+    v = pairs / secs
+    emit({
+        "impl": "reference", "metric": "aligned pairs/s (paired-end matching stage, bit-exact CpG report)",
+        "value": v, "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u8/u64 integer", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "pairs_per_step": sample, "maxpdist": L.maxpdist()},
+        "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": L.corenum, "kind": "reference",
+                         "sample": "%d pairs per step from consecutive 300k-pair chunks, decided orientation"
+                                   % sample},
+        "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "setup_seconds": {"index_build": t_build, "index_build_cores": L.corenum}})
+    ri.close()
+
+
 def run_reference(args):
     rank, world, local = dist_init(args.gpus)
     if rank != 0:
         return
     from fame_gb300 import CHUNKSIZE, HostIndex
+    if args.workload.startswith("pe"):
+        try:
+            from oracle import refbind
+            if not refbind.available():
+                import __graft_entry__
+                __graft_entry__.build()
+            if not refbind.available():
+                raise RuntimeError("reference sources not available to oracle/build_ref.sh")
+            L = refbind.RefLib()
+        except Exception as e:
+            emit({"impl": "reference", "unavailable": "reference build failed: %s" % e})
+            return
+        run_reference_pe(args, L)
+        return
     g, rs, readlen = make_workload(args.workload, args.reads)
     try:
         from oracle import refbind
