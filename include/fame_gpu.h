@@ -188,7 +188,10 @@ int fame_gpu_tallies(fame_gpu* g, uint16_t* meth, int reset);
  * sequences of up to max_reads records back to back into seqs (seq_cap bytes;
  * FAME_ERR_ARG when they do not fit) with offsets offs[n + 1], and returns the
  * record count in *n (0 at the end of the input); parsing is spread over
- * n_threads host threads (<= 0: up to 16). */
+ * n_threads host threads (<= 0: up to 16).  A plain regular file is mapped
+ * and parsed in place (it must not shrink while open); gzip input and pipes
+ * are read through a buffer.  Different readers may be used from different
+ * threads at the same time. */
 typedef struct fame_fastq fame_fastq;
 int fame_fastq_open(const char* path, int is_gz, int n_threads, fame_fastq** out);
 int fame_fastq_read(fame_fastq* f, uint32_t max_reads, char* seqs, uint64_t seq_cap, uint64_t* offs, uint32_t* n);
