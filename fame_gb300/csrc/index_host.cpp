@@ -352,14 +352,14 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
         // marks survivors; filtered k-mer sequences are collected per thread.
         BigVec<uint8_t> keep(total);
         std::vector<std::vector<uint64_t>> filt(T);
-        BigVec<uint32_t> newlen(HTABSIZE);
+        std::vector<uint64_t> kept_in(T + 1, 0);   // survivors per thread range (the compaction's partition)
         parallel_for(HTABSIZE, T, [&](uint64_t b, uint64_t e, int t) {
             std::vector<uint64_t> ks, sorted, seen;
             std::vector<uint32_t> masks;
+            uint64_t kept_sum = 0;
             for (uint64_t key = b; key < e; ++key) {
                 const uint32_t s0 = ix->tab32[key], s1 = ix->tab32[key + 1];
                 const uint32_t n = s1 - s0;
-                newlen[key] = 0;
                 if (n == 0) continue;
                 uint64_t* E = &ent[s0];
                 if (n > 1) std::sort(E, E + n, std::greater<uint64_t>());   // reverse insertion order
@@ -406,19 +406,15 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
                         keep[s0 + i] = 0;
                     }
                 }
-                newlen[key] = kept;
+                kept_sum += kept;
             }
+            kept_in[t + 1] = kept_sum;
         });
         phase("bucket order, filters");
         // compaction
         uint64_t nk = 0;
         {
-            std::vector<uint64_t> part(T + 1, 0);
-            parallel_for(HTABSIZE, T, [&](uint64_t b, uint64_t e, int t) {
-                uint64_t s = 0;
-                for (uint64_t i = b; i < e; ++i) s += newlen[i];
-                part[t + 1] = s;
-            });
+            std::vector<uint64_t> part(kept_in);
             for (int t = 0; t < T; ++t) part[t + 1] += part[t];
             nk = part[T];
             ix->kmer.resize(nk);
