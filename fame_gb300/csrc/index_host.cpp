@@ -9,6 +9,8 @@
 // being window, then N-free interval, then reverse strand before forward,
 // then k-mer position.  It parallelises the two hashing passes over windows
 // with atomic bucket counters and restores that order with a per-bucket sort.
+#include <unistd.h>
+
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -528,7 +530,24 @@ extern "C" int fame_index_read(const char* path, fame_host_index** out)
             for (auto& s : ix->seq) { uint64_t l = r.get<uint64_t>(); s.resize(l); r.bytes(&s[0], l); }
             n = r.get<uint64_t>();
             if (n != HTABSIZE + 1) throw std::length_error("tabIndex size");
-            ix->tab64.resize(n); r.bytes(ix->tab64.data(), n * 8);
+            ix->tab64.resize(n);
+            {
+                // the 8 GiB table: read by several threads at their own offsets
+                const off_t at = ftello(f);
+                const uint64_t bytes = n * 8;
+                const int T = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+                std::atomic<bool> good{at >= 0};
+                char* dst = reinterpret_cast<char*>(ix->tab64.data());
+                parallel_for(bytes, T, [&](uint64_t b, uint64_t e, int) {
+                    while (b < e && good.load(std::memory_order_relaxed)) {
+                        const ssize_t got = pread(fileno(f), dst + b, (size_t)std::min<uint64_t>(e - b, 1ull << 30),
+                                                  at + (off_t)b);
+                        if (got <= 0) { good = false; break; }
+                        b += (uint64_t)got;
+                    }
+                });
+                if (!good || fseeko(f, at + (off_t)bytes, SEEK_SET) != 0) r.ok = false;
+            }
             n = r.get<uint64_t>();
             ix->kmer.resize(n); r.bytes(ix->kmer.data(), n * sizeof(fame_kmer));
             uint64_t m = r.get<uint64_t>();      // metaCpGs (unused by the window index)
