@@ -657,15 +657,33 @@ extern "C" int fame_index_write(const fame_host_index* ix, const char* path)
         }
         // tabIndex as uint64
         w.put<uint64_t>(HTABSIZE + 1);
-        if (!ix->tab64.empty()) {
-            w.bytes(ix->tab64.data(), (HTABSIZE + 1) * 8);
-        } else {
-            std::vector<uint64_t> blk(1u << 20);
-            for (uint64_t i = 0; i <= HTABSIZE; i += blk.size()) {
-                const uint64_t n = std::min<uint64_t>(blk.size(), HTABSIZE + 1 - i);
-                for (uint64_t j = 0; j < n; ++j) blk[j] = ix->tab32[i + j];
-                w.bytes(blk.data(), n * 8);
-            }
+        {
+            // the 8 GiB table: written by several threads at their own offsets
+            const off_t at = (fflush(f) == 0) ? ftello(f) : (off_t)-1;
+            const uint64_t n = HTABSIZE + 1;
+            const int T = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+            std::atomic<bool> good{at >= 0};
+            parallel_for(n, T, [&](uint64_t b, uint64_t e, int) {
+                std::vector<uint64_t> blk(1u << 20);
+                for (uint64_t i = b; i < e && good.load(std::memory_order_relaxed); i += blk.size()) {
+                    const uint64_t m = std::min<uint64_t>(blk.size(), e - i);
+                    const uint64_t* src = blk.data();
+                    if (!ix->tab64.empty()) {
+                        src = ix->tab64.data() + i;
+                    } else {
+                        for (uint64_t j = 0; j < m; ++j) blk[j] = ix->tab32[i + j];
+                    }
+                    const char* p = reinterpret_cast<const char*>(src);
+                    uint64_t left = m * 8, done = 0;
+                    while (left) {
+                        const ssize_t put = pwrite(fileno(f), p + done, (size_t)left, at + (off_t)(8 * i + done));
+                        if (put <= 0) { good = false; break; }
+                        done += (uint64_t)put;
+                        left -= (uint64_t)put;
+                    }
+                }
+            });
+            if (!good || fseeko(f, at + (off_t)(n * 8), SEEK_SET) != 0) w.ok = false;
         }
         // k-mers: KMER::getCore and the T mask of each (the loaded layout)
         w.put<uint64_t>(ix->kmer.size());
