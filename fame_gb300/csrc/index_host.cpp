@@ -294,21 +294,16 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
         const uint64_t nwin = ix->win.size();
         const BaseBits bb(*ix, T);
         phase("windows");
-        // pass 1: bucket sizes (estimateTablesizes) and per-window entry counts
+        // pass 1: bucket sizes (estimateTablesizes)
         BigVec<uint32_t> cnt(HTABSIZE + 1);
         parallel_for(HTABSIZE + 1, T, [&](uint64_t b, uint64_t e, int) { std::memset(&cnt[b], 0, (e - b) * 4); });
-        std::vector<uint32_t> wcount(nwin, 0);
         parallel_for(nwin, T, [&](uint64_t b, uint64_t e, int) {
             std::vector<uint8_t> red(WINLEN), redr(WINLEN);
             std::vector<uint32_t> iv(2 * (WINLEN + 2));
-            for (uint64_t w = b; w < e; ++w) {
-                uint32_t k = 0;
+            for (uint64_t w = b; w < e; ++w)
                 window_kmers(*ix, w, red.data(), redr.data(), iv.data(), [&](uint32_t key, uint32_t, int) {
                     __atomic_fetch_add(&cnt[key], 1u, __ATOMIC_RELAXED);
-                    ++k;
                 });
-                wcount[w] = k;
-            }
         });
         phase("pass 1 (count)");
         // bucket starts
