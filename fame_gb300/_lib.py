@@ -40,7 +40,8 @@ class IndexView(C.Structure):
 
 class Counters(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("succ", "nonunique", "unsucc", "r1_fwd", "r1_rev", "invalid_len",
-                                          "invalid_n", "gather_bytes", "windows_scanned", "dp_reads")]
+                                          "invalid_n", "gather_bytes", "windows_scanned", "dp_reads", "heavy_tasks",
+                                          "reruns")]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -68,7 +69,7 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_gpu_tally_alloc", "fame_gpu_tally_read", "fame_gpu_tally_free", "fame_gpu_mem_info",
            "fame_report_cpg", "fame_report_sc_header", "fame_report_sc_rows", "fame_fastq_open", "fame_fastq_read",
            "fame_fastq_close", "fame_queue_stage", "fame_queue_submit_staged", "fame_match_fastq",
-           "fame_match_fastq_paired", "fame_index_write"]
+           "fame_match_fastq_paired", "fame_index_write", "fame_gpu_index_bytes", "fame_queue_wait"]
 
 _lib = None
 
@@ -107,11 +108,14 @@ def lib(build_if_missing: bool = True):
     L.fame_gpu_set_timing.argtypes = [_P, C.c_int]
     L.fame_gpu_stage_times.argtypes = [_P, _P, C.c_int]
     L.fame_gpu_last_launches.argtypes = [_P]
+    L.fame_gpu_index_bytes.argtypes = [_P]
+    L.fame_gpu_index_bytes.restype = C.c_uint64
     L.fame_gpu_match_pairs.argtypes = [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]
     L.fame_gpu_match_pairs_dev.argtypes = [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P]
     L.fame_queue_open.argtypes = [_P, C.c_uint32, C.c_uint32, C.c_uint64, _P]
     L.fame_queue_submit.argtypes = [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P]
     L.fame_queue_ready.argtypes = [_P, C.c_int]
+    L.fame_queue_wait.argtypes = [_P, C.c_int, C.c_uint32]
     L.fame_queue_collect.argtypes = [_P, C.c_int, _P, _P, _P]
     L.fame_queue_launches.argtypes = [_P]
     L.fame_queue_launches.restype = C.c_uint64
@@ -355,6 +359,10 @@ class GpuMatcher:
     def last_launches(self) -> int:
         return int(lib().fame_gpu_last_launches(self.h))
 
+    def index_bytes(self) -> int:
+        """Device bytes of the resident index tables."""
+        return int(lib().fame_gpu_index_bytes(self.h))
+
     # device / pinned memory helpers
     def alloc(self, nbytes: int) -> int:
         p = _P()
@@ -445,6 +453,15 @@ class GpuQueue:
 
     def ready(self, slot: int) -> bool:
         return lib().fame_queue_ready(self.h, slot) == 1
+
+    def wait(self, slot: int, timeout_ms: int) -> bool:
+        """True when the slot's chunk finished within timeout_ms, False when the
+        wait timed out (FAME_ERR_TIMEOUT); other errors raise."""
+        rc = lib().fame_queue_wait(self.h, slot, int(timeout_ms))
+        if rc == -7:
+            return False
+        _check(rc, self.gpu.h)
+        return True
 
     def collect(self, slot: int, mats=None, invalid=None):
         n = self.pending.pop(slot)

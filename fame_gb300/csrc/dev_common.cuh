@@ -93,7 +93,13 @@ constexpr uint32_t CAND_HOLE = 0xffffffffu;
 
 // The candidate buffer overflowed: the chunk's later stages do nothing and the
 // host reruns it with a larger buffer.
-__device__ __forceinline__ bool cand_overflow(const ChunkBufs& cb) { return cb.ctr[CTR_CAND] > cb.cand_cap; }
+// The later stages of a chunk stop when its candidate buffer overflowed (the
+// host reruns the chunk with a larger one) or the chunk already failed (a read
+// over FAME_MAX_READ_LEN, a capacity error): nothing is tallied then.
+__device__ __forceinline__ bool cand_overflow(const ChunkBufs& cb)
+{
+    return cb.ctr[CTR_CAND] > cb.cand_cap || cb.ctr[CTR_TOO_LONG] || cb.ctr[CTR_ERRFLAG];
+}
 
 __device__ __forceinline__ uint64_t rotl64(uint64_t v, unsigned s)
 {

@@ -6,11 +6,13 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -29,6 +31,7 @@ struct fame_gpu {
     std::string err;
     DevIndex ix{};
     std::vector<void*> index_allocs;
+    uint64_t index_bytes = 0;            // device bytes of the resident index tables
     uint64_t n_cpg = 0;
     uint32_t max_bucket = 0;
     // chunk buffers
@@ -65,9 +68,13 @@ struct fame_gpu {
     uint64_t pe_heavy_warp_bytes = 0;
     uint32_t pe_heavy_warps = 0;
     fame_queue* queue = nullptr;         // the batched form's slots, if open
+    uint8_t* noalloc_scratch = nullptr;  // device address of the no-allocation entry point's static array
 };
 
 void queue_quiesce(fame_queue* q);
+// Device address of the static scratch array of fame_gpu_call_cpgs_noalloc on
+// the current device (defined with the array, below).
+cudaError_t noalloc_scratch_address(void** p);
 
 namespace {
 
@@ -193,6 +200,27 @@ int grow_chunk(fame_gpu* g, uint64_t n, uint64_t bytes, uint64_t cand)
     return FAME_OK;
 }
 
+// fn(begin, end) over up to 16 host threads (the index upload's staging
+// loops, which are per-element and independent).  fn must not throw.
+template <class F>
+void host_par(uint64_t n, F fn)
+{
+    const int T = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (T <= 1 || n < (1u << 16)) { fn(0, n); return; }
+    std::vector<std::thread> th;
+    const uint64_t step = (n + T - 1) / T;
+    for (int t = 0; t < T; ++t) {
+        const uint64_t b = std::min<uint64_t>(n, (uint64_t)t * step), e = std::min<uint64_t>(n, b + step);
+        if (b >= e) break;
+        try {
+            th.emplace_back([=] { fn(b, e); });
+        } catch (...) {
+            fn(b, e);
+        }
+    }
+    for (auto& x : th) x.join();
+}
+
 uint32_t pow2_ceil_host(uint64_t v)
 {
     uint64_t p = 1;
@@ -257,13 +285,14 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         if (cudaMalloc(p, std::max<uint64_t>(bytes, 16)) != cudaSuccess)
             return set_err(g, FAME_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed");
         g->index_allocs.push_back(*p);
+        g->index_bytes += bytes;
         return FAME_OK;
     };
     int rc;
     // ---- tabIndex -> uint32 offsets
     uint32_t* d_tab;
     if ((rc = alloc_idx((void**)&d_tab, (HTABSIZE + 1) * 4))) return fail(rc);
-    const uint64_t CH = 1ull << 24;
+    const uint64_t CH = 1ull << 26;
     std::vector<uint32_t> stage(CH);
     if (v->tab_index32) {
         if (v->tab_index32[HTABSIZE] != v->n_kmer) return fail(set_err(g, FAME_ERR_INDEX, "tabIndex end != k-mer count"));
@@ -273,7 +302,9 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         if (v->tab_index[HTABSIZE] != v->n_kmer) return fail(set_err(g, FAME_ERR_INDEX, "tabIndex end != k-mer count"));
         for (uint64_t b = 0; b < HTABSIZE + 1; b += CH) {
             const uint64_t e = std::min<uint64_t>(HTABSIZE + 1, b + CH);
-            for (uint64_t i = b; i < e; ++i) stage[i - b] = (uint32_t)v->tab_index[i];
+            host_par(e - b, [&](uint64_t i0, uint64_t i1) {
+                for (uint64_t i = i0; i < i1; ++i) stage[i] = (uint32_t)v->tab_index[b + i];
+            });
             if (cudaMemcpy(d_tab + b, stage.data(), (e - b) * 4, cudaMemcpyHostToDevice) != cudaSuccess)
                 return fail(set_err(g, FAME_ERR_CUDA, "tabIndex upload failed"));
         }
@@ -284,13 +315,21 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
     if ((rc = alloc_idx((void**)&d_entry, v->n_kmer * 4))) return fail(rc);
     for (uint64_t b = 0; b < v->n_kmer; b += CH) {
         const uint64_t e = std::min<uint64_t>(v->n_kmer, b + CH);
-        for (uint64_t i = b; i < e; ++i) {
-            const uint32_t meta = v->kmer[i].meta;
-            if ((meta >> 31) || meta >= v->n_win)
-                return fail(set_err(g, FAME_ERR_INDEX, "k-mer entry " + std::to_string(i) + " has a start-CpG flag or an unknown window"));
-            const uint32_t fwd = (v->strand_bits[i >> 3] >> (i & 7)) & 1u;
-            stage[i - b] = meta | (fwd << 31);
-        }
+        std::atomic<uint64_t> bad{~0ull};
+        host_par(e - b, [&](uint64_t i0, uint64_t i1) {
+            for (uint64_t j = i0; j < i1; ++j) {
+                const uint64_t i = b + j;
+                const uint32_t meta = v->kmer[i].meta;
+                if ((meta >> 31) || meta >= v->n_win) {
+                    uint64_t cur = bad.load();
+                    while (i < cur && !bad.compare_exchange_weak(cur, i)) {}
+                }
+                const uint32_t fwd = (v->strand_bits[i >> 3] >> (i & 7)) & 1u;
+                stage[j] = meta | (fwd << 31);
+            }
+        });
+        if (bad.load() != ~0ull)
+            return fail(set_err(g, FAME_ERR_INDEX, "k-mer entry " + std::to_string(bad.load()) + " has a start-CpG flag or an unknown window"));
         if (cudaMemcpy(d_entry + b, stage.data(), (e - b) * 4, cudaMemcpyHostToDevice) != cudaSuccess)
             return fail(set_err(g, FAME_ERR_CUDA, "k-mer upload failed"));
     }
@@ -309,7 +348,9 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         if ((rc = alloc_idx((void**)&d_tm, v->n_kmer * 4))) return fail(rc);
         for (uint64_t b = 0; b < v->n_kmer; b += CH) {
             const uint64_t e = std::min<uint64_t>(v->n_kmer, b + CH);
-            for (uint64_t i = b; i < e; ++i) stage[i - b] = v->kmer[i].tmask;
+            host_par(e - b, [&](uint64_t i0, uint64_t i1) {
+                for (uint64_t i = i0; i < i1; ++i) stage[i] = v->kmer[b + i].tmask;
+            });
             if (cudaMemcpy(d_tm + b, stage.data(), (e - b) * 4, cudaMemcpyHostToDevice) != cudaSuccess)
                 return fail(set_err(g, FAME_ERR_CUDA, "tmask upload failed"));
         }
@@ -329,23 +370,39 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
     uint64_t tot = 0;
     for (uint32_t c = 0; c < v->n_chrom; ++c) { coff[c] = tot; clen[c] = v->chrom_len[c]; tot += (clen[c] + 31) / 32 * 32; }
     {
+        // 32 bases per step: two packed words and one N-mask word, so threads
+        // never share a word (chromosomes start at 32-base boundaries)
         std::vector<uint32_t> pack(tot / 16 + 1, 0), nm(tot / 32 + 1, 0);
         for (uint32_t c = 0; c < v->n_chrom; ++c) {
             const char* s = v->chrom_seq[c];
-            for (uint64_t i = 0; i < clen[c]; ++i) {
-                const uint64_t gi = coff[c] + i;
-                uint32_t code;
-                switch (s[i]) {
-                    case 'A': code = 0; break;
-                    case 'C': code = 1; break;
-                    case 'G': code = 2; break;
-                    case 'T': code = 3; break;
-                    case 'N': code = 0; nm[gi >> 5] |= 1u << (gi & 31); break;
-                    default:
-                        return fail(set_err(g, FAME_ERR_INDEX, "reference base outside ACGTN in chromosome " + std::to_string(c)));
+            const uint64_t L = clen[c];
+            std::atomic<int> bad{0};
+            host_par((L + 31) / 32, [&](uint64_t q0, uint64_t q1) {
+                for (uint64_t q = q0; q < q1; ++q) {
+                    uint32_t w0 = 0, w1 = 0, nmask = 0;
+                    const uint64_t i0 = 32 * q, i1 = std::min<uint64_t>(L, i0 + 32);
+                    for (uint64_t i = i0; i < i1; ++i) {
+                        const uint32_t k = (uint32_t)(i - i0);
+                        uint32_t code = 0;
+                        switch (s[i]) {
+                            case 'A': code = 0; break;
+                            case 'C': code = 1; break;
+                            case 'G': code = 2; break;
+                            case 'T': code = 3; break;
+                            case 'N': nmask |= 1u << k; break;
+                            default: bad = 1; break;
+                        }
+                        if (k < 16) w0 |= code << (2 * k);
+                        else w1 |= code << (2 * (k - 16));
+                    }
+                    const uint64_t gi = coff[c] + i0;
+                    pack[gi >> 4] = w0;
+                    pack[(gi >> 4) + 1] = w1;
+                    nm[gi >> 5] = nmask;
                 }
-                pack[gi >> 4] |= code << (2 * (gi & 15));
-            }
+            });
+            if (bad.load())
+                return fail(set_err(g, FAME_ERR_INDEX, "reference base outside ACGTN in chromosome " + std::to_string(c)));
         }
         uint32_t *d_pack, *d_nm;
         uint64_t *d_coff, *d_clen;
@@ -394,6 +451,7 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         cudaStreamSynchronize(g->stream);
         // the plain offset table is not needed any more (tab2 holds the offsets)
         cudaFree(d_tab);
+        g->index_bytes -= (HTABSIZE + 1) * 4;
         g->index_allocs.erase(std::remove(g->index_allocs.begin(), g->index_allocs.end(), (void*)d_tab),
                               g->index_allocs.end());
         if (cudaStreamSynchronize(g->stream) != cudaSuccess) { cudaFree(d_mx); return fail(set_err(g, FAME_ERR_CUDA, "bucket scan failed")); }
@@ -413,6 +471,16 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
     if (cudaMemset(g->d_meth, 0, 16 * std::max<uint64_t>(1, v->n_cpg)) != cudaSuccess) return fail(set_err(g, FAME_ERR_CUDA, "memset"));
     if ((rc = dev_alloc(g, &g->d_ctr, CTR_N))) return fail(rc);
     if (cudaMallocHost(&g->h_ctr, CTR_N * sizeof(unsigned long long)) != cudaSuccess) return fail(set_err(g, FAME_ERR_NOMEM, "pinned alloc"));
+    {
+        // resolved here, with the device current, so that it follows this
+        // context's lifetime (a module reloaded after a device reset may place
+        // the array elsewhere) and is known before any stream capture
+        void* p = nullptr;
+        const cudaError_t e = noalloc_scratch_address(&p);
+        if (e != cudaSuccess || !p)
+            return fail(set_err(g, FAME_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)));
+        g->noalloc_scratch = (uint8_t*)p;
+    }
     if (cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * LightLayout::BYTES) != cudaSuccess ||
         cudaFuncSetAttribute(k_dp_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * DPW_BYTES) != cudaSuccess)
         return fail(set_err(g, FAME_ERR_CUDA, "shared memory attribute"));
@@ -466,6 +534,11 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
     const int T = g->timing;
     g->launches = 0;
     if (g->queue) queue_quiesce(g->queue);   // the queue's slots share the heavy-path scratch
+    // The whole chunk is enqueued at once, every count read on the device
+    // (FROM_DEVICE): the heavy-read seeding and the automaton widths without
+    // work return at once, and the later stages stop when the candidate buffer
+    // overflowed, in which case nothing was tallied and the chunk runs again
+    // with a larger buffer.  One host wait per pass.
     for (int attempt = 0; attempt < 4; ++attempt) {
         cb.cand = g->d_cand;
         cb.cand_task = g->d_cand_task;
@@ -479,64 +552,44 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         const uint32_t ntask = n * norient;
         const uint32_t wpb = 4;
         const uint32_t blocks = std::min<uint32_t>((ntask + wpb - 1) / wpb, (uint32_t)g->sm_count * 64);
-        if (ntask) k_seed<<<std::max(1u, blocks), wpb * 32, wpb * LightLayout::BYTES, g->stream>>>(g->ix, cb, ntask);
+        k_seed<<<std::max(1u, blocks), wpb * 32, wpb * LightLayout::BYTES, g->stream>>>(g->ix, cb, ntask);
         if (T) cudaEventRecord(g->ev[2], g->stream);
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
-        CK(cudaStreamSynchronize(g->stream));
-        g->launches += 2;
-        if (g->h_ctr[CTR_TOO_LONG]) return set_err(g, FAME_ERR_READ, "read longer than FAME_MAX_READ_LEN");
-        const uint64_t nheavy = g->h_ctr[CTR_HEAVY];
-        float heavy_ms = 0;
-        if (nheavy) {
-            if (T) cudaEventRecord(g->ev[6], g->stream);
-            const uint32_t hb = (g->hs.nwarps + 3) / 4;
-            k_seed_heavy<<<hb, 128, 0, g->stream>>>(g->ix, cb, g->hs, (uint32_t)nheavy);
-            if (T) cudaEventRecord(g->ev[7], g->stream);
-            CK(cudaGetLastError());
-            CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
-            CK(cudaStreamSynchronize(g->stream));
-            if (T) cudaEventElapsedTime(&heavy_ms, g->ev[6], g->ev[7]);
-            g->launches += 1;
-            if (g->h_ctr[CTR_ERRFLAG]) return set_err(g, FAME_ERR_INDEX, "a read exceeded the heavy-path capacity");
-        }
-        const uint64_t ncand = g->h_ctr[CTR_CAND];
-        if (ncand > g->cap_cand) {
-            if ((rc = grow_chunk(g, n, 0, ncand + ncand / 4 + 4096))) return rc;
-            continue;  // nothing was tallied yet: redo the chunk with room for all candidates
-        }
-        if (T) {
-            cudaEventElapsedTime(&g->stage_ms[0], g->ev[0], g->ev[1]);
-            cudaEventElapsedTime(&g->stage_ms[1], g->ev[1], g->ev[2]);
-            g->stage_ms[5] = heavy_ms;
-            cudaEventRecord(g->ev[2], g->stream);
-        }
-        if (ncand) {
-            const uint32_t tb = 128;
-            const uint32_t grid = (uint32_t)std::min<uint64_t>((ncand + tb - 1) / tb, (uint64_t)g->sm_count * 32);
-            const uint64_t wmask = g->h_ctr[CTR_WMASK];
-            if (wmask & 2u) { k_shiftand<1><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
-            if (wmask & 4u) { k_shiftand<2><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
-            if (wmask & 8u) { k_shiftand<3><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
-            if (wmask & 16u) { k_shiftand<4><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, (uint32_t)ncand); g->launches++; }
-        }
+        k_seed_heavy<<<(g->hs.nwarps + 3) / 4, 128, 0, g->stream>>>(g->ix, cb, g->hs, FROM_DEVICE);
+        if (T) cudaEventRecord(g->ev[6], g->stream);
+        // the automaton widths a read of this index can need (reads shorter than
+        // readlen - 20 are invalid, longer than FAME_MAX_READ_LEN refused)
+        const uint32_t grid = (uint32_t)g->sm_count * 32;
+        const uint32_t wlo = std::min(4u, (g->ix.readlen - 20) / 64 + 1);
+        if (wlo <= 1) k_shiftand<1><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, FROM_DEVICE);
+        if (wlo <= 2) k_shiftand<2><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, FROM_DEVICE);
+        if (wlo <= 3) k_shiftand<3><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, FROM_DEVICE);
+        k_shiftand<4><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, FROM_DEVICE);
         if (T) cudaEventRecord(g->ev[3], g->stream);
         k_select<<<(n + 255) / 256, 256, 0, g->stream>>>(g->ix, cb);
         if (T) cudaEventRecord(g->ev[4], g->stream);
         k_dp_warp<<<g->dp_grid, 128, 4 * DPW_BYTES, g->stream>>>(g->ix, cb);
         if (T) cudaEventRecord(g->ev[5], g->stream);
-        g->launches += 2;
+        g->launches += 5 + (int)(5 - wlo);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
         CK(cudaStreamSynchronize(g->stream));
+        const unsigned long long* h = g->h_ctr;
+        if (h[CTR_TOO_LONG]) return set_err(g, FAME_ERR_READ, "read longer than FAME_MAX_READ_LEN");
+        if (h[CTR_ERRFLAG]) return set_err(g, FAME_ERR_INDEX, "a device capacity check failed");
+        const uint64_t ncand = h[CTR_CAND];
+        if (ncand > g->cap_cand) {
+            if ((rc = grow_chunk(g, n, 0, ncand + ncand / 4 + 4096))) return rc;
+            continue;  // nothing was tallied: redo the chunk with room for all candidates
+        }
         if (T) {
-            cudaEventElapsedTime(&g->stage_ms[2], g->ev[2], g->ev[3]);
+            cudaEventElapsedTime(&g->stage_ms[0], g->ev[0], g->ev[1]);
+            cudaEventElapsedTime(&g->stage_ms[1], g->ev[1], g->ev[2]);
+            cudaEventElapsedTime(&g->stage_ms[5], g->ev[2], g->ev[6]);
+            cudaEventElapsedTime(&g->stage_ms[2], g->ev[6], g->ev[3]);
             cudaEventElapsedTime(&g->stage_ms[3], g->ev[3], g->ev[4]);
             cudaEventElapsedTime(&g->stage_ms[4], g->ev[4], g->ev[5]);
         }
-        if (g->h_ctr[CTR_ERRFLAG]) return set_err(g, FAME_ERR_INDEX, "a device capacity check failed");
         if (cnt) {
-            const unsigned long long* h = g->h_ctr;
             cnt->succ += h[CTR_SUCC];
             cnt->nonunique += h[CTR_NONU];
             cnt->unsucc += h[CTR_UNSUCC];
@@ -547,6 +600,8 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
             cnt->gather_bytes += h[CTR_GATHER_BYTES];
             cnt->windows_scanned += h[CTR_CAND_USED];
             cnt->dp_reads += h[CTR_DP];
+            cnt->heavy_tasks += h[CTR_HEAVY];
+            cnt->reruns += (uint64_t)attempt;
         }
         return FAME_OK;
     }
@@ -845,6 +900,8 @@ extern "C" int fame_gpu_stage_times(fame_gpu* g, float* ms, int n)
 
 extern "C" int fame_gpu_last_launches(const fame_gpu* g) { return g ? g->launches : 0; }
 
+extern "C" uint64_t fame_gpu_index_bytes(const fame_gpu* g) { return g ? g->index_bytes : 0; }
+
 extern "C" int fame_gpu_stream(fame_gpu* g, void** stream)
 {
     if (!g || !stream) return FAME_ERR_ARG;
@@ -862,7 +919,6 @@ extern "C" int fame_gpu_stream(fame_gpu* g, void** stream)
 // banded-DP CpG kernel (k_dp in kernels.cuh) whose per-read DP matrices live
 // in one file-scope static device array instead of context scratch; the
 // caller passes its inputs and outputs in device memory it already has.
-#include <mutex>
 
 namespace {
 
@@ -876,26 +932,9 @@ constexpr uint32_t NOALLOC_ALIGN = 2 * FAME_MAX_READ_LEN + 4 * DP_BAND + 8;
 constexpr uint64_t NOALLOC_HEADER = 256;
 constexpr uint64_t NOALLOC_BYTES =
     NOALLOC_HEADER + (uint64_t)NOALLOC_SLOTS * NOALLOC_CELLS * 2 + (uint64_t)NOALLOC_SLOTS * NOALLOC_ALIGN;
+static_assert(CTR_N * sizeof(unsigned long long) <= NOALLOC_HEADER, "status counters exceed the array header");
 
 static __device__ __align__(256) uint8_t g_noalloc_scratch[NOALLOC_BYTES];
-
-constexpr int MAX_DEVICES = 64;
-void* g_scratch_addr[MAX_DEVICES] = {};
-std::mutex g_scratch_mu;
-
-// Device address of the static array on the current device (resolved once per
-// device; the host-side symbol is only a stand-in and is never passed to a kernel).
-void* scratch_address(int dev)
-{
-    if (dev < 0 || dev >= MAX_DEVICES) return nullptr;
-    std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) return nullptr;
-        g_scratch_addr[dev] = p;
-    }
-    return g_scratch_addr[dev];
-}
 
 __global__ void k_call_cpgs_static(DevIndex ix, ChunkBufs cb, DpScratch ds, const uint64_t* mats, const uint8_t* inval,
                                    uint32_t n, int orient)
@@ -917,21 +956,24 @@ __global__ void k_call_cpgs_static(DevIndex ix, ChunkBufs cb, DpScratch ds, cons
 
 }  // namespace
 
+// The host-side name of the array is only a stand-in: the kernel is given the
+// device address, which fame_gpu_open resolves with the device current.
+cudaError_t noalloc_scratch_address(void** p) { return cudaGetSymbolAddress(p, g_noalloc_scratch); }
+
 extern "C" int fame_gpu_call_cpgs_noalloc(fame_gpu* g, const char* seqs_dev, const uint64_t* offs_dev,
                                           const uint64_t* mats_dev, const uint8_t* invalid_dev, uint32_t n,
                                           int orient, uint32_t* meth_dev)
 {
-    if (!g || !meth_dev || (orient != 0 && orient != 1) || (n && (!seqs_dev || !offs_dev || !mats_dev || !invalid_dev)))
-        return FAME_ERR_ARG;
-    const int dev = g->device;
-    if (cudaSetDevice(dev) != cudaSuccess) return FAME_ERR_CUDA;
-    uint8_t* base = (uint8_t*)scratch_address(dev);
-    if (!base) return FAME_ERR_CUDA;
+    if (!g) return FAME_ERR_ARG;
+    if (!meth_dev || (orient != 0 && orient != 1) || (n && (!seqs_dev || !offs_dev || !mats_dev || !invalid_dev)))
+        return set_err(g, FAME_ERR_ARG, "fame_gpu_call_cpgs_noalloc: null buffer or orient not 0/1");
+    CK(cudaSetDevice(g->device));
+    uint8_t* base = g->noalloc_scratch;
+    if (!base) return set_err(g, FAME_ERR_CUDA, "no-allocation scratch address unknown");
     cudaStream_t s = g->stream;
-    unsigned long long* h = g->h_ctr;
     unsigned long long* d_ctr = (unsigned long long*)base;
-    if (cudaMemsetAsync(meth_dev, 0, 16 * g->n_cpg, s) != cudaSuccess) return FAME_ERR_CUDA;
-    if (cudaMemsetAsync(d_ctr, 0, NOALLOC_HEADER, s) != cudaSuccess) return FAME_ERR_CUDA;
+    CK(cudaMemsetAsync(meth_dev, 0, 16 * g->n_cpg, s));
+    CK(cudaMemsetAsync(d_ctr, 0, NOALLOC_HEADER, s));
     if (n) {
         ChunkBufs cb{};
         cb.seqs = seqs_dev;
@@ -947,13 +989,15 @@ extern "C" int fame_gpu_call_cpgs_noalloc(fame_gpu* g, const char* seqs_dev, con
         ds.align_cap = NOALLOC_ALIGN;
         k_call_cpgs_static<<<NOALLOC_SLOTS / 128, 128, 0, s>>>(g->ix, cb, ds, mats_dev, invalid_dev, n,
                                                               orient);
-        if (cudaGetLastError() != cudaSuccess) return FAME_ERR_CUDA;
+        CK(cudaGetLastError());
     }
-    if (cudaMemcpyAsync(h, d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) != cudaSuccess)
-        return FAME_ERR_CUDA;
-    if (cudaStreamSynchronize(s) != cudaSuccess) return FAME_ERR_CUDA;
-    if (h[CTR_TOO_LONG]) return FAME_ERR_READ;
-    if (h[CTR_ERRFLAG]) return FAME_ERR_ARG;
+    // status counters into this call's own host buffer (pageable, on the
+    // stack: no allocation, and nothing shared with the context's other calls)
+    unsigned long long h[CTR_N];
+    CK(cudaMemcpyAsync(h, d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h[CTR_TOO_LONG]) return set_err(g, FAME_ERR_READ, "a read is longer than FAME_MAX_READ_LEN");
+    if (h[CTR_ERRFLAG]) return set_err(g, FAME_ERR_ARG, "a match names no window of the index");
     return FAME_OK;
 }
 

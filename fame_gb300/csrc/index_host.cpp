@@ -20,8 +20,10 @@
 #include <cstring>
 #include <functional>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <unordered_map>
 #include <unordered_set>
@@ -60,18 +62,37 @@ struct SpacedRoller {
     }
 };
 
+// fn(begin, end, part) over `threads` contiguous parts.  An exception thrown by
+// a part is caught in its thread and rethrown here after every thread joined
+// (so it reaches the entry point's handler instead of ending the process);
+// parts whose thread cannot be started run on the calling thread.
 template <class F>
 void parallel_for(uint64_t n, int threads, F fn)
 {
     if (threads <= 1 || n < 2) { fn(0, n, 0); return; }
     std::vector<std::thread> th;
+    std::exception_ptr err;
+    std::mutex err_mu;
+    auto guarded = [&](uint64_t b, uint64_t e, int t) {
+        try {
+            fn(b, e, t);
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(err_mu);
+            if (!err) err = std::current_exception();
+        }
+    };
     const uint64_t step = (n + threads - 1) / threads;
     for (int t = 0; t < threads; ++t) {
         const uint64_t b = std::min<uint64_t>(n, t * step), e = std::min<uint64_t>(n, b + step);
         if (b >= e) break;
-        th.emplace_back([=] { fn(b, e, t); });
+        try {
+            th.emplace_back([=, &guarded] { guarded(b, e, t); });
+        } catch (const std::system_error&) {
+            guarded(b, e, t);
+        }
     }
     for (auto& x : th) x.join();
+    if (err) std::rethrow_exception(err);
 }
 
 // K-mers of one window in the reference's insertion order (RefGenome.cpp:621-759):
@@ -478,6 +499,9 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
     } catch (const std::bad_alloc&) {
         delete ix;
         return FAME_ERR_NOMEM;
+    } catch (const std::exception&) {   // a worker thread's failure, rethrown by parallel_for
+        delete ix;
+        return FAME_ERR_NOMEM;
     }
     *out = ix;
     return FAME_OK;
@@ -533,15 +557,19 @@ extern "C" int fame_index_read(const char* path, fame_host_index** out)
                 const int T = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
                 std::atomic<bool> good{at >= 0};
                 char* dst = reinterpret_cast<char*>(ix->tab64.data());
-                parallel_for(bytes, T, [&](uint64_t b, uint64_t e, int) {
-                    while (b < e && good.load(std::memory_order_relaxed)) {
-                        const ssize_t got = pread(fileno(f), dst + b, (size_t)std::min<uint64_t>(e - b, 1ull << 30),
-                                                  at + (off_t)b);
-                        if (got <= 0) { good = false; break; }
-                        b += (uint64_t)got;
-                    }
-                });
-                if (!good || fseeko(f, at + (off_t)bytes, SEEK_SET) != 0) r.ok = false;
+                if (at < 0) {
+                    r.bytes(dst, bytes);   // not seekable (a pipe): read in order through the stream
+                } else {
+                    parallel_for(bytes, T, [&](uint64_t b, uint64_t e, int) {
+                        while (b < e && good.load(std::memory_order_relaxed)) {
+                            const ssize_t got = pread(fileno(f), dst + b,
+                                                      (size_t)std::min<uint64_t>(e - b, 1ull << 30), at + (off_t)b);
+                            if (got <= 0) { good = false; break; }
+                            b += (uint64_t)got;
+                        }
+                    });
+                    if (!good || fseeko(f, at + (off_t)bytes, SEEK_SET) != 0) r.ok = false;
+                }
             }
             n = r.get<uint64_t>();
             ix->kmer.resize(n); r.bytes(ix->kmer.data(), n * sizeof(fame_kmer));
@@ -658,27 +686,38 @@ extern "C" int fame_index_write(const fame_host_index* ix, const char* path)
             const uint64_t n = HTABSIZE + 1;
             const int T = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
             std::atomic<bool> good{at >= 0};
-            parallel_for(n, T, [&](uint64_t b, uint64_t e, int) {
-                std::vector<uint64_t> blk(1u << 20);
-                for (uint64_t i = b; i < e && good.load(std::memory_order_relaxed); i += blk.size()) {
-                    const uint64_t m = std::min<uint64_t>(blk.size(), e - i);
-                    const uint64_t* src = blk.data();
-                    if (!ix->tab64.empty()) {
-                        src = ix->tab64.data() + i;
-                    } else {
+            constexpr uint64_t BLK = 1u << 20;
+            if (at < 0) {
+                // not seekable (a pipe): written in order through the stream
+                std::vector<uint64_t> blk(ix->tab64.empty() ? BLK : 0);
+                for (uint64_t i = 0; i < n && w.ok; i += BLK) {
+                    const uint64_t m = std::min<uint64_t>(BLK, n - i);
+                    const uint64_t* src = ix->tab64.empty() ? blk.data() : ix->tab64.data() + i;
+                    if (ix->tab64.empty())
                         for (uint64_t j = 0; j < m; ++j) blk[j] = ix->tab32[i + j];
-                    }
-                    const char* p = reinterpret_cast<const char*>(src);
-                    uint64_t left = m * 8, done = 0;
-                    while (left) {
-                        const ssize_t put = pwrite(fileno(f), p + done, (size_t)left, at + (off_t)(8 * i + done));
-                        if (put <= 0) { good = false; break; }
-                        done += (uint64_t)put;
-                        left -= (uint64_t)put;
-                    }
+                    w.bytes(src, m * 8);
                 }
-            });
-            if (!good || fseeko(f, at + (off_t)(n * 8), SEEK_SET) != 0) w.ok = false;
+            } else {
+                parallel_for(n, T, [&](uint64_t b, uint64_t e, int) {
+                    // a conversion block only when the offsets are held as uint32
+                    std::vector<uint64_t> blk(ix->tab64.empty() ? BLK : 0);
+                    for (uint64_t i = b; i < e && good.load(std::memory_order_relaxed); i += BLK) {
+                        const uint64_t m = std::min<uint64_t>(BLK, e - i);
+                        const uint64_t* src = ix->tab64.empty() ? blk.data() : ix->tab64.data() + i;
+                        if (ix->tab64.empty())
+                            for (uint64_t j = 0; j < m; ++j) blk[j] = ix->tab32[i + j];
+                        const char* p = reinterpret_cast<const char*>(src);
+                        uint64_t left = m * 8, done = 0;
+                        while (left) {
+                            const ssize_t put = pwrite(fileno(f), p + done, (size_t)left, at + (off_t)(8 * i + done));
+                            if (put <= 0) { good = false; break; }
+                            done += (uint64_t)put;
+                            left -= (uint64_t)put;
+                        }
+                    }
+                });
+                if (!good || fseeko(f, at + (off_t)(n * 8), SEEK_SET) != 0) w.ok = false;
+            }
         }
         // k-mers: KMER::getCore and the T mask of each (the loaded layout)
         w.put<uint64_t>(ix->kmer.size());
@@ -724,6 +763,9 @@ extern "C" int fame_index_write(const fame_host_index* ix, const char* path)
     } catch (const std::bad_alloc&) {
         fclose(f);
         return FAME_ERR_NOMEM;
+    } catch (const std::exception&) {
+        fclose(f);
+        return FAME_ERR_IO;
     }
     if (fclose(f) != 0) w.ok = false;
     if (!w.ok) return FAME_ERR_IO;

@@ -18,6 +18,9 @@
 //
 // Included into fame_gpu.cu (one translation unit for all kernels).
 
+#include <chrono>
+#include <thread>
+
 namespace {
 
 constexpr uint32_t QUEUE_GRAPHS = 8;
@@ -325,6 +328,24 @@ extern "C" int fame_queue_ready(fame_queue* q, int slot)
     return cudaEventQuery(s.done) == cudaSuccess ? 1 : 0;
 }
 
+extern "C" int fame_queue_wait(fame_queue* q, int slot, uint32_t timeout_ms)
+{
+    if (!q || slot < 0 || slot >= (int)q->slots.size()) return FAME_ERR_ARG;
+    const QSlot& s = q->slots[slot];
+    if (!s.busy) return FAME_OK;
+    // poll with a deadline instead of blocking in cudaEventSynchronize
+    const auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        const cudaError_t e = cudaEventQuery(s.done);
+        if (e == cudaSuccess) return FAME_OK;
+        if (e != cudaErrorNotReady)
+            return set_err(q->g, FAME_ERR_CUDA, std::string("queue slot wait: ") + cudaGetErrorString(e));
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (ms >= (double)timeout_ms) return FAME_ERR_TIMEOUT;
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
 extern "C" int fame_queue_collect(fame_queue* q, int slot, uint64_t* mats, uint8_t* invalid, fame_counters* cnt)
 {
     if (!q || slot < 0 || slot >= (int)q->slots.size()) return FAME_ERR_ARG;
@@ -341,6 +362,7 @@ extern "C" int fame_queue_collect(fame_queue* q, int slot, uint64_t* mats, uint8
         // rerun through the plain path (its buffers grow to fit); nothing was tallied
         int rc = run_chunk(g, s.d_seqs, s.d_offs, s.n, s.flags, s.d_mats, s.d_invalid, cnt, s.meth);
         if (rc) return rc;
+        if (cnt) cnt->reruns += 1;
         if (mats) CK(cudaMemcpy(mats, s.d_mats, s.n * sizeof(uint64_t), cudaMemcpyDeviceToHost));
         if (invalid) CK(cudaMemcpy(invalid, s.d_invalid, s.n, cudaMemcpyDeviceToHost));
         return FAME_OK;
@@ -358,6 +380,7 @@ extern "C" int fame_queue_collect(fame_queue* q, int slot, uint64_t* mats, uint8
         cnt->gather_bytes += h[CTR_GATHER_BYTES];
         cnt->windows_scanned += h[CTR_CAND_USED];
         cnt->dp_reads += h[CTR_DP];
+        cnt->heavy_tasks += h[CTR_HEAVY];
     }
     return FAME_OK;
 }

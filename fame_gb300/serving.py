@@ -22,7 +22,9 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._lib import CHUNKSIZE, FAME_BOTH_STRANDS, FAME_GET_STRANDED, FAME_MATCH_R1_FWD, GpuMatcher, GpuQueue
+from ._lib import CHUNKSIZE, FAME_BOTH_STRANDS, FAME_GET_STRANDED, FAME_MATCH_R1_FWD, FameError, GpuMatcher, GpuQueue
+
+FAME_ERR_NOMEM = -3
 
 
 @dataclass
@@ -48,6 +50,7 @@ class JobResult:
     arrival: float
     admitted: float
     finished: float
+    status: str = "ok"        # "refused: <why>" when the job could not be admitted at all
 
     @property
     def latency(self) -> float:
@@ -76,21 +79,25 @@ def _chunks(n, chunk):
 
 class ServingLoop:
     def __init__(self, gpu: GpuMatcher, slots: int = 4, chunk: int = CHUNKSIZE, max_active: int = 16,
-                 both_strands: bool = False, max_bytes_per_read: int = 256, mem_reserve: int = 2 << 30):
+                 both_strands: bool = False, max_bytes_per_read: int = 256, mem_reserve: int = 2 << 30,
+                 queue=None):
         self.gpu = gpu
         self.chunk = chunk
         self.max_active = max_active
         self.both = both_strands
         self.mem_reserve = mem_reserve
-        self.queue = GpuQueue(gpu, slots, chunk, chunk * max_bytes_per_read)
+        self.queue = queue if queue is not None else GpuQueue(gpu, slots, chunk, chunk * max_bytes_per_read)
         self.tally_bytes = 16 * max(1, gpu.n_cpg)
 
     def close(self):
         self.queue.close()
 
-    def _admissible(self) -> bool:
+    def _admissible(self):
+        """None when a job's tally array fits in free device memory above the
+        reserve, else the reason it does not."""
         free, _ = self.gpu.mem_info()
-        return free > self.tally_bytes + self.mem_reserve
+        need = self.tally_bytes + self.mem_reserve
+        return None if free > need else "device memory: %d bytes free, %d needed" % (free, need)
 
     def run(self, jobs, realtime: bool = True):
         """Serve `jobs` (arrival times in seconds from now when realtime, else
@@ -107,12 +114,32 @@ class ServingLoop:
 
         while pending or active:
             t = now()
-            # admission: arrived jobs, while device memory and the active limit allow
-            while pending and (not realtime or pending[0].arrival <= t) and len(active) < self.max_active \
-                    and self._admissible():
+            # admission: arrived jobs, while device memory and the active limit
+            # allow.  A job that does not fit waits for running jobs to free
+            # their tallies; with none running it can never fit and is refused.
+            while pending and (not realtime or pending[0].arrival <= t) and len(active) < self.max_active:
+                why = self._admissible()
+                tally = None
+                if why is None:
+                    try:
+                        tally = self.gpu.tally_alloc()
+                    except FameError as e:
+                        if e.code != FAME_ERR_NOMEM:
+                            raise
+                        why = "tally allocation failed: %s" % e
+                if tally is None:
+                    if not active:
+                        job = pending.pop(0)
+                        n = job.n_reads
+                        done.append(JobResult(job.job_id, n, None, dict(succ=0, nonunique=0, unsucc=0, r1_fwd=0,
+                                                                        r1_rev=0), np.zeros(n, np.uint64),
+                                              np.zeros(n, np.uint8), job.arrival, t, now(),
+                                              status="refused: " + why))
+                        continue
+                    break
                 job = pending.pop(0)
                 n = job.n_reads
-                active.append(_Active(job=job, tally=self.gpu.tally_alloc(), admitted=t,
+                active.append(_Active(job=job, tally=tally, admitted=t,
                                       chunks=_chunks(n, self.chunk), mats=np.zeros(n, np.uint64),
                                       invalid=np.zeros(n, np.uint8),
                                       flags=FAME_BOTH_STRANDS if self.both else FAME_GET_STRANDED))
@@ -190,6 +217,7 @@ def plain_per_job(gpu: GpuMatcher, jobs, chunk: int = CHUNKSIZE, both_strands: b
 
 
 def latency_summary(results):
+    results = [r for r in results if r.status == "ok"]
     lat = np.array([r.latency for r in results]) if results else np.zeros(1)
     return {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
             "mean_ms": float(lat.mean() * 1e3), "jobs": len(results)}

@@ -87,6 +87,9 @@ typedef struct {
     uint64_t gather_bytes;    /* algorithmic index-gather bytes of the call             */
     uint64_t windows_scanned; /* Shift-And window scans of the call                     */
     uint64_t dp_reads;        /* reads aligned with the banded DP                       */
+    uint64_t heavy_tasks;     /* (read, orientation) seedings run with the large-capacity
+                                 scratch (buckets beyond the shared-memory caps)         */
+    uint64_t reruns;          /* chunk passes repeated after the candidate buffer grew  */
 } fame_counters;
 
 typedef struct fame_gpu fame_gpu;
@@ -229,6 +232,10 @@ int fame_queue_submit(fame_queue* q, const char* seqs, const uint64_t* offs, uin
                       uint32_t* meth_dev, int* slot);
 /* 1 when the slot's chunk has finished, 0 while it runs. */
 int fame_queue_ready(fame_queue* q, int slot);
+/* Waits up to timeout_ms for the slot's chunk: FAME_OK when it has finished
+ * (or the slot holds none), FAME_ERR_TIMEOUT when the time ran out first (the
+ * chunk keeps running; wait again or collect later). */
+int fame_queue_wait(fame_queue* q, int slot, uint32_t timeout_ms);
 /* Waits for the slot's chunk and copies out its results (NULL to skip). */
 int fame_queue_collect(fame_queue* q, int slot, uint64_t* mats, uint8_t* invalid, fame_counters* cnt);
 /* Kernels launched through the queue so far. */
@@ -295,6 +302,8 @@ int fame_gpu_set_timing(fame_gpu* g, int enable);
 int fame_gpu_stage_times(fame_gpu* g, float* ms, int n);
 /* Number of kernel launches of the last match call. */
 int fame_gpu_last_launches(const fame_gpu* g);
+/* Device bytes held by the resident index tables of the context. */
+uint64_t fame_gpu_index_bytes(const fame_gpu* g);
 
 /* CpG calls that allocate no device memory.  No counterpart in the reference:
  * it is for callers that cannot allocate while they run (a serving loop that
@@ -309,10 +318,11 @@ int fame_gpu_last_launches(const fame_gpu* g);
  * caller; g only supplies the resident index and its stream.
  * Scratch: one static device array of about 10.5 MB per GPU that loads the
  * library (held until exit), shared by every call: calls that overlap on the
- * GPU race.  The first call on a device resolves the array's address and
- * should come before any stream capture.  Reads longer than
- * FAME_MAX_READ_LEN give FAME_ERR_READ; a match naming no window of the index
- * gives FAME_ERR_ARG. */
+ * GPU race (one context's calls run in order on its stream; calls from two
+ * contexts on one device must not overlap).  fame_gpu_open resolves the
+ * array's device address for its context, so no call here resolves anything.
+ * Reads longer than FAME_MAX_READ_LEN give FAME_ERR_READ; a match naming no
+ * window of the index gives FAME_ERR_ARG; fame_gpu_last_error has the detail. */
 int fame_gpu_call_cpgs_noalloc(fame_gpu* g, const char* seqs_dev, const uint64_t* offs_dev, const uint64_t* mats_dev,
                                const uint8_t* invalid_dev, uint32_t n, int orient, uint32_t* meth_dev);
 

@@ -171,3 +171,26 @@ def test_candidate_overflow_rerun():
         assert np.array_equal(gm.tallies(reset=True), t_ref)
     finally:
         gm.close()
+
+
+def test_bounded_wait_times_out_then_completes(gpu):
+    """fame_queue_wait gives FAME_ERR_TIMEOUT while a chunk still runs (a zero
+    timeout right after submitting 300k reads, whose copy alone takes longer),
+    leaves the chunk running, and returns FAME_OK once it has finished; the
+    collected results equal the plain call's."""
+    g = synth.make_genome([400_000, 300_000], seed=61, repeat_frac=0.1, n_families=8, fam_len=(300, 1500))
+    hi = HostIndex.build(g.seqs, readlen=100)
+    gm = GpuMatcher(hi, 0)
+    try:
+        rs = synth.make_reads(g, 300_000, seed=62, sub_rate=0.01, indel_rate=0.001)
+        seq, offs = rs.concat()
+        q = GpuQueue(gm, 2, 300_000, len(seq))
+        s = q.submit(seq, offs, FAME_MATCH_R1_FWD)
+        assert q.wait(s, 0) is False            # FAME_ERR_TIMEOUT: still running
+        assert q.wait(s, 60_000) is True        # finished within the minute
+        m, iv, c = q.collect(s)
+        q.close()
+        m2, iv2, c2 = gm.match_reads(seq, offs, FAME_MATCH_R1_FWD)
+        assert np.array_equal(m, m2) and np.array_equal(iv, iv2) and c.succ == c2.succ
+    finally:
+        gm.close()

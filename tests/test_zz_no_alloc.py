@@ -55,10 +55,28 @@ def test_noalloc_cpg_calls_match_regular_entry_point():
             got = np.zeros(4 * ncpg, np.uint32)
             gm.memcpy(got.ctypes.data, d_meth, 16 * ncpg, 2)
             assert np.array_equal((got & 0xFFFF).astype(np.uint16).reshape(-1, 4), expect), "call %d" % call
+        # reverse orientation (orient 1): the reverse complements of the same
+        # reads, matched with matchR1Fwd false (each read reverse-complemented
+        # back before matching), so the same hits, DP ones included
+        rc = np.concatenate([synth._COMP[raw[int(offs[i]):int(offs[i + 1])][::-1]] for i in range(n)])
+        gm.tallies(reset=True)
+        mats_r, inval_r, cnt_r = gm.match_reads(rc.tobytes(), offs, 0)
+        expect_r = gm.tallies(reset=True)
+        assert cnt_r.succ > 3000 and cnt_r.dp_reads > 500
+        gm.memcpy(d_seq, rc.ctypes.data, len(rc), 1)
+        gm.memcpy(d_mats, mats_r.ctypes.data, 8 * n, 1)
+        gm.memcpy(d_inv, inval_r.ctypes.data, n, 1)
+        for call in range(2):
+            assert f(gm.h, d_seq, d_offs, d_mats, d_inv, n, 1, d_meth) == 0
+            got = np.zeros(4 * ncpg, np.uint32)
+            gm.memcpy(got.ctypes.data, d_meth, 16 * ncpg, 2)
+            assert np.array_equal((got & 0xFFFF).astype(np.uint16).reshape(-1, 4), expect_r), "orient 1, call %d" % call
         # a read longer than FAME_MAX_READ_LEN is refused with FAME_ERR_READ
         long_offs = np.array([0, 300], np.uint64)
         gm.memcpy(d_offs, long_offs.ctypes.data, 16, 1)
         assert f(gm.h, d_seq, d_offs, d_mats, d_inv, 1, 0, d_meth) == -5
+        assert b"FAME_MAX_READ_LEN" in lib().fame_gpu_last_error(gm.h)
+        gm.memcpy(d_offs, offs.ctypes.data, 8 * (n + 1), 1)
         # the context stays usable
         m2, i2, c2 = gm.match_reads(seq, offs, FAME_MATCH_R1_FWD)
         assert np.array_equal(m2, mats) and np.array_equal(gm.tallies(reset=True), expect)
