@@ -1,29 +1,40 @@
-"""Benchmark: aligned reads/s of FAME's single-end matching stage on GB300.
+"""Benchmark: aligned reads/s of FAME's matching stage on one GB300.
 
-Workload (default): 8 chromosomes / 300 Mbp synthetic genome with 8 %
-interspersed repeats, 5M bisulfite reads of 100 bp (1 % substitutions, 0.1 %
-indels), seeded (fame_gb300/synth.py).  One step = one CHUNKSIZE (300,000
-read) chunk through ReadQueue::matchReads semantics on the GPU: seeding and
-index gathers, Shift-And over every candidate window, uniqueness selection,
-banded DP and CpG tallies.  The first chunk (both orientations, strand vote)
-runs in the warm-up; timed steps are the following chunks in the decided
+Default workload (se150_uneven_3gbp): a 24-chromosome, 3.0 Gbp synthetic
+genome with 45 % interspersed repeats and 20M single-end bisulfite reads of
+uneven trimmed length (60 % at 150 bp, 40 % uniform in 36-149 bp; 0.5-2 %
+errors per read; 5 % of the reads drawn from repeat copies), READLEN 150,
+seeded (fame_gb300/synth.py).  One step = one CHUNKSIZE (300,000 read) chunk
+through ReadQueue::matchReads semantics on the GPU: seeding and index
+gathers, Shift-And over every candidate window, uniqueness selection, banded
+DP and CpG tallies.  The first chunk (both orientations, strand vote) runs in
+the warm-up; timed steps are the following chunks in the decided
 orientation, as FAME's queryRoutine runs them.
 
-value: reads/s with reads resident in HBM (fame_gpu_match_reads_dev).
-e2e:   reads/s through fame_gpu_match_reads from pinned host buffers, host to
-       device copy of the chunk and device to host copy of the results timed.
-Both: per-step inputs are new reads, and each step gathers from a 9.8 GB index
-(8.6 GB bucket offsets with first entries + 1.2 GB entries), far larger than
-the 129 MB L2.
+value:    reads/s of the plain form with the reads resident in HBM
+          (fame_gpu_match_reads_dev), CUDA events on the library's stream.
+e2e:      reads/s through fame_gpu_match_reads from page-locked host buffers,
+          host-to-device copy of the chunk and device-to-host copy of the
+          results inside the timed region.
+batched:  the same chunks through the batched form (fame_queue_*: chunk slots
+          as CUDA graphs on their own streams) from the same host buffers.
+parity:   the reference's own matchReads (compiled from its sources,
+          oracle/_ref) on a sample of chunk 1, compared read by read and CpG by
+          CpG with the GPU's output for the same reads.
+Every step gathers from a device index of tens of GB and new reads: inputs
+far larger than the 129 MB L2.
 
---impl reference: the reference's own OpenMP matchReads (compiled from its
-sources by oracle/build_ref.sh) on the machine's host cores, on bounded samples of
-the same chunks.
+--workload pe100_3gbp: paired-end (20M pairs of 2 x 100 bp, MAXPDIST 400).
+--workload sc_serving: the serving form.
+--impl reference: the reference's own OpenMP matchReads / matchPairedReads on
+the machine's host cores, on bounded samples of the same chunks.
 """
 from __future__ import annotations
 
 import argparse
 import ctypes
+import gc
+import hashlib
 import json
 import os
 import subprocess
@@ -37,9 +48,25 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "aligned reads/s (single-end matching stage, bit-exact CpG report)"
-# DRAM bytes (read + write) of one steady-state k_seed launch of se100_300mbp, from
-# ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:'k_seed$' -s 2 -c 1
-SEED_TRAFFIC_PER_LAUNCH = 3.173e9 + 21.32e6
+PE_METRIC = "aligned read pairs/s (paired-end matching stage, bit-exact CpG report)"
+DEFAULT_WORKLOAD = "se150_uneven_3gbp"
+
+# Sources of the kernels whose ncu figures are quoted below; a figure is
+# reported only while the hash of these files equals the one it was captured with.
+KERNEL_SOURCES = ("fame_gb300/csrc/seed.cuh", "fame_gb300/csrc/kernels.cuh", "fame_gb300/csrc/dev_common.cuh",
+                  "fame_gb300/csrc/seedhash.h", "fame_gb300/csrc/qgram.h", "fame_gb300/csrc/editscan.h")
+# ncu figures per workload: DRAM bytes (read + write) of one steady-state k_seed
+# launch and the ALU-pipe utilisation of the two ALU-bound kernels, with the
+# source hash and the profile that holds the capture command.
+NCU_FIGURES = {}
+
+
+def kernel_source_hash() -> str:
+    h = hashlib.sha256()
+    for p in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, p), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
 
 
 def parse():
@@ -48,10 +75,11 @@ def parse():
     p.add_argument("--steps", type=int, default=12)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="se100_300mbp")
-    p.add_argument("--reads", type=int, default=0, help="override the workload's read count")
-    p.add_argument("--cpu-sample", type=int, default=60000, help="reads timed for the CPU baseline")
+    p.add_argument("--workload", default=DEFAULT_WORKLOAD)
+    p.add_argument("--reads", type=int, default=0, help="override the workload's read (pair) count")
+    p.add_argument("--cpu-sample", type=int, default=60000, help="reads (pairs) of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fastq", action="store_true", help="skip the whole-file leg")
     return p.parse_args()
 
 
@@ -202,26 +230,11 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-def make_pair_workload(name, n_pairs):
-    from fame_gb300 import synth
-    spec = synth.WORKLOADS[name]
-    g = synth.make_genome(**spec["genome"])
-    pk = dict(spec["pairs"])
-    if n_pairs:
-        pk["n_pairs"] = n_pairs
-    r1, r2 = synth.make_pairs(g, **pk)
-    return g, r1, r2
+# workloads and the reference library
 
-
-def make_workload(name, n_reads):
+def spec_of(name):
     from fame_gb300 import synth
-    spec = synth.WORKLOADS[name]
-    g = synth.make_genome(**spec["genome"])
-    rk = dict(spec["reads"])
-    if n_reads:
-        rk["n_reads"] = n_reads
-    rs = synth.make_reads(g, **rk)
-    return g, rs, rk.get("read_len", 100)
+    return synth.WORKLOADS[name]
 
 
 def chunk_list(rs, chunk):
@@ -244,45 +257,51 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(hi, seq, chunks, sample, readlen):
-    """The reference's OpenMP matchReads on a bounded sample of chunk 1 (steady state)."""
+def ref_library(readlen, maxpdist=550, build_if_missing=False):
+    """(RefLib of the reference compiled with these constants, None) or (None, why)."""
     try:
         from oracle import refbind
-        if not refbind.available():
-            raise RuntimeError("reference library not built")
-        L = refbind.RefLib()
-        if L.readlen != readlen:
-            raise RuntimeError("reference built for READLEN %d" % L.readlen)
-        t = hi.tables(sparse=False)
+        if not refbind.available(readlen, maxpdist) and build_if_missing:
+            import __graft_entry__
+            __graft_entry__.build()
+        if not refbind.available(readlen, maxpdist):
+            return None, "reference not built for READLEN %d / MAXPDIST %d (oracle/build_ref.sh)" % (readlen, maxpdist)
+        return refbind.RefLib(refbind.variant_path(readlen, maxpdist)), None
+    except Exception as e:   # a library that fails to load
+        return None, "reference library unavailable: %s" % e
 
-        class Arrays:
-            pass
 
-        a = Arrays()
-        a.chrom_seqs = hi.chrom_seqs()
-        a.chrom_names = hi.chrom_names()
-        for k, v in t.items():
-            setattr(a, k, v)
-        a.tab_index64 = hi.tab_index64
-        ri = L.from_arrays(a)
-        base, o = chunks[1] if len(chunks) > 1 else chunks[0]
-        n = min(sample, len(o) - 1)
-        o = o[:n + 1]
-        s = seq[base:base + int(o[-1])].tobytes()
-        secs, cnt = ri.time_se(s, o, both_strands=False, match_r1_fwd=True)
-        ri.close()
-        return {"value": n / secs, "unit": "reads/s", "cores": L.corenum, "kind": "reference",
-                "sample": "%d reads of chunk 1 (300k-read CHUNKSIZE), decided orientation, matchReads only, "
-                          "CORENUM=%d OpenMP threads" % (n, L.corenum), "seconds": secs,
-                "succ": int(cnt[0])}
-    except Exception as e:
-        from oracle.oracle import OracleIndex  # single-threaded C restatement
-        return {"value": None, "unit": "reads/s", "cores": 1, "kind": "port",
-                "sample": "reference unavailable (%s)" % e}
+def ref_index_from_host(L, hi):
+    """The reference's RefGenome filled with the tables of an index built by
+    fame_index_build (equal to the reference constructor's, tests/test_index_build.py)."""
+    t = hi.tables(sparse=False)
+
+    class Arrays:
+        pass
+
+    a = Arrays()
+    a.chrom_seqs = hi.chrom_seqs()
+    a.chrom_names = hi.chrom_names()
+    for k, v in t.items():
+        setattr(a, k, v)
+    a.tab_index64 = hi.tab_index64
+    ri = L.from_arrays(a)
+    del a, t
+    gc.collect()
+    return ri
+
+
+def compare_se(got, ref):
+    """Per-read and per-CpG comparison of two single-end results."""
+    bad_reads = int(((got["mat"] != ref["mat"]) | (got["invalid"] != ref["invalid"])).sum())
+    bad_cpgs = int((got["meth"] != ref["meth"]).any(1).sum())
+    return {"reads": int(len(got["mat"])), "mismatched_reads": bad_reads, "mismatched_cpgs": bad_cpgs,
+            "counters_equal": bool(np.array_equal(np.asarray(got["counters"], np.uint64),
+                                                  np.asarray(ref["counters"], np.uint64)))}
 
 
 # ---------------------------------------------------------------------------
-def fastq_file_leg(gm, rs):
+def fastq_file_leg(gm, rs, slots=3):
     """Whole-file form (fame_match_fastq): the workload's reads written as a
     plain FASTQ file, parsed by the native reader straight into queue slots
     while earlier chunks run, strand vote on chunk 0; host clock around the
@@ -290,7 +309,6 @@ def fastq_file_leg(gm, rs):
     cache); each call opens and frees its own queue."""
     import shutil
     import tempfile
-    from fame_gb300 import FAME_MAX_READ_LEN
     d = tempfile.mkdtemp(prefix="fame_bench_")
     try:
         path = os.path.join(d, "reads.fq")
@@ -301,12 +319,12 @@ def fastq_file_leg(gm, rs):
         times = []
         for _ in range(2):
             t0 = time.perf_counter()
-            cnt, n = gm.match_fastq(path, False, 0, slots=3, threads=0)
+            cnt, n = gm.match_fastq(path, False, 0, slots=slots, threads=0)
             times.append(time.perf_counter() - t0)
         gm.tallies(reset=True)
         return {"value": n / times[-1], "unit": "reads/s", "reads": n, "file_bytes": size,
-                "first_call_reads_per_s": n / times[0], "write_seconds": t_write, "slots": 3,
-                "matched": int(cnt.succ), "max_read_len": FAME_MAX_READ_LEN,
+                "first_call_reads_per_s": n / times[0], "write_seconds": t_write, "slots": slots,
+                "matched": int(cnt.succ),
                 "timing": "host clock around fame_match_fastq: parse + copy + match + tallies, file in page cache"}
     finally:
         shutil.rmtree(d, ignore_errors=True)
@@ -314,26 +332,34 @@ def fastq_file_leg(gm, rs):
 
 def run_gb300(args):
     import torch
-    from fame_gb300 import FAME_GET_STRANDED, FAME_MATCH_R1_FWD, GpuMatcher, HostIndex, CHUNKSIZE
+    from fame_gb300 import (CHUNKSIZE, FAME_GET_STRANDED, FAME_MATCH_R1_FWD, GpuMatcher, GpuQueue, HostIndex,
+                            synth)
+    from fame_gb300._lib import lib as _L
     rank, world, local = dist_init(args.gpus)
     t0 = time.time()
-    g, rs, readlen = make_workload(args.workload, args.reads)
+    g = synth.genome_of(args.workload)
+    rs, readlen = synth.reads_of(args.workload, g, args.reads)
     t_gen = time.time() - t0
     t0 = time.time()
     hi = HostIndex.build(g.seqs, readlen=readlen, threads=0)
     t_build = time.time() - t0
+    genome_bp, n_chrom = int(g.total_len), len(g.seqs)
+    del g
+    gc.collect()
     t0 = time.time()
     gm = GpuMatcher(hi, local)
     t_open = time.time() - t0
     seq, chunks = chunk_list(rs, CHUNKSIZE)
-    # device-resident copies of every chunk this rank handles (value) and pinned host copies (e2e)
+    # chunk 0 runs the strand vote in the warm-up; the timed steps cycle over this rank's later chunks
     mine = [i for i in range(len(chunks)) if i % world == rank] or [0]
-    dev = {}
-    pinned = {}
-    maxn = max(len(o) - 1 for _, o in chunks)
+    first = mine[0]
+    steady = [i for i in mine if i != 0] or mine
+    used = sorted({first} | set(steady[:max(args.steps, args.warmup, 1)]))
+    dev, pinned = {}, {}
+    maxn = max(len(chunks[i][1]) - 1 for i in used)
     d_mat = gm.alloc(8 * maxn)
     d_inv = gm.alloc(maxn)
-    for i in mine:
+    for i in used:
         base, o = chunks[i]
         nb = int(o[-1])
         d_s = gm.alloc(nb)
@@ -348,27 +374,21 @@ def run_gb300(args):
         pinned[i] = (hs, ho, len(o) - 1)
     h_mat = gm.host_alloc(8 * maxn).view(np.uint64)
     h_inv = gm.host_alloc(maxn)
-    p_stream = __import__("ctypes").c_void_p()
-    from fame_gb300._lib import lib as _L
-    _L().fame_gpu_stream(gm.h, __import__("ctypes").byref(p_stream))
+    p_stream = ctypes.c_void_p()
+    _L().fame_gpu_stream(gm.h, ctypes.byref(p_stream))
     stream = torch.cuda.ExternalStream(p_stream.value, device=local)
     clk = ClockSampler(local).start()
-    # warm-up: chunk 0 with the strand vote (getStranded), then decided orientation
-    first = mine[0]
+    # warm-up: chunk 0 with the strand vote (getStranded), then the decided orientation
     d_s, d_o, n = dev[first]
     c = gm.match_reads_dev(d_s, d_o, n, FAME_GET_STRANDED, d_mat, d_inv)
     flags = FAME_MATCH_R1_FWD if c.r1_fwd > c.r1_rev else 0
-    steady = [i for i in mine if i != 0] or mine
     for w in range(max(0, args.warmup - 1)):
         d_s, d_o, n = dev[steady[w % len(steady)]]
         gm.match_reads_dev(d_s, d_o, n, flags, d_mat, d_inv)
     gm.set_timing(True)
-    # ---- timed: device-resident reads
+    # ---- timed: plain form, reads resident in HBM
     stage = np.zeros(6)
-    reads = 0
-    gather = 0
-    scans = 0
-    launches = 0
+    reads = gather = scans = launches = heavy = reruns = dp = inv_len = succ = 0
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
     torch.cuda.synchronize()
@@ -381,18 +401,21 @@ def run_gb300(args):
         reads += n
         gather += c.gather_bytes
         scans += c.windows_scanned
+        heavy += c.heavy_tasks
+        reruns += c.reruns
+        dp += c.dp_reads
+        inv_len += c.invalid_len
+        succ += c.succ
         launches += gm.last_launches()
     ev1.record(stream)
     torch.cuda.synchronize()
     tw1 = time.perf_counter()
     clk.mark(tw0, tw1)
     barrier(world)
-    t_dev = ev0.elapsed_time(ev1) / 1e3
-    t_max = allreduce_max(t_dev, world)
+    t_max = allreduce_max(ev0.elapsed_time(ev1) / 1e3, world)
     total_reads = reads * world
-    # ---- timed: end to end from pinned host memory
-    e_reads = 0
-    h2d = d2h = 0
+    # ---- timed: end to end from page-locked host memory
+    e_reads = h2d = d2h = 0
     for w in range(args.warmup):   # untimed: the host-buffer path's first calls (its device staging grows)
         hs, ho, n = pinned[steady[w % len(steady)]]
         gm.match_reads(hs, ho, flags, mats=h_mat[:n], invalid=h_inv[:n])
@@ -412,10 +435,9 @@ def run_gb300(args):
     t_e2e = allreduce_max(ev0.elapsed_time(ev1) / 1e3, world)
     gm.set_timing(False)
     # ---- batched form: the same steps through the queue (CUDA-graph chunk
-    # slots on their own streams, copies of one chunk overlapping the kernels
-    # of another), from the same pinned host buffers; host clock between two
+    # slots on their own streams, the copies of one chunk overlapping the
+    # kernels of another), from the same host buffers; host clock between two
     # device synchronisations (the work spans several streams)
-    from fame_gb300 import GpuQueue
     nslots = 3
     q = GpuQueue(gm, nslots, maxn, max(int(p[0].nbytes) for p in pinned.values()))
     for w in range(nslots):
@@ -424,6 +446,7 @@ def run_gb300(args):
     launches_q0 = q.launches()
     b_reads = 0
     inflight = []
+    barrier(world)
     torch.cuda.synchronize()
     tb0 = time.perf_counter()
     for k in range(args.steps):
@@ -441,27 +464,47 @@ def run_gb300(args):
     clk.stop()
     t_b = allreduce_max(tb1 - tb0, world)
     batched = {"value": b_reads * world / t_b, "unit": "reads/s", "slots": nslots,
+               "vs_plain": (b_reads * world / t_b) / (total_reads / t_max),
                "gpu_launches": q.launches() - launches_q0,
                "timing": "host clock between device synchronisations; host buffers in and out"}
     q.close()
-    fastq = fastq_file_leg(gm, rs) if rank == 0 else None
-    # ---- roofline of the index-gather (seeding) kernel and the Shift-And kernel
+    fastq = fastq_file_leg(gm, rs) if (rank == 0 and not args.no_fastq) else None
+    # ---- parity sample: the first reads of chunk 1 in the decided orientation
+    # on the GPU (tallies of the sample alone), checked below against the reference
+    sample = None
+    if rank == 0 and not args.no_cpu_baseline:
+        sc = 1 if len(chunks) > 1 else 0
+        base, o = chunks[sc]
+        ns = min(args.cpu_sample, len(o) - 1)
+        so = o[:ns + 1].copy()
+        ss = seq[base:base + int(so[-1])].tobytes()
+        gm.tallies(reset=True)
+        m, iv, cc = gm.match_reads(ss, so, flags)
+        sample = dict(seq=ss, offs=so, chunk=sc,
+                      got=dict(mat=m, invalid=iv, meth=gm.tallies(reset=True),
+                               counters=[cc.succ, cc.nonunique, cc.unsucc]))
+    # ---- roofline of the index-gather kernel
     hbm, src = peaks()
     names = ["read_prep", "seed_gather", "shift_and", "select_exact_cpg", "banded_dp", "seed_heavy"]
     st = {names[i]: stage[i] / 1e3 for i in range(6)}
     dominant = max(names, key=lambda k: st[k])
-    traffic = SEED_TRAFFIC_PER_LAUNCH if args.workload == "se100_300mbp" and not args.reads else None
     seed_s = st["seed_gather"] + st["seed_heavy"]
     gbps = gather / seed_s / 1e9 if seed_s > 0 else 0.0
+    fig = NCU_FIGURES.get(args.workload) if not args.reads else None
+    src_hash = kernel_source_hash()
+    fig_ok = bool(fig) and fig.get("source_hash") == src_hash
+    traffic = fig["seed_traffic_per_launch"] if fig_ok else None
     out = {
         "metric": METRIC, "value": total_reads / t_max, "unit": "reads/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 integer",
-        "data": "synthetic (seeded; genome and bisulfite reads per the workload definition)",
-        "config": {"workload": args.workload, "genome_bp": int(g.total_len), "chromosomes": len(g.seqs),
-                   "reads_total": len(rs), "read_len": readlen, "chunk_reads": CHUNKSIZE,
+        "data": "synthetic (seeded genome and bisulfite reads per the workload definition, fame_gb300/synth.py)",
+        "config": {"workload": args.workload, "genome_bp": genome_bp, "chromosomes": n_chrom,
+                   "reads_total": len(rs), "read_len": readlen,
+                   "read_lengths": [int(rs.lens.min()), int(rs.lens.max())], "chunk_reads": CHUNKSIZE,
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2: each step gathers from a 9.8 GB index and new reads"},
+                   "l2": "inputs larger than L2: every step gathers from the device index (%.1f GB) and new reads"
+                         % (gm.index_bytes() / 1e9)},
         "e2e": {"value": e_reads * world / t_e2e, "unit": "reads/s", "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps)},
         "gpu_launches": launches,
@@ -469,35 +512,65 @@ def run_gb300(args):
         "fastq_file": fastq,
         "stage_seconds": st,
         "dominant_kernel": dominant,
+        "counts": {"reads": reads, "matched": succ, "invalid_len": inv_len, "dp_reads": dp,
+                   "windows_scanned_per_read": scans / max(1, reads), "heavy_seed_tasks": heavy,
+                   "candidate_overflow_reruns": reruns},
         "roofline": {"kernel": "k_seed (index gathers)", "bound": "hbm", "achieved": gbps, "peak": hbm,
                      "unit": "GB/s", "frac": gbps / hbm, "traffic": traffic,
                      "dram_achieved": traffic / (seed_s / args.steps) / 1e9 if (traffic and seed_s > 0) else None,
-                     "note": "algorithmic bytes = 8 B bucket bounds + 4 B per bucket entry per k-mer; peak %s; "
-                             "traffic = dram read + write of one steady-state launch (ncu, 1 pass); "
-                             "dram_achieved = traffic / launch time" % src},
+                     "note": "algorithmic bytes = 8 B bucket bounds + 4 B per bucket entry per k-mer lookup, "
+                             "counted on the device; peak %s; traffic = DRAM read + write of one steady-state "
+                             "launch from ncu (%s)" % (src, fig["profile"] if fig_ok else
+                                                       "no capture of the current kernel sources")},
         "alu_bound_kernels": {
-            "note": "stages bound by the integer/logic pipe, not by HBM or tensor cores: ALU-pipe utilisation "
-                    "from the committed ncu captures of the 20 Mbp workload (not measured by this run)",
-            "k_shiftand": {"stage_ms": 1e3 * st["shift_and"] / args.steps, "alu_pipe_of_peak": 0.647,
-                           "profile": "profiles/k_shiftand_se100_20mbp.md"},
-            "k_dp_warp": {"stage_ms": 1e3 * st["banded_dp"] / args.steps, "alu_pipe_of_peak": 0.684,
-                          "profile": "profiles/k_dp_warp_se100_20mbp.md"},
-        },
-        "windows_scanned_per_read": scans / max(1, reads),
+            "k_shiftand": {"stage_ms": 1e3 * st["shift_and"] / args.steps,
+                           "alu_pipe_of_peak": fig.get("shiftand_alu") if fig_ok else None},
+            "k_dp_warp": {"stage_ms": 1e3 * st["banded_dp"] / args.steps,
+                          "alu_pipe_of_peak": fig.get("dp_alu") if fig_ok else None},
+            "note": "stages bound by the integer/logic pipe, not by HBM or tensor cores; ALU-pipe figures from "
+                    "ncu captures of the same kernel sources (kernel source hash %s)" % src_hash},
         "host": host_placement(local),
         "clocks": clk.summary(),
         "setup_seconds": {"generate": t_gen, "index_build": t_build, "upload": t_open},
     }
-    if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(hi, seq, chunks, args.cpu_sample, readlen)
-    for i in mine:
+    for i in used:
         gm.free(dev[i][0])
         gm.free(dev[i][1])
     gm.close()
+    del dev, pinned, h_mat, h_inv
+    gc.collect()
+    if sample is not None:
+        out["cpu_baseline"], out["parity"] = cpu_baseline_se(hi, readlen, sample, flags)
     if rank == 0:
         emit(out)
 
 
+def cpu_baseline_se(hi, readlen, sample, flags):
+    """The reference's OpenMP matchReads on the sample (decided orientation, the
+    steady state), timed; its per-read results and tallies compared with the GPU's."""
+    from fame_gb300 import FAME_MATCH_R1_FWD
+    L, why = ref_library(readlen)
+    n = len(sample["offs"]) - 1
+    if L is None:
+        return {"value": None, "unit": "reads/s", "cores": 0, "kind": "reference", "sample": why}, \
+            {"reads": n, "checked": False, "why": why}
+    t0 = time.time()
+    ri = ref_index_from_host(L, hi)
+    t_load = time.time() - t0
+    secs, cnt, ref = ri.time_se(sample["seq"], sample["offs"], both_strands=False,
+                                match_r1_fwd=bool(flags & FAME_MATCH_R1_FWD), outputs=True)
+    ri.close()
+    ref["counters"] = [int(x) for x in cnt[:3]]
+    par = compare_se(sample["got"], ref)
+    par.update(checker="reference (oracle/_ref, its matchReads on the same index tables)", chunk=sample["chunk"])
+    base = {"value": n / secs, "unit": "reads/s", "cores": L.corenum, "kind": "reference",
+            "sample": "%d reads of chunk %d (300k-read CHUNKSIZE), decided orientation, matchReads only, "
+                      "CORENUM=%d OpenMP threads, READLEN %d" % (n, sample["chunk"], L.corenum, L.readlen),
+            "seconds": secs, "index_load_seconds": t_load}
+    return base, par
+
+
+# ---------------------------------------------------------------------------
 SERVING_METRIC = "aggregate reads/s of a single-cell job stream (serving form), with p50/p99 job latency"
 
 
@@ -558,83 +631,92 @@ def run_gb300_serving(args):
     emit(out)
 
 
-PE_METRIC = "aligned read pairs/s (paired-end matching stage, bit-exact CpG report)"
-PE_MAXPDIST = 550   # the MAXPDIST the reference library is compiled with (CONST.h:42)
-
-
+# ---------------------------------------------------------------------------
 def run_gb300_pe(args):
     """Paired-end form: one step = one 300k-pair chunk through matchPairedReads
     semantics (fame_gpu_match_pairs_dev; mates resident in HBM), e2e through
-    fame_gpu_match_pairs from pinned host buffers."""
-    import ctypes
+    fame_gpu_match_pairs from page-locked host buffers."""
     import torch
-    from fame_gb300 import FAME_GET_STRANDED, FAME_MATCH_R1_FWD, GpuMatcher, HostIndex, CHUNKSIZE
+    from fame_gb300 import CHUNKSIZE, FAME_GET_STRANDED, FAME_MATCH_R1_FWD, GpuMatcher, HostIndex, synth
     from fame_gb300._lib import lib as _L
+    spec = spec_of(args.workload)
+    maxpdist = int(spec.get("maxpdist", 550))
     t0 = time.time()
-    g, r1, r2 = make_pair_workload(args.workload, args.reads)
+    g = synth.genome_of(args.workload)
+    r1, r2 = synth.pairs_of(args.workload, g, args.reads)
     t_gen = time.time() - t0
     t0 = time.time()
     hi = HostIndex.build(g.seqs, readlen=100, threads=0)
     t_build = time.time() - t0
+    genome_bp = int(g.total_len)
+    del g
+    gc.collect()
+    t0 = time.time()
     gm = GpuMatcher(hi, 0)
+    t_open = time.time() - t0
     s1, o1 = r1.concat()
     s2, o2 = r2.concat()
     n = len(o1) - 1
     chunks = [(c0, min(n, c0 + CHUNKSIZE)) for c0 in range(0, n, CHUNKSIZE)]
-    dev, pinned = [], []
-    maxn = max(b - a for a, b in chunks)
+    steady = list(range(1, len(chunks))) or [0]
+    used = sorted({0} | set(steady[:max(args.steps, args.warmup, 1)]))
+    dev, pinned = {}, {}
+    maxn = max(chunks[i][1] - chunks[i][0] for i in used)
     d_mat = gm.alloc(16 * maxn)
     d_inv = gm.alloc(2 * maxn)
-    for a, b in chunks:
-        m1 = np.frombuffer(s1, np.uint8)[int(o1[a]):int(o1[b])]
-        m2 = np.frombuffer(s2, np.uint8)[int(o2[a]):int(o2[b])]
+    b1a, b2a = np.frombuffer(s1, np.uint8), np.frombuffer(s2, np.uint8)
+    for i in used:
+        a, b = chunks[i]
+        m1 = b1a[int(o1[a]):int(o1[b])]
+        m2 = b2a[int(o2[a]):int(o2[b])]
         oo = np.concatenate([o1[a:b + 1] - o1[a], (o2[a + 1:b + 1] - o2[a]) + (o1[b] - o1[a])]).astype(np.uint64)
         buf = np.concatenate([m1, m2])
         d_s = gm.alloc(len(buf))
         d_o = gm.alloc(8 * len(oo))
         gm.memcpy(d_s, buf.ctypes.data, len(buf), 1)
         gm.memcpy(d_o, oo.ctypes.data, 8 * len(oo), 1)
-        dev.append((d_s, d_o, b - a))
+        dev[i] = (d_s, d_o, b - a)
         h1 = gm.host_alloc(len(m1)); h1[:] = m1
         h2 = gm.host_alloc(len(m2)); h2[:] = m2
         ho1 = gm.host_alloc(8 * (b - a + 1)).view(np.uint64); ho1[:] = o1[a:b + 1] - o1[a]
         ho2 = gm.host_alloc(8 * (b - a + 1)).view(np.uint64); ho2[:] = o2[a:b + 1] - o2[a]
-        pinned.append((h1, ho1, h2, ho2, b - a))
+        pinned[i] = (h1, ho1, h2, ho2, b - a)
     p_stream = ctypes.c_void_p()
     _L().fame_gpu_stream(gm.h, ctypes.byref(p_stream))
     stream = torch.cuda.ExternalStream(p_stream.value, device=0)
     clk = ClockSampler(0).start()
     d_s, d_o, nn = dev[0]
-    c = gm.match_pairs_dev(d_s, d_o, nn, FAME_GET_STRANDED, PE_MAXPDIST, d_mat, d_inv)
+    c = gm.match_pairs_dev(d_s, d_o, nn, FAME_GET_STRANDED, maxpdist, d_mat, d_inv)
     flags = FAME_MATCH_R1_FWD if c.r1_fwd > c.r1_rev else 0
-    steady = list(range(1, len(chunks))) or [0]
     for w in range(max(0, args.warmup - 1)):
         d_s, d_o, nn = dev[steady[w % len(steady)]]
-        gm.match_pairs_dev(d_s, d_o, nn, flags, PE_MAXPDIST, d_mat, d_inv)
+        gm.match_pairs_dev(d_s, d_o, nn, flags, maxpdist, d_mat, d_inv)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    pairs = 0
-    launches = 0
-    heavy = 0
+    pairs = launches = heavy = paired = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ev0.record(stream)
     for k in range(args.steps):
         d_s, d_o, nn = dev[steady[k % len(steady)]]
-        c = gm.match_pairs_dev(d_s, d_o, nn, flags, PE_MAXPDIST, d_mat, d_inv)
+        c = gm.match_pairs_dev(d_s, d_o, nn, flags, maxpdist, d_mat, d_inv)
         pairs += nn
         heavy += c.heavy_pairs
+        paired += c.paired
         launches += gm.last_launches()
     ev1.record(stream)
     torch.cuda.synchronize()
     clk.mark(t0, time.perf_counter())
     t_dev = ev0.elapsed_time(ev1) / 1e3
+    for w in range(args.warmup):
+        h1, ho1, h2, ho2, nn = pinned[steady[w % len(steady)]]
+        gm.match_pairs(h1, ho1, h2, ho2, flags, maxpdist)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ev0.record(stream)
     e_pairs = h2d = d2h = 0
     for k in range(args.steps):
         h1, ho1, h2, ho2, nn = pinned[steady[k % len(steady)]]
-        gm.match_pairs(h1, ho1, h2, ho2, flags, PE_MAXPDIST)
+        gm.match_pairs(h1, ho1, h2, ho2, flags, maxpdist)
         e_pairs += nn
         h2d += h1.nbytes + h2.nbytes + 16 * (nn + 1)
         d2h += 18 * nn
@@ -643,175 +725,157 @@ def run_gb300_pe(args):
     clk.mark(t0, time.perf_counter())
     clk.stop()
     t_e2e = ev0.elapsed_time(ev1) / 1e3
+    # parity sample: the first pairs of chunk 1 in the decided orientation
+    sample = None
+    if not args.no_cpu_baseline:
+        sc = 1 if len(chunks) > 1 else 0
+        c0, c1 = chunks[sc]
+        ns = min(args.cpu_sample, c1 - c0)
+        p1 = o1[c0:c0 + ns + 1]
+        p2 = o2[c0:c0 + ns + 1]
+        q1, q2 = s1[int(p1[0]):int(p1[-1])], s2[int(p2[0]):int(p2[-1])]
+        gm.tallies(reset=True)
+        m1, m2, i1, i2, cc = gm.match_pairs(q1, p1 - p1[0], q2, p2 - p2[0], flags, maxpdist)
+        sample = dict(s1=q1, o1=p1 - p1[0], s2=q2, o2=p2 - p2[0], chunk=sc,
+                      got=dict(mat1=m1, mat2=m2, inv1=i1, inv2=i2, meth=gm.tallies(reset=True),
+                               counters=[cc.succ, cc.nonunique, cc.unsucc, cc.paired, cc.too_short]))
     out = {
         "metric": PE_METRIC, "value": pairs / t_dev, "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 integer",
-        "data": "synthetic (seeded; genome and bisulfite read pairs per the workload definition)",
-        "config": {"workload": args.workload, "genome_bp": int(g.total_len), "pairs_total": n, "read_len": 100,
-                   "chunk_pairs": CHUNKSIZE, "maxpdist": PE_MAXPDIST, "parallelism": "single GPU",
-                   "l2": "inputs larger than L2: each step gathers from an 11 GB index and new pairs"},
+        "data": "synthetic (seeded genome and bisulfite read pairs per the workload definition)",
+        "config": {"workload": args.workload, "genome_bp": genome_bp, "pairs_total": n, "read_len": 100,
+                   "chunk_pairs": CHUNKSIZE, "maxpdist": maxpdist, "parallelism": "single GPU",
+                   "l2": "inputs larger than L2: every step gathers from the device index (%.1f GB) and new pairs"
+                         % (gm.index_bytes() / 1e9)},
         "e2e": {"value": e_pairs / t_e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps)},
-        "gpu_launches": launches, "heavy_pairs": heavy, "clocks": clk.summary(),
-        "setup_seconds": {"generate": t_gen, "index_build": t_build},
+        "gpu_launches": launches, "counts": {"pairs": pairs, "paired": paired, "heavy_pairs": heavy},
+        "clocks": clk.summary(),
+        "setup_seconds": {"generate": t_gen, "index_build": t_build, "upload": t_open},
     }
-    if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline_pe(hi, s1, o1, s2, o2, chunks, args.cpu_sample)
-    for d_s, d_o, _ in dev:
+    for d_s, d_o, _ in dev.values():
         gm.free(d_s)
         gm.free(d_o)
     gm.close()
+    del dev, pinned
+    gc.collect()
+    if sample is not None:
+        out["cpu_baseline"], out["parity"] = cpu_baseline_pe(hi, maxpdist, sample, flags)
     emit(out)
 
 
-def cpu_baseline_pe(hi, s1, o1, s2, o2, chunks, sample):
-    """The reference's OpenMP matchPairedReads on a bounded sample of chunk 1."""
-    try:
-        from oracle import refbind
-        if not refbind.available():
-            raise RuntimeError("reference library not built")
-        L = refbind.RefLib()
-        t = hi.tables(sparse=False)
-
-        class Arrays:
-            pass
-
-        a = Arrays()
-        a.chrom_seqs = hi.chrom_seqs()
-        a.chrom_names = hi.chrom_names()
-        for k, v in t.items():
-            setattr(a, k, v)
-        a.tab_index64 = hi.tab_index64
-        ri = L.from_arrays(a)
-        c0, c1 = chunks[1] if len(chunks) > 1 else chunks[0]
-        nn = min(sample, c1 - c0)
-        p1 = o1[c0:c0 + nn + 1]
-        p2 = o2[c0:c0 + nn + 1]
-        secs, cnt = ri.time_pe(s1[int(p1[0]):int(p1[-1])], p1 - p1[0], s2[int(p2[0]):int(p2[-1])], p2 - p2[0],
-                               both_strands=False, match_r1_fwd=True)
-        ri.close()
-        return {"value": nn / secs, "unit": "pairs/s", "cores": L.corenum, "kind": "reference",
-                "sample": "%d pairs of chunk 1, decided orientation, matchPairedReads only, CORENUM=%d OpenMP "
-                          "threads, MAXPDIST %d" % (nn, L.corenum, L.maxpdist()), "seconds": secs,
-                "succ": int(cnt[0])}
-    except Exception as e:
-        return {"value": None, "unit": "pairs/s", "cores": 1, "kind": "port", "sample": "reference unavailable (%s)" % e}
-
-
-def run_reference_pe(args, L):
-    """The paired workload through the reference's matchPairedReads (bounded
-    samples of consecutive chunks, decided orientation), pairs/s."""
-    from fame_gb300 import CHUNKSIZE
-    g, r1, r2 = make_pair_workload(args.workload, args.reads)
-    fasta = "/tmp/fame_bench_%s.fa" % args.workload
-    g.write_fasta(fasta)
-    t0 = time.time()
-    ri = L.build(fasta)
-    t_build = time.time() - t0
-    s1, o1 = r1.concat()
-    s2, o2 = r2.concat()
-    n = len(o1) - 1
-    sample = min(args.cpu_sample, CHUNKSIZE)
-    starts = list(range(CHUNKSIZE, n, CHUNKSIZE)) or [0]
-
-    def step(k):
-        c0 = starts[k % len(starts)]
-        nn = min(sample, n - c0)
-        p1 = o1[c0:c0 + nn + 1]
-        p2 = o2[c0:c0 + nn + 1]
-        secs, _ = ri.time_pe(s1[int(p1[0]):int(p1[-1])], p1 - p1[0], s2[int(p2[0]):int(p2[-1])], p2 - p2[0],
-                             both_strands=False, match_r1_fwd=True)
-        return secs, nn
-
-    for k in range(args.warmup):
-        step(k)
-    secs = 0.0
-    pairs = 0
-    for k in range(args.steps):
-        s_, nn = step(k)
-        secs += s_
-        pairs += nn
-    v = pairs / secs
-    emit({
-        "impl": "reference", "metric": "aligned pairs/s (paired-end matching stage, bit-exact CpG report)",
-        "value": v, "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u8/u64 integer", "data": "synthetic (seeded)",
-        "config": {"workload": args.workload, "pairs_per_step": sample, "maxpdist": L.maxpdist()},
-        "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": L.corenum, "kind": "reference",
-                         "sample": "%d pairs per step from consecutive 300k-pair chunks, decided orientation"
-                                   % sample},
-        "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "setup_seconds": {"index_build": t_build, "index_build_cores": L.corenum}})
+def cpu_baseline_pe(hi, maxpdist, sample, flags):
+    """The reference's OpenMP matchPairedReads on the sample, timed; per-mate
+    results and tallies compared with the GPU's."""
+    from fame_gb300 import FAME_MATCH_R1_FWD
+    L, why = ref_library(100, maxpdist)
+    n = len(sample["o1"]) - 1
+    if L is None:
+        return {"value": None, "unit": "pairs/s", "cores": 0, "kind": "reference", "sample": why}, \
+            {"pairs": n, "checked": False, "why": why}
+    ri = ref_index_from_host(L, hi)
+    secs, cnt, ref = ri.time_pe(sample["s1"], sample["o1"], sample["s2"], sample["o2"], both_strands=False,
+                                match_r1_fwd=bool(flags & FAME_MATCH_R1_FWD), outputs=True)
     ri.close()
+    got = sample["got"]
+    bad = int(((got["mat1"] != ref["mat1"]) | (got["mat2"] != ref["mat2"]) | (got["inv1"] != ref["inv1"]) |
+               (got["inv2"] != ref["inv2"])).sum())
+    par = {"pairs": n, "mismatched_pairs": bad, "mismatched_cpgs": int((got["meth"] != ref["meth"]).any(1).sum()),
+           "counters_equal": bool(np.array_equal(np.asarray(got["counters"], np.uint64), cnt[:5])),
+           "checker": "reference (oracle/_ref, its matchPairedReads on the same index tables)",
+           "chunk": sample["chunk"]}
+    base = {"value": n / secs, "unit": "pairs/s", "cores": L.corenum, "kind": "reference",
+            "sample": "%d pairs of chunk %d, decided orientation, matchPairedReads only, CORENUM=%d OpenMP "
+                      "threads, MAXPDIST %d" % (n, sample["chunk"], L.corenum, L.maxpdist()), "seconds": secs}
+    return base, par
 
 
+# ---------------------------------------------------------------------------
 def run_reference(args):
+    """The reference's own OpenMP matching on the machine's host cores, on bounded
+    samples of the same chunks (decided orientation).  Its index: the
+    reference's own constructor for the 300 Mbp workloads; for the 3 Gbp ones
+    (about 70 minutes in that constructor) the tables fame_index_build
+    produces, loaded into the reference's RefGenome (the same tables)."""
     rank, world, local = dist_init(args.gpus)
     if rank != 0:
         return
-    from fame_gb300 import CHUNKSIZE, HostIndex
-    if args.workload.startswith("pe"):
-        try:
-            from oracle import refbind
-            if not refbind.available():
-                import __graft_entry__
-                __graft_entry__.build()
-            if not refbind.available():
-                raise RuntimeError("reference sources not available to oracle/build_ref.sh")
-            L = refbind.RefLib()
-        except Exception as e:
-            emit({"impl": "reference", "unavailable": "reference build failed: %s" % e})
-            return
-        run_reference_pe(args, L)
+    from fame_gb300 import CHUNKSIZE, HostIndex, synth
+    spec = spec_of(args.workload)
+    paired = "pairs" in spec
+    readlen = 100 if paired else int(spec["reads"].get("read_len", 100))
+    maxpdist = int(spec.get("maxpdist", 550)) if paired else 550
+    L, why = ref_library(readlen, maxpdist, build_if_missing=True)
+    if L is None:
+        emit({"impl": "reference", "unavailable": why})
         return
-    g, rs, readlen = make_workload(args.workload, args.reads)
-    try:
-        from oracle import refbind
-        if not refbind.available():
-            import __graft_entry__
-            __graft_entry__.build()
-        if not refbind.available():
-            raise RuntimeError("reference sources not available to oracle/build_ref.sh")
-        L = refbind.RefLib()
+    g = synth.genome_of(args.workload)
+    if paired:
+        r1, r2 = synth.pairs_of(args.workload, g, args.reads)
+    else:
+        rs, _ = synth.reads_of(args.workload, g, args.reads)
+    t0 = time.time()
+    if spec.get("large"):
+        hi = HostIndex.build(g.seqs, readlen=readlen, threads=0)
+        del g
+        gc.collect()
+        ri = ref_index_from_host(L, hi)
+        hi.close()
+        how = "tables of fame_index_build loaded into the reference's RefGenome"
+    else:
         fasta = "/tmp/fame_bench_%s.fa" % args.workload
         g.write_fasta(fasta)
-        t0 = time.time()
-        ri = L.build(fasta)  # the reference's own readReference + RefGenome constructor
-        t_build = time.time() - t0
-        kind = "reference"
-    except Exception as e:
-        emit({"impl": "reference", "unavailable": "reference build failed: %s" % e})
-        return
-    seq, chunks = chunk_list(rs, CHUNKSIZE)
+        ri = L.build(fasta)   # the reference's own readReference + RefGenome constructor
+        how = "the reference's own constructor"
+    t_index = time.time() - t0
     sample = min(args.cpu_sample, CHUNKSIZE)
-    steady = list(range(1, len(chunks))) or [0]
+    if paired:
+        s1, o1 = r1.concat()
+        s2, o2 = r2.concat()
+        n = len(o1) - 1
+        starts = list(range(CHUNKSIZE, n, CHUNKSIZE)) or [0]
 
-    def step(k):
-        base, o = chunks[steady[k % len(steady)]]
-        o = o[:sample + 1]
-        return ri.time_se(seq[base:base + int(o[-1])].tobytes(), o, both_strands=False, match_r1_fwd=True), len(o) - 1
+        def step(k):
+            c0 = starts[k % len(starts)]
+            nn = min(sample, n - c0)
+            p1 = o1[c0:c0 + nn + 1]
+            p2 = o2[c0:c0 + nn + 1]
+            secs, _ = ri.time_pe(s1[int(p1[0]):int(p1[-1])], p1 - p1[0], s2[int(p2[0]):int(p2[-1])], p2 - p2[0],
+                                 both_strands=False, match_r1_fwd=True)
+            return secs, nn
+        metric, unit = PE_METRIC, "pairs/s"
+    else:
+        seq, chunks = chunk_list(rs, CHUNKSIZE)
+        steady = list(range(1, len(chunks))) or [0]
 
+        def step(k):
+            base, o = chunks[steady[k % len(steady)]]
+            o = o[:sample + 1]
+            secs, _ = ri.time_se(seq[base:base + int(o[-1])].tobytes(), o, both_strands=False, match_r1_fwd=True)
+            return secs, len(o) - 1
+        metric, unit = METRIC, "reads/s"
     for k in range(args.warmup):
         step(k)
     secs = 0.0
-    reads = 0
+    units = 0
     for k in range(args.steps):
-        (s, _), n = step(k)
-        secs += s
-        reads += n
-    v = reads / secs
+        s_, n_ = step(k)
+        secs += s_
+        units += n_
+    v = units / secs
     emit({
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "reads/s", "n_gpus": world,
+        "impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 integer",
-        "data": "synthetic (seeded)", "config": {"workload": args.workload, "reads_per_step": sample},
-        "cpu_baseline": {"value": v, "unit": "reads/s", "cores": L.corenum, "kind": kind,
-                         "sample": "%d reads per step from consecutive 300k-read chunks, decided orientation"
-                                   % sample},
-        "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "setup_seconds": {"index_build": t_build, "index_build_cores": L.corenum}})
+        "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "per_step": sample, "read_len": readlen,
+                   "maxpdist": maxpdist if paired else None},
+        "cpu_baseline": {"value": v, "unit": unit, "cores": L.corenum, "kind": "reference",
+                         "sample": "%d %s per step from consecutive 300k chunks, decided orientation; index: %s"
+                                   % (sample, "pairs" if paired else "reads", how)},
+        "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "setup_seconds": {"index": t_index, "index_cores": L.corenum}})
     ri.close()
 
 
@@ -820,9 +884,9 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
-    elif a.workload.startswith("pe"):
+    elif "pairs" in spec_of(a.workload):
         run_gb300_pe(a)
-    elif a.workload.startswith("sc_serving"):
+    elif "jobs" in spec_of(a.workload):
         run_gb300_serving(a)
     else:
         run_gb300(a)

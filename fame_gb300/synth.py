@@ -74,8 +74,8 @@ class ReadSet:
         return ReadSet(self.seqs[idx], self.lens[idx], self.chrom[idx], self.start[idx], self.fwd[idx])
 
     def write_fastq(self, path: str, block: int = 500_000) -> None:
-        """Records "@r<i>" / sequence / "+" / all-'I' qualities; reads of one
-        length are written as fixed-width blocks (names "@r"), others one by one."""
+        """Records "@r" / sequence / "+" / all-'I' qualities (FAME reads the
+        sequence line only), written in blocks."""
         lens = self.lens
         if len(self) and (lens == lens[0]).all():
             L = int(lens[0])
@@ -91,9 +91,25 @@ class ReadSet:
                     f.write(rec.tobytes())
             return
         with open(path, "wb") as f:
-            for i in range(len(self)):
-                s = self.seqs[i, : self.lens[i]].tobytes()
-                f.write(b"@r%d\n%s\n+\n%s\n" % (i, s, b"I" * len(s)))
+            # reads of different lengths: records laid out with offsets, in blocks
+            for b0 in range(0, len(self), block):
+                L = lens[b0:b0 + block].astype(np.int64)
+                rl = 2 * L + 7
+                start = np.zeros(len(L) + 1, np.int64)
+                np.cumsum(rl, out=start[1:])
+                rec = np.full(int(start[-1]), ord("I"), np.uint8)
+                st = start[:-1]
+                rec[st] = ord("@")
+                rec[st + 1] = ord("r")
+                rec[st + 2] = ord("\n")
+                for k, ch in ((3, "\n"), (4, "+"), (5, "\n")):
+                    rec[st + L + k] = ord(ch)
+                rec[start[1:] - 1] = ord("\n")
+                cols = np.arange(self.seqs.shape[1])[None, :]
+                m = cols < L[:, None]
+                pos = (st[:, None] + 3 + cols)[m]
+                rec[pos] = self.seqs[b0:b0 + block][m]
+                f.write(rec.tobytes())
 
 
 def _random_bases(rng, n, base_p):
@@ -273,13 +289,62 @@ WORKLOADS = {
     # the 300 Mbp genome above, 1.5M pairs of 2 x 100 bp, inner distance U[20, 400]
     "pe100_300mbp": dict(genome=dict(chrom_lengths=[37_500_000] * 8, seed=11, meth_p=0.7, repeat_frac=0.08),
                          pairs=dict(n_pairs=1_500_000, seed=13, inner=(20, 400), sub_rate=0.01, indel_rate=0.001)),
-    # 24 chromosomes / 3.0 Gbp, 45% repeats, READLEN 150 uneven trimmed reads
-    "se150_uneven_3gbp": dict(genome=dict(chrom_lengths=_mammal_lengths(), seed=21, meth_p=0.75,
+    # 24 chromosomes / 3.0 Gbp (250 Mbp down to 50 Mbp), 45% repeats, methylation 0.75; READLEN 150:
+    # 20M SE reads, 60% at 150 bp and 40% uniform in 36-149 bp, 0.5-2% errors per read (a tenth of them
+    # 1-bp indels), 5% of the reads drawn from repeat copies
+    "se150_uneven_3gbp": dict(large=True,
+                              genome=dict(chrom_lengths=_mammal_lengths(), seed=21, meth_p=0.75,
                                           repeat_frac=0.45),
                               reads=dict(n_reads=20_000_000, seed=22, read_len=150,
                                          length_sampler=_uneven_len, error_sampler=_per_read_err,
                                          sub_rate=0.01, indel_rate=0.001, repeat_read_frac=0.05)),
+    # the 3 Gbp workload's models on a 30 Mbp genome (4 chromosomes) with 1.2M reads: quick checks
+    "se150_uneven_30mbp": dict(large=True,
+                               genome=dict(chrom_lengths=[10_000_000, 8_000_000, 7_000_000, 5_000_000], seed=31,
+                                           meth_p=0.75, repeat_frac=0.45),
+                               reads=dict(n_reads=1_200_000, seed=32, read_len=150,
+                                          length_sampler=_uneven_len, error_sampler=_per_read_err,
+                                          sub_rate=0.01, indel_rate=0.001, repeat_read_frac=0.05)),
+    "pe100_30mbp": dict(large=True, maxpdist=400,
+                        genome=dict(chrom_lengths=[10_000_000, 8_000_000, 7_000_000, 5_000_000], seed=31,
+                                    meth_p=0.75, repeat_frac=0.45),
+                        pairs=dict(n_pairs=1_200_000, seed=33, inner=(20, 400), sub_rate=0.01, indel_rate=0.001)),
+    # the 3 Gbp genome above; 20M pairs of 2 x 100 bp, inner distance U[20, 400], mate on the opposite
+    # strand, 1% substitutions / 0.1% indels; MAXPDIST 400
+    "pe100_3gbp": dict(large=True, maxpdist=400,
+                       genome=dict(chrom_lengths=_mammal_lengths(), seed=21, meth_p=0.75, repeat_frac=0.45),
+                       pairs=dict(n_pairs=20_000_000, seed=23, inner=(20, 400), sub_rate=0.01, indel_rate=0.001)),
 }
+
+
+def genome_of(name, threads=0):
+    """The workload's genome (genome-scale generator for the 3 Gbp workloads)."""
+    spec = WORKLOADS[name]
+    if spec.get("large"):
+        return make_genome_large(**spec["genome"], threads=threads)
+    return make_genome(**spec["genome"])
+
+
+def reads_of(name, genome, n_reads=0, threads=0):
+    """(ReadSet, READLEN) of a single-end workload; n_reads overrides the count."""
+    spec = WORKLOADS[name]
+    rk = dict(spec["reads"])
+    if n_reads:
+        rk["n_reads"] = n_reads
+    if spec.get("large"):
+        return make_reads_large(genome, **rk, threads=threads), rk.get("read_len", 100)
+    return make_reads(genome, **rk), rk.get("read_len", 100)
+
+
+def pairs_of(name, genome, n_pairs=0, threads=0):
+    """(mate 1 ReadSet, mate 2 ReadSet) of a paired-end workload."""
+    spec = WORKLOADS[name]
+    pk = dict(spec["pairs"])
+    if n_pairs:
+        pk["n_pairs"] = n_pairs
+    if spec.get("large"):
+        return make_pairs_large(genome, **pk, threads=threads)
+    return make_pairs(genome, **pk)
 
 
 def make_pairs(genome: Genome, n_pairs, seed, read_len=100, inner=(20, 400), sub_rate=0.01, indel_rate=0.001):
@@ -323,3 +388,304 @@ def make_pairs(genome: Genome, n_pairs, seed, read_len=100, inner=(20, 400), sub
     r1 = ReadSet(errs(m1), lens.copy(), fr.chrom, fr.start, fr.fwd)
     r2 = ReadSet(errs(m2), lens.copy(), fr.chrom, fr.start, ~fr.fwd)
     return r1, r2
+
+
+# --- genome-scale generators (3 Gbp workloads) --------------------------------
+#
+# The same models as make_genome / make_reads, restated for multi-gigabase
+# inputs: every per-base step is a vectorised numpy operation (numpy's bulk
+# random fills and array ops release the GIL), chromosomes and read batches
+# run on a thread pool, and each chromosome / read batch draws from its own
+# PCG64 stream spawned from the seed, so the output does not depend on the
+# thread count.  Methylation is kept as sorted positions of methylated CpG Cs
+# per chromosome instead of a per-base mask, and bisulfite conversion is
+# applied per read fragment.
+
+def _threads(n=0):
+    import os
+    return n if n > 0 else max(1, min(32, os.cpu_count() or 1))
+
+
+def _base_lut(base_p):
+    # 65536-entry table with the composition to 1/65536
+    counts = np.floor(np.asarray(base_p, dtype=np.float64) * 65536).astype(np.int64)
+    counts[np.argmax(counts)] += 65536 - counts.sum()
+    return np.repeat(BASES, counts)
+
+
+def _fast_bases(rng, n, lut):
+    return lut[rng.integers(0, 65536, size=n, dtype=np.uint16)]
+
+
+@dataclasses.dataclass
+class LargeGenome:
+    names: list
+    seqs: list            # list of uint8 arrays (ASCII)
+    meth_pos: list        # per chromosome: sorted int64 positions of the C of each methylated CpG
+    cpg_pos: list         # per chromosome: sorted int64 positions of the C of every CpG
+    repeat_copies: np.ndarray   # (k, 3) int64: chrom, start, length
+
+    @property
+    def total_len(self) -> int:
+        return int(sum(len(s) for s in self.seqs))
+
+    def write_fasta(self, path: str, width: int = 80) -> None:
+        Genome.write_fasta(self, path, width)
+
+
+def make_genome_large(chrom_lengths, seed, base_p=(0.295, 0.205, 0.205, 0.295), cpg_frac=0.01, meth_p=0.75,
+                      repeat_frac=0.45, n_families=2000, fam_len=(300, 6000), divergence=(0.10, 0.20),
+                      names=None, threads=0) -> LargeGenome:
+    """i.i.d. bases, repeat copies pasted at `repeat_frac` of each chromosome
+    (families of log-uniform length, per-copy divergence, either strand), CpGs
+    thinned to `cpg_frac` of positions, each kept CpG methylated with `meth_p`."""
+    import concurrent.futures as cf
+    lut = _base_lut(base_p)
+    nchr = len(chrom_lengths)
+    kids = np.random.SeedSequence(seed).spawn(nchr + 1)
+    frng = np.random.default_rng(kids[-1])
+    lo, hi = np.log(fam_len[0]), np.log(fam_len[1])
+    flen = np.exp(frng.uniform(lo, hi, size=n_families)).astype(np.int64)
+    foff = np.zeros(n_families + 1, np.int64)
+    np.cumsum(flen, out=foff[1:])
+    fcat = _fast_bases(frng, int(foff[-1]), lut)
+    mean_len = float(flen.mean())
+
+    def one(ci):
+        rng = np.random.default_rng(kids[ci])
+        L = int(chrom_lengths[ci])
+        s = _fast_bases(rng, L, lut)
+        copies = np.zeros((0, 3), np.int64)
+        if repeat_frac > 0:
+            target = repeat_frac * L
+            k = int(target / mean_len * 1.3) + 16
+            f = rng.integers(0, n_families, size=k)
+            ln = flen[f]
+            keep = np.searchsorted(np.cumsum(ln), target) + 1
+            f, ln = f[:keep], ln[:keep]
+            ok = ln < L
+            f, ln = f[ok], ln[ok]
+            k = len(f)
+            st = (rng.random(k) * (L - ln)).astype(np.int64)
+            flip = rng.random(k) < 0.5
+            div = rng.uniform(divergence[0], divergence[1], size=k)
+            copies = np.stack([np.full(k, ci, np.int64), st, ln], axis=1)
+            i = 0
+            while i < k:   # sub-batches of about 8M copied bases
+                j = min(k, i + max(1, int(8e6 // mean_len)))
+                lb = ln[i:j]
+                tot = int(lb.sum())
+                cstart = np.zeros(j - i, np.int64)
+                np.cumsum(lb[:-1], out=cstart[1:])
+                rep = np.repeat(np.arange(j - i), lb)
+                pos = np.arange(tot, dtype=np.int64) - cstart[rep]
+                fl = flip[i:j][rep]
+                src = np.where(fl, foff[f[i:j]][rep] + lb[rep] - 1 - pos, foff[f[i:j]][rep] + pos)
+                b = fcat[src]
+                b = np.where(fl, _COMP[b], b)
+                mut = rng.random(tot, dtype=np.float32) < div[i:j][rep]
+                nm = int(mut.sum())
+                if nm:
+                    b[mut] = BASES[(_IDX[b[mut]] + rng.integers(1, 4, size=nm)) % 4]
+                for c in range(j - i):
+                    a = int(st[i + c])
+                    s[a:a + int(lb[c])] = b[cstart[c]:cstart[c] + lb[c]]
+                i = j
+        is_cg = (s[:-1] == C) & (s[1:] == G)
+        pos = np.flatnonzero(is_cg)
+        frac = len(pos) / max(1, L)
+        keep_p = min(1.0, cpg_frac / frac) if frac > 0 else 1.0
+        kp = rng.random(len(pos)) < keep_p
+        drop = pos[~kp]
+        s[drop + 1] = np.where(rng.random(len(drop)) < 0.5, A, T).astype(np.uint8)
+        kept = pos[kp]
+        mk = kept[rng.random(len(kept)) < meth_p]
+        return s, mk.astype(np.int64), kept.astype(np.int64), copies
+
+    with cf.ThreadPoolExecutor(_threads(threads)) as ex:
+        res = list(ex.map(one, range(nchr)))
+    if names is None:
+        names = ["chr%d" % (i + 1) for i in range(nchr)]
+    return LargeGenome(list(names), [r[0] for r in res], [r[1] for r in res], [r[2] for r in res],
+                       np.concatenate([r[3] for r in res]) if res else np.zeros((0, 3), np.int64))
+
+
+def _convert_fragments(genome: LargeGenome, chrom, start, fwd, W, cell_p=None, cell_key=0):
+    """Bisulfite-converted fragments of W bases: rows for forward reads are the
+    converted forward strand at [start, start + W); rows for reverse reads are
+    the reverse complement of the forward-coordinate image of the converted
+    reverse strand.  Methylation of a CpG: the genome's state, or, when cell_p
+    is given, a per-(cell, site) draw with probability cell_p (a hash of the
+    cell key and the site, the same for every read of the cell)."""
+    n = len(chrom)
+    out = np.empty((n, W), np.uint8)
+    cols = np.arange(W, dtype=np.int64)
+    for ci in np.unique(chrom):
+        sel = np.flatnonzero(chrom == ci)
+        s = genome.seqs[ci]
+        idx = start[sel, None] + cols[None, :]
+        frag = s[idx]
+        if cell_p is None:
+            mp = genome.meth_pos[ci]
+        else:
+            cp = genome.cpg_pos[ci]
+            h = (cp.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15)) ^ np.uint64(cell_key * 0xBF58476D1CE4E5B9 & 0xFFFFFFFFFFFFFFFF)
+            h ^= h >> np.uint64(31)
+            h *= np.uint64(0x94D049BB133111EB)
+            h ^= h >> np.uint64(29)
+            mp = cp[(h >> np.uint64(11)).astype(np.float64) / float(1 << 53) < cell_p]
+        # methylated C positions -> their C (pos) and G (pos + 1) are protected
+        j = np.searchsorted(mp, idx[:, 0])
+        prot = np.zeros(idx.shape, bool)
+        # each fragment holds at most W / 2 CpGs: walk the sorted list in step
+        for step in range(W):
+            jj = j + step
+            inb = jj < len(mp)
+            p = np.where(inb, mp[np.minimum(jj, len(mp) - 1)], -1) - idx[:, 0]
+            live = inb & (p >= 0) & (p < W)
+            if not live.any():
+                break
+            r = np.flatnonzero(live)
+            prot[r, p[r]] = True
+            q = p[r] + 1
+            ok = q < W
+            prot[r[ok], q[ok]] = True
+        f = fwd[sel]
+        ff = frag[f]
+        pf = prot[f]
+        ff[(ff == C) & ~pf] = T
+        fr = frag[~f]
+        pr = prot[~f]
+        fr[(fr == G) & ~pr] = A
+        out[sel[f]] = ff
+        out[sel[~f]] = _COMP[fr[:, ::-1]]
+    return out
+
+
+def make_reads_large(genome: LargeGenome, n_reads, seed, read_len=100, sub_rate=0.01, indel_rate=0.001,
+                     length_sampler=None, error_sampler=None, repeat_read_frac=0.0, batch=250_000, threads=0,
+                     cell_p=None, cell_key=0) -> ReadSet:
+    """Single-end bisulfite reads as make_reads (uniform starts, 50/50 strand,
+    conversion, substitutions and 1-bp indels at indel_rate / sub_rate times
+    each read's substitution rate, optional repeat-copy starts), batches drawn
+    from their own spawned streams on a thread pool."""
+    import concurrent.futures as cf
+    ss = np.random.SeedSequence(seed)
+    top, *kids = ss.spawn(1 + (n_reads + batch - 1) // batch)
+    rng = np.random.default_rng(top)
+    nchr = len(genome.seqs)
+    clen = np.array([len(s) for s in genome.seqs], dtype=np.int64)
+    pad = 8
+    lens = (np.full(n_reads, read_len, dtype=np.int32) if length_sampler is None
+            else np.asarray(length_sampler(rng, n_reads), dtype=np.int32))
+    maxL = int(lens.max()) if n_reads else read_len
+    W = maxL + pad
+    chrom = rng.choice(nchr, size=n_reads, p=clen / clen.sum())
+    start = (rng.random(n_reads) * (clen[chrom] - W)).astype(np.int64)
+    if repeat_read_frac > 0 and len(genome.repeat_copies):
+        rr = rng.random(n_reads) < repeat_read_frac
+        cps = genome.repeat_copies
+        pick = cps[rng.integers(0, len(cps), size=int(rr.sum()))]
+        off = (rng.random(len(pick)) * np.maximum(1, pick[:, 2] - maxL)).astype(np.int64)
+        chrom[rr] = pick[:, 0]
+        start[rr] = np.minimum(pick[:, 1] + off, clen[pick[:, 0]] - W)
+    fwd = rng.random(n_reads) < 0.5
+    rates = (np.full(n_reads, sub_rate) if error_sampler is None
+             else np.asarray(error_sampler(rng, n_reads), dtype=np.float64))
+    irates = rates * (indel_rate / sub_rate if sub_rate > 0 else 0.0)
+    out = np.zeros((n_reads, maxL), dtype=np.uint8)
+
+    def one(bi):
+        b0 = bi * batch
+        b1 = min(n_reads, b0 + batch)
+        nb = b1 - b0
+        r = np.random.default_rng(kids[bi])
+        frag = _convert_fragments(genome, chrom[b0:b1], start[b0:b1], fwd[b0:b1], W, cell_p, cell_key)
+        sub = r.random((nb, W), dtype=np.float32) < rates[b0:b1, None]
+        ns = int(sub.sum())
+        if ns:
+            frag[sub] = BASES[(_IDX[frag[sub]] + r.integers(1, 4, size=ns)) % 4]
+        nev = r.binomial(maxL, np.minimum(1.0, irates[b0:b1]))
+        j = np.arange(W)[None, :]
+        for _ in range(int(nev.max()) if nb else 0):
+            rows = np.flatnonzero(nev > 0)
+            nev[rows] -= 1
+            p = r.integers(0, maxL, size=len(rows))
+            ins = r.random(len(rows)) < 0.5
+            src = np.where(j < p[:, None], j, np.where(ins[:, None], j - 1, j + 1))
+            src = np.clip(src, 0, W - 1)
+            new = np.take_along_axis(frag[rows], src, axis=1)
+            new[ins, p[ins]] = BASES[r.integers(0, 4, size=int(ins.sum()))]
+            frag[rows] = new
+        blk = frag[:, :maxL]
+        blk[np.arange(maxL)[None, :] >= lens[b0:b1, None]] = 0
+        out[b0:b1] = blk
+
+    with cf.ThreadPoolExecutor(_threads(threads)) as ex:
+        list(ex.map(one, range(len(kids))))
+    return ReadSet(out, lens, chrom.astype(np.int32), start, fwd)
+
+
+def _errors_inplace(r, frag, rates, irates, maxL):
+    """Substitutions at each row's rate, then 1-bp indels (one event per pass)
+    inside the first maxL columns; frag is (n, W) with W > maxL."""
+    nb, W = frag.shape
+    sub = r.random((nb, W), dtype=np.float32) < rates[:, None]
+    ns = int(sub.sum())
+    if ns:
+        frag[sub] = BASES[(_IDX[frag[sub]] + r.integers(1, 4, size=ns)) % 4]
+    nev = r.binomial(maxL, np.minimum(1.0, irates))
+    j = np.arange(W)[None, :]
+    for _ in range(int(nev.max()) if nb else 0):
+        rows = np.flatnonzero(nev > 0)
+        nev[rows] -= 1
+        p = r.integers(0, maxL, size=len(rows))
+        ins = r.random(len(rows)) < 0.5
+        src = np.where(j < p[:, None], j, np.where(ins[:, None], j - 1, j + 1))
+        src = np.clip(src, 0, W - 1)
+        new = np.take_along_axis(frag[rows], src, axis=1)
+        new[ins, p[ins]] = BASES[r.integers(0, 4, size=int(ins.sum()))]
+        frag[rows] = new
+
+
+def make_pairs_large(genome: LargeGenome, n_pairs, seed, read_len=100, inner=(20, 400), sub_rate=0.01,
+                     indel_rate=0.001, batch=250_000, threads=0):
+    """Paired-end bisulfite reads as make_pairs: a fragment of read_len + inner +
+    read_len bases (inner uniform in the closed range) from a random strand;
+    mate 1 is its first read_len bases, mate 2 the reverse complement of its
+    last read_len bases; substitutions and 1-bp indels per mate."""
+    import concurrent.futures as cf
+    ss = np.random.SeedSequence(seed)
+    top, *kids = ss.spawn(1 + (n_pairs + batch - 1) // batch)
+    rng = np.random.default_rng(top)
+    nchr = len(genome.seqs)
+    clen = np.array([len(s) for s in genome.seqs], dtype=np.int64)
+    flen = read_len + rng.integers(inner[0], inner[1] + 1, size=n_pairs) + read_len
+    W = 2 * read_len + inner[1] + 8
+    chrom = rng.choice(nchr, size=n_pairs, p=clen / clen.sum())
+    start = (rng.random(n_pairs) * (clen[chrom] - W)).astype(np.int64)
+    fwd = rng.random(n_pairs) < 0.5
+    m1 = np.zeros((n_pairs, read_len), np.uint8)
+    m2 = np.zeros((n_pairs, read_len), np.uint8)
+    cols = np.arange(read_len)
+
+    def one(bi):
+        b0 = bi * batch
+        b1 = min(n_pairs, b0 + batch)
+        r = np.random.default_rng(kids[bi])
+        frag = _convert_fragments(genome, chrom[b0:b1], start[b0:b1], fwd[b0:b1], W)
+        fl = flen[b0:b1]
+        a = frag[:, :read_len + 8].copy()
+        b = _COMP[np.take_along_axis(frag, (fl - 1)[:, None] - np.arange(read_len + 8)[None, :] % W, axis=1)]
+        rates = np.full(b1 - b0, sub_rate)
+        irates = rates * (indel_rate / sub_rate if sub_rate > 0 else 0.0)
+        _errors_inplace(r, a, rates, irates, read_len)
+        _errors_inplace(r, b, rates, irates, read_len)
+        m1[b0:b1] = a[:, :read_len]
+        m2[b0:b1] = b[:, :read_len]
+
+    with cf.ThreadPoolExecutor(_threads(threads)) as ex:
+        list(ex.map(one, range(len(kids))))
+    lens = np.full(n_pairs, read_len, np.int32)
+    return (ReadSet(m1, lens, chrom.astype(np.int32), start, fwd),
+            ReadSet(m2, lens.copy(), chrom.astype(np.int32), start, ~fwd))

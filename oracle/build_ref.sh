@@ -1,21 +1,27 @@
 #!/usr/bin/env bash
 # Test infrastructure: compiles the reference FAME sources (the oracle) into
-# oracle/_ref/libfame_ref.so together with oracle/ref_driver.cpp.
+# shared libraries under oracle/_ref together with oracle/ref_driver.cpp.
 #
-# Stage 1 (only where the reference tree is present, FAME_REFERENCE_DIR,
-# default /root/reference): copy the files the matching path needs into
-# oracle/_ref/src (git-ignored) and set CORENUM (a #define in CONST.h:38 that
-# -D cannot override) to the core count of the machine that runs it.
+# Stage 1 (only where the reference tree is present: FAME_REFERENCE_DIR, by
+# default a checkout named "reference" beside this repository): copy the files
+# the matching path needs into oracle/_ref/src (git-ignored).
 # Stage 2 (also on machines without the reference tree, from the staged
-# copy): compile.  Nothing is written outside oracle/_ref.
+# copy): one build per constant set, each from its own copy of the sources
+# with CONST.h patched (CORENUM, READLEN and MAXPDIST are #defines or
+# constexprs in CONST.h:35-42 that -D cannot override; quoted includes find
+# the copy's own CONST.h):
+#   libfame_ref.so        READLEN 100, MAXPDIST 550 (the reference's values)
+#   libfame_ref_rl150.so  READLEN 150, MAXPDIST 550
+#   libfame_ref_pd400.so  READLEN 100, MAXPDIST 400
+# CORENUM is the core count of the machine that builds them.  The reference
+# Makefile's -march=native is passed where the compiler accepts it.  Nothing
+# is written outside oracle/_ref.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
 SRC="$OUT/src"
-REF="${FAME_REFERENCE_DIR:-/root/reference}"
+REF="${FAME_REFERENCE_DIR:-$HERE/../../reference}"
 CORES="${FAME_REF_CORENUM:-$(nproc)}"
-READLEN="${FAME_REF_READLEN:-100}"
-MAXPDIST="${FAME_REF_MAXPDIST:-550}"
 
 mkdir -p "$OUT"
 if [ -f "$REF/ReadQueue.cpp" ]; then
@@ -35,13 +41,34 @@ if [ ! -f "$SRC/ReadQueue.cpp" ]; then
   echo "build_ref: reference sources not available (neither $REF nor a staged copy)" >&2
   exit 3
 fi
-# per-machine thread count, read length and pair distance (CONST.h:35, 38, 42)
-sed -i -E "s/^#define CORENUM .*/#define CORENUM ${CORES}/" "$SRC/CONST.h"
-sed -i -E "s/^constexpr unsigned int READLEN = .*;/constexpr unsigned int READLEN = ${READLEN};/" "$SRC/CONST.h"
-sed -i -E "s/^constexpr uint32_t MAXPDIST = .*;/constexpr uint32_t MAXPDIST = ${MAXPDIST};/" "$SRC/CONST.h"
+ARCHFLAG=""
+if echo 'int main(){return 0;}' | g++ -march=native -x c++ - -o /dev/null 2>/dev/null; then
+  ARCHFLAG="-march=native"
+fi
 
-CXXFLAGS="-std=c++14 -O3 -fopenmp -fPIC -w -Dprivate=public -I$SRC -I$SRC/hopscotch-map/include/tsl"
-g++ $CXXFLAGS -shared -o "$OUT/libfame_ref.so" \
-    "$HERE/ref_driver.cpp" "$SRC/RefGenome.cpp" "$SRC/RefReader_istr.cpp" "$SRC/Read.cpp" \
-    "$SRC/CONST.cpp" "$SRC/DnaBitStr.cpp" "$SRC/gzstream/gzstream.C" -lz
-echo "build_ref: built $OUT/libfame_ref.so (CORENUM=$CORES READLEN=$READLEN MAXPDIST=$MAXPDIST)"
+build_variant() {   # readlen maxpdist library-name
+  local rl="$1" pd="$2" name="$3"
+  local vs="$OUT/src_${rl}_${pd}"
+  rm -rf "$vs"
+  cp -r "$SRC" "$vs"
+  sed -i -E "s/^#define CORENUM .*/#define CORENUM ${CORES}/" "$vs/CONST.h"
+  sed -i -E "s/^constexpr unsigned int READLEN = .*;/constexpr unsigned int READLEN = ${rl};/" "$vs/CONST.h"
+  sed -i -E "s/^constexpr uint32_t MAXPDIST = .*;/constexpr uint32_t MAXPDIST = ${pd};/" "$vs/CONST.h"
+  local flags="-std=c++14 -O3 $ARCHFLAG -fopenmp -fPIC -w -Dprivate=public -I$vs -I$vs/hopscotch-map/include/tsl"
+  # ref_driver.cpp is compiled from a copy inside the variant's tree so that its
+  # quoted includes resolve to the variant's CONST.h
+  cp "$HERE/ref_driver.cpp" "$vs/ref_driver.cpp"
+  g++ $flags -shared -o "$OUT/$name.tmp" \
+      "$vs/ref_driver.cpp" "$vs/RefGenome.cpp" "$vs/RefReader_istr.cpp" "$vs/Read.cpp" \
+      "$vs/CONST.cpp" "$vs/DnaBitStr.cpp" "$vs/gzstream/gzstream.C" -lz
+  mv "$OUT/$name.tmp" "$OUT/$name"
+  echo "build_ref: built $OUT/$name (CORENUM=$CORES READLEN=$rl MAXPDIST=$pd ${ARCHFLAG:-no -march=native})"
+}
+
+pids=()
+build_variant 100 550 libfame_ref.so & pids+=($!)
+build_variant 150 550 libfame_ref_rl150.so & pids+=($!)
+build_variant 100 400 libfame_ref_pd400.so & pids+=($!)
+rc=0
+for p in "${pids[@]}"; do wait "$p" || rc=1; done
+exit $rc

@@ -375,9 +375,13 @@ extern "C" {
 // Steady-state timing of ReadQueue::matchReads (ReadQueue.cpp:404-933): the
 // orientation is already decided (matchR1Fwd given, getStranded false), as for
 // every chunk after the first in queryRoutine (main.cpp:383-388).  Only the
-// matchReads calls are timed.  counters: [succ, nonunique, unsucc]
+// matchReads calls are timed.  counters: [succ, nonunique, unsucc].  When
+// given (non-null), mats / invalid receive each read's MATCH::match (0 when
+// invalid) and isInvalid, and meth the methLevels of the run (4 per CpG),
+// all read after the timed calls.
 int fame_ref_time_se(void* ref, const char* seqs, const uint64_t* offs, uint32_t n, int both_strands,
-                     int match_r1_fwd, uint64_t* counters, double* seconds)
+                     int match_r1_fwd, uint64_t* counters, double* seconds, uint64_t* mats, uint8_t* invalid,
+                     uint16_t* meth)
 {
     RefGenome& r = *static_cast<RefGenome*>(ref);
     ReadQueue* rq = in_tmp([&] { return new ReadQueue("/dev/null", r, false, both_strands != 0); });
@@ -396,7 +400,19 @@ int fame_ref_time_se(void* ref, const char* seqs, const uint64_t* offs, uint32_t
         rq->matchReads(cn, succ, nonu, unsucc, false);
         auto t1 = std::chrono::steady_clock::now();
         secs += std::chrono::duration<double>(t1 - t0).count();
+        if (mats && invalid)
+            for (uint32_t j = 0; j < cn; ++j) {
+                invalid[c0 + j] = rq->readBuffer[j].isInvalid ? 1 : 0;
+                mats[c0 + j] = rq->readBuffer[j].isInvalid ? 0 : rq->readBuffer[j].mat;
+            }
     }
+    if (meth)
+        for (size_t i = 0; i < r.cpgTable.size(); ++i) {
+            meth[4 * i + 0] = rq->methLevels[i].methFwd;
+            meth[4 * i + 1] = rq->methLevels[i].unmethFwd;
+            meth[4 * i + 2] = rq->methLevels[i].methRev;
+            meth[4 * i + 3] = rq->methLevels[i].unmethRev;
+        }
     counters[0] = succ; counters[1] = nonu; counters[2] = unsucc;
     *seconds = secs;
     delete rq;
@@ -457,9 +473,12 @@ int fame_ref_match_pe(void* ref, const char* s1, const uint64_t* o1, const char*
 
 // Seconds spent in matchPairedReads for already-stranded chunks (the steady
 // state of queryRoutinePaired after decideStrand); counters: [succ, nonunique,
-// unsucc, succPaired, tooShort].
+// unsucc, succPaired, tooShort].  When given (non-null), mats (2n: mate 1
+// then mate 2 of each pair, 0 when invalid), invalid (2n, same order) and meth
+// (4 per CpG) receive the run's results, read after the timed calls.
 int fame_ref_time_pe(void* ref, const char* s1, const uint64_t* o1, const char* s2, const uint64_t* o2, uint32_t n,
-                     int both_strands, int match_r1_fwd, uint64_t* counters, double* seconds)
+                     int both_strands, int match_r1_fwd, uint64_t* counters, double* seconds, uint64_t* mats,
+                     uint8_t* invalid, uint16_t* meth)
 {
     RefGenome& r = *static_cast<RefGenome*>(ref);
     ReadQueue* rq = in_tmp([&] { return new ReadQueue("/dev/null", "/dev/null", r, false, both_strands != 0); });
@@ -480,7 +499,23 @@ int fame_ref_time_pe(void* ref, const char* s1, const uint64_t* o1, const char* 
         rq->matchPairedReads(cn, succ, nonu, unsucc, paired, tooShort, false);
         auto t1 = std::chrono::steady_clock::now();
         secs += std::chrono::duration<double>(t1 - t0).count();
+        if (mats && invalid)
+            for (uint32_t j = 0; j < cn; ++j) {
+                const Read& a = rq->readBuffer[j];
+                const Read& b = rq->readBuffer2[j];
+                invalid[c0 + j] = a.isInvalid ? 1 : 0;
+                invalid[n + c0 + j] = b.isInvalid ? 1 : 0;
+                mats[c0 + j] = a.isInvalid ? 0 : a.mat;
+                mats[n + c0 + j] = b.isInvalid ? 0 : b.mat;
+            }
     }
+    if (meth)
+        for (size_t i = 0; i < r.cpgTable.size(); ++i) {
+            meth[4 * i + 0] = rq->methLevels[i].methFwd;
+            meth[4 * i + 1] = rq->methLevels[i].unmethFwd;
+            meth[4 * i + 2] = rq->methLevels[i].methRev;
+            meth[4 * i + 3] = rq->methLevels[i].unmethRev;
+        }
     counters[0] = succ; counters[1] = nonu; counters[2] = unsucc; counters[3] = paired; counters[4] = tooShort;
     *seconds = secs;
     delete rq;

@@ -9,6 +9,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_ref", "libfame_ref.so")
+# the constant sets oracle/build_ref.sh compiles: (READLEN, MAXPDIST) -> library
+VARIANTS = {(100, 550): LIB_PATH,
+            (150, 550): os.path.join(HERE, "_ref", "libfame_ref_rl150.so"),
+            (100, 400): os.path.join(HERE, "_ref", "libfame_ref_pd400.so")}
 
 _P = C.c_void_p
 
@@ -17,8 +21,14 @@ def _ptr(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
 
 
-def available() -> bool:
-    return os.path.exists(LIB_PATH)
+def variant_path(readlen: int = 100, maxpdist: int = 550) -> str:
+    """Library of the reference compiled with these CONST.h values (KeyError if none is built)."""
+    return VARIANTS[(int(readlen), int(maxpdist))]
+
+
+def available(readlen: int = 100, maxpdist: int = 550) -> bool:
+    p = VARIANTS.get((int(readlen), int(maxpdist)))
+    return p is not None and os.path.exists(p)
 
 
 class RefLib:
@@ -136,25 +146,43 @@ class RefIndex:
                                      _ptr(mats), _ptr(inval), _ptr(meth), _ptr(cnt), _ptr(secs))
         return dict(mat=mats, invalid=inval, meth=meth.reshape(-1, 4), counters=cnt, seconds=float(secs[0]))
 
-    def time_se(self, seq_bytes: bytes, offs: np.ndarray, both_strands: bool = False, match_r1_fwd: bool = True):
-        """Seconds spent in matchReads for already-stranded chunks, and [succ, nonunique, unsucc]."""
+    def _n_cpg(self) -> int:
+        sz = np.zeros(7, dtype=np.uint64)
+        self.L.lib.fame_ref_sizes(self.h, _ptr(sz))
+        return int(sz[0])
+
+    def time_se(self, seq_bytes: bytes, offs: np.ndarray, both_strands: bool = False, match_r1_fwd: bool = True,
+                outputs: bool = False):
+        """Seconds spent in matchReads for already-stranded chunks, and [succ,
+        nonunique, unsucc]; with outputs, also a dict of the run's per-read mat
+        and invalid and its methLevels (read after the timed calls)."""
         import ctypes as C
         f = self.L.lib.fame_ref_time_se
-        f.argtypes = [_P, _P, _P, C.c_uint32, C.c_int, C.c_int, _P, _P]
+        f.argtypes = [_P, _P, _P, C.c_uint32, C.c_int, C.c_int, _P, _P, _P, _P, _P]
         n = len(offs) - 1
         cnt = np.zeros(3, np.uint64)
         secs = np.zeros(1, np.float64)
         buf = np.frombuffer(seq_bytes, dtype=np.uint8)
         offs = np.ascontiguousarray(offs, dtype=np.uint64)
-        f(self.h, _ptr(buf), _ptr(offs), n, int(both_strands), int(match_r1_fwd), _ptr(cnt), _ptr(secs))
+        out = None
+        if outputs:
+            out = dict(mat=np.zeros(n, np.uint64), invalid=np.zeros(n, np.uint8),
+                       meth=np.zeros(4 * self._n_cpg(), np.uint16))
+        f(self.h, _ptr(buf), _ptr(offs), n, int(both_strands), int(match_r1_fwd), _ptr(cnt), _ptr(secs),
+          *((_ptr(out["mat"]), _ptr(out["invalid"]), _ptr(out["meth"])) if out else (None, None, None)))
+        if out:
+            out["meth"] = out["meth"].reshape(-1, 4)
+            return float(secs[0]), cnt, out
         return float(secs[0]), cnt
 
-    def time_pe(self, s1: bytes, o1, s2: bytes, o2, both_strands: bool = False, match_r1_fwd: bool = True):
+    def time_pe(self, s1: bytes, o1, s2: bytes, o2, both_strands: bool = False, match_r1_fwd: bool = True,
+                outputs: bool = False):
         """Seconds spent in matchPairedReads for already-stranded chunks, and
-        [succ, nonunique, unsucc, succPaired, tooShort]."""
+        [succ, nonunique, unsucc, succPaired, tooShort]; with outputs, also a
+        dict of mat1, mat2, inv1, inv2 and methLevels of the run."""
         import ctypes as C
         f = self.L.lib.fame_ref_time_pe
-        f.argtypes = [_P, _P, _P, _P, _P, C.c_uint32, C.c_int, C.c_int, _P, _P]
+        f.argtypes = [_P, _P, _P, _P, _P, C.c_uint32, C.c_int, C.c_int, _P, _P, _P, _P, _P]
         n = len(o1) - 1
         cnt = np.zeros(5, np.uint64)
         secs = np.zeros(1, np.float64)
@@ -162,8 +190,16 @@ class RefIndex:
         b2 = np.frombuffer(s2, np.uint8)
         o1 = np.ascontiguousarray(o1, np.uint64)
         o2 = np.ascontiguousarray(o2, np.uint64)
+        mats = inv = meth = None
+        if outputs:
+            mats = np.zeros(2 * n, np.uint64)
+            inv = np.zeros(2 * n, np.uint8)
+            meth = np.zeros(4 * self._n_cpg(), np.uint16)
         f(self.h, _ptr(b1), _ptr(o1), _ptr(b2), _ptr(o2), n, int(both_strands), int(match_r1_fwd), _ptr(cnt),
-          _ptr(secs))
+          _ptr(secs), _ptr(mats), _ptr(inv), _ptr(meth))
+        if outputs:
+            return float(secs[0]), cnt, dict(mat1=mats[:n], mat2=mats[n:], inv1=inv[:n], inv2=inv[n:],
+                                             meth=meth.reshape(-1, 4))
         return float(secs[0]), cnt
 
     def match_pe(self, s1: bytes, o1, s2: bytes, o2, chunk: int = 0, both_strands: bool = False):
