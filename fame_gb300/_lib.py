@@ -69,7 +69,8 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_gpu_tally_alloc", "fame_gpu_tally_read", "fame_gpu_tally_free", "fame_gpu_mem_info",
            "fame_report_cpg", "fame_report_sc_header", "fame_report_sc_rows", "fame_fastq_open", "fame_fastq_read",
            "fame_fastq_close", "fame_queue_stage", "fame_queue_submit_staged", "fame_match_fastq",
-           "fame_match_fastq_paired", "fame_index_write", "fame_gpu_index_bytes", "fame_queue_wait"]
+           "fame_match_fastq_paired", "fame_index_write", "fame_gpu_index_bytes", "fame_queue_wait",
+           "fame_gpu_set_seed_tier"]
 
 _lib = None
 
@@ -108,6 +109,7 @@ def lib(build_if_missing: bool = True):
     L.fame_gpu_set_timing.argtypes = [_P, C.c_int]
     L.fame_gpu_stage_times.argtypes = [_P, _P, C.c_int]
     L.fame_gpu_last_launches.argtypes = [_P]
+    L.fame_gpu_set_seed_tier.argtypes = [_P, C.c_int]
     L.fame_gpu_index_bytes.argtypes = [_P]
     L.fame_gpu_index_bytes.restype = C.c_uint64
     L.fame_gpu_match_pairs.argtypes = [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]
@@ -358,6 +360,13 @@ class GpuMatcher:
 
     def last_launches(self) -> int:
         return int(lib().fame_gpu_last_launches(self.h))
+
+    def seed_tier(self, mode: int = -1) -> int:
+        """Set (0 or 1) or read (-1) where seeding starts: fame_gpu_set_seed_tier."""
+        rc = lib().fame_gpu_set_seed_tier(self.h, int(mode))
+        if mode >= 0:
+            _check(rc, self.h)
+        return rc if mode < 0 else mode
 
     def index_bytes(self) -> int:
         """Device bytes of the resident index tables."""

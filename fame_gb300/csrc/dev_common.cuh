@@ -56,7 +56,8 @@ struct ChunkBufs {
     uint8_t* dp_orient;
     uint32_t* meth;          // 4 x n_cpg counters (uint16 semantics after the fact)
     unsigned long long* ctr; // device counters, see CTR_*
-    uint32_t* heavy;         // tasks handed to the heavy path
+    uint32_t* heavy;         // tasks over the shared-memory caps (single-end: seeded by the middle tier)
+    uint32_t* heavy2;        // tasks over the middle tier's caps (seeded by the large-capacity tier)
     uint8_t* cand_flags;     // per candidate, bit 0: scan from startPos - 1 even at 0 (paired second mate); may be null
     uint32_t cand_first;     // first candidate the Shift-And launch scans
 };
@@ -80,6 +81,7 @@ enum {
     CTR_PAIRED,         // pairs with both mates in CpG windows
     CTR_TOOSHORT,       // the paired path's tooShort count
     CTR_CAND_USED,      // candidate slots holding a candidate (CTR_CAND counts reserved ones)
+    CTR_HEAVY2,         // tasks handed on to the large-capacity seeding tier
     CTR_N
 };
 

@@ -48,10 +48,13 @@ struct fame_gpu {
     uint64_t* d_dp_mat = nullptr;
     uint8_t* d_dp_orient = nullptr;
     uint32_t* d_heavy = nullptr;
+    uint32_t* d_heavy2 = nullptr;
     unsigned long long* d_ctr = nullptr;
     unsigned long long* h_ctr = nullptr;  // pinned
     uint32_t* d_meth = nullptr;
-    HeavyScratch hs{};
+    HeavyScratch hs{};                   // large-capacity seeding tier (caps from the largest bucket)
+    HeavyScratch ms{};                   // middle seeding tier (genome-scale buckets, many warps)
+    int seed_mid_first = 0;              // 1: every task seeds in the middle tier (k_seed_route), no light attempt
     int timing = 0;
     cudaEvent_t ev[8]{};
     float stage_ms[6]{};
@@ -107,6 +110,9 @@ void dev_free(T*& p)
     if (p) cudaFree((void*)p);
     p = nullptr;
 }
+
+// Bucket entries a read's k-mers may gather in the middle seeding tier.
+constexpr uint32_t MID_OPS = 4096;
 
 // Heavy-pair caps: keys per map and phase, value-table slots, replayed buckets
 // (bucket_count = summed bucket sizes / 5 <= 224 k-mers x KMERCUTOFF / 5).
@@ -172,12 +178,12 @@ int grow_chunk(fame_gpu* g, uint64_t n, uint64_t bytes, uint64_t cand)
         const uint64_t c = std::max<uint64_t>(n, 1024);
         dev_free(g->d_offs); dev_free(g->d_rflags); dev_free(g->d_task_cand); dev_free(g->d_mats);
         dev_free(g->d_invalid); dev_free(g->d_dp_list); dev_free(g->d_dp_mat); dev_free(g->d_dp_orient);
-        dev_free(g->d_heavy);
+        dev_free(g->d_heavy); dev_free(g->d_heavy2);
         if ((rc = dev_alloc(g, &g->d_offs, c + 1)) || (rc = dev_alloc(g, &g->d_rflags, c)) ||
             (rc = dev_alloc(g, &g->d_task_cand, 2 * c)) || (rc = dev_alloc(g, &g->d_mats, c)) ||
             (rc = dev_alloc(g, &g->d_invalid, c)) || (rc = dev_alloc(g, &g->d_dp_list, c)) ||
             (rc = dev_alloc(g, &g->d_dp_mat, c)) || (rc = dev_alloc(g, &g->d_dp_orient, c)) ||
-            (rc = dev_alloc(g, &g->d_heavy, 2 * c)))
+            (rc = dev_alloc(g, &g->d_heavy, 2 * c)) || (rc = dev_alloc(g, &g->d_heavy2, 2 * c)))
             return rc;
         g->cap_reads = c;
     }
@@ -244,8 +250,9 @@ extern "C" int fame_gpu_close(fame_gpu* g)
     dev_free(g->d_seqs); dev_free(g->d_offs); dev_free(g->d_rflags); dev_free(g->d_task_cand);
     dev_free(g->d_cand); dev_free(g->d_cand_task); dev_free(g->d_hits); dev_free(g->d_hit_n);
     dev_free(g->d_mats); dev_free(g->d_invalid); dev_free(g->d_dp_list); dev_free(g->d_dp_mat);
-    dev_free(g->d_dp_orient); dev_free(g->d_heavy); dev_free(g->d_ctr); dev_free(g->d_meth);
+    dev_free(g->d_dp_orient); dev_free(g->d_heavy); dev_free(g->d_heavy2); dev_free(g->d_ctr); dev_free(g->d_meth);
     dev_free(g->hs.base);
+    dev_free(g->ms.base);
     dev_free(g->d_pe_heavy);
     dev_free(g->d_pe_recs);
     dev_free(g->d_cand_flags);
@@ -465,6 +472,19 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         g->hs.nwarps = (uint32_t)std::max<uint64_t>(8, std::min<uint64_t>(256, (4ull << 30) / g->hs.bytes_per_warp));
         if (cudaMalloc(&g->hs.base, g->hs.bytes_per_warp * g->hs.nwarps) != cudaSuccess)
             return fail(set_err(g, FAME_ERR_NOMEM, "heavy-path scratch allocation failed"));
+        // middle tier: reads whose k-mers gather up to MID_OPS bucket entries
+        // (genome-scale indexes hold about three entries per bucket, so most
+        // reads exceed the shared-memory caps), 16 warps per SM
+        g->ms.ops_cap = MID_OPS;
+        g->ms.dt_cap = pow2_ceil_host(2 * MID_OPS + 2);
+        g->ms.slot_cap = 2 * pow2_ceil_host(MID_OPS + 1) + 64;
+        g->ms.bytes_per_warp = heavy_bytes_per_warp(g->ms.ops_cap, g->ms.dt_cap, g->ms.slot_cap);
+        g->ms.nwarps = (uint32_t)g->sm_count * 16;
+        // with more than one entry per bucket on average (genome-scale
+        // indexes) nearly every read exceeds the shared-memory caps
+        g->seed_mid_first = v->n_kmer > HTABSIZE ? 1 : 0;
+        if (cudaMalloc(&g->ms.base, g->ms.bytes_per_warp * g->ms.nwarps) != cudaSuccess)
+            return fail(set_err(g, FAME_ERR_NOMEM, "middle-tier seeding scratch allocation failed"));
     }
     // ---- tallies, counters, DP scratch
     if ((rc = dev_alloc(g, &g->d_meth, 4 * std::max<uint64_t>(1, v->n_cpg)))) return fail(rc);
@@ -531,6 +551,7 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
     cb.meth = meth ? meth : g->d_meth;
     cb.ctr = g->d_ctr;
     cb.heavy = g->d_heavy;
+    cb.heavy2 = g->d_heavy2;
     const int T = g->timing;
     g->launches = 0;
     if (g->queue) queue_quiesce(g->queue);   // the queue's slots share the heavy-path scratch
@@ -552,9 +573,15 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         const uint32_t ntask = n * norient;
         const uint32_t wpb = 4;
         const uint32_t blocks = std::min<uint32_t>((ntask + wpb - 1) / wpb, (uint32_t)g->sm_count * 64);
-        k_seed<<<std::max(1u, blocks), wpb * 32, wpb * LightLayout::BYTES, g->stream>>>(g->ix, cb, ntask);
+        if (g->seed_mid_first)
+            k_seed_route<<<(ntask + 255) / 256, 256, 0, g->stream>>>(cb, ntask);
+        else
+            k_seed<<<std::max(1u, blocks), wpb * 32, wpb * LightLayout::BYTES, g->stream>>>(g->ix, cb, ntask);
         if (T) cudaEventRecord(g->ev[2], g->stream);
-        k_seed_heavy<<<(g->hs.nwarps + 3) / 4, 128, 0, g->stream>>>(g->ix, cb, g->hs, FROM_DEVICE);
+        k_seed_tier<<<(g->ms.nwarps + 3) / 4, 128, 0, g->stream>>>(g->ix, cb, g->ms, FROM_DEVICE, cb.heavy, CTR_HEAVY,
+                                                                   cb.heavy2, CTR_HEAVY2);
+        k_seed_tier<<<(g->hs.nwarps + 3) / 4, 128, 0, g->stream>>>(g->ix, cb, g->hs, FROM_DEVICE, cb.heavy2,
+                                                                   CTR_HEAVY2, nullptr, 0);
         if (T) cudaEventRecord(g->ev[6], g->stream);
         // the automaton widths a read of this index can need (reads shorter than
         // readlen - 20 are invalid, longer than FAME_MAX_READ_LEN refused)
@@ -569,7 +596,7 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         if (T) cudaEventRecord(g->ev[4], g->stream);
         k_dp_warp<<<g->dp_grid, 128, 4 * DPW_BYTES, g->stream>>>(g->ix, cb);
         if (T) cudaEventRecord(g->ev[5], g->stream);
-        g->launches += 5 + (int)(5 - wlo);
+        g->launches += 6 + (int)(5 - wlo);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
         CK(cudaStreamSynchronize(g->stream));
@@ -901,6 +928,16 @@ extern "C" int fame_gpu_stage_times(fame_gpu* g, float* ms, int n)
 extern "C" int fame_gpu_last_launches(const fame_gpu* g) { return g ? g->launches : 0; }
 
 extern "C" uint64_t fame_gpu_index_bytes(const fame_gpu* g) { return g ? g->index_bytes : 0; }
+
+extern "C" int fame_gpu_set_seed_tier(fame_gpu* g, int mode)
+{
+    if (!g) return FAME_ERR_ARG;
+    if (mode < 0) return g->seed_mid_first;
+    if (mode > 1) return set_err(g, FAME_ERR_ARG, "seed tier mode must be 0 or 1");
+    if (g->queue) queue_quiesce(g->queue);
+    g->seed_mid_first = mode;
+    return FAME_OK;
+}
 
 extern "C" int fame_gpu_stream(fame_gpu* g, void** stream)
 {

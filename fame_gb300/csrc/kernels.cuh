@@ -1029,6 +1029,30 @@ __global__ void __launch_bounds__(128, 8) k_seed(DevIndex ix, ChunkBufs cb, uint
     cand_res_finish(cb, res);
 }
 
+// Every valid task of the chunk straight to the middle tier's list (indexes
+// whose buckets are too large for the shared-memory caps of k_seed: there the
+// light attempt would only repeat its bucket reads).
+__global__ void k_seed_route(ChunkBufs cb, uint32_t ntask)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int norient = __popc(cb.orient_mask);
+    const uint32_t first_o = (cb.orient_mask & 1u) ? 0 : 1;
+    bool take = false;
+    uint32_t task = 0;
+    if (t < ntask) {
+        const uint32_t r = norient == 2 ? (t >> 1) : t;
+        const uint32_t o = norient == 2 ? (t & 1) : first_o;
+        take = cb.rflags[r] == 0;
+        task = 2 * r + o;
+    }
+    const unsigned bm = __ballot_sync(0xffffffffu, take);
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == 0 && bm) base = (uint32_t)atomicAdd(cb.ctr + CTR_HEAVY, (unsigned long long)__popc(bm));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (take) cb.heavy[base + __popc(bm & ((1u << lane) - 1))] = task;
+}
+
 // Heavy path: one warp per task with its working memory in global scratch.
 struct HeavyScratch {
     uint8_t* base;
@@ -1069,19 +1093,31 @@ __host__ __device__ inline uint64_t heavy_bytes_per_warp(uint64_t ops_cap, uint6
            2 * al(ops_cap * 4) + al(slot_cap * 4) + 3 * al(ops_cap * 4);
 }
 
-__global__ void k_seed_heavy(DevIndex ix, ChunkBufs cb, HeavyScratch hs, uint32_t nheavy)
+// Seeding tiers with working memory in global scratch, one warp per task:
+// the tasks of `list` (its length ntask, or the counter ctr_in when ntask is
+// FROM_DEVICE).  A task over this tier's caps goes to `spill` (counter
+// ctr_spill) for the next tier; without a next tier it is a capacity error.
+// The middle tier has many warps and caps for genome-scale bucket sizes; the
+// large-capacity tier has few warps sized by the largest bucket.
+__global__ void k_seed_tier(DevIndex ix, ChunkBufs cb, HeavyScratch hs, uint32_t ntask, const uint32_t* list,
+                            int ctr_in, uint32_t* spill, int ctr_spill)
 {
     const uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (w >= hs.nwarps) return;
-    if (nheavy == FROM_DEVICE) nheavy = (uint32_t)cb.ctr[CTR_HEAVY];
+    if (ntask == FROM_DEVICE) ntask = (uint32_t)cb.ctr[ctr_in];
     const SeedMem s = heavy_mem(hs, w);
     CandRes res;
-    for (uint32_t i = w; i < nheavy; i += hs.nwarps) {
-        const uint32_t task = cb.heavy[i];
+    for (uint32_t i = w; i < ntask; i += hs.nwarps) {
+        const uint32_t task = list[i];
         const int bad = seed_task(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES, res);
         if (bad && (threadIdx.x & 31) == 0) {
-            atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull);
-            cb.task_cand[task] = make_uint4(0, 0, 0, 0);
+            if (spill) {
+                const uint32_t h = (uint32_t)atomicAdd(cb.ctr + ctr_spill, 1ull);
+                spill[h] = task;
+            } else {
+                atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull);
+                cb.task_cand[task] = make_uint4(0, 0, 0, 0);
+            }
         }
         __syncwarp();
     }

@@ -40,6 +40,7 @@ struct QSlot {
     uint64_t* d_dp_mat = nullptr;
     uint8_t* d_dp_orient = nullptr;
     uint32_t* d_heavy = nullptr;
+    uint32_t* d_heavy2 = nullptr;
     unsigned long long* d_ctr = nullptr;
     // page-locked staging
     char* h_seqs = nullptr;
@@ -47,7 +48,8 @@ struct QSlot {
     uint64_t* h_mats = nullptr;
     uint8_t* h_invalid = nullptr;
     unsigned long long* h_ctr = nullptr;
-    HeavyScratch hs{};
+    HeavyScratch hs{};      // this slot's part of the context's large-capacity tier
+    HeavyScratch ms{};      // and of its middle tier
     uint64_t cap_cand = 0;
     // the chunk in flight
     bool busy = false;
@@ -84,7 +86,7 @@ void qslot_free(fame_gpu* g, QSlot& s)
     s.graphs.clear();
     dev_free(s.d_seqs); dev_free(s.d_offs); dev_free(s.d_rflags); dev_free(s.d_task_cand); dev_free(s.d_cand);
     dev_free(s.d_cand_task); dev_free(s.d_hits); dev_free(s.d_hit_n); dev_free(s.d_mats); dev_free(s.d_invalid);
-    dev_free(s.d_dp_list); dev_free(s.d_dp_mat); dev_free(s.d_dp_orient); dev_free(s.d_heavy); dev_free(s.d_ctr);
+    dev_free(s.d_dp_list); dev_free(s.d_dp_mat); dev_free(s.d_dp_orient); dev_free(s.d_heavy); dev_free(s.d_heavy2); dev_free(s.d_ctr);
     host_free_near(g, s.h_seqs);
     host_free_near(g, s.h_offs);
     host_free_near(g, s.h_mats);
@@ -121,6 +123,7 @@ ChunkBufs qslot_bufs(fame_gpu* g, QSlot& s, uint32_t n, uint32_t flags, uint32_t
     cb.meth = meth ? meth : g->d_meth;
     cb.ctr = s.d_ctr;
     cb.heavy = s.d_heavy;
+    cb.heavy2 = s.d_heavy2;
     return cb;
 }
 
@@ -133,8 +136,14 @@ void qslot_enqueue(fame_gpu* g, QSlot& s, uint32_t n, uint32_t flags, uint32_t* 
     k_prep<<<(n + 255) / 256, 256, 0, s.stream>>>(cb, g->ix.readlen);
     const uint32_t ntask = n * norient;
     const uint32_t blocks = std::min<uint32_t>((ntask + 3) / 4, (uint32_t)g->sm_count * 64);
-    k_seed<<<std::max(1u, blocks), 128, 4 * LightLayout::BYTES, s.stream>>>(g->ix, cb, ntask);
-    k_seed_heavy<<<(s.hs.nwarps + 3) / 4, 128, 0, s.stream>>>(g->ix, cb, s.hs, FROM_DEVICE);
+    if (g->seed_mid_first)
+        k_seed_route<<<(ntask + 255) / 256, 256, 0, s.stream>>>(cb, ntask);
+    else
+        k_seed<<<std::max(1u, blocks), 128, 4 * LightLayout::BYTES, s.stream>>>(g->ix, cb, ntask);
+    k_seed_tier<<<(s.ms.nwarps + 3) / 4, 128, 0, s.stream>>>(g->ix, cb, s.ms, FROM_DEVICE, cb.heavy, CTR_HEAVY,
+                                                             cb.heavy2, CTR_HEAVY2);
+    k_seed_tier<<<(s.hs.nwarps + 3) / 4, 128, 0, s.stream>>>(g->ix, cb, s.hs, FROM_DEVICE, cb.heavy2, CTR_HEAVY2,
+                                                             nullptr, 0);
     const uint32_t grid = (uint32_t)g->sm_count * 32;
     k_shiftand<1><<<grid, 32 * SA_WARPS, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
     k_shiftand<2><<<grid, 32 * SA_WARPS, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
@@ -147,7 +156,7 @@ void qslot_enqueue(fame_gpu* g, QSlot& s, uint32_t n, uint32_t flags, uint32_t* 
     cudaMemcpyAsync(s.h_ctr, s.d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s.stream);
 }
 
-constexpr uint64_t QUEUE_KERNELS_PER_CHUNK = 10;
+constexpr uint64_t QUEUE_KERNELS_PER_CHUNK = 11;
 
 int qslot_graph(fame_gpu* g, fame_queue* q, QSlot& s, uint32_t n, uint32_t flags, uint32_t* meth, cudaGraphExec_t* out)
 {
@@ -213,6 +222,7 @@ extern "C" int fame_queue_open(fame_gpu* g, uint32_t nslots, uint32_t max_reads,
             (rc = dev_alloc(g, &s.d_mats, max_reads)) || (rc = dev_alloc(g, &s.d_invalid, max_reads)) ||
             (rc = dev_alloc(g, &s.d_dp_list, max_reads)) || (rc = dev_alloc(g, &s.d_dp_mat, max_reads)) ||
             (rc = dev_alloc(g, &s.d_dp_orient, max_reads)) || (rc = dev_alloc(g, &s.d_heavy, 2ull * max_reads)) ||
+            (rc = dev_alloc(g, &s.d_heavy2, 2ull * max_reads)) ||
             (rc = dev_alloc(g, &s.d_ctr, CTR_N)))
             return fail(rc);
         s.h_seqs = (char*)host_alloc_near(g, max_bytes);
@@ -227,6 +237,9 @@ extern "C" int fame_queue_open(fame_gpu* g, uint32_t nslots, uint32_t max_reads,
         s.hs = g->hs;
         s.hs.nwarps = hw;
         s.hs.base = g->hs.base + (uint64_t)i * hw * g->hs.bytes_per_warp;   // nslots <= 8 <= hs.nwarps
+        s.ms = g->ms;
+        s.ms.nwarps = std::max(1u, g->ms.nwarps / nslots);
+        s.ms.base = g->ms.base + (uint64_t)i * s.ms.nwarps * g->ms.bytes_per_warp;
     }
     g->queue = q;
     *out = q;

@@ -304,6 +304,13 @@ int fame_gpu_stage_times(fame_gpu* g, float* ms, int n);
 int fame_gpu_last_launches(const fame_gpu* g);
 /* Device bytes held by the resident index tables of the context. */
 uint64_t fame_gpu_index_bytes(const fame_gpu* g);
+/* Where a read's seeding starts (no counterpart in the reference; results do
+ * not depend on it): 0 = a warp with shared-memory working space, reads whose
+ * bucket entries exceed it moving on to global-memory tiers; 1 = every read
+ * in the global-memory middle tier.  fame_gpu_open picks 1 when the index
+ * holds more entries than buckets, else 0.  mode < 0 returns the current
+ * mode. */
+int fame_gpu_set_seed_tier(fame_gpu* g, int mode);
 
 /* CpG calls that allocate no device memory.  No counterpart in the reference:
  * it is for callers that cannot allocate while they run (a serving loop that

@@ -27,7 +27,7 @@ mkdir -p "$OUT"
 if [ -f "$REF/ReadQueue.cpp" ]; then
   rm -rf "$SRC"
   mkdir -p "$SRC/spaced_nthash" "$SRC/gzstream" "$SRC/hopscotch-map/include/tsl"
-  for f in CONST.h CONST.cpp structs.h RefGenome.h RefGenome.cpp RefReader_istr.h RefReader_istr.cpp \
+  for f in main.cpp CONST.h CONST.cpp structs.h RefGenome.h RefGenome.cpp RefReader_istr.h RefReader_istr.cpp \
            ReadQueue.h ReadQueue.cpp Read.h Read.cpp ShiftAnd.h LevenshtDP.h BandedMatrix.h \
            DnaBitStr.h DnaBitStr.cpp BitFunctions.h; do
     cp "$REF/$f" "$SRC/$f"

@@ -534,3 +534,44 @@ int fame_ref_sort_desc(const uint32_t* keys, const uint8_t* counts, uint32_t n, 
     return 0;
 }
 }
+
+extern "C" {
+// printMethylationLevels (ReadQueue.cpp:1860-1893) of the given tallies (4
+// uint16 per CpG in cpgTable order): writes <basename>_cpg.tsv.
+int fame_ref_print_cpg(void* ref, const uint16_t* meth, const char* basename)
+{
+    RefGenome& r = *static_cast<RefGenome*>(ref);
+    ReadQueue* rq = in_tmp([&] { return new ReadQueue("/dev/null", r, false, false); });
+    for (size_t i = 0; i < r.cpgTable.size(); ++i) {
+        rq->methLevels[i].methFwd = meth[4 * i + 0];
+        rq->methLevels[i].unmethFwd = meth[4 * i + 1];
+        rq->methLevels[i].methRev = meth[4 * i + 2];
+        rq->methLevels[i].unmethRev = meth[4 * i + 3];
+    }
+    std::string fn(basename);
+    rq->printMethylationLevels(fn);
+    delete rq;
+    return 0;
+}
+
+// The single-cell matrix: the single-cell ReadQueue's header
+// (ReadQueue.cpp:182-215) and printSCMethylationLevels (1894-1921) for each
+// of n cells (ids[c], tallies meth + 4 * n_cpg * c), written to path.
+int fame_ref_print_sc(void* ref, const char* path, uint32_t n, const char* const* ids, const uint16_t* meth)
+{
+    RefGenome& r = *static_cast<RefGenome*>(ref);
+    ReadQueue* rq = in_tmp([&] { return new ReadQueue(path, r, false, false, false); });
+    const size_t nc = r.cpgTable.size();
+    for (uint32_t c = 0; c < n; ++c) {
+        for (size_t i = 0; i < nc; ++i) {
+            rq->methLevels[i].methFwd = meth[4 * (nc * c + i) + 0];
+            rq->methLevels[i].unmethFwd = meth[4 * (nc * c + i) + 1];
+            rq->methLevels[i].methRev = meth[4 * (nc * c + i) + 2];
+            rq->methLevels[i].unmethRev = meth[4 * (nc * c + i) + 3];
+        }
+        rq->printSCMethylationLevels(std::string(ids[c]));
+    }
+    delete rq;
+    return 0;
+}
+}

@@ -224,6 +224,22 @@ class RefIndex:
           _ptr(i2), _ptr(meth), _ptr(cnt), _ptr(secs))
         return dict(mat1=m1, mat2=m2, inv1=i1, inv2=i2, meth=meth.reshape(-1, 4), counters=cnt, seconds=float(secs[0]))
 
+    def print_cpg(self, meth, basename: str) -> str:
+        """The reference's printMethylationLevels of these tallies; returns the file path."""
+        f = self.L.lib.fame_ref_print_cpg
+        f.argtypes = [_P, _P, C.c_char_p]
+        m = np.ascontiguousarray(meth, np.uint16)
+        f(self.h, _ptr(m), basename.encode())
+        return basename + "_cpg.tsv"
+
+    def print_sc(self, path: str, cells):
+        """The reference's single-cell matrix for [(cell id, tallies)]."""
+        f = self.L.lib.fame_ref_print_sc
+        f.argtypes = [_P, C.c_char_p, C.c_uint32, _P, _P]
+        ids = (C.c_char_p * len(cells))(*[c.encode() for c, _ in cells])
+        m = np.ascontiguousarray(np.stack([np.asarray(x, np.uint16) for _, x in cells]), np.uint16)
+        f(self.h, path.encode(), len(cells), C.cast(ids, C.c_void_p), _ptr(m))
+
     def seed_order(self, seq: bytes, cap: int = 1 << 20):
         keys = np.zeros(cap, np.uint32)
         cnts = np.zeros(cap, np.uint32)

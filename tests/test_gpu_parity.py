@@ -70,6 +70,20 @@ def test_golden_reference_parity(gpu, golden, name, chunk, both):
     assert_same(r, ref, name)
 
 
+@pytest.mark.parametrize("name,chunk,both", [("default", 0, False), ("chunk1000", 1000, False), ("both", 777, True)])
+def test_golden_parity_middle_seeding_tier(gpu, golden, name, chunk, both):
+    """Every read seeded by the global-memory middle tier (the genome-scale
+    route) gives the reference's results too."""
+    assert gpu.seed_tier() == 0
+    gpu.seed_tier(1)
+    try:
+        r = run_mode(gpu, golden["read_seq"].tobytes(), golden["read_offs"], chunk, both)
+    finally:
+        gpu.seed_tier(0)
+    ref = {k: golden[name + "_" + k] for k in ("mat", "invalid", "meth", "counters")}
+    assert_same(r, ref, name + " (middle tier)")
+
+
 def test_readqueue_mirror(golden, product_index, gpu):
     seq = golden["read_seq"].tobytes()
     offs = golden["read_offs"]
