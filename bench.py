@@ -387,7 +387,8 @@ def run_gb300(args):
         gm.match_reads_dev(d_s, d_o, n, flags, d_mat, d_inv)
     gm.set_timing(True)
     # ---- timed: plain form, reads resident in HBM
-    stage = np.zeros(6)
+    stage = np.zeros(len(GpuMatcher.STAGES))
+    tiers = np.zeros(4)
     reads = gather = scans = launches = heavy = reruns = dp = inv_len = succ = 0
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
@@ -398,6 +399,7 @@ def run_gb300(args):
         d_s, d_o, n = dev[steady[k % len(steady)]]
         c = gm.match_reads_dev(d_s, d_o, n, flags, d_mat, d_inv)
         stage += gm.stage_times()
+        tiers += gm.seed_tier_counts()
         reads += n
         gather += c.gather_bytes
         scans += c.windows_scanned
@@ -434,10 +436,20 @@ def run_gb300(args):
     clk.mark(te0, time.perf_counter())
     t_e2e = allreduce_max(ev0.elapsed_time(ev1) / 1e3, world)
     gm.set_timing(False)
-    # ---- batched form: the same steps through the queue (CUDA-graph chunk
-    # slots on their own streams, the copies of one chunk overlapping the
-    # kernels of another), from the same host buffers; host clock between two
-    # device synchronisations (the work spans several streams)
+    # ---- batched form: launch shapes autotuned on the first steady chunk
+    # (fame_gpu_autotune: seeding tiers, window-scan and DP grids; it checks
+    # that every shape gives the same results), then the same steps through
+    # the queue (CUDA-graph chunk slots on their own streams, persistent
+    # seeding and scan kernels taking work from device queues, the copies of
+    # one chunk overlapping the kernels of another), from the same host
+    # buffers; host clock between two device synchronisations (the work spans
+    # several streams)
+    import tempfile
+    tune_path = os.path.join(tempfile.gettempdir(), "fame_tuning_%d.json" % os.getpid())
+    t0 = time.time()
+    d_s, d_o, n = dev[steady[0]]
+    tuning = gm.autotune(d_s, d_o, n, flags, tune_path)
+    t_tune = time.time() - t0
     nslots = 3
     q = GpuQueue(gm, nslots, maxn, max(int(p[0].nbytes) for p in pinned.values()))
     for w in range(nslots):
@@ -466,6 +478,13 @@ def run_gb300(args):
     batched = {"value": b_reads * world / t_b, "unit": "reads/s", "slots": nslots,
                "vs_plain": (b_reads * world / t_b) / (total_reads / t_max),
                "gpu_launches": q.launches() - launches_q0,
+               "tuning": {k: tuning[k] for k in ("seed_mode", "sa_blocks_per_sm", "dp_blocks_per_sm")},
+               "tuning_seconds": t_tune,
+               "tuning_trials": [[t["seed_mode"], t["sa_blocks_per_sm"], t["dp_blocks_per_sm"],
+                                  round(t["stage_ms"][1] + t["stage_ms"][5], 3), round(t["stage_ms"][2], 3),
+                                  round(t["stage_ms"][4], 3)] for t in tuning["trials"]],
+               "tuning_trials_columns": ["seed_mode", "sa_blocks_per_sm", "dp_blocks_per_sm", "seed_ms",
+                                         "shift_and_ms", "dp_ms"],
                "timing": "host clock between device synchronisations; host buffers in and out"}
     q.close()
     fastq = fastq_file_leg(gm, rs) if (rank == 0 and not args.no_fastq) else None
@@ -485,9 +504,10 @@ def run_gb300(args):
                                counters=[cc.succ, cc.nonunique, cc.unsucc]))
     # ---- roofline of the index-gather kernel
     hbm, src = peaks()
-    names = ["read_prep", "seed_gather", "shift_and", "select_exact_cpg", "banded_dp", "seed_heavy"]
-    st = {names[i]: stage[i] / 1e3 for i in range(6)}
-    dominant = max(names, key=lambda k: st[k])
+    names = ["read_prep", "seed_gather", "shift_and", "select_exact_cpg", "banded_dp", "seed_heavy",
+             "seed_mid_small", "seed_mid_large", "seed_global"]
+    st = {names[i]: stage[i] / 1e3 for i in range(len(names))}
+    dominant = max(names[:6], key=lambda k: st[k])
     seed_s = st["seed_gather"] + st["seed_heavy"]
     gbps = gather / seed_s / 1e9 if seed_s > 0 else 0.0
     fig = NCU_FIGURES.get(args.workload) if not args.reads else None
@@ -514,6 +534,8 @@ def run_gb300(args):
         "dominant_kernel": dominant,
         "counts": {"reads": reads, "matched": succ, "invalid_len": inv_len, "dp_reads": dp,
                    "windows_scanned_per_read": scans / max(1, reads), "heavy_seed_tasks": heavy,
+                   "seed_tier_tasks": {"mid_small": int(tiers[0]), "mid_large": int(tiers[1]),
+                                       "global": int(tiers[2]), "large_capacity": int(tiers[3])},
                    "candidate_overflow_reruns": reruns},
         "roofline": {"kernel": "k_seed (index gathers)", "bound": "hbm", "achieved": gbps, "peak": hbm,
                      "unit": "GB/s", "frac": gbps / hbm, "traffic": traffic,

@@ -70,7 +70,8 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_report_cpg", "fame_report_sc_header", "fame_report_sc_rows", "fame_fastq_open", "fame_fastq_read",
            "fame_fastq_close", "fame_queue_stage", "fame_queue_submit_staged", "fame_match_fastq",
            "fame_match_fastq_paired", "fame_index_write", "fame_gpu_index_bytes", "fame_queue_wait",
-           "fame_gpu_set_seed_tier"]
+           "fame_gpu_set_seed_tier", "fame_gpu_autotune", "fame_gpu_load_tuning",
+           "fame_gpu_seed_tier_counts"]
 
 _lib = None
 
@@ -110,6 +111,9 @@ def lib(build_if_missing: bool = True):
     L.fame_gpu_stage_times.argtypes = [_P, _P, C.c_int]
     L.fame_gpu_last_launches.argtypes = [_P]
     L.fame_gpu_set_seed_tier.argtypes = [_P, C.c_int]
+    L.fame_gpu_autotune.argtypes = [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_char_p]
+    L.fame_gpu_load_tuning.argtypes = [_P, C.c_char_p]
+    L.fame_gpu_seed_tier_counts.argtypes = [_P, _P]
     L.fame_gpu_index_bytes.argtypes = [_P]
     L.fame_gpu_index_bytes.restype = C.c_uint64
     L.fame_gpu_match_pairs.argtypes = [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]
@@ -353,20 +357,41 @@ class GpuMatcher:
     def set_timing(self, on: bool):
         _check(lib().fame_gpu_set_timing(self.h, int(on)), self.h)
 
+    STAGES = ("read_prep", "seed", "shift_and", "select", "banded_dp", "seed_tiers", "seed_mid_small",
+              "seed_mid_large", "seed_global")
+
     def stage_times(self):
-        ms = np.zeros(6, np.float32)
-        lib().fame_gpu_stage_times(self.h, _ptr(ms), 6)
+        """fame_gpu_stage_times: per-stage milliseconds of the last single-end chunk (STAGES)."""
+        ms = np.zeros(len(self.STAGES), np.float32)
+        lib().fame_gpu_stage_times(self.h, _ptr(ms), len(ms))
         return ms
+
+    def seed_tier_counts(self):
+        """fame_gpu_seed_tier_counts: tasks entering each seeding tier after the light one, last chunk."""
+        out = np.zeros(4, np.uint64)
+        _check(lib().fame_gpu_seed_tier_counts(self.h, _ptr(out)), self.h)
+        return out
 
     def last_launches(self) -> int:
         return int(lib().fame_gpu_last_launches(self.h))
 
     def seed_tier(self, mode: int = -1) -> int:
-        """Set (0 or 1) or read (-1) where seeding starts: fame_gpu_set_seed_tier."""
+        """Set (0 to 3) or read (-1) the seeding mode: fame_gpu_set_seed_tier."""
         rc = lib().fame_gpu_set_seed_tier(self.h, int(mode))
         if mode >= 0:
             _check(rc, self.h)
         return rc if mode < 0 else mode
+
+    def autotune(self, seqs_dev, offs_dev, n: int, flags: int, json_path: str) -> dict:
+        """fame_gpu_autotune on a chunk in device memory; returns the JSON it wrote."""
+        import json
+        _check(lib().fame_gpu_autotune(self.h, seqs_dev, offs_dev, n, flags, json_path.encode()), self.h)
+        with open(json_path) as f:
+            return json.load(f)
+
+    def load_tuning(self, json_path: str):
+        """fame_gpu_load_tuning: apply the shapes of an autotuner file."""
+        _check(lib().fame_gpu_load_tuning(self.h, json_path.encode()), self.h)
 
     def index_bytes(self) -> int:
         """Device bytes of the resident index tables."""

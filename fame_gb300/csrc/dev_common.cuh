@@ -56,8 +56,8 @@ struct ChunkBufs {
     uint8_t* dp_orient;
     uint32_t* meth;          // 4 x n_cpg counters (uint16 semantics after the fact)
     unsigned long long* ctr; // device counters, see CTR_*
-    uint32_t* heavy;         // tasks over the shared-memory caps (single-end: seeded by the middle tier)
-    uint32_t* heavy2;        // tasks over the middle tier's caps (seeded by the large-capacity tier)
+    uint32_t* heavy;         // seeding tasks for the middle tiers; the tiers' lists alternate between
+    uint32_t* heavy2;        // heavy and heavy2 (pairs: heavy = per-pair path, heavy2 = paired middle tier)
     uint8_t* cand_flags;     // per candidate, bit 0: scan from startPos - 1 even at 0 (paired second mate); may be null
     uint32_t cand_first;     // first candidate the Shift-And launch scans
 };
@@ -81,7 +81,11 @@ enum {
     CTR_PAIRED,         // pairs with both mates in CpG windows
     CTR_TOOSHORT,       // the paired path's tooShort count
     CTR_CAND_USED,      // candidate slots holding a candidate (CTR_CAND counts reserved ones)
-    CTR_HEAVY2,         // tasks handed on to the large-capacity seeding tier
+    CTR_HEAVY2,         // seeding tasks handed on by the first middle tier (pairs: pairs for the paired middle tier)
+    CTR_HEAVY3,         // seeding tasks handed on by the second middle tier
+    CTR_HEAVY4,         // seeding tasks handed on by the global-memory tier to the large-capacity one
+    CTR_QMID,           // work-queue position of the first middle seeding tier (pairs: of the paired middle tier)
+    CTR_QMID2,          // work-queue position of the second middle seeding tier
     CTR_N
 };
 

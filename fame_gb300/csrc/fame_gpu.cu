@@ -53,14 +53,19 @@ struct fame_gpu {
     unsigned long long* h_ctr = nullptr;  // pinned
     uint32_t* d_meth = nullptr;
     HeavyScratch hs{};                   // large-capacity seeding tier (caps from the largest bucket)
-    HeavyScratch ms{};                   // middle seeding tier (genome-scale buckets, many warps)
-    int seed_mid_first = 0;              // 1: every task seeds in the middle tier (k_seed_route), no light attempt
+    HeavyScratch ms{};                   // global-memory middle seeding tier (genome-scale buckets, many warps)
+    int seed_mid_first = 0;              // 1: every task seeds in the middle tiers (k_seed_route), no light attempt
+    int mid_skip_small = 0;              // 1: the middle tiers start at the larger one
+    uint32_t mid_grid[2] = {0, 0};       // resident blocks of the smaller and the larger middle tier
     int timing = 0;
-    cudaEvent_t ev[8]{};
-    float stage_ms[6]{};
+    cudaEvent_t ev[12]{};
+    float stage_ms[FAME_STAGES]{};
+    uint64_t tier_tasks[4]{};            // tasks entering each seeding tier after the light one, last chunk
     int launches = 0;
     int sm_count = 0;
     uint32_t dp_grid = 0;   // resident blocks of k_dp_warp on the whole device
+    uint32_t dp_blocks = 0; // blocks k_dp_warp is launched with (the autotuner may pick fewer)
+    uint32_t sa_blocks_per_sm = 32;      // k_shiftand blocks per SM (its warps loop over the candidates)
     // paired path
     PeIndex px{};
     uint64_t pe_warp_bytes = 0;          // shared memory per warp of k_pe_seed
@@ -68,6 +73,9 @@ struct fame_gpu {
     PeTaskRec* d_pe_recs = nullptr;      // per pair orientation
     uint64_t cap_pe_recs = 0;
     uint8_t* d_pe_heavy = nullptr;       // global scratch of k_pe_heavy
+    uint8_t* d_pe_mid = nullptr;         // global scratch of k_pe_seed_mid
+    uint64_t pe_mid_warp_bytes = 0;
+    uint32_t pe_mid_warps = 0;
     uint64_t pe_heavy_warp_bytes = 0;
     uint32_t pe_heavy_warps = 0;
     fame_queue* queue = nullptr;         // the batched form's slots, if open
@@ -75,6 +83,9 @@ struct fame_gpu {
 };
 
 void queue_quiesce(fame_queue* q);
+// Waits for the queue's slots and drops their captured graphs (launch shapes
+// changed; the next chunk of each shape is captured again).
+void queue_drop_graphs(fame_queue* q);
 // Device address of the static scratch array of fame_gpu_call_cpgs_noalloc on
 // the current device (defined with the array, below).
 cudaError_t noalloc_scratch_address(void** p);
@@ -253,6 +264,7 @@ extern "C" int fame_gpu_close(fame_gpu* g)
     dev_free(g->d_dp_orient); dev_free(g->d_heavy); dev_free(g->d_heavy2); dev_free(g->d_ctr); dev_free(g->d_meth);
     dev_free(g->hs.base);
     dev_free(g->ms.base);
+    dev_free(g->d_pe_mid);
     dev_free(g->d_pe_heavy);
     dev_free(g->d_pe_recs);
     dev_free(g->d_cand_flags);
@@ -485,6 +497,19 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         g->seed_mid_first = v->n_kmer > HTABSIZE ? 1 : 0;
         if (cudaMalloc(&g->ms.base, g->ms.bytes_per_warp * g->ms.nwarps) != cudaSuccess)
             return fail(set_err(g, FAME_ERR_NOMEM, "middle-tier seeding scratch allocation failed"));
+        // shared-memory middle tiers: resident blocks per SM from their
+        // shared-memory footprints
+        const void* fns[2] = {(const void*)k_seed_mid<MID_S_OPS, MID_S_DT, MID_S_WPB>,
+                              (const void*)k_seed_mid<MID_L_OPS, MID_L_DT, MID_L_WPB>};
+        const uint32_t sbytes[2] = {MID_S_WPB * MidS::BYTES, MID_L_WPB * MidL::BYTES};
+        const int threads[2] = {32 * MID_S_WPB, 32 * MID_L_WPB};
+        for (int k = 0; k < 2; ++k) {
+            int nb = 0;
+            if (cudaFuncSetAttribute(fns[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sbytes[k]) != cudaSuccess ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fns[k], threads[k], sbytes[k]) != cudaSuccess || nb < 1)
+                return fail(set_err(g, FAME_ERR_CUDA, "k_seed_mid does not fit an SM"));
+            g->mid_grid[k] = (uint32_t)(g->sm_count * nb);
+        }
     }
     // ---- tallies, counters, DP scratch
     if ((rc = dev_alloc(g, &g->d_meth, 4 * std::max<uint64_t>(1, v->n_cpg)))) return fail(rc);
@@ -509,11 +534,13 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_dp_warp, 128, 4 * DPW_BYTES) != cudaSuccess || nb < 1)
             return fail(set_err(g, FAME_ERR_CUDA, "k_dp_warp does not fit an SM"));
         g->dp_grid = (uint32_t)(g->sm_count * nb);
-        uint64_t off[28], hoff[28];
+        g->dp_blocks = g->dp_grid;
+        uint64_t off[28], hoff[28], moff[28];
         g->pe_warp_bytes = pe_layout(PE_LIGHT, off);
         pe_layout(PE_HEAVY, hoff);
+        g->pe_mid_warp_bytes = pe_layout(PE_MID, moff);
         // pe_kmers keeps its per-read arrays (8 * 256 + 96 bytes) in layout regions 11 .. 16
-        if (off[17] - off[11] < PE_KMER_AREA || hoff[17] - hoff[11] < PE_KMER_AREA)
+        if (off[17] - off[11] < PE_KMER_AREA || hoff[17] - hoff[11] < PE_KMER_AREA || moff[17] - moff[11] < PE_KMER_AREA)
             return fail(set_err(g, FAME_ERR_CUDA, "paired layout: k-mer area too small"));
         const size_t pe_smem = PE_SEED_WARPS * g->pe_warp_bytes;   // the largest layout (mates up to 255 bases)
         if (cudaFuncSetAttribute(k_pe_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pe_smem) != cudaSuccess ||
@@ -526,6 +553,38 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
 }
 
 namespace {
+
+// The seeding tiers after the light one (or k_seed_route), every count read
+// on the device: the shared-memory middle tiers (unless skipped, the smaller
+// first), then the global-memory tier and the large-capacity one, each over
+// the tasks the tier before could not hold.  The task lists alternate
+// between cb.heavy and cb.heavy2 (a list is fully taken before the next tier
+// writes over it).  ev, when given, receives an event after each middle tier
+// and after the global-memory tier.  Returns the launches.
+int seed_tiers(fame_gpu* g, const ChunkBufs& cb, cudaStream_t st, const HeavyScratch& ms, const HeavyScratch& hs,
+               cudaEvent_t* ev = nullptr)
+{
+    uint32_t* lists[2] = {cb.heavy, cb.heavy2};
+    int cur = 0, ctr = CTR_HEAVY, launches = 0;
+    const int spill_ctr[3] = {CTR_HEAVY2, CTR_HEAVY3, CTR_HEAVY4};
+    int k = 0;
+    if (!g->mid_skip_small) {
+        k_seed_mid<MID_S_OPS, MID_S_DT, MID_S_WPB><<<g->mid_grid[0], 32 * MID_S_WPB, MID_S_WPB * MidS::BYTES, st>>>(
+            g->ix, cb, lists[cur], ctr, CTR_QMID, lists[cur ^ 1], spill_ctr[k]);
+        cur ^= 1; ctr = spill_ctr[k++]; ++launches;
+    }
+    if (ev) cudaEventRecord(ev[0], st);
+    k_seed_mid<MID_L_OPS, MID_L_DT, MID_L_WPB><<<g->mid_grid[1], 32 * MID_L_WPB, MID_L_WPB * MidL::BYTES, st>>>(
+        g->ix, cb, lists[cur], ctr, CTR_QMID2, lists[cur ^ 1], spill_ctr[k]);
+    cur ^= 1; ctr = spill_ctr[k++]; ++launches;
+    if (ev) cudaEventRecord(ev[1], st);
+    k_seed_tier<<<(ms.nwarps + 3) / 4, 128, 0, st>>>(g->ix, cb, ms, FROM_DEVICE, lists[cur], ctr, lists[cur ^ 1],
+                                                     spill_ctr[k]);
+    cur ^= 1; ctr = spill_ctr[k]; ++launches;
+    if (ev) cudaEventRecord(ev[2], st);
+    k_seed_tier<<<(hs.nwarps + 3) / 4, 128, 0, st>>>(g->ix, cb, hs, FROM_DEVICE, lists[cur], ctr, nullptr, 0);
+    return launches + 1;
+}
 
 int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t n, uint32_t flags, uint64_t* d_mats,
               uint8_t* d_invalid, fame_counters* cnt, uint32_t* meth = nullptr)
@@ -578,14 +637,11 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         else
             k_seed<<<std::max(1u, blocks), wpb * 32, wpb * LightLayout::BYTES, g->stream>>>(g->ix, cb, ntask);
         if (T) cudaEventRecord(g->ev[2], g->stream);
-        k_seed_tier<<<(g->ms.nwarps + 3) / 4, 128, 0, g->stream>>>(g->ix, cb, g->ms, FROM_DEVICE, cb.heavy, CTR_HEAVY,
-                                                                   cb.heavy2, CTR_HEAVY2);
-        k_seed_tier<<<(g->hs.nwarps + 3) / 4, 128, 0, g->stream>>>(g->ix, cb, g->hs, FROM_DEVICE, cb.heavy2,
-                                                                   CTR_HEAVY2, nullptr, 0);
+        const int tier_launches = seed_tiers(g, cb, g->stream, g->ms, g->hs, T ? g->ev + 7 : nullptr);
         if (T) cudaEventRecord(g->ev[6], g->stream);
         // the automaton widths a read of this index can need (reads shorter than
         // readlen - 20 are invalid, longer than FAME_MAX_READ_LEN refused)
-        const uint32_t grid = (uint32_t)g->sm_count * 32;
+        const uint32_t grid = (uint32_t)g->sm_count * g->sa_blocks_per_sm;
         const uint32_t wlo = std::min(4u, (g->ix.readlen - 20) / 64 + 1);
         if (wlo <= 1) k_shiftand<1><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, FROM_DEVICE);
         if (wlo <= 2) k_shiftand<2><<<grid, 32 * SA_WARPS, 0, g->stream>>>(g->ix, cb, FROM_DEVICE);
@@ -594,9 +650,9 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         if (T) cudaEventRecord(g->ev[3], g->stream);
         k_select<<<(n + 255) / 256, 256, 0, g->stream>>>(g->ix, cb);
         if (T) cudaEventRecord(g->ev[4], g->stream);
-        k_dp_warp<<<g->dp_grid, 128, 4 * DPW_BYTES, g->stream>>>(g->ix, cb);
+        k_dp_warp<<<g->dp_blocks, 128, 4 * DPW_BYTES, g->stream>>>(g->ix, cb);
         if (T) cudaEventRecord(g->ev[5], g->stream);
-        g->launches += 6 + (int)(5 - wlo);
+        g->launches += 4 + tier_launches + (int)(5 - wlo);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(g->h_ctr, g->d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream));
         CK(cudaStreamSynchronize(g->stream));
@@ -612,6 +668,9 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
             cudaEventElapsedTime(&g->stage_ms[0], g->ev[0], g->ev[1]);
             cudaEventElapsedTime(&g->stage_ms[1], g->ev[1], g->ev[2]);
             cudaEventElapsedTime(&g->stage_ms[5], g->ev[2], g->ev[6]);
+            cudaEventElapsedTime(&g->stage_ms[6], g->ev[2], g->ev[7]);
+            cudaEventElapsedTime(&g->stage_ms[7], g->ev[7], g->ev[8]);
+            cudaEventElapsedTime(&g->stage_ms[8], g->ev[8], g->ev[6]);
             cudaEventElapsedTime(&g->stage_ms[2], g->ev[6], g->ev[3]);
             cudaEventElapsedTime(&g->stage_ms[3], g->ev[3], g->ev[4]);
             cudaEventElapsedTime(&g->stage_ms[4], g->ev[4], g->ev[5]);
@@ -629,6 +688,21 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
             cnt->dp_reads += h[CTR_DP];
             cnt->heavy_tasks += h[CTR_HEAVY];
             cnt->reruns += (uint64_t)attempt;
+        }
+        {
+            // the tasks each tier received: its input list's length
+            const unsigned long long* h = g->h_ctr;
+            if (g->mid_skip_small) {
+                g->tier_tasks[0] = 0;
+                g->tier_tasks[1] = h[CTR_HEAVY];
+                g->tier_tasks[2] = h[CTR_HEAVY2];
+                g->tier_tasks[3] = h[CTR_HEAVY3];
+            } else {
+                g->tier_tasks[0] = h[CTR_HEAVY];
+                g->tier_tasks[1] = h[CTR_HEAVY2];
+                g->tier_tasks[2] = h[CTR_HEAVY3];
+                g->tier_tasks[3] = h[CTR_HEAVY4];
+            }
         }
         return FAME_OK;
     }
@@ -706,6 +780,11 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
     cb.meth = g->d_meth;
     cb.ctr = g->d_ctr;
     cb.heavy = g->d_heavy;
+    cb.heavy2 = g->d_heavy2;
+    if (!g->d_pe_mid) {
+        g->pe_mid_warps = (uint32_t)g->sm_count * 8;
+        CK(cudaMalloc((void**)&g->d_pe_mid, g->pe_mid_warp_bytes * g->pe_mid_warps));
+    }
     PeIndex px = g->px;
     px.ctx = (uint32_t)((double)maxpdist / WINLEN) + 1;
     px.maxdist = maxpdist + g->ix.readlen;
@@ -749,8 +828,11 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
                 grid = (uint32_t)(g->sm_count * nb);
         }
         k_pe_seed<<<grid, 32 * PE_SEED_WARPS, PE_SEED_WARPS * wbytes, g->stream>>>(g->ix, px, cb, g->d_pe_recs,
-                                                                                  (uint32_t)wbytes, caps);
-        g->launches++;
+                                                                                  (uint32_t)wbytes, caps,
+                                                                                  g->seed_mid_first);
+        k_pe_seed_mid<<<g->pe_mid_warps / 4, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_recs, g->d_pe_mid,
+                                                                  g->pe_mid_warp_bytes, PE_MID);
+        g->launches += 2;
         if ((rc = sync_ctr())) return rc;
         const uint64_t nc1 = g->h_ctr[CTR_CAND];
         if (nc1 > g->cap_cand) {
@@ -921,8 +1003,15 @@ extern "C" int fame_gpu_set_timing(fame_gpu* g, int enable)
 extern "C" int fame_gpu_stage_times(fame_gpu* g, float* ms, int n)
 {
     if (!g || !ms) return FAME_ERR_ARG;
-    for (int i = 0; i < n && i < 6; ++i) ms[i] = g->stage_ms[i];
-    return 6;
+    for (int i = 0; i < n && i < FAME_STAGES; ++i) ms[i] = g->stage_ms[i];
+    return FAME_STAGES;
+}
+
+extern "C" int fame_gpu_seed_tier_counts(const fame_gpu* g, uint64_t* out)
+{
+    if (!g || !out) return FAME_ERR_ARG;
+    for (int i = 0; i < 4; ++i) out[i] = g->tier_tasks[i];
+    return FAME_OK;
 }
 
 extern "C" int fame_gpu_last_launches(const fame_gpu* g) { return g ? g->launches : 0; }
@@ -932,10 +1021,11 @@ extern "C" uint64_t fame_gpu_index_bytes(const fame_gpu* g) { return g ? g->inde
 extern "C" int fame_gpu_set_seed_tier(fame_gpu* g, int mode)
 {
     if (!g) return FAME_ERR_ARG;
-    if (mode < 0) return g->seed_mid_first;
-    if (mode > 1) return set_err(g, FAME_ERR_ARG, "seed tier mode must be 0 or 1");
-    if (g->queue) queue_quiesce(g->queue);
-    g->seed_mid_first = mode;
+    if (mode < 0) return g->seed_mid_first + 2 * g->mid_skip_small;
+    if (mode > 3) return set_err(g, FAME_ERR_ARG, "seed tier mode must be 0 to 3");
+    if (g->queue) queue_drop_graphs(g->queue);
+    g->seed_mid_first = mode & 1;
+    g->mid_skip_small = (mode >> 1) & 1;
     return FAME_OK;
 }
 
@@ -1039,9 +1129,19 @@ extern "C" int fame_gpu_call_cpgs_noalloc(fame_gpu* g, const char* seqs_dev, con
 }
 
 #include "queue.cuh"
+#include "tune.cuh"
 
 void queue_quiesce(fame_queue* q)
 {
     for (auto& s : q->slots)
         if (s.stream) cudaStreamSynchronize(s.stream);
+}
+
+void queue_drop_graphs(fame_queue* q)
+{
+    queue_quiesce(q);
+    for (auto& s : q->slots) {
+        for (auto& gr : s.graphs) cudaGraphExecDestroy(gr.exec);
+        s.graphs.clear();
+    }
 }

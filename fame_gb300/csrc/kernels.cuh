@@ -1000,6 +1000,7 @@ __device__ __forceinline__ SeedMem light_mem(uint8_t* base)
     s.stk = (uint32_t*)(base + LightLayout::STK);
     s.ovf = (uint32_t*)(base + LightLayout::OVF);
     s.stage = (uint32_t*)(base + LightLayout::STAGE);
+    s.pre = (uint64_t*)(base + LightLayout::OPS);
     s.ops_cap = L_OPS; s.dt_cap = L_DT; s.slot_cap = L_SLOT; s.stk_cap = L_OPS; s.ovf_cap = L_OVF;
     return s;
 }
@@ -1028,6 +1029,103 @@ __global__ void __launch_bounds__(128, 8) k_seed(DevIndex ix, ChunkBufs cb, uint
     }
     cand_res_finish(cb, res);
 }
+
+// Middle seeding tiers, for genome-scale indexes (about three entries per
+// bucket: a read gathers hundreds of entries, over the light tier's caps).
+// One warp per task with its whole working set in shared memory, so that the
+// dependent steps of the count (load an op, probe the count table, add) wait
+// on shared memory only: the read, its per-k-mer bucket starts and prefix,
+// the inserted keys and their counts, and a union of the op lists with the
+// count table (packed: first op and count in one word; the prefix hashes sit
+// there first) or, after the count, of the replayed buckets, the pending
+// stack, the overflow list and the staged candidates.  OPS bucket entries at
+// most; DT count-table slots (a power of two > 2 * OPS).
+template <uint32_t OPS, uint32_t DT>
+struct MidLayout {
+    static_assert(DT >= 2 * OPS + 2 && (DT & (DT - 1)) == 0 && OPS < 65536, "count table too small");
+    static constexpr uint32_t R16(uint32_t b) { return (b + 15) / 16 * 16; }
+    static constexpr uint32_t SLOT_N = DT + 64;    // replayed buckets: 2 * pow2_ceil(OPS + 1) + 64 at most
+    static constexpr uint32_t OVF_N = 256;
+    static constexpr uint32_t KST = 0;                                // 224 x u32
+    static constexpr uint32_t KPRE = KST + 224 * 4;                   // 225 x u32
+    static constexpr uint32_t SEQ = KPRE + 228 * 4;                   // 256 B
+    static constexpr uint32_t INS = SEQ + 256;
+    static constexpr uint32_t INSC = INS + R16(OPS * 4);
+    static constexpr uint32_t U = INSC + R16(OPS * 4);
+    // phase A: hash, gather, count
+    static constexpr uint32_t OPSA = U;
+    static constexpr uint32_t OPK = OPSA + R16(OPS * 4);
+    static constexpr uint32_t DTK = OPK + R16(OPS);
+    static constexpr uint32_t DTC = DTK + DT * 4;
+    static constexpr uint32_t END_A = DTC + DT * 4;
+    // phase B: replay
+    static constexpr uint32_t SLOT = U;
+    static constexpr uint32_t STK = SLOT + R16(SLOT_N * 4);
+    static constexpr uint32_t OVF = STK + R16(OPS * 4);
+    static constexpr uint32_t STAGE = OVF + OVF_N * 4;
+    static constexpr uint32_t END_B = STAGE + R16(OPS * 4);
+    static constexpr uint32_t BYTES = R16(END_A > END_B ? END_A : END_B);
+    static_assert(DTK % 8 == 0 && END_A - DTK >= 8 * (FAME_MAX_READ_LEN + 1), "prefix hashes do not fit");
+};
+
+template <uint32_t OPS, uint32_t DT>
+__device__ __forceinline__ SeedMem mid_mem(uint8_t* sm)
+{
+    using L = MidLayout<OPS, DT>;
+    SeedMem s;
+    s.kst = (uint32_t*)(sm + L::KST);
+    s.kpre = (uint32_t*)(sm + L::KPRE);
+    s.seq = sm + L::SEQ;
+    s.ins = (uint32_t*)(sm + L::INS);
+    s.ins_cnt = (uint32_t*)(sm + L::INSC);
+    s.ops = (uint32_t*)(sm + L::OPSA);
+    s.opk = sm + L::OPK;
+    s.pre = (uint64_t*)(sm + L::DTK);
+    s.dt_key = (uint32_t*)(sm + L::DTK);
+    s.dt_first = nullptr;   // packed into dt_cnt
+    s.dt_cnt = (uint32_t*)(sm + L::DTC);
+    s.slot = (uint32_t*)(sm + L::SLOT);
+    s.stk = (uint32_t*)(sm + L::STK);
+    s.ovf = (uint32_t*)(sm + L::OVF);
+    s.stage = (uint32_t*)(sm + L::STAGE);
+    s.ops_cap = OPS; s.dt_cap = DT; s.slot_cap = L::SLOT_N; s.stk_cap = OPS; s.ovf_cap = L::OVF_N;
+    return s;
+}
+
+// The tasks of `list` (its length in counter ctr_in), taken one at a time
+// per warp from a work queue (counter ctr_q, zero at launch): a task's cost
+// follows its read's bucket sizes, so fixed strides would leave warps idle
+// behind a few long tasks.  A task over the caps goes to `spill` (counter
+// ctr_spill) for the next tier.  Launched with WPB warps per block and
+// WPB * MidLayout<OPS, DT>::BYTES of dynamic shared memory.
+template <uint32_t OPS, uint32_t DT, int WPB>
+__global__ void __launch_bounds__(32 * WPB) k_seed_mid(DevIndex ix, ChunkBufs cb, const uint32_t* list, int ctr_in,
+                                                       int ctr_q, uint32_t* spill, int ctr_spill)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const uint32_t wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const SeedMem s = mid_mem<OPS, DT>(smem + wib * MidLayout<OPS, DT>::BYTES);
+    const uint32_t ntask = (uint32_t)cb.ctr[ctr_in];
+    CandRes res;
+    while (true) {
+        uint32_t i = 0;
+        if (lane == 0) i = (uint32_t)atomicAdd(cb.ctr + ctr_q, 1ull);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= ntask) break;
+        const uint32_t task = list[i];
+        const int over = seed_task(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES, res);
+        if (over && lane == 0) spill[(uint32_t)atomicAdd(cb.ctr + ctr_spill, 1ull)] = task;
+        __syncwarp();
+    }
+    cand_res_finish(cb, res);
+}
+
+// the two middle tiers: reads gathering up to 511 entries (12 warps per SM),
+// then up to 1023 (6 warps per SM)
+constexpr uint32_t MID_S_OPS = 511, MID_S_DT = 1024, MID_L_OPS = 1023, MID_L_DT = 2048;
+constexpr int MID_S_WPB = 4, MID_L_WPB = 2;
+using MidS = MidLayout<MID_S_OPS, MID_S_DT>;
+using MidL = MidLayout<MID_L_OPS, MID_L_DT>;
 
 // Every valid task of the chunk straight to the middle tier's list (indexes
 // whose buckets are too large for the shared-memory caps of k_seed: there the
@@ -1082,6 +1180,7 @@ __device__ __forceinline__ SeedMem heavy_mem(const HeavyScratch& hs, uint32_t w)
     s.stk = (uint32_t*)take(oc * 4);
     s.ovf = (uint32_t*)take(oc * 4);
     s.stage = (uint32_t*)take(oc * 4);
+    s.pre = (uint64_t*)s.ops;   // ops, opk and the count table: far more than 8 * 256 bytes
     s.ops_cap = hs.ops_cap; s.dt_cap = hs.dt_cap; s.slot_cap = hs.slot_cap; s.stk_cap = hs.ops_cap; s.ovf_cap = hs.ops_cap;
     return s;
 }

@@ -163,6 +163,9 @@ __device__ inline PeMem pe_mem(uint8_t* base, PeCaps c)
 
 // shared-memory caps of k_pe_seed (one warp; it keeps no matches)
 constexpr PeCaps PE_LIGHT{64, 256, 256 + NBHD - 1, 64, 0, 320, PE_KMAX};
+// caps of the paired middle tier (global scratch, many warps): genome-scale
+// indexes, about three entries per bucket, a few hundred keys per mate
+constexpr PeCaps PE_MID{1024, 4096, 4096 + NBHD - 1 + 64, 256, 0, 4096, PE_KMAX};
 
 __device__ __forceinline__ uint32_t vt_hash(uint32_t k, uint32_t mask) { return (k * 0x9E3779B1u) >> 8 & mask; }
 
@@ -1411,7 +1414,51 @@ __device__ bool pe_lists(const PeMem& s, const PeState& st, const ChunkBufs& cb,
     return true;
 }
 
-__global__ void k_pe_seed(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs, uint32_t warp_bytes, PeCaps caps)
+// Stage A of pair r, both orientations: maps, walk lists and the first walk's
+// candidates.  Returns true when a capacity of `caps` is exceeded (the pair
+// must then be done by another tier; what was written for it is reset or
+// overwritten there).  All lanes of the warp call it.
+__device__ bool pe_seed_pair(const DevIndex& ix, const PeIndex& px, const ChunkBufs& cb, PeTaskRec* recs,
+                             const PeMem& s, const PeCaps& caps, uint32_t r)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t n = cb.n;
+    const uint32_t i1 = r, i2 = n + r;
+    const uint32_t n1 = (uint32_t)(cb.offs[i1 + 1] - cb.offs[i1]);
+    const uint32_t n2 = (uint32_t)(cb.offs[i2 + 1] - cb.offs[i2]);
+    bool fb = n1 > caps.kmax + KMERLEN - 1 || n2 > caps.kmax + KMERLEN - 1;   // over the k-mer arrays
+    for (int o = 0; o < 2 && !fb; ++o) {
+        if (!((cb.orient_mask >> o) & 1u)) continue;
+        PeState st;
+        const int m = pe_maps(ix, px, cb, s, i1, i2, n1, n2, o, st);
+        if (m < 0) { fb = true; break; }
+        if (m == 0) continue;
+        PeTaskRec& t = recs[2 * r + o];
+        const bool ok = pe_lists(s, st, cb, t, i1, o);
+        if (lane == 0) t.state = ok ? PT_WALK : PT_FALLBACK;
+        fb = !ok;
+        __syncwarp();
+    }
+    return fb;
+}
+
+__device__ __forceinline__ void pe_rec_reset(PeTaskRec* recs, uint32_t r)
+{
+    for (int o = 0; o < 2; ++o) {
+        recs[2 * r + o].state = PT_NONE;
+        recs[2 * r + o].m1n = 0;
+        recs[2 * r + o].n1[0] = recs[2 * r + o].n1[1] = 0;
+        recs[2 * r + o].n2[0] = recs[2 * r + o].n2[1] = 0;
+    }
+}
+
+// Stage A in shared memory, warp per pair.  A pair over the shared-memory caps
+// goes to the paired middle tier's list (cb.heavy2, counter CTR_HEAVY2); with
+// route_mid every valid pair goes there at once (genome-scale indexes, where
+// nearly every pair is over these caps and the attempt would only repeat its
+// bucket reads).
+__global__ void k_pe_seed(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs, uint32_t warp_bytes, PeCaps caps,
+                          int route_mid)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const int lane = threadIdx.x & 31;
@@ -1420,31 +1467,36 @@ __global__ void k_pe_seed(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs
     const PeMem s = pe_mem(smem + (threadIdx.x >> 5) * warp_bytes, caps);
     const uint32_t n = cb.n;
     for (uint32_t r = wid; r < n; r += nw) {
-        if (lane == 0)
-            for (int o = 0; o < 2; ++o) {
-                recs[2 * r + o].state = PT_NONE;
-                recs[2 * r + o].m1n = 0;
-                recs[2 * r + o].n1[0] = recs[2 * r + o].n1[1] = 0;
-                recs[2 * r + o].n2[0] = recs[2 * r + o].n2[1] = 0;
-            }
+        if (lane == 0) pe_rec_reset(recs, r);
         if ((cb.rflags[r] | cb.rflags[n + r]) & 7u) continue;   // k_pe_prep finished the pair
-        const uint32_t i1 = r, i2 = n + r;
-        const uint32_t n1 = (uint32_t)(cb.offs[i1 + 1] - cb.offs[i1]);
-        const uint32_t n2 = (uint32_t)(cb.offs[i2 + 1] - cb.offs[i2]);
-        bool fb = n1 > caps.kmax + KMERLEN - 1 || n2 > caps.kmax + KMERLEN - 1;   // over the k-mer arrays
-        for (int o = 0; o < 2 && !fb; ++o) {
-            if (!((cb.orient_mask >> o) & 1u)) continue;
-            PeState st;
-            const int m = pe_maps(ix, px, cb, s, i1, i2, n1, n2, o, st);
-            if (m < 0) { fb = true; break; }
-            if (m == 0) continue;
-            PeTaskRec& t = recs[2 * r + o];
-            const bool ok = pe_lists(s, st, cb, t, i1, o);
-            if (lane == 0) t.state = ok ? PT_WALK : PT_FALLBACK;
-            fb = !ok;
-            __syncwarp();
+        const bool over = route_mid ? true : pe_seed_pair(ix, px, cb, recs, s, caps, r);
+        if (over && lane == 0) {
+            pe_rec_reset(recs, r);
+            cb.heavy2[(uint32_t)atomicAdd(cb.ctr + CTR_HEAVY2, 1ull)] = r;
         }
-        if (fb && lane == 0) {
+        __syncwarp();
+    }
+}
+
+// Stage A of the paired middle tier: the pairs of cb.heavy2 with the caps of a
+// genome-scale index, working memory in global scratch (warp_bytes per warp),
+// warp per pair, pairs taken from a work queue (counter CTR_QMID).  A pair
+// over these caps too is marked for the per-pair path (k_pe_heavy).
+__global__ void k_pe_seed_mid(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs, uint8_t* scratch,
+                              uint64_t warp_bytes, PeCaps caps)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const PeMem s = pe_mem(scratch + (uint64_t)wid * warp_bytes, caps);
+    const uint32_t npairs = (uint32_t)cb.ctr[CTR_HEAVY2];
+    while (true) {
+        uint32_t k = 0;
+        if (lane == 0) k = (uint32_t)atomicAdd(cb.ctr + CTR_QMID, 1ull);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= npairs) break;
+        const uint32_t r = cb.heavy2[k];
+        const bool over = pe_seed_pair(ix, px, cb, recs, s, caps, r);
+        if (over && lane == 0) {
             recs[2 * r].state = PT_FALLBACK;
             recs[2 * r + 1].state = PT_FALLBACK;
         }

@@ -140,23 +140,20 @@ void qslot_enqueue(fame_gpu* g, QSlot& s, uint32_t n, uint32_t flags, uint32_t* 
         k_seed_route<<<(ntask + 255) / 256, 256, 0, s.stream>>>(cb, ntask);
     else
         k_seed<<<std::max(1u, blocks), 128, 4 * LightLayout::BYTES, s.stream>>>(g->ix, cb, ntask);
-    k_seed_tier<<<(s.ms.nwarps + 3) / 4, 128, 0, s.stream>>>(g->ix, cb, s.ms, FROM_DEVICE, cb.heavy, CTR_HEAVY,
-                                                             cb.heavy2, CTR_HEAVY2);
-    k_seed_tier<<<(s.hs.nwarps + 3) / 4, 128, 0, s.stream>>>(g->ix, cb, s.hs, FROM_DEVICE, cb.heavy2, CTR_HEAVY2,
-                                                             nullptr, 0);
-    const uint32_t grid = (uint32_t)g->sm_count * 32;
+    seed_tiers(g, cb, s.stream, s.ms, s.hs);
+    const uint32_t grid = (uint32_t)g->sm_count * g->sa_blocks_per_sm;
     k_shiftand<1><<<grid, 32 * SA_WARPS, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
     k_shiftand<2><<<grid, 32 * SA_WARPS, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
     k_shiftand<3><<<grid, 32 * SA_WARPS, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
     k_shiftand<4><<<grid, 32 * SA_WARPS, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);
     k_select<<<(n + 255) / 256, 256, 0, s.stream>>>(g->ix, cb);
-    k_dp_warp<<<g->dp_grid, 128, 4 * DPW_BYTES, s.stream>>>(g->ix, cb);
+    k_dp_warp<<<g->dp_blocks, 128, 4 * DPW_BYTES, s.stream>>>(g->ix, cb);
     cudaMemcpyAsync(s.h_mats, s.d_mats, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, s.stream);
     cudaMemcpyAsync(s.h_invalid, s.d_invalid, n, cudaMemcpyDeviceToHost, s.stream);
     cudaMemcpyAsync(s.h_ctr, s.d_ctr, CTR_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s.stream);
 }
 
-constexpr uint64_t QUEUE_KERNELS_PER_CHUNK = 11;
+constexpr uint64_t QUEUE_KERNELS_PER_CHUNK = 13;
 
 int qslot_graph(fame_gpu* g, fame_queue* q, QSlot& s, uint32_t n, uint32_t flags, uint32_t* meth, cudaGraphExec_t* out)
 {

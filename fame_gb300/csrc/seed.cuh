@@ -36,14 +36,15 @@ struct SeedMem {
     uint32_t* ops;       // gathered entries
     uint8_t* opk;        // k-mer index of each op (< 256)
     uint32_t* dt_key;    // distinct (window, strand) keys
-    uint32_t* dt_first;
-    uint32_t* dt_cnt;
+    uint32_t* dt_first;  // first op of each key; null: packed into dt_cnt (bits 0-15, ops < 65536)
+    uint32_t* dt_cnt;    // count of each key (packed: bits 16-31, which wrap like the reference's uint16 count)
     uint32_t* ins;       // inserted keys, first-touch order
     uint32_t* ins_cnt;
     uint32_t* slot;      // replayed bucket array (index into ins, EMPTY_KEY if free)
     uint32_t* stk;       // pending insertions (top = next)
     uint32_t* ovf;       // overflow list
     uint32_t* stage;     // candidates of this task
+    uint64_t* pre;       // prefix hashes of the read (8 * (len + 1) bytes), dead once the bucket bounds are read
     uint32_t ops_cap, dt_cap, slot_cap, stk_cap, ovf_cap;
 };
 
@@ -203,12 +204,12 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
     // 1. hashes and bucket bounds (getSeedRefs pass 1, ReadQueue.cpp:2331-2354):
     //    every lane first hashes its k-mers, then issues all of its bucket
     //    reads before using any, so their DRAM latencies overlap.  Hashes by
-    //    the prefix form of seedhash.h: P[j] (j <= len, 8 bytes each) in the
-    //    ops / count area, which is dead until the gather.
+    //    the prefix form of seedhash.h: P[j] (j <= len, 8 bytes each) in an
+    //    area that is dead until the gather or the count.
     const uint32_t nk = len - KMERLEN + 1;
     uint32_t sigma = 0;
     unsigned long long gb = 0;
-    uint64_t* P = (uint64_t*)s.ops;
+    uint64_t* P = s.pre;
     {
         uint64_t carry = 0;   // P[b]
         for (uint32_t b = 0; b <= len; b += 32) {
@@ -318,6 +319,8 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
     //    bucket are skipped, ReadQueue.cpp:2380-2387, 2421-2428)
     const uint32_t dsz = min(s.dt_cap, pow2_ceil(2 * T + 2));
     const uint32_t dmask = dsz - 1;
+    const bool packed = s.dt_first == nullptr;
+    const uint32_t cnt_shift = packed ? 16 : 0;
     for (uint32_t i = lane; i < dsz; i += 32) s.dt_key[i] = EMPTY_KEY;
     __syncwarp();
     for (uint32_t b0 = 0; b0 < T; b0 += 32) {
@@ -337,12 +340,16 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
                 if (cur == e) break;
                 if (cur == EMPTY_KEY) {
                     const uint32_t old = atomicCAS(&s.dt_key[h], EMPTY_KEY, e);
-                    if (old == EMPTY_KEY) { s.dt_first[h] = i; s.dt_cnt[h] = 0; break; }
+                    if (old == EMPTY_KEY) {
+                        if (packed) s.dt_cnt[h] = i;
+                        else { s.dt_first[h] = i; s.dt_cnt[h] = 0; }
+                        break;
+                    }
                     if (old == e) break;
                 }
                 h = (h + 1) & dmask;
             }
-            s.dt_cnt[h] += __popc(grp);
+            s.dt_cnt[h] += (uint32_t)__popc(grp) << cnt_shift;
         }
         __syncwarp();
     }
@@ -360,7 +367,8 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
             if (!(i > s.kpre[k] && s.ops[i - 1] == e) && (k == 0 || k - 1 < maxQPos)) {
                 uint32_t h = dt_hash(e, dmask);
                 while (s.dt_key[h] != e) h = (h + 1) & dmask;
-                if (s.dt_first[h] == i) { take = true; c = s.dt_cnt[h]; }
+                const uint32_t v = s.dt_cnt[h];
+                if ((packed ? (v & 0xffffu) : s.dt_first[h]) == i) { take = true; c = v >> cnt_shift; }
             }
         }
         const unsigned bm = __ballot_sync(0xffffffffu, take);

@@ -294,23 +294,54 @@ int fame_gpu_host_free(fame_gpu* g, void* ptr);
 /* The CUDA stream (cudaStream_t) all work of the context runs on. */
 int fame_gpu_stream(fame_gpu* g, void** stream);
 
-/* Per-stage device time of the last match call, in milliseconds, measured with
- * CUDA events on the library's stream when enabled.  Stages: 0 read prep,
- * 1 seed/gather/order, 2 Shift-And, 3 select + exact CpG calls, 4 banded DP +
- * CpG calls, 5 heavy-read seeding.  Returns the number of stages. */
+/* Per-stage device time of the last single-end match call, in milliseconds,
+ * measured with CUDA events on the library's stream when enabled.  Stages:
+ * 0 read prep, 1 light seeding (or routing to the middle tiers), 2 Shift-And,
+ * 3 select + exact CpG calls, 4 banded DP + CpG calls, 5 the other seeding
+ * tiers, split into 6 the smaller shared-memory middle tier, 7 the larger one
+ * and 8 the global-memory tiers.  Returns the number of stages (FAME_STAGES). */
+#define FAME_STAGES 9
 int fame_gpu_set_timing(fame_gpu* g, int enable);
 int fame_gpu_stage_times(fame_gpu* g, float* ms, int n);
+/* Seeding tasks that entered each tier after the light one in the last
+ * single-end chunk: out[0] the smaller shared-memory middle tier (up to 511
+ * gathered bucket entries), out[1] the larger one (up to 1023), out[2] the
+ * global-memory tier, out[3] the large-capacity tier.  No counterpart in the
+ * reference (diagnostics). */
+int fame_gpu_seed_tier_counts(const fame_gpu* g, uint64_t* out);
 /* Number of kernel launches of the last match call. */
 int fame_gpu_last_launches(const fame_gpu* g);
 /* Device bytes held by the resident index tables of the context. */
 uint64_t fame_gpu_index_bytes(const fame_gpu* g);
-/* Where a read's seeding starts (no counterpart in the reference; results do
- * not depend on it): 0 = a warp with shared-memory working space, reads whose
- * bucket entries exceed it moving on to global-memory tiers; 1 = every read
- * in the global-memory middle tier.  fame_gpu_open picks 1 when the index
- * holds more entries than buckets, else 0.  mode < 0 returns the current
- * mode. */
+/* How reads are seeded (no counterpart in the reference; results do not
+ * depend on it).  Each tier is one warp per (read, orientation) task; a task
+ * over a tier's capacity moves on to the next.  Bit 0: 0 = the light tier
+ * first (small shared-memory working space, up to 128 gathered bucket
+ * entries); 1 = every read starts in the middle tiers (genome-scale indexes).
+ * The middle tiers keep the whole working set in shared memory and take
+ * their tasks from device work queues: one for up to 511 gathered entries
+ * (12 warps per SM), then one for up to 1023; bit 1 = 1 skips the first.
+ * After them come a global-memory tier (up to 4096) and a large-capacity one
+ * sized by the index's largest bucket.  fame_gpu_open sets bit 0 when the
+ * index holds more entries than buckets.  mode < 0 returns the current mode.
+ * Waits for the context's queue and drops its captured graphs. */
 int fame_gpu_set_seed_tier(fame_gpu* g, int mode);
+
+/* Autotuner of the launch shapes (no counterpart in the reference): runs the
+ * chunk (n reads already in device memory, as for fame_gpu_match_reads_dev,
+ * with these flags) a few times per stage with different shapes (the seeding
+ * modes of fame_gpu_set_seed_tier, the window-scan and banded-DP grids),
+ * checks that every shape gives the same per-read results, keeps the fastest
+ * shape per stage and, when json_path is given, writes the choice and every
+ * trial's stage times there (CUDA events: read prep, light seeding, window
+ * scans, selection, DP, other seeding tiers).  The context's tallies are not
+ * touched.  The shapes apply to the plain calls and to the queue alike; the
+ * queue's captured graphs are dropped.  Allocates and frees device memory. */
+int fame_gpu_autotune(fame_gpu* g, const char* seqs_dev, const uint64_t* offs_dev, uint32_t n, uint32_t flags,
+                      const char* json_path);
+/* Applies the shapes of a file written by fame_gpu_autotune (FAME_ERR_IO when
+ * the file cannot be read or holds no valid shape). */
+int fame_gpu_load_tuning(fame_gpu* g, const char* json_path);
 
 /* CpG calls that allocate no device memory.  No counterpart in the reference:
  * it is for callers that cannot allocate while they run (a serving loop that

@@ -78,6 +78,22 @@ def test_golden_modes(gpu, pe_golden, mode):
     assert_same(got, {k: pe_golden["%s_%s" % (name, k)] for k in KEYS}, name)
 
 
+@pytest.mark.parametrize("mode", PE_MODES, ids=[m[0] for m in PE_MODES])
+def test_golden_modes_middle_tier(gpu, pe_golden, mode):
+    """Every pair seeded by the paired middle tier (the route genome-scale
+    indexes take: global working memory with genome-scale caps, pairs from a
+    work queue) gives the reference's results too."""
+    name, chunk, both = mode
+    s1, o1, s2, o2 = golden_pairs(pe_golden)
+    assert gpu.seed_tier() == 0
+    gpu.seed_tier(1)
+    try:
+        got = run_pairs(gpu, s1, o1, s2, o2, chunk, both, int(pe_golden["maxpdist"]))
+    finally:
+        gpu.seed_tier(0)
+    assert_same(got, {k: pe_golden["%s_%s" % (name, k)] for k in KEYS}, name + " (middle tier)")
+
+
 def test_paired_read_queue_mirror(gpu, pe_golden, product_index):
     """PairedReadQueue (the host mirror of the two-file ReadQueue) gives the
     reference's tallies and counters through the same C ABI."""

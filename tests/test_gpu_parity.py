@@ -70,18 +70,20 @@ def test_golden_reference_parity(gpu, golden, name, chunk, both):
     assert_same(r, ref, name)
 
 
+@pytest.mark.parametrize("mode", [1, 3], ids=["mid2048", "mid1024"])
 @pytest.mark.parametrize("name,chunk,both", [("default", 0, False), ("chunk1000", 1000, False), ("both", 777, True)])
-def test_golden_parity_middle_seeding_tier(gpu, golden, name, chunk, both):
-    """Every read seeded by the global-memory middle tier (the genome-scale
-    route) gives the reference's results too."""
+def test_golden_parity_middle_seeding_tier(gpu, golden, name, chunk, both, mode):
+    """Every read seeded by the middle tiers (the genome-scale route: the
+    shared-memory tier with either count-table size, then the global-memory
+    ones) gives the reference's results too."""
     assert gpu.seed_tier() == 0
-    gpu.seed_tier(1)
+    gpu.seed_tier(mode)
     try:
         r = run_mode(gpu, golden["read_seq"].tobytes(), golden["read_offs"], chunk, both)
     finally:
         gpu.seed_tier(0)
     ref = {k: golden[name + "_" + k] for k in ("mat", "invalid", "meth", "counters")}
-    assert_same(r, ref, name + " (middle tier)")
+    assert_same(r, ref, name + " (middle tier, mode %d)" % mode)
 
 
 def test_readqueue_mirror(golden, product_index, gpu):
@@ -183,15 +185,20 @@ def test_oracle_parity_read_lengths():
 
 
 def test_oracle_parity_heavy_reads():
-    """Near-identical repeat copies give reads hundreds of bucket entries, which
-    take the global-memory seeding path; the result must not change."""
+    """Near-identical repeat copies give reads hundreds to thousands of bucket
+    entries, which pass through every seeding tier (the shared-memory middle
+    tier, then the global-memory ones); the result must not change, whichever
+    tier a read starts in and whatever the middle tier's table size."""
     from oracle.oracle import OracleIndex
     g, seq, offs = _workload(31, 1500, repeats=0.5, copies_div=(0.0, 0.005), chrom=(250_000,))
     hi = HostIndex.build(g.seqs, readlen=100)
     oi = OracleIndex.build(g.seqs, readlen=100)
+    ref = _oracle_run(oi, seq, offs, 0, False)
     gm = GpuMatcher(hi, 0)
     try:
-        assert_same(run_mode(gm, seq, offs, 0, False), _oracle_run(oi, seq, offs, 0, False), "heavy")
+        for mode in range(4):
+            gm.seed_tier(mode)
+            assert_same(run_mode(gm, seq, offs, 0, False), ref, "heavy, seed mode %d" % mode)
     finally:
         gm.close()
 
