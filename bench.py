@@ -388,7 +388,7 @@ def run_gb300(args):
     gm.set_timing(True)
     # ---- timed: plain form, reads resident in HBM
     stage = np.zeros(len(GpuMatcher.STAGES))
-    tiers = np.zeros(4)
+    tiers = np.zeros(5)
     reads = gather = scans = launches = heavy = reruns = dp = inv_len = succ = 0
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
@@ -535,7 +535,8 @@ def run_gb300(args):
         "counts": {"reads": reads, "matched": succ, "invalid_len": inv_len, "dp_reads": dp,
                    "windows_scanned_per_read": scans / max(1, reads), "heavy_seed_tasks": heavy,
                    "seed_tier_tasks": {"mid_small": int(tiers[0]), "mid_large": int(tiers[1]),
-                                       "global": int(tiers[2]), "large_capacity": int(tiers[3])},
+                                       "global": int(tiers[2]), "large_capacity": int(tiers[3]),
+                                       "replayed_orders": int(tiers[4])},
                    "candidate_overflow_reruns": reruns},
         "roofline": {"kernel": "k_seed (index gathers)", "bound": "hbm", "achieved": gbps, "peak": hbm,
                      "unit": "GB/s", "frac": gbps / hbm, "traffic": traffic,

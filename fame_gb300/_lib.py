@@ -71,7 +71,7 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_fastq_close", "fame_queue_stage", "fame_queue_submit_staged", "fame_match_fastq",
            "fame_match_fastq_paired", "fame_index_write", "fame_gpu_index_bytes", "fame_queue_wait",
            "fame_gpu_set_seed_tier", "fame_gpu_autotune", "fame_gpu_load_tuning",
-           "fame_gpu_seed_tier_counts"]
+           "fame_gpu_seed_tier_counts", "fame_gpu_map_order_probe"]
 
 _lib = None
 
@@ -114,6 +114,7 @@ def lib(build_if_missing: bool = True):
     L.fame_gpu_autotune.argtypes = [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_char_p]
     L.fame_gpu_load_tuning.argtypes = [_P, C.c_char_p]
     L.fame_gpu_seed_tier_counts.argtypes = [_P, _P]
+    L.fame_gpu_map_order_probe.argtypes = [_P, _P, C.c_uint32, C.c_uint32, _P, _P]
     L.fame_gpu_index_bytes.argtypes = [_P]
     L.fame_gpu_index_bytes.restype = C.c_uint64
     L.fame_gpu_match_pairs.argtypes = [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]
@@ -366,9 +367,19 @@ class GpuMatcher:
         lib().fame_gpu_stage_times(self.h, _ptr(ms), len(ms))
         return ms
 
+    def map_order_probe(self, keys, bucket_count: int):
+        """fame_gpu_map_order_probe: the device replay's iteration order of distinct keys, and its final
+        bucket count."""
+        keys = np.ascontiguousarray(keys, dtype=np.uint32)
+        order = np.zeros(max(1, len(keys)), np.uint32)
+        fb = np.zeros(1, np.uint64)
+        k = lib().fame_gpu_map_order_probe(self.h, _ptr(keys), len(keys), int(bucket_count), _ptr(order), _ptr(fb))
+        _check(min(k, 0), self.h)
+        return order[:k].copy(), int(fb[0])
+
     def seed_tier_counts(self):
         """fame_gpu_seed_tier_counts: tasks entering each seeding tier after the light one, last chunk."""
-        out = np.zeros(4, np.uint64)
+        out = np.zeros(5, np.uint64)
         _check(lib().fame_gpu_seed_tier_counts(self.h, _ptr(out)), self.h)
         return out
 

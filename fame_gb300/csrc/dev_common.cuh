@@ -8,9 +8,11 @@
 namespace fame {
 
 // The index as it lives in HBM (read-only for the whole context lifetime).
-//   tab2   : per bucket {start offset (tabIndex), first entry of the bucket (0 if
-//            empty)}, HTABSIZE + 1 entries: one read gives a k-mer's bounds and,
-//            for the common one-entry bucket, its entry
+//   rec    : per bucket 32 bytes {start offset (tabIndex), size, its first
+//            REC_INLINE entries}, HTABSIZE records: one aligned sector gives a
+//            k-mer's bounds and, for buckets of up to REC_INLINE entries (at
+//            genome scale nearly every bucket a read's k-mer lands in), all
+//            of its entries
 //   entry  : one uint32 per k-mer entry: window id | forward-strand << 31
 //            (kmerTableSmall.meta with strandTable folded into bit 31; the
 //            start-CpG bit the reference reserves there is never set by the
@@ -19,10 +21,15 @@ namespace fame {
 //            chromosomes concatenated at 32-base aligned offsets
 //   gnmask : one bit per base, set for N
 //   win    : {startPos, chrom, startInd, endInd} per window (metaWindows)
+constexpr uint32_t REC_INLINE = 6;   // bucket entries held in a bucket's record
+
 struct DevIndex {
     uint32_t readlen;
     uint32_t n_chrom;
-    const uint2* tab2;
+    // bucket records, 32 bytes per bucket k: rec[2k] = {start, size, e0, e1},
+    // rec[2k + 1] = {e2, e3, e4, e5} (the bucket's first REC_INLINE entries,
+    // 0 past its size); one aligned sector holds a lookup for most buckets
+    const uint4* rec;
     const uint32_t* entry;
     const uint32_t* gpack;
     const uint32_t* gnmask;
@@ -86,6 +93,7 @@ enum {
     CTR_HEAVY4,         // seeding tasks handed on by the global-memory tier to the large-capacity one
     CTR_QMID,           // work-queue position of the first middle seeding tier (pairs: of the paired middle tier)
     CTR_QMID2,          // work-queue position of the second middle seeding tier
+    CTR_REPLAY,         // seeding tasks whose candidate order needed the map replay
     CTR_N
 };
 

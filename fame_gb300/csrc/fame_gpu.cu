@@ -60,7 +60,8 @@ struct fame_gpu {
     int timing = 0;
     cudaEvent_t ev[12]{};
     float stage_ms[FAME_STAGES]{};
-    uint64_t tier_tasks[4]{};            // tasks entering each seeding tier after the light one, last chunk
+    uint64_t tier_tasks[5]{};            // tasks entering each seeding tier after the light one, last chunk;
+                                         // [4]: tasks whose candidate order needed the map replay
     int launches = 0;
     int sm_count = 0;
     uint32_t dp_grid = 0;   // resident blocks of k_dp_warp on the whole device
@@ -353,13 +354,13 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
             return fail(set_err(g, FAME_ERR_CUDA, "k-mer upload failed"));
     }
     g->ix.entry = d_entry;
-    // ---- bucket offsets with each bucket's first entry beside its start
+    // ---- bucket records: start, size and the first entries of each bucket in one sector
     {
-        uint2* d_tab2;
-        if ((rc = alloc_idx((void**)&d_tab2, (HTABSIZE + 1) * 8))) return fail(rc);
-        k_build_tab2<<<g->sm_count * 8, 256, 0, g->stream>>>(d_tab, d_entry, HTABSIZE, d_tab2);
-        if (cudaGetLastError() != cudaSuccess) return fail(set_err(g, FAME_ERR_CUDA, "tab2 build failed"));
-        g->ix.tab2 = d_tab2;
+        uint4* d_rec;
+        if ((rc = alloc_idx((void**)&d_rec, HTABSIZE * 32))) return fail(rc);
+        k_build_rec<<<g->sm_count * 8, 256, 0, g->stream>>>(d_tab, d_entry, HTABSIZE, d_rec);
+        if (cudaGetLastError() != cudaSuccess) return fail(set_err(g, FAME_ERR_CUDA, "bucket record build failed"));
+        g->ix.rec = d_rec;
     }
     // ---- paired path: tmask per entry (kmerTableSmall.tmask), filteredKmers sorted
     {
@@ -468,7 +469,7 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         unsigned int mx = 0;
         cudaMemcpyAsync(&mx, d_mx, 4, cudaMemcpyDeviceToHost, g->stream);
         cudaStreamSynchronize(g->stream);
-        // the plain offset table is not needed any more (tab2 holds the offsets)
+        // the plain offset table is not needed any more (the records hold the offsets)
         cudaFree(d_tab);
         g->index_bytes -= (HTABSIZE + 1) * 4;
         g->index_allocs.erase(std::remove(g->index_allocs.begin(), g->index_allocs.end(), (void*)d_tab),
@@ -526,7 +527,7 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
             return fail(set_err(g, FAME_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)));
         g->noalloc_scratch = (uint8_t*)p;
     }
-    if (cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * LightLayout::BYTES) != cudaSuccess ||
+    if (cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * LightR::BYTES) != cudaSuccess ||
         cudaFuncSetAttribute(k_dp_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * DPW_BYTES) != cudaSuccess)
         return fail(set_err(g, FAME_ERR_CUDA, "shared memory attribute"));
     {
@@ -635,7 +636,7 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         if (g->seed_mid_first)
             k_seed_route<<<(ntask + 255) / 256, 256, 0, g->stream>>>(cb, ntask);
         else
-            k_seed<<<std::max(1u, blocks), wpb * 32, wpb * LightLayout::BYTES, g->stream>>>(g->ix, cb, ntask);
+            k_seed<<<std::max(1u, blocks), wpb * 32, wpb * LightR::BYTES, g->stream>>>(g->ix, cb, ntask);
         if (T) cudaEventRecord(g->ev[2], g->stream);
         const int tier_launches = seed_tiers(g, cb, g->stream, g->ms, g->hs, T ? g->ev + 7 : nullptr);
         if (T) cudaEventRecord(g->ev[6], g->stream);
@@ -703,6 +704,7 @@ int run_chunk(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
                 g->tier_tasks[2] = h[CTR_HEAVY3];
                 g->tier_tasks[3] = h[CTR_HEAVY4];
             }
+            g->tier_tasks[4] = h[CTR_REPLAY];
         }
         return FAME_OK;
     }
@@ -1007,10 +1009,40 @@ extern "C" int fame_gpu_stage_times(fame_gpu* g, float* ms, int n)
     return FAME_STAGES;
 }
 
+extern "C" int fame_gpu_map_order_probe(fame_gpu* g, const uint32_t* keys, uint32_t n, uint32_t bucket_count,
+                                        uint32_t* order, uint64_t* final_buckets)
+{
+    if (!g || (n && (!keys || !order)) || !final_buckets || n > 65536) return FAME_ERR_ARG;
+    CK(cudaSetDevice(g->device));
+    for (uint32_t i = 0; i < n; ++i)
+        if (keys[i] >> 31) return set_err(g, FAME_ERR_ARG, "map order probe: keys must leave bit 31 clear");
+    const uint32_t cap = 4 * std::max<uint32_t>(n, bucket_count) + 256;
+    uint32_t *d_keys = nullptr, *d_scratch = nullptr, *d_order = nullptr, *d_out = nullptr;
+    auto done = [&](int rc) {
+        dev_free(d_keys); dev_free(d_scratch); dev_free(d_order); dev_free(d_out);
+        return rc;
+    };
+    int rc;
+    if ((rc = dev_alloc(g, &d_keys, n)) || (rc = dev_alloc(g, &d_scratch, 3ull * cap)) ||
+        (rc = dev_alloc(g, &d_order, n)) || (rc = dev_alloc(g, &d_out, 3)))
+        return done(rc);
+    uint32_t out[3] = {0, 0, 0};
+    if (n && cudaMemcpy(d_keys, keys, 4ull * n, cudaMemcpyHostToDevice) != cudaSuccess)
+        return done(set_err(g, FAME_ERR_CUDA, "map order probe: upload"));
+    k_map_order_probe<<<1, 32, 0, g->stream>>>(d_keys, n, bucket_count, d_scratch, cap, d_order, d_out);
+    if (cudaStreamSynchronize(g->stream) != cudaSuccess ||
+        cudaMemcpy(out, d_out, sizeof(out), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        (out[0] && cudaMemcpy(order, d_order, 4ull * out[0], cudaMemcpyDeviceToHost) != cudaSuccess))
+        return done(set_err(g, FAME_ERR_CUDA, "map order probe failed"));
+    if (out[2]) return done(set_err(g, FAME_ERR_INDEX, "map order probe: a capacity was exceeded"));
+    *final_buckets = out[1];
+    return done((int)out[0]);
+}
+
 extern "C" int fame_gpu_seed_tier_counts(const fame_gpu* g, uint64_t* out)
 {
     if (!g || !out) return FAME_ERR_ARG;
-    for (int i = 0; i < 4; ++i) out[i] = g->tier_tasks[i];
+    for (int i = 0; i < 5; ++i) out[i] = g->tier_tasks[i];
     return FAME_OK;
 }
 

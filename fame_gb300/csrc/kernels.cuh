@@ -955,62 +955,70 @@ __global__ void k_prep(ChunkBufs cb, uint32_t readlen)
     if ((threadIdx.x & 31) == 0 && wbit) atomicOr(cb.ctr + CTR_WMASK, (unsigned long long)wbit);
 }
 
-// Light path: one warp per task, working memory in shared memory.
-constexpr uint32_t L_OPS = 128, L_DT = 256, L_SLOT = 512 + NBHD - 1, L_OVF = 32;
-struct LightLayout {
-    // per warp, in bytes
-    static constexpr uint32_t KST = 0;                          // 224 x u32
-    static constexpr uint32_t KPRE = KST + 224 * 4;             // 225 x u32
-    static constexpr uint32_t INS = KPRE + 228 * 4;             // L_OPS x u32
-    static constexpr uint32_t INSC = INS + L_OPS * 4;           // L_OPS x u32
-    static constexpr uint32_t U = INSC + L_OPS * 4;             // union region
-    // phase A (hash/gather/count): seq, ops, opk, dt
-    static constexpr uint32_t SEQ = U;                          // 256 B
-    static constexpr uint32_t OPS = SEQ + 256;                  // L_OPS x u32
-    static constexpr uint32_t OPK = OPS + L_OPS * 4;            // L_OPS x u8
-    static constexpr uint32_t DTK = OPK + L_OPS;                // L_DT x u32
-    static constexpr uint32_t DTF = DTK + L_DT * 4;
-    static constexpr uint32_t DTC = DTF + L_DT * 4;
-    static constexpr uint32_t END_A = DTC + L_DT * 4;
-    // phase B (replay): slot, stk, ovf, stage
-    static constexpr uint32_t SLOT = U;
-    static constexpr uint32_t STK = SLOT + ((L_SLOT * 4 + 15) / 16) * 16;
-    static constexpr uint32_t OVF = STK + L_OPS * 4;
-    static constexpr uint32_t STAGE = OVF + L_OVF * 4;
-    static constexpr uint32_t END_B = STAGE + L_OPS * 4;
-    static constexpr uint32_t BYTES = ((END_A > END_B ? END_A : END_B) + 15) / 16 * 16;
-    // the hash pass keeps its prefix array (8 bytes per read base + 1) in ops .. count
-    static_assert(END_A - OPS >= 8 * (FAME_MAX_READ_LEN + 1) && OPS % 8 == 0, "prefix array does not fit");
+// Shared-memory working set of one warp for seed_task_rec: up to OPS
+// gathered bucket entries, a DT-slot count table (a power of two > 2 * OPS).
+// The per-k-mer arrays, the count table (prefix hashes first) and, once the
+// insertion order is listed, the replay's buckets, stack, overflow list and
+// staged candidates share one region.
+template <uint32_t OPS, uint32_t DT, uint32_t OVF_N>
+struct SeedLayoutR {
+    static_assert(DT >= 2 * OPS && (DT & (DT - 1)) == 0 && OPS <= 1024, "count table too small");
+    static constexpr uint32_t R16(uint32_t b) { return (b + 15) / 16 * 16; }
+    static constexpr uint32_t SLOT_N = DT + 64;    // replayed buckets: pow2_ceil(OPS + 1) + 61 at most
+    static constexpr uint32_t SEQ = 0;             // 256 B
+    static constexpr uint32_t KSZ = SEQ + 256;     // 224 x u16
+    static constexpr uint32_t KPRE = KSZ + 448;    // 225 x u32
+    static constexpr uint32_t DTK = KPRE + 912;
+    static constexpr uint32_t DTV = DTK + DT * 4;
+    static constexpr uint32_t END_U = DTV + DT * 4;
+    static constexpr uint32_t REACHED = END_U;     // 34 x u32
+    static constexpr uint32_t BITMAP = REACHED + 144;
+    static constexpr uint32_t INS = BITMAP + R16((OPS + 31) / 32 * 4);
+    static constexpr uint32_t INSC = INS + R16(OPS * 4);
+    static constexpr uint32_t BYTES = INSC + R16(OPS * 2);
+    // the replay, over [0, END_U)
+    static constexpr uint32_t SLOT = 0;
+    static constexpr uint32_t STK = SLOT + R16(SLOT_N * 4);
+    static constexpr uint32_t OVF = STK + R16(OPS * 4);
+    static constexpr uint32_t STAGE = OVF + R16(OVF_N * 4);
+    static constexpr uint32_t END_B = STAGE + R16(OPS * 4);
+    static_assert(END_B <= END_U, "the replay does not fit the shared region");
+    static_assert(DTK % 8 == 0 && END_U - DTK >= 8 * (FAME_MAX_READ_LEN + 1), "prefix hashes do not fit");
 };
 
-__device__ __forceinline__ SeedMem light_mem(uint8_t* base)
+template <class L, uint32_t OPS, uint32_t DT, uint32_t OVF_N>
+__device__ __forceinline__ SeedMemR seed_mem_r(uint8_t* base)
 {
-    SeedMem s;
-    s.kst = (uint32_t*)(base + LightLayout::KST);
-    s.kpre = (uint32_t*)(base + LightLayout::KPRE);
-    s.ins = (uint32_t*)(base + LightLayout::INS);
-    s.ins_cnt = (uint32_t*)(base + LightLayout::INSC);
-    s.seq = base + LightLayout::SEQ;
-    s.ops = (uint32_t*)(base + LightLayout::OPS);
-    s.opk = base + LightLayout::OPK;
-    s.dt_key = (uint32_t*)(base + LightLayout::DTK);
-    s.dt_first = (uint32_t*)(base + LightLayout::DTF);
-    s.dt_cnt = (uint32_t*)(base + LightLayout::DTC);
-    s.slot = (uint32_t*)(base + LightLayout::SLOT);
-    s.stk = (uint32_t*)(base + LightLayout::STK);
-    s.ovf = (uint32_t*)(base + LightLayout::OVF);
-    s.stage = (uint32_t*)(base + LightLayout::STAGE);
-    s.pre = (uint64_t*)(base + LightLayout::OPS);
-    s.ops_cap = L_OPS; s.dt_cap = L_DT; s.slot_cap = L_SLOT; s.stk_cap = L_OPS; s.ovf_cap = L_OVF;
+    SeedMemR s;
+    s.seq = base + L::SEQ;
+    s.ksz = (uint16_t*)(base + L::KSZ);
+    s.kpre = (uint32_t*)(base + L::KPRE);
+    s.pre = (uint64_t*)(base + L::DTK);
+    s.dt_key = (uint32_t*)(base + L::DTK);
+    s.dt_val = (uint32_t*)(base + L::DTV);
+    s.reached = (uint32_t*)(base + L::REACHED);
+    s.bitmap = (uint32_t*)(base + L::BITMAP);
+    s.ins = (uint32_t*)(base + L::INS);
+    s.ins_cnt = (uint16_t*)(base + L::INSC);
+    s.slot = (uint32_t*)(base + L::SLOT);
+    s.stk = (uint32_t*)(base + L::STK);
+    s.ovf = (uint32_t*)(base + L::OVF);
+    s.stage = (uint32_t*)(base + L::STAGE);
+    s.ops_cap = OPS; s.dt_cap = DT; s.slot_cap = L::SLOT_N; s.stk_cap = OPS; s.ovf_cap = OVF_N;
     return s;
 }
 
+// Light tier: up to 128 gathered entries (the common read of an index with
+// fewer entries than buckets), many warps per SM.
+constexpr uint32_t L_OPS = 128, L_DT = 256, L_OVF = 32;
+using LightR = SeedLayoutR<L_OPS, L_DT, L_OVF>;
+
 // tasks: all (read, orientation) pairs of the chunk in orientation-major order
-__global__ void __launch_bounds__(128, 8) k_seed(DevIndex ix, ChunkBufs cb, uint32_t ntask)
+__global__ void __launch_bounds__(128) k_seed(DevIndex ix, ChunkBufs cb, uint32_t ntask)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const uint32_t wib = threadIdx.x >> 5;
-    const SeedMem s = light_mem(smem + wib * LightLayout::BYTES);
+    const SeedMemR s = seed_mem_r<LightR, L_OPS, L_DT, L_OVF>(smem + wib * LightR::BYTES);
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     const int norient = __popc(cb.orient_mask);
     const uint32_t first_o = (cb.orient_mask & 1u) ? 0 : 1;
@@ -1020,7 +1028,7 @@ __global__ void __launch_bounds__(128, 8) k_seed(DevIndex ix, ChunkBufs cb, uint
         const uint32_t o = norient == 2 ? (t & 1) : first_o;
         if (cb.rflags[r]) continue;
         const uint32_t task = 2 * r + o;
-        const int heavy = seed_task(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES, res);
+        const int heavy = seed_task_rec(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES, res);
         if (heavy && (threadIdx.x & 31) == 0) {
             const uint32_t h = (uint32_t)atomicAdd(cb.ctr + CTR_HEAVY, 1ull);
             cb.heavy[h] = task;
@@ -1032,79 +1040,23 @@ __global__ void __launch_bounds__(128, 8) k_seed(DevIndex ix, ChunkBufs cb, uint
 
 // Middle seeding tiers, for genome-scale indexes (about three entries per
 // bucket: a read gathers hundreds of entries, over the light tier's caps).
-// One warp per task with its whole working set in shared memory, so that the
-// dependent steps of the count (load an op, probe the count table, add) wait
-// on shared memory only: the read, its per-k-mer bucket starts and prefix,
-// the inserted keys and their counts, and a union of the op lists with the
-// count table (packed: first op and count in one word; the prefix hashes sit
-// there first) or, after the count, of the replayed buckets, the pending
-// stack, the overflow list and the staged candidates.  OPS bucket entries at
-// most; DT count-table slots (a power of two > 2 * OPS).
-template <uint32_t OPS, uint32_t DT>
-struct MidLayout {
-    static_assert(DT >= 2 * OPS + 2 && (DT & (DT - 1)) == 0 && OPS < 65536, "count table too small");
-    static constexpr uint32_t R16(uint32_t b) { return (b + 15) / 16 * 16; }
-    static constexpr uint32_t SLOT_N = DT + 64;    // replayed buckets: 2 * pow2_ceil(OPS + 1) + 64 at most
-    static constexpr uint32_t OVF_N = 256;
-    static constexpr uint32_t KST = 0;                                // 224 x u32
-    static constexpr uint32_t KPRE = KST + 224 * 4;                   // 225 x u32
-    static constexpr uint32_t SEQ = KPRE + 228 * 4;                   // 256 B
-    static constexpr uint32_t INS = SEQ + 256;
-    static constexpr uint32_t INSC = INS + R16(OPS * 4);
-    static constexpr uint32_t U = INSC + R16(OPS * 4);
-    // phase A: hash, gather, count
-    static constexpr uint32_t OPSA = U;
-    static constexpr uint32_t OPK = OPSA + R16(OPS * 4);
-    static constexpr uint32_t DTK = OPK + R16(OPS);
-    static constexpr uint32_t DTC = DTK + DT * 4;
-    static constexpr uint32_t END_A = DTC + DT * 4;
-    // phase B: replay
-    static constexpr uint32_t SLOT = U;
-    static constexpr uint32_t STK = SLOT + R16(SLOT_N * 4);
-    static constexpr uint32_t OVF = STK + R16(OPS * 4);
-    static constexpr uint32_t STAGE = OVF + OVF_N * 4;
-    static constexpr uint32_t END_B = STAGE + R16(OPS * 4);
-    static constexpr uint32_t BYTES = R16(END_A > END_B ? END_A : END_B);
-    static_assert(DTK % 8 == 0 && END_A - DTK >= 8 * (FAME_MAX_READ_LEN + 1), "prefix hashes do not fit");
-};
-
-template <uint32_t OPS, uint32_t DT>
-__device__ __forceinline__ SeedMem mid_mem(uint8_t* sm)
-{
-    using L = MidLayout<OPS, DT>;
-    SeedMem s;
-    s.kst = (uint32_t*)(sm + L::KST);
-    s.kpre = (uint32_t*)(sm + L::KPRE);
-    s.seq = sm + L::SEQ;
-    s.ins = (uint32_t*)(sm + L::INS);
-    s.ins_cnt = (uint32_t*)(sm + L::INSC);
-    s.ops = (uint32_t*)(sm + L::OPSA);
-    s.opk = sm + L::OPK;
-    s.pre = (uint64_t*)(sm + L::DTK);
-    s.dt_key = (uint32_t*)(sm + L::DTK);
-    s.dt_first = nullptr;   // packed into dt_cnt
-    s.dt_cnt = (uint32_t*)(sm + L::DTC);
-    s.slot = (uint32_t*)(sm + L::SLOT);
-    s.stk = (uint32_t*)(sm + L::STK);
-    s.ovf = (uint32_t*)(sm + L::OVF);
-    s.stage = (uint32_t*)(sm + L::STAGE);
-    s.ops_cap = OPS; s.dt_cap = DT; s.slot_cap = L::SLOT_N; s.stk_cap = OPS; s.ovf_cap = L::OVF_N;
-    return s;
-}
-
-// The tasks of `list` (its length in counter ctr_in), taken one at a time
-// per warp from a work queue (counter ctr_q, zero at launch): a task's cost
-// follows its read's bucket sizes, so fixed strides would leave warps idle
-// behind a few long tasks.  A task over the caps goes to `spill` (counter
-// ctr_spill) for the next tier.  Launched with WPB warps per block and
-// WPB * MidLayout<OPS, DT>::BYTES of dynamic shared memory.
+// One warp per task with its whole working set in shared memory
+// (SeedLayoutR), tasks taken one at a time per warp from a work queue
+// (counter ctr_q, zero at launch): a task's cost follows its read's bucket
+// sizes, so fixed strides would leave warps idle behind a few long tasks.
+// The tasks of `list` (its length in counter ctr_in); a task over the caps
+// goes to `spill` (counter ctr_spill) for the next tier.  Launched with WPB
+// warps per block and WPB * SeedLayoutR<OPS, DT, MID_OVF>::BYTES of dynamic
+// shared memory.
+constexpr uint32_t MID_OVF = 256;
 template <uint32_t OPS, uint32_t DT, int WPB>
 __global__ void __launch_bounds__(32 * WPB) k_seed_mid(DevIndex ix, ChunkBufs cb, const uint32_t* list, int ctr_in,
                                                        int ctr_q, uint32_t* spill, int ctr_spill)
 {
     extern __shared__ __align__(16) uint8_t smem[];
+    using L = SeedLayoutR<OPS, DT, MID_OVF>;
     const uint32_t wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const SeedMem s = mid_mem<OPS, DT>(smem + wib * MidLayout<OPS, DT>::BYTES);
+    const SeedMemR s = seed_mem_r<L, OPS, DT, MID_OVF>(smem + wib * L::BYTES);
     const uint32_t ntask = (uint32_t)cb.ctr[ctr_in];
     CandRes res;
     while (true) {
@@ -1113,19 +1065,70 @@ __global__ void __launch_bounds__(32 * WPB) k_seed_mid(DevIndex ix, ChunkBufs cb
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= ntask) break;
         const uint32_t task = list[i];
-        const int over = seed_task(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES, res);
+        const int over = seed_task_rec(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES, res);
         if (over && lane == 0) spill[(uint32_t)atomicAdd(cb.ctr + ctr_spill, 1ull)] = task;
         __syncwarp();
     }
     cand_res_finish(cb, res);
 }
 
-// the two middle tiers: reads gathering up to 511 entries (12 warps per SM),
-// then up to 1023 (6 warps per SM)
+// the two middle tiers: reads gathering up to 511 entries, then up to 1023
 constexpr uint32_t MID_S_OPS = 511, MID_S_DT = 1024, MID_L_OPS = 1023, MID_L_DT = 2048;
 constexpr int MID_S_WPB = 4, MID_L_WPB = 2;
-using MidS = MidLayout<MID_S_OPS, MID_S_DT>;
-using MidL = MidLayout<MID_L_OPS, MID_L_DT>;
+using MidS = SeedLayoutR<MID_S_OPS, MID_S_DT, MID_OVF>;
+using MidL = SeedLayoutR<MID_L_OPS, MID_L_DT, MID_OVF>;
+
+// One warp replays tsl::hopscotch_map insertions of keys[0..n) (distinct,
+// bit 31 clear) into a map made with bucket_count buckets, as the seeding
+// tiers do, and writes the iteration order; out = {keys written, final
+// bucket count, 1 when a cap was exceeded}.  scratch holds the replayed
+// buckets, the stack and the overflow list (cap words each).  A test hook
+// for the device replay.
+__global__ void k_map_order_probe(const uint32_t* keys, uint32_t n, uint32_t bucket_count, uint32_t* scratch,
+                                  uint32_t cap, uint32_t* order, uint32_t* out)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    if (threadIdx.x >= 32) return;
+    SeedMem s{};
+    s.ins = (uint32_t*)keys;
+    s.slot = scratch;
+    s.stk = scratch + cap;
+    s.ovf = scratch + 2 * cap;
+    s.slot_cap = cap; s.stk_cap = cap; s.ovf_cap = cap;
+    MapSim m;
+    sim_init(m, bucket_count);
+    m.nb = 0; m.novf = 0; m.sp = 0;
+    bool fail = m.size > s.slot_cap;
+    if (!fail) {
+        for (uint32_t b = lane; b < m.size; b += 32) s.slot[b] = EMPTY_KEY;
+        __syncwarp();
+        for (uint32_t x = 0; x < n && !fail; ++x) {
+            if (m.sp >= s.stk_cap) { fail = true; break; }
+            if (lane == 0) s.stk[m.sp] = x;
+            m.sp++;
+            __syncwarp();
+            while (m.sp > 0)
+                if (!sim_step_w(m, s)) { fail = true; break; }
+        }
+    }
+    uint32_t no = 0;
+    if (!fail) {
+        for (uint32_t b0 = 0; b0 < m.size + m.novf; b0 += 32) {
+            const uint32_t b = b0 + lane;
+            uint32_t x = EMPTY_KEY;
+            if (b < m.size) x = s.slot[b];
+            else if (b < m.size + m.novf) x = s.ovf[b - m.size];
+            const unsigned bm = __ballot_sync(0xffffffffu, x != EMPTY_KEY);
+            if (x != EMPTY_KEY) order[no + __popc(bm & ((1u << lane) - 1))] = keys[x];
+            no += __popc(bm);
+        }
+    }
+    if (lane == 0) {
+        out[0] = no;
+        out[1] = m.B;
+        out[2] = fail ? 1u : 0u;
+    }
+}
 
 // Every valid task of the chunk straight to the middle tier's list (indexes
 // whose buckets are too large for the shared-memory caps of k_seed: there the
@@ -1223,14 +1226,17 @@ __global__ void k_seed_tier(DevIndex ix, ChunkBufs cb, HeavyScratch hs, uint32_t
     cand_res_finish(cb, res);
 }
 
-// tab2[k] = {tab[k], first entry of bucket k or 0}, k <= n (the bucket-offset
-// table with each bucket's first entry beside its start).
-__global__ void k_build_tab2(const uint32_t* tab, const uint32_t* entry, uint64_t n, uint2* tab2)
+// The bucket records of buckets 0 .. n - 1 from the offset table (n + 1
+// offsets) and the entries (DevIndex::rec).
+__global__ void k_build_rec(const uint32_t* tab, const uint32_t* entry, uint64_t n, uint4* rec)
 {
-    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k <= n; k += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t b0 = tab[k];
-        const uint32_t e = (k < n && tab[k + 1] > b0) ? entry[b0] : 0u;
-        tab2[k] = make_uint2(b0, e);
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b0 = tab[k], sz = tab[k + 1] - b0;
+        uint32_t e[REC_INLINE];
+#pragma unroll
+        for (uint32_t j = 0; j < REC_INLINE; ++j) e[j] = j < sz ? entry[b0 + j] : 0u;
+        rec[2 * k] = make_uint4(b0, sz, e[0], e[1]);
+        rec[2 * k + 1] = make_uint4(e[2], e[3], e[4], e[5]);
     }
 }
 

@@ -276,8 +276,9 @@ __device__ uint32_t pe_kmers(const DevIndex& ix, const PeIndex& px, const PeMem&
         const uint32_t p = lane + 32 * jj;
         if (p < nk) {
             const uint32_t key = sh_prefix_hash([&](uint32_t j) { return P[j]; }, p, HTAB_MASK);
-            b0[jj] = __ldg((const uint32_t*)(ix.tab2 + key));
-            b1[jj] = __ldg((const uint32_t*)(ix.tab2 + key + 1));
+            const uint2 t = __ldg((const uint2*)(ix.rec + 2ull * key));   // {start, size}
+            b0[jj] = t.x;
+            b1[jj] = t.x + t.y;
         }
     }
 #pragma unroll

@@ -139,7 +139,7 @@ void qslot_enqueue(fame_gpu* g, QSlot& s, uint32_t n, uint32_t flags, uint32_t* 
     if (g->seed_mid_first)
         k_seed_route<<<(ntask + 255) / 256, 256, 0, s.stream>>>(cb, ntask);
     else
-        k_seed<<<std::max(1u, blocks), 128, 4 * LightLayout::BYTES, s.stream>>>(g->ix, cb, ntask);
+        k_seed<<<std::max(1u, blocks), 128, 4 * LightR::BYTES, s.stream>>>(g->ix, cb, ntask);
     seed_tiers(g, cb, s.stream, s.ms, s.hs);
     const uint32_t grid = (uint32_t)g->sm_count * g->sa_blocks_per_sm;
     k_shiftand<1><<<grid, 32 * SA_WARPS, 0, s.stream>>>(g->ix, cb, FROM_DEVICE);

@@ -11,10 +11,13 @@
 //
 // One warp handles one (read, orientation) task:
 //   1. lanes hash k-mers (one k-mer per lane per step) and read tabIndex
-//   2. warp prefix sum of bucket sizes; entries gathered into an op list
-//   3. consecutive duplicates dropped; per (window, strand): count and first op
-//      (warp __match_any_sync groups + open addressing table)
-//   4. keys whose first op may insert (k-mer index <= maxQPos) listed in op order
+//   2. warp prefix sum of bucket sizes; entries gathered in op order
+//   3. as they arrive: consecutive duplicates dropped; per (window, strand):
+//      count and first op (warp __match_any_sync groups + open addressing
+//      table), the keys whose count reaches QTHRESH noted
+//   4. when neither strand map has two candidates (the common case) the
+//      candidates are staged at once; otherwise the keys whose first op may
+//      insert (k-mer index <= maxQPos) are listed in op order and
 //   5. lane 0 replays the hopscotch insertions of each map; lanes compact the
 //      windows with count >= QTHRESH in bucket order (forward map first)
 #pragma once
@@ -158,6 +161,126 @@ __device__ bool sim_step(MapSim& m, const SeedMem& s)
     return sim_rehash(m, s, next);
 }
 
+// The same replay run by a whole warp (every lane calls with the same state;
+// the state stays warp-uniform).  Scans of up to 62 buckets take one or two
+// warp steps instead of a loop per bucket; lane 0 writes the buckets and
+// the stack, and a __syncwarp orders every write before the next read.
+
+__device__ __forceinline__ uint32_t warp_min_u32(uint32_t v)
+{
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, d));
+    return v;
+}
+
+// rehash_impl: the bucket elements pushed in descending bucket order (so the
+// lowest bucket ends on top of the stack), the overflow list kept.
+__device__ bool sim_rehash_w(MapSim& m, const SeedMem& s, uint32_t count)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t need = (uint32_t)ceilf((float)m.nb / 0.9f);
+    if (need > count) count = need;
+    uint32_t sp = m.sp;
+    for (uint32_t top = m.size; top > 0; top = top > 32 ? top - 32 : 0) {
+        const int b = (int)top - 1 - (int)lane;   // lane 0 takes the highest bucket of this step
+        const uint32_t x = b >= 0 ? s.slot[b] : EMPTY_KEY;
+        const unsigned bm = __ballot_sync(0xffffffffu, x != EMPTY_KEY);
+        if (sp + __popc(bm) > s.stk_cap) return false;
+        if (x != EMPTY_KEY) s.stk[sp + __popc(bm & ((1u << lane) - 1))] = x;
+        sp += __popc(bm);
+    }
+    m.sp = sp;
+    m.nb = m.novf;
+    sim_init(m, count);
+    __syncwarp();
+    if (m.size > s.slot_cap) return false;
+    for (uint32_t b = lane; b < m.size; b += 32) s.slot[b] = EMPTY_KEY;
+    __syncwarp();
+    return true;
+}
+
+// insert_impl for the element on top of the stack.
+__device__ bool sim_step_w(MapSim& m, const SeedMem& s)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t x = s.stk[m.sp - 1];
+    const uint32_t k = sim_key(s, x);
+    const uint32_t next = (m.mask + 1) * 2;
+    if (m.nb - m.novf >= m.max_thr) return sim_rehash_w(m, s, next);
+    const uint32_t ib = k & m.mask;
+    // find_empty_bucket: the first empty bucket in [ib, ib + MAX_PROBES)
+    uint32_t ie = m.size;
+    {
+        const uint32_t lim = min(ib + MAX_PROBES, m.size);
+        for (uint32_t b0 = ib; b0 < lim; b0 += 32) {
+            const uint32_t b = b0 + lane;
+            const unsigned em = __ballot_sync(0xffffffffu, b < lim && s.slot[b] == EMPTY_KEY);
+            if (em) { ie = b0 + __ffs(em) - 1; break; }
+        }
+    }
+    if (ie < m.size) {
+        while (true) {
+            if (ie - ib < NBHD) {
+                if (lane == 0) s.slot[ie] = x;
+                m.nb++;
+                m.sp--;
+                __syncwarp();
+                return true;
+            }
+            // swap_empty_bucket_closer: of the elements at ts in [ie - NBHD + 1, ie)
+            // whose home bucket tc lies in [ie - NBHD + 1, ts], the one with the
+            // smallest tc, then the smallest ts, moves to ie
+            const uint32_t lo = ie - NBHD + 1;
+            uint32_t best = 0xffffffffu;
+            for (uint32_t t0 = lo; t0 < ie; t0 += 32) {
+                const uint32_t ts = t0 + lane;
+                if (ts < ie) {
+                    const uint32_t y = s.slot[ts];
+                    if (y != EMPTY_KEY) {
+                        const uint32_t tc = sim_key(s, y) & m.mask;
+                        if (tc >= lo && tc <= ts) best = min(best, ((tc - lo) << 8) | (ts - lo));
+                    }
+                }
+            }
+            best = warp_min_u32(best);
+            if (best == 0xffffffffu) break;
+            const uint32_t ts = lo + (best & 0xffu);
+            if (lane == 0) {
+                s.slot[ie] = s.slot[ts];
+                s.slot[ts] = EMPTY_KEY;
+            }
+            __syncwarp();
+            ie = ts;
+        }
+    }
+    // will_neighborhood_change_on_rehash
+    const uint32_t nmask = next - 1;
+    bool changes = false;
+    {
+        const uint32_t lim = min(m.size, ib + NBHD);
+        for (uint32_t b0 = ib; b0 < lim && !changes; b0 += 32) {
+            const uint32_t b = b0 + lane;
+            bool ch = false;
+            if (b < lim) {
+                const uint32_t y = s.slot[b];
+                const uint32_t ky = y == EMPTY_KEY ? 0 : sim_key(s, y);
+                ch = (ky & m.mask) != (ky & nmask);
+            }
+            changes = __any_sync(0xffffffffu, ch);
+        }
+    }
+    if (m.nb < m.min_thr || !changes) {
+        if (m.novf >= s.ovf_cap) return false;
+        if (lane == 0) s.ovf[m.novf] = x;
+        m.novf++;
+        m.nb++;
+        m.sp--;
+        __syncwarp();
+        return true;
+    }
+    return sim_rehash_w(m, s, next);
+}
+
 // A warp's reservation of candidate slots: tasks take contiguous runs from
 // it, so the candidate counter sees one atomic per CAND_RES_CHUNK slots
 // instead of one per task.  Slots a warp reserves and leaves unused are
@@ -182,6 +305,35 @@ __device__ __forceinline__ void cand_res_finish(const ChunkBufs& cb, CandRes& re
     cand_res_release(cb, res);
     if ((threadIdx.x & 31) == 0 && res.used) atomicAdd(cb.ctr + CTR_CAND_USED, (unsigned long long)res.used);
     res.used = 0;
+}
+
+// Publishes a task's candidates (stage[0 .. nstage), the first nf from the
+// forward map), contiguous, from the warp's slot reservation.
+__device__ __forceinline__ void seed_publish(const ChunkBufs& cb, CandRes& res, uint32_t task, const uint32_t* stage,
+                                             uint32_t nstage, uint32_t nf)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (nstage) {
+        if (nstage > res.left) {
+            cand_res_release(cb, res);
+            const uint32_t want = max(nstage, CAND_RES_CHUNK);
+            if (lane == 0) res.base = (uint32_t)atomicAdd(cb.ctr + CTR_CAND, (unsigned long long)want);
+            res.base = __shfl_sync(0xffffffffu, res.base, 0);
+            res.left = want;
+        }
+        base = res.base;
+        res.base += nstage;
+        res.left -= nstage;
+        res.used += nstage;
+    }
+    if ((uint64_t)base + nstage <= cb.cand_cap) {
+        for (uint32_t j = lane; j < nstage; j += 32) {
+            cb.cand[base + j] = stage[j];
+            cb.cand_task[base + j] = task;
+        }
+    }
+    if (lane == 0) cb.task_cand[task] = make_uint4(base, nf, nstage - nf, 0);
 }
 
 // Warp-cooperative seeding of one task.  Returns 0 on success, 1 when the task
@@ -236,10 +388,10 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
             const uint32_t p = lane + 32 * j;
             if (p < nk) {
                 const uint32_t key = s.kst[p];
-                const uint2 t = __ldg(ix.tab2 + key);
+                const uint4 t = __ldg(ix.rec + 2ull * key);
                 b0[j] = t.x;
-                e0[j] = t.y;
-                b1[j] = __ldg((const uint32_t*)(ix.tab2 + key + 1));
+                e0[j] = t.z;
+                b1[j] = t.x + t.y;
             }
         }
 #pragma unroll
@@ -292,109 +444,503 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
         const uint32_t b = s.kpre[p], n = s.kpre[p + 1] - b;
         for (uint32_t j = 0; j < n; ++j) s.opk[b + j] = (uint8_t)p;
     }
-    __syncwarp();
-    for (uint32_t base = 0; base < T; base += 256) {
-        uint32_t e[8];
-        bool ld[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const uint32_t i = base + lane + 32 * j;
-            ld[j] = false;
-            if (i < T) {
-                const uint32_t p = s.opk[i];
-                const uint32_t k = i - s.kpre[p];
-                if (k > 0) {
-                    e[j] = __ldg(ix.entry + s.kst[p] + k);
-                    ld[j] = true;
-                }
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const uint32_t i = base + lane + 32 * j;
-            if (ld[j]) s.ops[i] = e[j];
-        }
-    }
-    // 3. distinct keys with counts and first op (consecutive duplicates within a
-    //    bucket are skipped, ReadQueue.cpp:2380-2387, 2421-2428)
+    // the count table (the prefix hashes that may share its memory are dead)
     const uint32_t dsz = min(s.dt_cap, pow2_ceil(2 * T + 2));
     const uint32_t dmask = dsz - 1;
     const bool packed = s.dt_first == nullptr;
     const uint32_t cnt_shift = packed ? 16 : 0;
     for (uint32_t i = lane; i < dsz; i += 32) s.dt_key[i] = EMPTY_KEY;
+    // keys whose count reached QTHRESH, by count-table slot (in the memory of
+    // the inserted keys, which are listed later and only when needed)
+    uint32_t* reached = s.ins;
+    const uint32_t reached_cap = min(32u, s.ops_cap);
+    uint32_t nreached = 0;
     __syncwarp();
-    for (uint32_t b0 = 0; b0 < T; b0 += 32) {
-        const uint32_t i = b0 + lane;
-        bool valid = false;
-        uint32_t e = 0;
-        if (i < T) {
-            e = s.ops[i];
-            valid = !(i > s.kpre[s.opk[i]] && s.ops[i - 1] == e);
+    // 3. count the distinct keys as their entries arrive, with each key's
+    //    first op (consecutive duplicates within a bucket are skipped,
+    //    ReadQueue.cpp:2380-2387, 2421-2428): ops in order, 32 at a time;
+    //    an op's predecessor is the previous lane's entry (lane 0: lane 31's
+    //    of the step before)
+    uint32_t last = EMPTY_KEY;
+    for (uint32_t base = 0; base < T; base += 256) {
+        uint32_t e[8];
+        bool inner[8];   // not the first entry of its bucket
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint32_t i = base + lane + 32 * j;
+            e[j] = EMPTY_KEY;
+            inner[j] = false;
+            if (i < T) {
+                const uint32_t p = s.opk[i];
+                const uint32_t k = i - s.kpre[p];
+                inner[j] = k > 0;
+                e[j] = k > 0 ? __ldg(ix.entry + s.kst[p] + k) : s.ops[i];
+            }
         }
-        const unsigned vm = __ballot_sync(0xffffffffu, valid);
-        const unsigned grp = __match_any_sync(0xffffffffu, valid ? e : EMPTY_KEY) & vm;
-        if (valid && (__ffs(grp) - 1) == lane) {
-            uint32_t h = dt_hash(e, dmask);
-            while (true) {
-                const uint32_t cur = s.dt_key[h];
-                if (cur == e) break;
-                if (cur == EMPTY_KEY) {
-                    const uint32_t old = atomicCAS(&s.dt_key[h], EMPTY_KEY, e);
-                    if (old == EMPTY_KEY) {
-                        if (packed) s.dt_cnt[h] = i;
-                        else { s.dt_first[h] = i; s.dt_cnt[h] = 0; }
-                        break;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint32_t i = base + lane + 32 * j;
+            if (inner[j]) s.ops[i] = e[j];
+            uint32_t prev = __shfl_up_sync(0xffffffffu, e[j], 1);
+            if (lane == 0) prev = last;
+            last = __shfl_sync(0xffffffffu, e[j], 31);
+            const bool valid = i < T && !(inner[j] && prev == e[j]);
+            const unsigned vm = __ballot_sync(0xffffffffu, valid);
+            const unsigned grp = __match_any_sync(0xffffffffu, valid ? e[j] : EMPTY_KEY) & vm;
+            bool reach = false;
+            uint32_t h = 0;
+            if (valid && (__ffs(grp) - 1) == lane) {
+                const uint32_t key = e[j];
+                h = dt_hash(key, dmask);
+                while (true) {
+                    const uint32_t cur = s.dt_key[h];
+                    if (cur == key) break;
+                    if (cur == EMPTY_KEY) {
+                        const uint32_t old = atomicCAS(&s.dt_key[h], EMPTY_KEY, key);
+                        if (old == EMPTY_KEY) {
+                            if (packed) s.dt_cnt[h] = i;
+                            else { s.dt_first[h] = i; s.dt_cnt[h] = 0; }
+                            break;
+                        }
+                        if (old == key) break;
                     }
-                    if (old == e) break;
+                    h = (h + 1) & dmask;
                 }
-                h = (h + 1) & dmask;
+                const uint32_t before = s.dt_cnt[h] >> cnt_shift;
+                const uint32_t add = (uint32_t)__popc(grp);
+                s.dt_cnt[h] += add << cnt_shift;
+                reach = before < QTHRESH && before + add >= QTHRESH;
             }
-            s.dt_cnt[h] += (uint32_t)__popc(grp) << cnt_shift;
+            const unsigned rm = __ballot_sync(0xffffffffu, reach);
+            if (reach) {
+                const uint32_t at = nreached + __popc(rm & ((1u << lane) - 1));
+                if (at < reached_cap) reached[at] = h;
+            }
+            nreached += __popc(rm);
+            __syncwarp();   // this op's count-table writes before the next op's probes
         }
-        __syncwarp();
     }
-    // 4. inserted keys in first-touch order: the first op of a key inserts iff
-    //    its k-mer is the first one or cIdx < maxQPos (ReadQueue.cpp:2371, 2430)
     const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
-    uint32_t nins = 0;
-    for (uint32_t b0 = 0; b0 < T; b0 += 32) {
-        const uint32_t i = b0 + lane;
-        bool take = false;
-        uint32_t e = 0, c = 0;
-        if (i < T) {
-            e = s.ops[i];
-            const uint32_t k = s.opk[i];
-            if (!(i > s.kpre[k] && s.ops[i - 1] == e) && (k == 0 || k - 1 < maxQPos)) {
-                uint32_t h = dt_hash(e, dmask);
-                while (s.dt_key[h] != e) h = (h + 1) & dmask;
-                const uint32_t v = s.dt_cnt[h];
-                if ((packed ? (v & 0xffffu) : s.dt_first[h]) == i) { take = true; c = v >> cnt_shift; }
+    uint32_t nstage = 0, nf = 0;
+    // 4. the candidates (keys inserted into the map, ReadQueue.cpp:2371, 2430:
+    //    their first op's k-mer is the first one or cIdx < maxQPos; with a
+    //    count >= QTHRESH).  A strand map with at most one candidate needs no
+    //    insertion order: its walk sees that candidate alone, wherever the
+    //    other keys sit.  When both maps have at most one, they are staged
+    //    at once (forward map first, the order saQuerySeedSetRef walks).
+    //    Counts stay below 65536 here, so no uint16 wrap can hide a crossing.
+    bool ordered = false;
+    if (T < 65536 && nreached <= reached_cap) {
+        uint32_t key = 0;
+        bool cand = false;
+        if (lane < nreached) {
+            const uint32_t h = reached[lane];
+            const uint32_t first = packed ? (s.dt_cnt[h] & 0xffffu) : s.dt_first[h];
+            const uint32_t k = s.opk[first];
+            cand = k == 0 || k - 1 < maxQPos;
+            key = s.dt_key[h];
+        }
+        const unsigned fm = __ballot_sync(0xffffffffu, cand && (key >> 31));
+        const unsigned bm = __ballot_sync(0xffffffffu, cand && !(key >> 31));
+        if (__popc(fm) <= 1 && __popc(bm) <= 1) {
+            nf = __popc(fm);
+            nstage = nf + __popc(bm);
+            if (cand) s.stage[(key >> 31) ? 0 : nf] = key;
+            ordered = true;
+        }
+    }
+    __syncwarp();
+    if (!ordered) {
+        if (lane == 0) atomicAdd(cb.ctr + CTR_REPLAY, 1ull);
+        // 4b. inserted keys in first-touch order: the first op of a key
+        //     inserts iff its k-mer is the first one or cIdx < maxQPos
+        //     (ReadQueue.cpp:2371, 2430)
+        uint32_t nins = 0;
+        for (uint32_t b0 = 0; b0 < T; b0 += 32) {
+            const uint32_t i = b0 + lane;
+            bool take = false;
+            uint32_t e = 0, c = 0;
+            if (i < T) {
+                e = s.ops[i];
+                const uint32_t k = s.opk[i];
+                if (!(i > s.kpre[k] && s.ops[i - 1] == e) && (k == 0 || k - 1 < maxQPos)) {
+                    uint32_t h = dt_hash(e, dmask);
+                    while (s.dt_key[h] != e) h = (h + 1) & dmask;
+                    const uint32_t v = s.dt_cnt[h];
+                    if ((packed ? (v & 0xffffu) : s.dt_first[h]) == i) { take = true; c = v >> cnt_shift; }
+                }
+            }
+            const unsigned bm = __ballot_sync(0xffffffffu, take);
+            if (take) {
+                const uint32_t at = nins + __popc(bm & ((1u << lane) - 1));
+                s.ins[at] = e;
+                s.ins_cnt[at] = c;
+            }
+            nins += __popc(bm);
+            __syncwarp();
+        }
+        // 5. replay both maps (forward map first, the order saQuerySeedSetRef
+        //    walks) on lane 0; the ops/dt memory is dead from here and may
+        //    alias slot/stk/ovf
+        bool fail = false;
+        for (int dir = 1; dir >= 0; --dir) {
+            uint32_t ndc = 0, only = 0;
+            for (uint32_t b0 = 0; b0 < nins; b0 += 32) {
+                const uint32_t x = b0 + lane;
+                const uint32_t v = x < nins ? s.ins[x] : 0u;
+                const bool take = x < nins && (v >> 31) == (uint32_t)dir && (s.ins_cnt[x] & 0xffffu) >= QTHRESH;
+                const unsigned bm = __ballot_sync(0xffffffffu, take);
+                if (bm) {
+                    const uint32_t first = __shfl_sync(0xffffffffu, v, __ffs(bm) - 1);
+                    if (ndc == 0) only = first;
+                }
+                ndc += __popc(bm);
+            }
+            if (ndc <= 1) {
+                if (ndc == 1 && lane == 0) s.stage[nstage] = only;
+                nstage += ndc;
+                __syncwarp();
+                if (dir == 1) nf = nstage;
+                continue;
+            }
+            MapSim m;
+            sim_init(m, sigma / 5);
+            m.nb = 0; m.novf = 0; m.sp = 0;
+            if (m.size > s.slot_cap) { fail = true; }
+            if (!fail) {
+                for (uint32_t b = lane; b < m.size; b += 32) s.slot[b] = EMPTY_KEY;
+                __syncwarp();
+                // this map's keys in first-touch order, each inserted by the warp
+                for (uint32_t b0 = 0; b0 < nins && !fail; b0 += 32) {
+                    const uint32_t xl = b0 + lane;
+                    unsigned todo = __ballot_sync(0xffffffffu, xl < nins && (s.ins[xl] >> 31) == (uint32_t)dir);
+                    while (todo && !fail) {
+                        const uint32_t x = b0 + __ffs(todo) - 1;
+                        todo &= todo - 1;
+                        if (m.sp >= s.stk_cap) { fail = true; break; }
+                        if (lane == 0) s.stk[m.sp] = x;
+                        m.sp++;
+                        __syncwarp();
+                        while (m.sp > 0) {
+                            if (!sim_step_w(m, s)) { fail = true; break; }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+            if (fail) break;
+            // iteration order: buckets in array order, then the overflow list
+            for (uint32_t b0 = 0; b0 < m.size + m.novf; b0 += 32) {
+                const uint32_t b = b0 + lane;
+                uint32_t x = EMPTY_KEY;
+                if (b < m.size) x = s.slot[b];
+                else if (b < m.size + m.novf) x = s.ovf[b - m.size];
+                const bool take = x != EMPTY_KEY && (s.ins_cnt[x] & 0xffffu) >= QTHRESH;
+                const unsigned bm = __ballot_sync(0xffffffffu, take);
+                if (take) s.stage[nstage + __popc(bm & ((1u << lane) - 1))] = s.ins[x];
+                nstage += __popc(bm);
+            }
+            __syncwarp();
+            if (dir == 1) nf = nstage;
+        }
+        if (fail) return 1;
+    }
+    // 6. publish the candidates
+    seed_publish(cb, res, task, s.stage, nstage, nf);
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Seeding from the bucket records (the light and middle tiers): the same
+// results as seed_task with less memory traffic and working memory.  Each
+// lane owns k-mers; a k-mer's record (one aligned sector) gives its bucket's
+// bounds and first REC_INLINE entries, so for most buckets one DRAM line
+// serves the whole lookup; longer buckets stream the rest of their entries
+// from the entry table, each load issued REC_INLINE sub-steps before its use.
+// The count runs lane-major: sub-step j takes entry j of every lane's bucket
+// (ops are ordered by k-mer, then entry, so a key's first op is the smallest
+// (k-mer, entry) pair that reaches it: the lowest lane of a sub-step, kept
+// as a minimum across sub-steps).  Consecutive duplicates within a bucket
+// are the lane's own previous entry.  The insertion order the map replay
+// needs is rebuilt only when a strand map has two or more candidates: keys
+// ranked by their first op's dense index (k-mer prefix of bucket sizes plus
+// entry) through a bitmap.
+// ---------------------------------------------------------------------------
+struct SeedMemR {
+    uint8_t* seq;        // oriented read, 256 bytes
+    uint64_t* pre;       // prefix hashes (aliases the count table)
+    uint16_t* ksz;       // bucket size per k-mer
+    uint32_t* kpre;      // exclusive prefix of bucket sizes (nk + 1), for the replay order
+    uint32_t* dt_key;    // count table: distinct (window, strand) keys
+    uint32_t* dt_val;    //   first op (k-mer << 11 | entry) | count << 19
+    uint32_t* reached;   // 32 count-table slots whose count reached QTHRESH, then 2 staged candidates
+    uint32_t* bitmap;    // one bit per op (ops_cap bits, at most 1024)
+    uint32_t* ins;       // inserted keys in first-touch order (replay only)
+    uint16_t* ins_cnt;   //   and their counts
+    uint32_t* slot;      // replayed buckets, pending stack, overflow list and the
+    uint32_t* stk;       // staged candidates: over the dead per-k-mer arrays and
+    uint32_t* ovf;       // count table once the insertion order is listed
+    uint32_t* stage;
+    uint32_t ops_cap, dt_cap, slot_cap, stk_cap, ovf_cap;
+};
+
+constexpr uint32_t OPID_BITS = 19;             // op id: k-mer << 11 | entry (buckets hold <= KMERCUTOFF < 2048)
+constexpr uint32_t OPID_MASK = (1u << OPID_BITS) - 1;
+
+__device__ __noinline__ int seed_rec_replay(const ChunkBufs& cb, const SeedMemR& s, uint32_t task, uint32_t nk,
+                                            uint32_t T, uint32_t maxQPos, CandRes& res);
+
+__device__ int seed_task_rec(const DevIndex& ix, const ChunkBufs& cb, const SeedMemR& s, uint32_t task,
+                             unsigned long long* gather_bytes_acc, CandRes& res)
+{
+    constexpr uint32_t FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t r = task >> 1, o = task & 1;
+    const uint64_t off0 = cb.offs[r];
+    const uint32_t len = (uint32_t)(cb.offs[r + 1] - off0);
+    const char* raw = cb.seqs + off0;
+    for (uint32_t p = lane; p < len; p += 32) {
+        const uint8_t c = (uint8_t)raw[p];
+        if (o == 0) s.seq[p] = c;
+        else s.seq[len - 1 - p] = rc_byte(c);
+    }
+    __syncwarp();
+    // 1. hashes (getSeedRefs pass 1, ReadQueue.cpp:2331-2354) by the prefix
+    //    form of seedhash.h, then every lane's record loads before any use
+    const uint32_t nk = len - KMERLEN + 1;
+    uint64_t* P = s.pre;
+    {
+        uint64_t carry = 0;
+        for (uint32_t b = 0; b <= len; b += 32) {
+            const uint32_t j = b + lane;
+            const uint64_t u = j < len ? sh_u(s.seq[j], j) : 0ull;
+            uint64_t inc = u;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint64_t t = __shfl_up_sync(FULL, inc, d);
+                if (lane >= (uint32_t)d) inc ^= t;
+            }
+            if (j <= len) P[j] = carry ^ inc ^ u;
+            carry ^= __shfl_sync(FULL, inc, 31);
+        }
+    }
+    __syncwarp();
+    constexpr int KPL = (FAME_MAX_READ_LEN - KMERLEN + 1 + 31) / 32;   // k-mers per lane, at most
+    uint32_t key[KPL];
+    uint4 lo[KPL];     // {start, size, e0, e1}
+#pragma unroll
+    for (int jj = 0; jj < KPL; ++jj) {
+        const uint32_t p = lane + 32 * jj;
+        key[jj] = p < nk ? sh_prefix_hash([&](uint32_t j) { return P[j]; }, p, HTAB_MASK) : 0u;
+    }
+#pragma unroll
+    for (int jj = 0; jj < KPL; ++jj) {
+        const uint32_t p = lane + 32 * jj;
+        lo[jj] = p < nk ? __ldg(ix.rec + 2ull * key[jj]) : make_uint4(0, 0, 0, 0);
+    }
+    __syncwarp();   // the prefix hashes are dead: the count table may take their memory
+    const uint32_t dsz = s.dt_cap;
+    const uint32_t dmask = dsz - 1;
+    for (uint32_t i = lane; i < dsz; i += 32) s.dt_key[i] = EMPTY_KEY;
+    uint32_t T = 0;
+    unsigned long long gb = 0;
+#pragma unroll
+    for (int jj = 0; jj < KPL; ++jj) {
+        const uint32_t p = lane + 32 * jj;
+        if (p < nk) {
+            s.ksz[p] = (uint16_t)lo[jj].y;
+            T += lo[jj].y;
+            gb += 8 + 4ull * lo[jj].y;
+        }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        T += __shfl_xor_sync(FULL, T, d);
+        gb += __shfl_xor_sync(FULL, gb, d);
+    }
+    if (T > s.ops_cap) return 1;
+    if (lane == 0) atomicAdd(gather_bytes_acc, gb);
+    uint32_t nreached = 0;
+    __syncwarp();
+    // 2-3. count the distinct keys, sub-step j taking entry j of each lane's
+    //      bucket (consecutive duplicates within a bucket skipped,
+    //      ReadQueue.cpp:2380-2387, 2421-2428)
+#pragma unroll
+    for (int jj = 0; jj < KPL; ++jj) {
+        if (32u * jj >= nk) continue;   // warp-uniform; no break, so the loop unrolls and lo / key stay in registers
+        const uint32_t p = lane + 32 * jj;
+        const uint32_t sz = lo[jj].y, start = lo[jj].x;
+        uint32_t q0 = lo[jj].z, q1 = lo[jj].w, q2 = 0, q3 = 0, q4 = 0, q5 = 0;
+        if (sz > 2) {
+            const uint4 hi = __ldg(ix.rec + 2ull * key[jj] + 1);
+            q2 = hi.x; q3 = hi.y; q4 = hi.z; q5 = hi.w;
+        }
+        uint32_t jmax = sz;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) jmax = max(jmax, __shfl_xor_sync(FULL, jmax, d));
+        uint32_t prev = EMPTY_KEY;
+        for (uint32_t j = 0; j < jmax; ++j) {
+            const uint32_t e = q0;
+            q0 = q1; q1 = q2; q2 = q3; q3 = q4; q4 = q5;
+            q5 = j + REC_INLINE < sz ? __ldg(ix.entry + start + j + REC_INLINE) : 0u;
+            const bool valid = j < sz && !(j > 0 && prev == e);
+            prev = e;
+            const unsigned vm = __ballot_sync(FULL, valid);
+            const unsigned grp = __match_any_sync(FULL, valid ? e : EMPTY_KEY) & vm;
+            bool reach = false;
+            uint32_t h = 0;
+            if (valid && (uint32_t)(__ffs(grp) - 1) == lane) {
+                const uint32_t f = (p << 11) | j;
+                h = dt_hash(e, dmask);
+                bool fresh = false;
+                while (true) {
+                    const uint32_t cur = s.dt_key[h];
+                    if (cur == e) break;
+                    if (cur == EMPTY_KEY) {
+                        const uint32_t old = atomicCAS(&s.dt_key[h], EMPTY_KEY, e);
+                        if (old == EMPTY_KEY) { fresh = true; break; }
+                        if (old == e) break;
+                    }
+                    h = (h + 1) & dmask;
+                }
+                const uint32_t v = fresh ? f : s.dt_val[h];
+                const uint32_t before = fresh ? 0u : v >> OPID_BITS;
+                const uint32_t add = (uint32_t)__popc(grp);
+                s.dt_val[h] = min(v & OPID_MASK, f) | ((before + add) << OPID_BITS);
+                reach = before < QTHRESH && before + add >= QTHRESH;
+            }
+            const unsigned rm = __ballot_sync(FULL, reach);
+            if (reach) {
+                const uint32_t at = nreached + __popc(rm & ((1u << lane) - 1));
+                if (at < 32) s.reached[at] = h;
+            }
+            nreached += __popc(rm);
+            __syncwarp();   // this sub-step's count-table writes before the next one's probes
+        }
+    }
+    const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
+    // a key is a candidate when it was inserted (its first op's k-mer is the
+    // first one or cIdx < maxQPos, ReadQueue.cpp:2371, 2430) with a count
+    // >= QTHRESH (counts stay below 8192 here: no uint16 wrap)
+    auto inserted = [&](uint32_t v) {
+        const uint32_t kp = (v & OPID_MASK) >> 11;
+        return kp == 0 || kp - 1 < maxQPos;
+    };
+    // 4. both strand maps with at most one candidate: no insertion order needed
+    if (nreached <= 32) {
+        uint32_t k = 0;
+        bool cand = false;
+        if (lane < nreached) {
+            const uint32_t h = s.reached[lane];
+            cand = inserted(s.dt_val[h]);
+            k = s.dt_key[h];
+        }
+        const unsigned fm = __ballot_sync(FULL, cand && (k >> 31));
+        const unsigned bm = __ballot_sync(FULL, cand && !(k >> 31));
+        if (__popc(fm) <= 1 && __popc(bm) <= 1) {
+            uint32_t* stg = s.reached + 32;
+            const uint32_t nf = __popc(fm), nstage = nf + __popc(bm);
+            if (cand) stg[(k >> 31) ? 0 : nf] = k;
+            __syncwarp();
+            seed_publish(cb, res, task, stg, nstage, nf);
+            return 0;
+        }
+    }
+    return seed_rec_replay(cb, s, task, nk, T, maxQPos, res);
+}
+
+// The rest of seed_task_rec when a strand map has two or more candidates
+// (about one task in eight at genome scale): the insertion order and the
+// replay, kept out of line so that the common path's registers stay its own.
+__device__ __noinline__ int seed_rec_replay(const ChunkBufs& cb, const SeedMemR& s, uint32_t task, uint32_t nk,
+                                            uint32_t T, uint32_t maxQPos, CandRes& res)
+{
+    constexpr uint32_t FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t dsz = s.dt_cap;
+    auto inserted = [&](uint32_t v) {
+        const uint32_t kp = (v & OPID_MASK) >> 11;
+        return kp == 0 || kp - 1 < maxQPos;
+    };
+    if (lane == 0) atomicAdd(cb.ctr + CTR_REPLAY, 1ull);
+    // 4b. the inserted keys in first-touch order: each key's first op as a
+    //     dense index (prefix of bucket sizes over the k-mers, plus the entry)
+    //     marks one bit; a key's rank is the number of marks below its own
+    {
+        const uint32_t per = (nk + 31) / 32;
+        const uint32_t b = min(nk, lane * per), e = min(nk, b + per);
+        uint32_t loc = 0;
+        for (uint32_t p = b; p < e; ++p) loc += s.ksz[p];
+        uint32_t inc = loc;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(FULL, inc, d);
+            if (lane >= (uint32_t)d) inc += t;
+        }
+        uint32_t run = inc - loc;
+        for (uint32_t p = b; p < e; ++p) { s.kpre[p] = run; run += s.ksz[p]; }
+    }
+    const uint32_t nwords = (s.ops_cap + 31) / 32;   // <= 32
+    for (uint32_t w = lane; w < nwords; w += 32) s.bitmap[w] = 0;
+    __syncwarp();
+    auto dense = [&](uint32_t v) { return s.kpre[(v & OPID_MASK) >> 11] + (v & 0x7ffu); };
+    for (uint32_t b0 = 0; b0 < dsz; b0 += 32) {
+        const uint32_t h = b0 + lane;
+        if (s.dt_key[h] != EMPTY_KEY) {
+            const uint32_t v = s.dt_val[h];
+            if (inserted(v)) {
+                const uint32_t d = dense(v);
+                atomicOr(&s.bitmap[d >> 5], 1u << (d & 31));
             }
         }
-        const unsigned bm = __ballot_sync(0xffffffffu, take);
-        if (take) {
-            const uint32_t at = nins + __popc(bm & ((1u << lane) - 1));
-            s.ins[at] = e;
-            s.ins_cnt[at] = c;
-        }
-        nins += __popc(bm);
-        __syncwarp();
     }
+    __syncwarp();
+    const uint32_t word = lane < nwords ? s.bitmap[lane] : 0u;
+    uint32_t wbase = __popc(word);
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, wbase, d);
+        if (lane >= (uint32_t)d) wbase += t;
+    }
+    const uint32_t nins = __shfl_sync(FULL, wbase, 31);
+    wbase -= __popc(word);
+    for (uint32_t b0 = 0; b0 < dsz; b0 += 32) {
+        const uint32_t h = b0 + lane;
+        const uint32_t kk = s.dt_key[h];
+        bool take = false;
+        uint32_t d = 0, v = 0;
+        if (kk != EMPTY_KEY) {
+            v = s.dt_val[h];
+            take = inserted(v);
+            if (take) d = dense(v);
+        }
+        const uint32_t wb = __shfl_sync(FULL, wbase, take ? (d >> 5) : 0);
+        if (take) {
+            const uint32_t rank = wb + __popc(s.bitmap[d >> 5] & ((1u << (d & 31)) - 1));
+            s.ins[rank] = kk;
+            s.ins_cnt[rank] = (uint16_t)(v >> OPID_BITS);
+        }
+    }
+    __syncwarp();   // the count table and per-k-mer arrays are dead from here
     // 5. replay both maps (forward map first, the order saQuerySeedSetRef walks)
-    //    on lane 0; the ops/dt memory is dead from here and may alias slot/stk/ovf
+    SeedMem sm{};
+    sm.ins = s.ins;
+    sm.slot = s.slot;
+    sm.stk = s.stk;
+    sm.ovf = s.ovf;
+    sm.slot_cap = s.slot_cap;
+    sm.stk_cap = s.stk_cap;
+    sm.ovf_cap = s.ovf_cap;
     uint32_t nstage = 0, nf = 0;
-    bool fail = false;
     for (int dir = 1; dir >= 0; --dir) {
-        // A map with at most one candidate (count >= QTHRESH) needs no replay:
-        // its walk sees that candidate alone, wherever the other keys sit.
         uint32_t ndc = 0, only = 0;
         for (uint32_t b0 = 0; b0 < nins; b0 += 32) {
             const uint32_t x = b0 + lane;
             const uint32_t v = x < nins ? s.ins[x] : 0u;
-            const bool take = x < nins && (v >> 31) == (uint32_t)dir && (s.ins_cnt[x] & 0xffffu) >= QTHRESH;
-            const unsigned bm = __ballot_sync(0xffffffffu, take);
+            const bool take = x < nins && (v >> 31) == (uint32_t)dir && s.ins_cnt[x] >= QTHRESH;
+            const unsigned bm = __ballot_sync(FULL, take);
             if (bm) {
-                const uint32_t first = __shfl_sync(0xffffffffu, v, __ffs(bm) - 1);
+                const uint32_t first = __shfl_sync(FULL, v, __ffs(bm) - 1);
                 if (ndc == 0) only = first;
             }
             ndc += __popc(bm);
@@ -407,65 +953,41 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
             continue;
         }
         MapSim m;
-        sim_init(m, sigma / 5);
+        sim_init(m, T / 5);   // bucket_count = summed bucket sizes / 5 (sigma, getSeedRefs)
         m.nb = 0; m.novf = 0; m.sp = 0;
-        if (m.size > s.slot_cap) { fail = true; }
-        if (!__any_sync(0xffffffffu, fail)) {
-            for (uint32_t b = lane; b < m.size; b += 32) s.slot[b] = EMPTY_KEY;
-            __syncwarp();
-            if (lane == 0) {
-                for (uint32_t x = 0; x < nins && !fail; ++x) {
-                    if ((s.ins[x] >> 31) != (uint32_t)dir) continue;
-                    if (m.sp >= s.stk_cap) { fail = true; break; }
-                    s.stk[m.sp++] = x;
-                    while (m.sp > 0) {
-                        if (!sim_step(m, s)) { fail = true; break; }
-                    }
-                }
+        if (m.size > sm.slot_cap) return 1;
+        for (uint32_t b = lane; b < m.size; b += 32) sm.slot[b] = EMPTY_KEY;
+        __syncwarp();
+        for (uint32_t b0 = 0; b0 < nins; b0 += 32) {
+            const uint32_t xl = b0 + lane;
+            unsigned todo = __ballot_sync(FULL, xl < nins && (s.ins[xl] >> 31) == (uint32_t)dir);
+            while (todo) {
+                const uint32_t x = b0 + __ffs(todo) - 1;
+                todo &= todo - 1;
+                if (m.sp >= sm.stk_cap) return 1;
+                if (lane == 0) sm.stk[m.sp] = x;
+                m.sp++;
+                __syncwarp();
+                while (m.sp > 0)
+                    if (!sim_step_w(m, sm)) return 1;
             }
-            fail = __shfl_sync(0xffffffffu, fail, 0);
-            m.size = __shfl_sync(0xffffffffu, m.size, 0);
-            m.novf = __shfl_sync(0xffffffffu, m.novf, 0);
-            __syncwarp();
         }
-        if (fail) break;
+        __syncwarp();
         // iteration order: buckets in array order, then the overflow list
         for (uint32_t b0 = 0; b0 < m.size + m.novf; b0 += 32) {
             const uint32_t b = b0 + lane;
             uint32_t x = EMPTY_KEY;
-            if (b < m.size) x = s.slot[b];
-            else if (b < m.size + m.novf) x = s.ovf[b - m.size];
-            const bool take = x != EMPTY_KEY && (s.ins_cnt[x] & 0xffffu) >= QTHRESH;
-            const unsigned bm = __ballot_sync(0xffffffffu, take);
+            if (b < m.size) x = sm.slot[b];
+            else if (b < m.size + m.novf) x = sm.ovf[b - m.size];
+            const bool take = x != EMPTY_KEY && s.ins_cnt[x] >= QTHRESH;
+            const unsigned bm = __ballot_sync(FULL, take);
             if (take) s.stage[nstage + __popc(bm & ((1u << lane) - 1))] = s.ins[x];
             nstage += __popc(bm);
         }
         __syncwarp();
         if (dir == 1) nf = nstage;
     }
-    if (fail) return 1;
-    // 6. publish the candidates, contiguous, from the warp's reservation
-    uint32_t base = 0;
-    if (nstage) {
-        if (nstage > res.left) {
-            cand_res_release(cb, res);
-            const uint32_t want = max(nstage, CAND_RES_CHUNK);
-            if (lane == 0) res.base = (uint32_t)atomicAdd(cb.ctr + CTR_CAND, (unsigned long long)want);
-            res.base = __shfl_sync(0xffffffffu, res.base, 0);
-            res.left = want;
-        }
-        base = res.base;
-        res.base += nstage;
-        res.left -= nstage;
-        res.used += nstage;
-    }
-    if ((uint64_t)base + nstage <= cb.cand_cap) {
-        for (uint32_t j = lane; j < nstage; j += 32) {
-            cb.cand[base + j] = s.stage[j];
-            cb.cand_task[base + j] = task;
-        }
-    }
-    if (lane == 0) cb.task_cand[task] = make_uint4(base, nf, nstage - nf, 0);
+    seed_publish(cb, res, task, s.stage, nstage, nf);
     return 0;
 }
 

@@ -306,9 +306,19 @@ int fame_gpu_stage_times(fame_gpu* g, float* ms, int n);
 /* Seeding tasks that entered each tier after the light one in the last
  * single-end chunk: out[0] the smaller shared-memory middle tier (up to 511
  * gathered bucket entries), out[1] the larger one (up to 1023), out[2] the
- * global-memory tier, out[3] the large-capacity tier.  No counterpart in the
+ * global-memory tier, out[3] the large-capacity tier; out[4] the tasks (of
+ * any tier) whose candidate order needed the replay of the map's insertions
+ * (a strand map with two or more candidates).  No counterpart in the
  * reference (diagnostics). */
 int fame_gpu_seed_tier_counts(const fame_gpu* g, uint64_t* out);
+/* Test hook (no counterpart in the reference): replays, on the device, the
+ * insertion of keys[0..n) (distinct, bit 31 clear, n <= 65536) into a
+ * tsl::hopscotch_map made with bucket_count buckets -- the replay the seeding
+ * kernels use to order a read's candidate windows -- and writes the map's
+ * iteration order to order[] and its final bucket count.  Returns the number
+ * of keys written, or an error code.  Allocates device memory. */
+int fame_gpu_map_order_probe(fame_gpu* g, const uint32_t* keys, uint32_t n, uint32_t bucket_count, uint32_t* order,
+                             uint64_t* final_buckets);
 /* Number of kernel launches of the last match call. */
 int fame_gpu_last_launches(const fame_gpu* g);
 /* Device bytes held by the resident index tables of the context. */

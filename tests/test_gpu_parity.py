@@ -337,3 +337,18 @@ def test_single_cell_batches(golden, product_index, gpu, oracle_index, tmp_path)
         ref = oracle_index.match_se(b"".join(rr), o, chunk=1000, both_strands=False)["meth"]
         for col in range(4):
             assert np.array_equal(rows[(cid, col)], ref[:, col].astype(np.int64)), (cid, col)
+
+
+def test_device_map_orders_match_reference(gpu, kernels_golden):
+    """The warp replay of tsl::hopscotch_map that orders a read's candidate
+    windows, run on the device over the 400 adversarial key sequences whose
+    iteration orders and final bucket counts the compiled reference's own map
+    produced (tests/golden/make_golden.py): clustered keys, displacement
+    chains, overflow lists and rehashes."""
+    for c in kernels_golden["hopscotch"]:
+        keys = np.asarray(c["keys"], np.uint32)
+        _, first = np.unique(keys, return_index=True)
+        distinct = keys[np.sort(first)]          # the map ignores repeated inserts
+        order, fb = gpu.map_order_probe(distinct, int(c["bucket_count"]))
+        assert np.array_equal(order, c["order"]), (len(keys), int(c["bucket_count"]))
+        assert fb == int(c["final_buckets"])
