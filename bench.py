@@ -416,6 +416,14 @@ def run_gb300(args):
     barrier(world)
     t_max = allreduce_max(ev0.elapsed_time(ev1) / 1e3, world)
     total_reads = reads * world
+    # ---- host-to-device copy rate of one chunk's page-locked bases (synchronous copies, host clock)
+    hs0, _, _ = pinned[steady[0]]
+    d_s0 = dev[steady[0]][0]
+    gm.memcpy(d_s0, hs0.ctypes.data, hs0.nbytes, 1)
+    tc0 = time.perf_counter()
+    for _ in range(3):
+        gm.memcpy(d_s0, hs0.ctypes.data, hs0.nbytes, 1)
+    h2d_gbps = 3 * hs0.nbytes / (time.perf_counter() - tc0) / 1e9
     # ---- timed: end to end from page-locked host memory
     e_reads = h2d = d2h = 0
     for w in range(args.warmup):   # untimed: the host-buffer path's first calls (its device staging grows)
@@ -526,7 +534,7 @@ def run_gb300(args):
                    "l2": "inputs larger than L2: every step gathers from the device index (%.1f GB) and new reads"
                          % (gm.index_bytes() / 1e9)},
         "e2e": {"value": e_reads * world / t_e2e, "unit": "reads/s", "h2d_bytes_per_step": int(h2d / args.steps),
-                "d2h_bytes_per_step": int(d2h / args.steps)},
+                "d2h_bytes_per_step": int(d2h / args.steps), "h2d_copy_gbps": h2d_gbps},
         "gpu_launches": launches,
         "batched": batched,
         "fastq_file": fastq,
@@ -610,17 +618,34 @@ def run_gb300_serving(args):
                     js["lo"], js["hi"]).astype(np.int64)
     arrivals = np.cumsum(rng.exponential(1.0 / js["rate"], js["n_jobs"]))
     t0 = time.time()
-    g = synth.make_genome(**spec["genome"])
-    rs = synth.make_reads(g, int(sizes.sum()), seed=js["seed"] + 1, sub_rate=js["sub_rate"],
-                          indel_rate=js["indel_rate"])
+    jobs = []
+    cell_p = None
+    if spec.get("large"):
+        # genome-scale genome; every cell its own methylation probability (Beta) and its own reads
+        g = synth.genome_of(args.workload)
+        cell_p = rng.beta(*js["cell_beta"], size=js["n_jobs"])
+        for i, n in enumerate(sizes):
+            rs = synth.make_reads_large(g, int(n), seed=js["seed"] + 1 + i, read_len=100, sub_rate=js["sub_rate"],
+                                        indel_rate=js["indel_rate"], cell_p=float(cell_p[i]), cell_key=i)
+            s_, o_ = rs.concat()
+            jobs.append(Job("cell%d" % i, s_, o_, arrival=float(arrivals[i])))
+    else:
+        g = synth.make_genome(**spec["genome"])
+        rs = synth.make_reads(g, int(sizes.sum()), seed=js["seed"] + 1, sub_rate=js["sub_rate"],
+                              indel_rate=js["indel_rate"])
+        seq, offs = rs.concat()
+        a = 0
+        for i, n in enumerate(sizes):
+            o = offs[a:a + n + 1]
+            jobs.append(Job("cell%d" % i, seq[int(o[0]):int(o[-1])], o - o[0], arrival=float(arrivals[i])))
+            a += int(n)
     t_gen = time.time() - t0
-    seq, offs = rs.concat()
-    jobs, a = [], 0
-    for i, n in enumerate(sizes):
-        o = offs[a:a + n + 1]
-        jobs.append(Job("cell%d" % i, seq[int(o[0]):int(o[-1])], o - o[0], arrival=float(arrivals[i])))
-        a += int(n)
+    t0 = time.time()
     hi = HostIndex.build(g.seqs, readlen=100, threads=0)
+    t_build = time.time() - t0
+    genome_bp = int(g.total_len)
+    del g
+    gc.collect()
     gm = GpuMatcher(hi, 0)
     loop = ServingLoop(gm, slots=4, max_active=16)
     loop.run(jobs[:2], realtime=False)                       # warm-up (graphs, buffers)
@@ -642,14 +667,17 @@ def run_gb300_serving(args):
         "metric": SERVING_METRIC, "value": total / t_serv, "unit": "reads/s", "n_gpus": 1, "steps": 1,
         "warmup": 1, "ms_per_step": 1e3 * t_serv, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8/u64 integer", "data": "synthetic (seeded jobs and arrival trace)",
-        "config": {"workload": args.workload, "jobs": len(jobs), "reads_total": total,
+        "config": {"workload": args.workload, "genome_bp": genome_bp, "jobs": len(jobs), "reads_total": total,
                    "arrival_rate_per_s": js["rate"], "reads_per_job_median": js["median"],
-                   "reads_per_job_range": [int(sizes.min()), int(sizes.max())], "slots": 4},
+                   "reads_per_job_range": [int(sizes.min()), int(sizes.max())], "slots": 4,
+                   "cell_methylation_p": (None if cell_p is None else
+                                          {"beta": list(js["cell_beta"]),
+                                           "range": [float(cell_p.min()), float(cell_p.max())]})},
         "latency": {"serving": latency_summary(served), "plain_per_job": latency_summary(plain)},
         "plain_per_job_reads_per_s": total / t_plain,
         "results_identical_to_plain": bool(same),
         "timing": "host clock over the whole trace (arrival-driven); per-job latency = completion - arrival",
-        "clocks": clk.summary(), "setup_seconds": {"generate": t_gen},
+        "clocks": clk.summary(), "setup_seconds": {"generate": t_gen, "index_build": t_build},
     }
     emit(out)
 

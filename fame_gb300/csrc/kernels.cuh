@@ -955,59 +955,6 @@ __global__ void k_prep(ChunkBufs cb, uint32_t readlen)
     if ((threadIdx.x & 31) == 0 && wbit) atomicOr(cb.ctr + CTR_WMASK, (unsigned long long)wbit);
 }
 
-// Shared-memory working set of one warp for seed_task_rec: up to OPS
-// gathered bucket entries, a DT-slot count table (a power of two > 2 * OPS).
-// The per-k-mer arrays, the count table (prefix hashes first) and, once the
-// insertion order is listed, the replay's buckets, stack, overflow list and
-// staged candidates share one region.
-template <uint32_t OPS, uint32_t DT, uint32_t OVF_N>
-struct SeedLayoutR {
-    static_assert(DT >= 2 * OPS && (DT & (DT - 1)) == 0 && OPS <= 1024, "count table too small");
-    static constexpr uint32_t R16(uint32_t b) { return (b + 15) / 16 * 16; }
-    static constexpr uint32_t SLOT_N = DT + 64;    // replayed buckets: pow2_ceil(OPS + 1) + 61 at most
-    static constexpr uint32_t SEQ = 0;             // 256 B
-    static constexpr uint32_t KSZ = SEQ + 256;     // 224 x u16
-    static constexpr uint32_t KPRE = KSZ + 448;    // 225 x u32
-    static constexpr uint32_t DTK = KPRE + 912;
-    static constexpr uint32_t DTV = DTK + DT * 4;
-    static constexpr uint32_t END_U = DTV + DT * 4;
-    static constexpr uint32_t REACHED = END_U;     // 34 x u32
-    static constexpr uint32_t BITMAP = REACHED + 144;
-    static constexpr uint32_t INS = BITMAP + R16((OPS + 31) / 32 * 4);
-    static constexpr uint32_t INSC = INS + R16(OPS * 4);
-    static constexpr uint32_t BYTES = INSC + R16(OPS * 2);
-    // the replay, over [0, END_U)
-    static constexpr uint32_t SLOT = 0;
-    static constexpr uint32_t STK = SLOT + R16(SLOT_N * 4);
-    static constexpr uint32_t OVF = STK + R16(OPS * 4);
-    static constexpr uint32_t STAGE = OVF + R16(OVF_N * 4);
-    static constexpr uint32_t END_B = STAGE + R16(OPS * 4);
-    static_assert(END_B <= END_U, "the replay does not fit the shared region");
-    static_assert(DTK % 8 == 0 && END_U - DTK >= 8 * (FAME_MAX_READ_LEN + 1), "prefix hashes do not fit");
-};
-
-template <class L, uint32_t OPS, uint32_t DT, uint32_t OVF_N>
-__device__ __forceinline__ SeedMemR seed_mem_r(uint8_t* base)
-{
-    SeedMemR s;
-    s.seq = base + L::SEQ;
-    s.ksz = (uint16_t*)(base + L::KSZ);
-    s.kpre = (uint32_t*)(base + L::KPRE);
-    s.pre = (uint64_t*)(base + L::DTK);
-    s.dt_key = (uint32_t*)(base + L::DTK);
-    s.dt_val = (uint32_t*)(base + L::DTV);
-    s.reached = (uint32_t*)(base + L::REACHED);
-    s.bitmap = (uint32_t*)(base + L::BITMAP);
-    s.ins = (uint32_t*)(base + L::INS);
-    s.ins_cnt = (uint16_t*)(base + L::INSC);
-    s.slot = (uint32_t*)(base + L::SLOT);
-    s.stk = (uint32_t*)(base + L::STK);
-    s.ovf = (uint32_t*)(base + L::OVF);
-    s.stage = (uint32_t*)(base + L::STAGE);
-    s.ops_cap = OPS; s.dt_cap = DT; s.slot_cap = L::SLOT_N; s.stk_cap = OPS; s.ovf_cap = OVF_N;
-    return s;
-}
-
 // Light tier: up to 128 gathered entries (the common read of an index with
 // fewer entries than buckets), many warps per SM.
 constexpr uint32_t L_OPS = 128, L_DT = 256, L_OVF = 32;
@@ -1018,7 +965,7 @@ __global__ void __launch_bounds__(128) k_seed(DevIndex ix, ChunkBufs cb, uint32_
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const uint32_t wib = threadIdx.x >> 5;
-    const SeedMemR s = seed_mem_r<LightR, L_OPS, L_DT, L_OVF>(smem + wib * LightR::BYTES);
+    uint8_t* const base = smem + wib * LightR::BYTES;
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     const int norient = __popc(cb.orient_mask);
     const uint32_t first_o = (cb.orient_mask & 1u) ? 0 : 1;
@@ -1028,7 +975,7 @@ __global__ void __launch_bounds__(128) k_seed(DevIndex ix, ChunkBufs cb, uint32_
         const uint32_t o = norient == 2 ? (t & 1) : first_o;
         if (cb.rflags[r]) continue;
         const uint32_t task = 2 * r + o;
-        const int heavy = seed_task_rec(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES, res);
+        const int heavy = seed_task_rec<LightR, L_OPS, L_DT, L_OVF>(ix, cb, base, task, cb.ctr + CTR_GATHER_BYTES, res);
         if (heavy && (threadIdx.x & 31) == 0) {
             const uint32_t h = (uint32_t)atomicAdd(cb.ctr + CTR_HEAVY, 1ull);
             cb.heavy[h] = task;
@@ -1056,7 +1003,7 @@ __global__ void __launch_bounds__(32 * WPB) k_seed_mid(DevIndex ix, ChunkBufs cb
     extern __shared__ __align__(16) uint8_t smem[];
     using L = SeedLayoutR<OPS, DT, MID_OVF>;
     const uint32_t wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const SeedMemR s = seed_mem_r<L, OPS, DT, MID_OVF>(smem + wib * L::BYTES);
+    uint8_t* const base = smem + wib * L::BYTES;
     const uint32_t ntask = (uint32_t)cb.ctr[ctr_in];
     CandRes res;
     while (true) {
@@ -1065,7 +1012,7 @@ __global__ void __launch_bounds__(32 * WPB) k_seed_mid(DevIndex ix, ChunkBufs cb
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= ntask) break;
         const uint32_t task = list[i];
-        const int over = seed_task_rec(ix, cb, s, task, cb.ctr + CTR_GATHER_BYTES, res);
+        const int over = seed_task_rec<L, OPS, DT, MID_OVF>(ix, cb, base, task, cb.ctr + CTR_GATHER_BYTES, res);
         if (over && lane == 0) spill[(uint32_t)atomicAdd(cb.ctr + ctr_spill, 1ull)] = task;
         __syncwarp();
     }
@@ -1102,13 +1049,9 @@ __global__ void k_map_order_probe(const uint32_t* keys, uint32_t n, uint32_t buc
     if (!fail) {
         for (uint32_t b = lane; b < m.size; b += 32) s.slot[b] = EMPTY_KEY;
         __syncwarp();
-        for (uint32_t x = 0; x < n && !fail; ++x) {
-            if (m.sp >= s.stk_cap) { fail = true; break; }
-            if (lane == 0) s.stk[m.sp] = x;
-            m.sp++;
-            __syncwarp();
-            while (m.sp > 0)
-                if (!sim_step_w(m, s)) { fail = true; break; }
+        for (uint32_t b0 = 0; b0 < n && !fail; b0 += 32) {
+            const unsigned todo = __ballot_sync(0xffffffffu, b0 + lane < n);
+            fail = !sim_insert_batch_w(m, s, b0, todo);
         }
     }
     uint32_t no = 0;

@@ -377,6 +377,47 @@ __device__ bool pe_replay(const PeMem& s, const uint32_t* seq, uint32_t n, uint3
     return true;
 }
 
+// The same replay run by the whole warp (every lane calls; nout and the
+// return value are warp-uniform): insertions batched as in the single-end
+// seeding (sim_insert_batch_w), the iteration order taken with ballots.
+__device__ bool pe_replay_w(const PeMem& s, const uint32_t* seq, uint32_t n, uint32_t bucket_count, uint32_t* out,
+                            uint32_t& nout)
+{
+    constexpr uint32_t FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31;
+    SeedMem sm{};
+    sm.ins = (uint32_t*)seq;
+    sm.slot = s.slot;
+    sm.stk = s.stk;
+    sm.ovf = s.ovf;
+    sm.slot_cap = s.c.slot_cap;
+    sm.stk_cap = 2 * s.c.icap;
+    sm.ovf_cap = s.c.ovf_cap;
+    MapSim m;
+    sim_init(m, bucket_count);
+    m.nb = 0; m.novf = 0; m.sp = 0;
+    if (m.size > s.c.slot_cap) return false;
+    for (uint32_t b = lane; b < m.size; b += 32) s.slot[b] = EMPTY_KEY;
+    __syncwarp();
+    for (uint32_t b0 = 0; b0 < n; b0 += 32) {
+        const unsigned todo = __ballot_sync(FULL, b0 + lane < n);
+        if (!sim_insert_batch_w(m, sm, b0, todo)) return false;
+    }
+    uint32_t no = 0;
+    for (uint32_t b0 = 0; b0 < m.size + m.novf; b0 += 32) {
+        const uint32_t b = b0 + lane;
+        uint32_t x = EMPTY_KEY;
+        if (b < m.size) x = s.slot[b];
+        else if (b < m.size + m.novf) x = s.ovf[b - m.size];
+        const unsigned bm = __ballot_sync(FULL, x != EMPTY_KEY);
+        if (x != EMPTY_KEY) out[no + __popc(bm & ((1u << lane) - 1))] = seq[x];
+        no += __popc(bm);
+    }
+    __syncwarp();
+    nout = no;
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // std::sort of libstdc++ (introsort with median-of-three pivot, heap sort past
 // the depth limit, final insertion sort with a 16-element threshold) with
@@ -1198,24 +1239,38 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
         __syncwarp();
         return 1;
     }
-    if (lane == 0) {
-        // a strand map with two or more keys to scan: replay its insertions
-        for (int dir = 0; dir < 2 && !st.over; ++dir) {
-            uint32_t nt = 0;
-            if (!pe_replay(s, s.ins1[dir], st.n1[dir], sigma / 5, s.ord[dir], nt)) { st.over = true; break; }
-            uint32_t ns = 0;
-            for (uint32_t q = 0; q < nt; ++q) {
-                const uint32_t key = s.ord[dir][q];
+    // a strand map with two or more keys to scan: replay its insertions (the warp)
+    bool over = false;
+    for (int dir = 0; dir < 2 && !over; ++dir) {
+        uint32_t nt = 0;
+        if (!pe_replay_w(s, s.ins1[dir], n1d[dir], sigma / 5, s.ord[dir], nt)) { over = true; break; }
+        // kept keys are present with count1 >= QTHRESH; keys the second mate re-inserted
+        // after the rebuild dropped them come later, from ins2
+        uint32_t ns = 0;
+        for (uint32_t b0 = 0; b0 < nt; b0 += 32) {
+            const uint32_t q = b0 + lane;
+            bool keep = false;
+            uint32_t key = 0;
+            if (q < nt) {
+                key = s.ord[dir][q];
                 const int h = pm_find(s, dir, key);
-                // kept keys are present with count1 >= QTHRESH; keys the second mate re-inserted
-                // after the rebuild dropped them come later, from ins2
-                if (h >= 0 && pv_c1(s.vv[dir][h]) >= QTHRESH) s.seq[ns++] = key;
+                keep = h >= 0 && pv_c1(s.vv[dir][h]) >= QTHRESH;
             }
-            for (uint32_t x = 0; x < st.n2[dir]; ++x) s.seq[ns++] = s.ins2[dir][x];
-            if (!pe_replay(s, s.seq, ns, 20, s.ord[dir], st.nord[dir])) { st.over = true; break; }
+            const unsigned bm = __ballot_sync(FULL, keep);
+            if (keep) s.seq[ns + __popc(bm & ((1u << lane) - 1))] = key;
+            ns += __popc(bm);
         }
+        for (uint32_t x = lane; x < n2d[dir]; x += 32) s.seq[ns + x] = s.ins2[dir][x];
+        ns += n2d[dir];
+        __syncwarp();
+        uint32_t no = 0;
+        if (!pe_replay_w(s, s.seq, ns, 20, s.ord[dir], no)) { over = true; break; }
+        if (lane == 0) st.nord[dir] = no;
     }
-    if (__shfl_sync(0xffffffffu, st.over, 0)) return -1;
+    if (over) {
+        if (lane == 0) st.over = true;
+        return -1;
+    }
     __syncwarp();
     return 1;
 }

@@ -281,6 +281,54 @@ __device__ bool sim_step_w(MapSim& m, const SeedMem& s)
     return sim_rehash_w(m, s, next);
 }
 
+// Inserts, in lane order, the keys ins[xb + lane] of the lanes in `todo`
+// (the stack empty on entry and on return).  Each step tries every pending
+// key at once: a key whose first empty bucket from its home lies in its
+// neighbourhood, that no earlier pending key wants too, and that keeps the
+// load under the rehash threshold is placed exactly where one insert_impl
+// after another would place it; the pending keys before the first one that
+// fails these tests go in together, and that one runs the full
+// insert_impl (displacements, overflow list, rehash) on its own.  False when
+// a cap is exceeded.
+__device__ bool sim_insert_batch_w(MapSim& m, const SeedMem& s, uint32_t xb, unsigned todo)
+{
+    constexpr uint32_t FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31;
+    while (todo) {
+        const bool act = (todo >> lane) & 1u;
+        const uint32_t rank = __popc(todo & ((1u << lane) - 1));
+        uint32_t ie = m.size;
+        bool ok = false;
+        if (act && m.size > 0) {
+            const uint32_t ib = sim_key(s, xb + lane) & m.mask;
+            const uint32_t lim = min(ib + MAX_PROBES, m.size);
+            for (uint32_t b = ib; b < lim; ++b)
+                if (s.slot[b] == EMPTY_KEY) { ie = b; break; }
+            ok = ie < m.size && ie - ib < NBHD && m.nb + rank - m.novf < m.max_thr;
+        }
+        // the first pending key that wants a bucket an earlier one wants too fails
+        const unsigned grp = __match_any_sync(FULL, act ? ie : 0xfffffff0u - lane) & todo;
+        if (act && (__ffs(grp) - 1) != (int)lane) ok = false;
+        const unsigned bad = __ballot_sync(FULL, act && !ok);
+        const unsigned good = bad ? (todo & ((1u << (__ffs(bad) - 1)) - 1)) : todo;
+        if ((good >> lane) & 1u) s.slot[ie] = xb + lane;
+        m.nb += __popc(good);
+        todo &= ~good;
+        __syncwarp();
+        if (bad) {
+            const uint32_t k = __ffs(bad) - 1;
+            todo &= ~(1u << k);
+            if (m.sp >= s.stk_cap) return false;
+            if (lane == 0) s.stk[m.sp] = xb + k;
+            m.sp++;
+            __syncwarp();
+            while (m.sp > 0)
+                if (!sim_step_w(m, s)) return false;
+        }
+    }
+    return true;
+}
+
 // A warp's reservation of candidate slots: tasks take contiguous runs from
 // it, so the candidate counter sees one atomic per CAND_RES_CHUNK slots
 // instead of one per task.  Slots a warp reserves and leaves unused are
@@ -652,29 +700,35 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
 
 // ---------------------------------------------------------------------------
 // Seeding from the bucket records (the light and middle tiers): the same
-// results as seed_task with less memory traffic and working memory.  Each
-// lane owns k-mers; a k-mer's record (one aligned sector) gives its bucket's
-// bounds and first REC_INLINE entries, so for most buckets one DRAM line
-// serves the whole lookup; longer buckets stream the rest of their entries
-// from the entry table, each load issued REC_INLINE sub-steps before its use.
-// The count runs lane-major: sub-step j takes entry j of every lane's bucket
-// (ops are ordered by k-mer, then entry, so a key's first op is the smallest
-// (k-mer, entry) pair that reaches it: the lowest lane of a sub-step, kept
-// as a minimum across sub-steps).  Consecutive duplicates within a bucket
-// are the lane's own previous entry.  The insertion order the map replay
-// needs is rebuilt only when a strand map has two or more candidates: keys
-// ranked by their first op's dense index (k-mer prefix of bucket sizes plus
-// entry) through a bitmap.
+// results as seed_task with less memory traffic and working memory.
+//
+// Each lane owns k-mers (p = lane + 32 jj).  A k-mer's record (one aligned
+// sector) gives its bucket's bounds and first REC_INLINE entries, so for
+// most buckets one DRAM line serves the whole lookup; longer buckets stream
+// the rest of their entries from the entry table, each load issued
+// REC_INLINE entries before its use.  The count needs no order: sub-step j
+// takes entry j of every lane's bucket, skipping an entry equal to its
+// predecessor in the bucket (consecutive duplicates, ReadQueue.cpp:2380-2387,
+// 2421-2428), and the lanes that hold one key add their ops through one
+// leader (warp match groups).  A key is inserted into the
+// map (ReadQueue.cpp:2371, 2430) iff its first op's k-mer index is at most
+// maxQPos; ops come in k-mer order, so that holds iff some op of the key has
+// such an index, i.e. iff the key's count exceeds its count of ops from the
+// k-mers past maxQPos (both counts share one word).  When a strand map has
+// two or more candidates the insertion order is needed for the map replay:
+// the ops are then walked in order, 32 at a time, and each inserted key is
+// listed at its first op.
 // ---------------------------------------------------------------------------
 struct SeedMemR {
     uint8_t* seq;        // oriented read, 256 bytes
     uint64_t* pre;       // prefix hashes (aliases the count table)
     uint16_t* ksz;       // bucket size per k-mer
     uint32_t* kpre;      // exclusive prefix of bucket sizes (nk + 1), for the replay order
+    uint32_t* kst;       // bucket start per k-mer, for the replay order
     uint32_t* dt_key;    // count table: distinct (window, strand) keys
-    uint32_t* dt_val;    //   first op (k-mer << 11 | entry) | count << 19
-    uint32_t* reached;   // 32 count-table slots whose count reached QTHRESH, then 2 staged candidates
-    uint32_t* bitmap;    // one bit per op (ops_cap bits, at most 1024)
+    uint32_t* dt_val;    //   count | count of ops past maxQPos << 13 | listed << 31
+    uint32_t* reached;   // [0, 32) count-table slots whose count reached QTHRESH,
+                         // [33, 35) the staged candidates of the common case
     uint32_t* ins;       // inserted keys in first-touch order (replay only)
     uint16_t* ins_cnt;   //   and their counts
     uint32_t* slot;      // replayed buckets, pending stack, overflow list and the
@@ -684,15 +738,75 @@ struct SeedMemR {
     uint32_t ops_cap, dt_cap, slot_cap, stk_cap, ovf_cap;
 };
 
-constexpr uint32_t OPID_BITS = 19;             // op id: k-mer << 11 | entry (buckets hold <= KMERCUTOFF < 2048)
-constexpr uint32_t OPID_MASK = (1u << OPID_BITS) - 1;
+constexpr uint32_t DTV_TAIL = 1u << 13;        // dt_val: one op from a k-mer past maxQPos (counts < 8192)
+constexpr uint32_t DTV_LISTED = 1u << 31;      // dt_val: the key is in the insertion order
+__device__ __forceinline__ uint32_t dtv_count(uint32_t v) { return v & (DTV_TAIL - 1); }
+__device__ __forceinline__ bool dtv_inserted(uint32_t v) { return dtv_count(v) > ((v >> 13) & (DTV_TAIL - 1)); }
 
-__device__ __noinline__ int seed_rec_replay(const ChunkBufs& cb, const SeedMemR& s, uint32_t task, uint32_t nk,
-                                            uint32_t T, uint32_t maxQPos, CandRes& res);
+// Shared-memory working set of one warp for seed_task_rec: up to OPS
+// gathered bucket entries, a DT-slot count table (a power of two >= 2 * OPS).
+// The per-k-mer arrays, the count table (prefix hashes first) and, once the
+// insertion order is listed, the replay's buckets, stack, overflow list and
+// staged candidates share one region.
+template <uint32_t OPS, uint32_t DT, uint32_t OVF_N>
+struct SeedLayoutR {
+    static_assert(DT >= 2 * OPS && (DT & (DT - 1)) == 0 && OPS < DTV_TAIL, "count table too small");
+    static constexpr uint32_t R16(uint32_t b) { return (b + 15) / 16 * 16; }
+    static constexpr uint32_t SLOT_N = DT + 64;    // replayed buckets: pow2_ceil(OPS + 1) + 61 at most
+    static constexpr uint32_t SEQ = 0;             // 256 B
+    static constexpr uint32_t KSZ = SEQ + 256;     // 224 x u16
+    static constexpr uint32_t KPRE = KSZ + 448;    // 225 x u32
+    static constexpr uint32_t DTK = KPRE + 912;
+    static constexpr uint32_t DTV = DTK + DT * 4;
+    static constexpr uint32_t END_U = DTV + DT * 4;
+    static constexpr uint32_t KST = END_U;         // 224 x u32
+    static constexpr uint32_t REACHED = KST + 896; // 36 x u32
+    static constexpr uint32_t INS = REACHED + 144;
+    static constexpr uint32_t INSC = INS + R16(OPS * 4);
+    static constexpr uint32_t BYTES = INSC + R16(OPS * 2);
+    // the replay, over [0, END_U)
+    static constexpr uint32_t SLOT = 0;
+    static constexpr uint32_t STK = SLOT + R16(SLOT_N * 4);
+    static constexpr uint32_t OVF = STK + R16(OPS * 4);
+    static constexpr uint32_t STAGE = OVF + R16(OVF_N * 4);
+    static constexpr uint32_t END_B = STAGE + R16(OPS * 4);
+    static_assert(END_B <= END_U, "the replay does not fit the shared region");
+    static_assert(DTK % 8 == 0 && END_U - DTK >= 8 * (FAME_MAX_READ_LEN + 1), "prefix hashes do not fit");
+};
 
-__device__ int seed_task_rec(const DevIndex& ix, const ChunkBufs& cb, const SeedMemR& s, uint32_t task,
-                             unsigned long long* gather_bytes_acc, CandRes& res)
+template <class L, uint32_t OPS, uint32_t DT, uint32_t OVF_N>
+__device__ __forceinline__ SeedMemR seed_mem_r(uint8_t* base)
 {
+    SeedMemR s;
+    s.seq = base + L::SEQ;
+    s.ksz = (uint16_t*)(base + L::KSZ);
+    s.kpre = (uint32_t*)(base + L::KPRE);
+    s.kst = (uint32_t*)(base + L::KST);
+    s.pre = (uint64_t*)(base + L::DTK);
+    s.dt_key = (uint32_t*)(base + L::DTK);
+    s.dt_val = (uint32_t*)(base + L::DTV);
+    s.reached = (uint32_t*)(base + L::REACHED);
+    s.ins = (uint32_t*)(base + L::INS);
+    s.ins_cnt = (uint16_t*)(base + L::INSC);
+    s.slot = (uint32_t*)(base + L::SLOT);
+    s.stk = (uint32_t*)(base + L::STK);
+    s.ovf = (uint32_t*)(base + L::OVF);
+    s.stage = (uint32_t*)(base + L::STAGE);
+    s.ops_cap = OPS; s.dt_cap = DT; s.slot_cap = L::SLOT_N; s.stk_cap = OPS; s.ovf_cap = OVF_N;
+    return s;
+}
+
+template <class L, uint32_t OPS, uint32_t DT, uint32_t OVF_N>
+__device__ __noinline__ int seed_rec_replay(uint8_t* base, const uint32_t* entry, unsigned long long* ctr,
+                                            uint32_t nk, uint32_t T, uint32_t maxQPos);
+
+// base: the warp's working memory (layout L).  Returns 0 when the task's
+// candidates are published, 1 when the task is over the caps.
+template <class L, uint32_t OPS, uint32_t DT, uint32_t OVF_N>
+__device__ __forceinline__ int seed_task_rec(const DevIndex& ix, const ChunkBufs& cb, uint8_t* base, uint32_t task,
+                                             unsigned long long* gather_bytes_acc, CandRes& res)
+{
+    const SeedMemR s = seed_mem_r<L, OPS, DT, OVF_N>(base);
     constexpr uint32_t FULL = 0xffffffffu;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t r = task >> 1, o = task & 1;
@@ -739,9 +853,10 @@ __device__ int seed_task_rec(const DevIndex& ix, const ChunkBufs& cb, const Seed
         lo[jj] = p < nk ? __ldg(ix.rec + 2ull * key[jj]) : make_uint4(0, 0, 0, 0);
     }
     __syncwarp();   // the prefix hashes are dead: the count table may take their memory
-    const uint32_t dsz = s.dt_cap;
-    const uint32_t dmask = dsz - 1;
-    for (uint32_t i = lane; i < dsz; i += 32) s.dt_key[i] = EMPTY_KEY;
+    for (uint32_t i = lane; i < DT; i += 32) {
+        s.dt_key[i] = EMPTY_KEY;
+        s.dt_val[i] = 0;
+    }
     uint32_t T = 0;
     unsigned long long gb = 0;
 #pragma unroll
@@ -749,6 +864,7 @@ __device__ int seed_task_rec(const DevIndex& ix, const ChunkBufs& cb, const Seed
         const uint32_t p = lane + 32 * jj;
         if (p < nk) {
             s.ksz[p] = (uint16_t)lo[jj].y;
+            s.kst[p] = lo[jj].x;
             T += lo[jj].y;
             gb += 8 + 4ull * lo[jj].y;
         }
@@ -758,13 +874,12 @@ __device__ int seed_task_rec(const DevIndex& ix, const ChunkBufs& cb, const Seed
         T += __shfl_xor_sync(FULL, T, d);
         gb += __shfl_xor_sync(FULL, gb, d);
     }
-    if (T > s.ops_cap) return 1;
+    if (T > OPS) return 1;
     if (lane == 0) atomicAdd(gather_bytes_acc, gb);
+    const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
     uint32_t nreached = 0;
     __syncwarp();
-    // 2-3. count the distinct keys, sub-step j taking entry j of each lane's
-    //      bucket (consecutive duplicates within a bucket skipped,
-    //      ReadQueue.cpp:2380-2387, 2421-2428)
+    // 2-3. count the entries of every lane's buckets
 #pragma unroll
     for (int jj = 0; jj < KPL; ++jj) {
         if (32u * jj >= nk) continue;   // warp-uniform; no break, so the loop unrolls and lo / key stay in registers
@@ -779,6 +894,9 @@ __device__ int seed_task_rec(const DevIndex& ix, const ChunkBufs& cb, const Seed
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) jmax = max(jmax, __shfl_xor_sync(FULL, jmax, d));
         uint32_t prev = EMPTY_KEY;
+        // sub-step j takes entry j of every lane's bucket; lanes holding the
+        // same key add their ops through one leader (same-address atomics from
+        // a whole warp would serialise)
         for (uint32_t j = 0; j < jmax; ++j) {
             const uint32_t e = q0;
             q0 = q1; q1 = q2; q2 = q3; q3 = q4; q4 = q5;
@@ -786,28 +904,25 @@ __device__ int seed_task_rec(const DevIndex& ix, const ChunkBufs& cb, const Seed
             const bool valid = j < sz && !(j > 0 && prev == e);
             prev = e;
             const unsigned vm = __ballot_sync(FULL, valid);
+            const unsigned tm = __ballot_sync(FULL, valid && p > maxQPos);
             const unsigned grp = __match_any_sync(FULL, valid ? e : EMPTY_KEY) & vm;
             bool reach = false;
             uint32_t h = 0;
             if (valid && (uint32_t)(__ffs(grp) - 1) == lane) {
-                const uint32_t f = (p << 11) | j;
-                h = dt_hash(e, dmask);
-                bool fresh = false;
+                h = dt_hash(e, DT - 1);
                 while (true) {
                     const uint32_t cur = s.dt_key[h];
                     if (cur == e) break;
                     if (cur == EMPTY_KEY) {
                         const uint32_t old = atomicCAS(&s.dt_key[h], EMPTY_KEY, e);
-                        if (old == EMPTY_KEY) { fresh = true; break; }
-                        if (old == e) break;
+                        if (old == EMPTY_KEY || old == e) break;
                     }
-                    h = (h + 1) & dmask;
+                    h = (h + 1) & (DT - 1);
                 }
-                const uint32_t v = fresh ? f : s.dt_val[h];
-                const uint32_t before = fresh ? 0u : v >> OPID_BITS;
-                const uint32_t add = (uint32_t)__popc(grp);
-                s.dt_val[h] = min(v & OPID_MASK, f) | ((before + add) << OPID_BITS);
-                reach = before < QTHRESH && before + add >= QTHRESH;
+                const uint32_t v = s.dt_val[h];
+                const uint32_t n = (uint32_t)__popc(grp);
+                s.dt_val[h] = v + n + (uint32_t)__popc(grp & tm) * DTV_TAIL;
+                reach = dtv_count(v) < QTHRESH && dtv_count(v) + n >= QTHRESH;
             }
             const unsigned rm = __ballot_sync(FULL, reach);
             if (reach) {
@@ -818,27 +933,22 @@ __device__ int seed_task_rec(const DevIndex& ix, const ChunkBufs& cb, const Seed
             __syncwarp();   // this sub-step's count-table writes before the next one's probes
         }
     }
-    const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
-    // a key is a candidate when it was inserted (its first op's k-mer is the
-    // first one or cIdx < maxQPos, ReadQueue.cpp:2371, 2430) with a count
-    // >= QTHRESH (counts stay below 8192 here: no uint16 wrap)
-    auto inserted = [&](uint32_t v) {
-        const uint32_t kp = (v & OPID_MASK) >> 11;
-        return kp == 0 || kp - 1 < maxQPos;
-    };
-    // 4. both strand maps with at most one candidate: no insertion order needed
+    __syncwarp();
+    // 4. both strand maps with at most one candidate (count >= QTHRESH,
+    //    inserted): no insertion order needed; staged at once, forward map
+    //    first (the order saQuerySeedSetRef walks)
     if (nreached <= 32) {
         uint32_t k = 0;
         bool cand = false;
         if (lane < nreached) {
             const uint32_t h = s.reached[lane];
-            cand = inserted(s.dt_val[h]);
+            cand = dtv_inserted(s.dt_val[h]);
             k = s.dt_key[h];
         }
         const unsigned fm = __ballot_sync(FULL, cand && (k >> 31));
         const unsigned bm = __ballot_sync(FULL, cand && !(k >> 31));
         if (__popc(fm) <= 1 && __popc(bm) <= 1) {
-            uint32_t* stg = s.reached + 32;
+            uint32_t* stg = s.reached + 33;
             const uint32_t nf = __popc(fm), nstage = nf + __popc(bm);
             if (cand) stg[(k >> 31) ? 0 : nf] = k;
             __syncwarp();
@@ -846,26 +956,28 @@ __device__ int seed_task_rec(const DevIndex& ix, const ChunkBufs& cb, const Seed
             return 0;
         }
     }
-    return seed_rec_replay(cb, s, task, nk, T, maxQPos, res);
+    const int staged = seed_rec_replay<L, OPS, DT, OVF_N>(base, ix.entry, cb.ctr, nk, T, maxQPos);
+    if (staged < 0) return 1;
+    seed_publish(cb, res, task, s.stage, (uint32_t)staged & 0xffffu, (uint32_t)staged >> 16);
+    return 0;
 }
 
 // The rest of seed_task_rec when a strand map has two or more candidates
 // (about one task in eight at genome scale): the insertion order and the
 // replay, kept out of line so that the common path's registers stay its own.
-__device__ __noinline__ int seed_rec_replay(const ChunkBufs& cb, const SeedMemR& s, uint32_t task, uint32_t nk,
-                                            uint32_t T, uint32_t maxQPos, CandRes& res)
+// Returns nstage | nf << 16 with the candidates in s.stage, or -1 when a cap
+// is exceeded.
+template <class L, uint32_t OPS, uint32_t DT, uint32_t OVF_N>
+__device__ __noinline__ int seed_rec_replay(uint8_t* base, const uint32_t* entry, unsigned long long* ctr,
+                                            uint32_t nk, uint32_t T, uint32_t maxQPos)
 {
     constexpr uint32_t FULL = 0xffffffffu;
+    const SeedMemR s = seed_mem_r<L, OPS, DT, OVF_N>(base);
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t dsz = s.dt_cap;
-    auto inserted = [&](uint32_t v) {
-        const uint32_t kp = (v & OPID_MASK) >> 11;
-        return kp == 0 || kp - 1 < maxQPos;
-    };
-    if (lane == 0) atomicAdd(cb.ctr + CTR_REPLAY, 1ull);
-    // 4b. the inserted keys in first-touch order: each key's first op as a
-    //     dense index (prefix of bucket sizes over the k-mers, plus the entry)
-    //     marks one bit; a key's rank is the number of marks below its own
+    if (lane == 0) atomicAdd(ctr + CTR_REPLAY, 1ull);
+    // 4b. the inserted keys in first-touch order: the ops in order (dense index
+    //     = prefix of bucket sizes over the k-mers plus the entry), 32 at a
+    //     time; each inserted key is listed at its first op
     {
         const uint32_t per = (nk + 31) / 32;
         const uint32_t b = min(nk, lane * per), e = min(nk, b + per);
@@ -879,50 +991,48 @@ __device__ __noinline__ int seed_rec_replay(const ChunkBufs& cb, const SeedMemR&
         }
         uint32_t run = inc - loc;
         for (uint32_t p = b; p < e; ++p) { s.kpre[p] = run; run += s.ksz[p]; }
+        if (lane == 31) s.kpre[nk] = inc;
     }
-    const uint32_t nwords = (s.ops_cap + 31) / 32;   // <= 32
-    for (uint32_t w = lane; w < nwords; w += 32) s.bitmap[w] = 0;
     __syncwarp();
-    auto dense = [&](uint32_t v) { return s.kpre[(v & OPID_MASK) >> 11] + (v & 0x7ffu); };
-    for (uint32_t b0 = 0; b0 < dsz; b0 += 32) {
-        const uint32_t h = b0 + lane;
-        if (s.dt_key[h] != EMPTY_KEY) {
-            const uint32_t v = s.dt_val[h];
-            if (inserted(v)) {
-                const uint32_t d = dense(v);
-                atomicOr(&s.bitmap[d >> 5], 1u << (d & 31));
+    uint32_t nins = 0;
+    for (uint32_t q0 = 0; q0 < T; q0 += 32) {
+        const uint32_t q = q0 + lane;
+        bool valid = false;
+        uint32_t e = 0;
+        if (q < T) {
+            // the op's k-mer: the last p with kpre[p] <= q
+            uint32_t lo = 0, hi = nk;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (s.kpre[mid] <= q) lo = mid;
+                else hi = mid;
             }
+            const uint32_t j = q - s.kpre[lo];
+            const uint32_t* bk = entry + s.kst[lo];
+            e = __ldg(bk + j);
+            valid = !(j > 0 && __ldg(bk + j - 1) == e) && lo <= maxQPos;
         }
-    }
-    __syncwarp();
-    const uint32_t word = lane < nwords ? s.bitmap[lane] : 0u;
-    uint32_t wbase = __popc(word);
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t t = __shfl_up_sync(FULL, wbase, d);
-        if (lane >= (uint32_t)d) wbase += t;
-    }
-    const uint32_t nins = __shfl_sync(FULL, wbase, 31);
-    wbase -= __popc(word);
-    for (uint32_t b0 = 0; b0 < dsz; b0 += 32) {
-        const uint32_t h = b0 + lane;
-        const uint32_t kk = s.dt_key[h];
+        const unsigned vm = __ballot_sync(FULL, valid);
+        const unsigned grp = __match_any_sync(FULL, valid ? e : EMPTY_KEY) & vm;
         bool take = false;
-        uint32_t d = 0, v = 0;
-        if (kk != EMPTY_KEY) {
-            v = s.dt_val[h];
-            take = inserted(v);
-            if (take) d = dense(v);
+        uint32_t c = 0;
+        if (valid && (uint32_t)(__ffs(grp) - 1) == lane) {
+            uint32_t h = dt_hash(e, DT - 1);
+            while (s.dt_key[h] != e) h = (h + 1) & (DT - 1);
+            const uint32_t old = atomicOr(&s.dt_val[h], DTV_LISTED);
+            if (!(old & DTV_LISTED)) { take = true; c = dtv_count(old); }
         }
-        const uint32_t wb = __shfl_sync(FULL, wbase, take ? (d >> 5) : 0);
+        const unsigned tm = __ballot_sync(FULL, take);
         if (take) {
-            const uint32_t rank = wb + __popc(s.bitmap[d >> 5] & ((1u << (d & 31)) - 1));
-            s.ins[rank] = kk;
-            s.ins_cnt[rank] = (uint16_t)(v >> OPID_BITS);
+            const uint32_t at = nins + __popc(tm & ((1u << lane) - 1));
+            s.ins[at] = e;
+            s.ins_cnt[at] = (uint16_t)c;
         }
+        nins += __popc(tm);
+        __syncwarp();
     }
-    __syncwarp();   // the count table and per-k-mer arrays are dead from here
-    // 5. replay both maps (forward map first, the order saQuerySeedSetRef walks)
+    // 5. replay both maps (forward map first, the order saQuerySeedSetRef
+    //    walks); the count table and per-k-mer arrays are dead from here
     SeedMem sm{};
     sm.ins = s.ins;
     sm.slot = s.slot;
@@ -953,24 +1063,15 @@ __device__ __noinline__ int seed_rec_replay(const ChunkBufs& cb, const SeedMemR&
             continue;
         }
         MapSim m;
-        sim_init(m, T / 5);   // bucket_count = summed bucket sizes / 5 (sigma, getSeedRefs)
+        sim_init(m, T / 5);   // bucket_count = summed bucket sizes / 5 (getSeedRefs)
         m.nb = 0; m.novf = 0; m.sp = 0;
-        if (m.size > sm.slot_cap) return 1;
+        if (m.size > sm.slot_cap) return -1;
         for (uint32_t b = lane; b < m.size; b += 32) sm.slot[b] = EMPTY_KEY;
         __syncwarp();
         for (uint32_t b0 = 0; b0 < nins; b0 += 32) {
             const uint32_t xl = b0 + lane;
-            unsigned todo = __ballot_sync(FULL, xl < nins && (s.ins[xl] >> 31) == (uint32_t)dir);
-            while (todo) {
-                const uint32_t x = b0 + __ffs(todo) - 1;
-                todo &= todo - 1;
-                if (m.sp >= sm.stk_cap) return 1;
-                if (lane == 0) sm.stk[m.sp] = x;
-                m.sp++;
-                __syncwarp();
-                while (m.sp > 0)
-                    if (!sim_step_w(m, sm)) return 1;
-            }
+            const unsigned todo = __ballot_sync(FULL, xl < nins && (s.ins[xl] >> 31) == (uint32_t)dir);
+            if (!sim_insert_batch_w(m, sm, b0, todo)) return -1;
         }
         __syncwarp();
         // iteration order: buckets in array order, then the overflow list
@@ -987,8 +1088,7 @@ __device__ __noinline__ int seed_rec_replay(const ChunkBufs& cb, const SeedMemR&
         __syncwarp();
         if (dir == 1) nf = nstage;
     }
-    seed_publish(cb, res, task, s.stage, nstage, nf);
-    return 0;
+    return (int)(nstage | nf << 16);
 }
 
 }  // namespace fame

@@ -309,6 +309,13 @@ WORKLOADS = {
                         genome=dict(chrom_lengths=[10_000_000, 8_000_000, 7_000_000, 5_000_000], seed=31,
                                     meth_p=0.75, repeat_frac=0.45),
                         pairs=dict(n_pairs=1_200_000, seed=33, inner=(20, 400), sub_rate=0.01, indel_rate=0.001)),
+    # the 3 Gbp genome above; single-cell jobs of SE 100 bp reads (READLEN 100): Poisson arrivals at 20
+    # jobs/s, log-normal read counts (median 200k, clipped to [2k, 2M]), each cell with its own CpG
+    # methylation probability drawn from Beta(6, 2)
+    "sc_serving_3gbp": dict(large=True,
+                            genome=dict(chrom_lengths=_mammal_lengths(), seed=21, meth_p=0.75, repeat_frac=0.45),
+                            jobs=dict(n_jobs=24, rate=20.0, median=200_000, sigma=1.0, lo=2_000, hi=2_000_000,
+                                      seed=24, sub_rate=0.01, indel_rate=0.001, cell_beta=(6.0, 2.0))),
     # the 3 Gbp genome above; 20M pairs of 2 x 100 bp, inner distance U[20, 400], mate on the opposite
     # strand, 1% substitutions / 0.1% indels; MAXPDIST 400
     "pe100_3gbp": dict(large=True, maxpdist=400,
