@@ -744,6 +744,12 @@ def run_gb300_pe(args):
         gm.match_pairs_dev(d_s, d_o, nn, flags, maxpdist, d_mat, d_inv)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     pairs = launches = heavy = paired = 0
+    # per-stage CUDA-event times, from one extra untimed chunk
+    gm.set_timing(True)
+    d_s, d_o, nn = dev[steady[0]]
+    gm.match_pairs_dev(d_s, d_o, nn, flags, maxpdist, d_mat, d_inv)
+    pe_stages = {k: float(v) for k, v in zip(GpuMatcher.PAIR_STAGES, gm.pair_stage_times())}
+    gm.set_timing(False)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ev0.record(stream)
@@ -802,6 +808,7 @@ def run_gb300_pe(args):
         "e2e": {"value": e_pairs / t_e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps)},
         "gpu_launches": launches, "counts": {"pairs": pairs, "paired": paired, "heavy_pairs": heavy},
+        "stage_ms_one_chunk": pe_stages,
         "clocks": clk.summary(),
         "setup_seconds": {"generate": t_gen, "index_build": t_build, "upload": t_open},
     }

@@ -71,7 +71,7 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_fastq_close", "fame_queue_stage", "fame_queue_submit_staged", "fame_match_fastq",
            "fame_match_fastq_paired", "fame_index_write", "fame_gpu_index_bytes", "fame_queue_wait",
            "fame_gpu_set_seed_tier", "fame_gpu_autotune", "fame_gpu_load_tuning",
-           "fame_gpu_seed_tier_counts", "fame_gpu_map_order_probe"]
+           "fame_gpu_seed_tier_counts", "fame_gpu_map_order_probe", "fame_gpu_pair_stage_times"]
 
 _lib = None
 
@@ -114,6 +114,7 @@ def lib(build_if_missing: bool = True):
     L.fame_gpu_autotune.argtypes = [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_char_p]
     L.fame_gpu_load_tuning.argtypes = [_P, C.c_char_p]
     L.fame_gpu_seed_tier_counts.argtypes = [_P, _P]
+    L.fame_gpu_pair_stage_times.argtypes = [_P, _P, C.c_int]
     L.fame_gpu_map_order_probe.argtypes = [_P, _P, C.c_uint32, C.c_uint32, _P, _P]
     L.fame_gpu_index_bytes.argtypes = [_P]
     L.fame_gpu_index_bytes.restype = C.c_uint64
@@ -351,7 +352,7 @@ class GpuMatcher:
         return cnt, int(n.value)
 
     def tallies(self, reset: bool = False) -> np.ndarray:
-        out = np.zeros(4 * self.n_cpg, np.uint16)
+        out = np.empty(4 * self.n_cpg, np.uint16)
         _check(lib().fame_gpu_tallies(self.h, _ptr(out), int(reset)), self.h)
         return out.reshape(-1, 4)
 
@@ -376,6 +377,15 @@ class GpuMatcher:
         k = lib().fame_gpu_map_order_probe(self.h, _ptr(keys), len(keys), int(bucket_count), _ptr(order), _ptr(fb))
         _check(min(k, 0), self.h)
         return order[:k].copy(), int(fb[0])
+
+    PAIR_STAGES = ("mate_checks", "seed", "seed_mid", "scans_first", "walks_first", "scans_second",
+                   "walks_second_choice", "per_pair_and_dp")
+
+    def pair_stage_times(self):
+        """fame_gpu_pair_stage_times: per-stage milliseconds of the last paired chunk (PAIR_STAGES)."""
+        ms = np.zeros(len(self.PAIR_STAGES), np.float32)
+        lib().fame_gpu_pair_stage_times(self.h, _ptr(ms), len(ms))
+        return ms
 
     def seed_tier_counts(self):
         """fame_gpu_seed_tier_counts: tasks entering each seeding tier after the light one, last chunk."""
@@ -437,7 +447,7 @@ class GpuMatcher:
         return p.value
 
     def tally_read(self, meth_dev: int, reset: bool = False) -> np.ndarray:
-        out = np.zeros(4 * self.n_cpg, np.uint16)
+        out = np.empty(4 * self.n_cpg, np.uint16)
         _check(lib().fame_gpu_tally_read(self.h, meth_dev, _ptr(out), int(reset)), self.h)
         return out.reshape(-1, 4)
 

@@ -52,6 +52,7 @@ struct fame_gpu {
     unsigned long long* d_ctr = nullptr;
     unsigned long long* h_ctr = nullptr;  // pinned
     uint32_t* d_meth = nullptr;
+    uint16_t* d_meth16 = nullptr;        // packed tallies on their way to the host (allocated at first read)
     HeavyScratch hs{};                   // large-capacity seeding tier (caps from the largest bucket)
     HeavyScratch ms{};                   // global-memory middle seeding tier (genome-scale buckets, many warps)
     int seed_mid_first = 0;              // 1: every task seeds in the middle tiers (k_seed_route), no light attempt
@@ -60,6 +61,7 @@ struct fame_gpu {
     int timing = 0;
     cudaEvent_t ev[12]{};
     float stage_ms[FAME_STAGES]{};
+    float pe_stage_ms[FAME_PAIR_STAGES]{};
     uint64_t tier_tasks[5]{};            // tasks entering each seeding tier after the light one, last chunk;
                                          // [4]: tasks whose candidate order needed the map replay
     int launches = 0;
@@ -74,9 +76,10 @@ struct fame_gpu {
     PeTaskRec* d_pe_recs = nullptr;      // per pair orientation
     uint64_t cap_pe_recs = 0;
     uint8_t* d_pe_heavy = nullptr;       // global scratch of k_pe_heavy
-    uint8_t* d_pe_mid = nullptr;         // global scratch of k_pe_seed_mid
-    uint64_t pe_mid_warp_bytes = 0;
-    uint32_t pe_mid_warps = 0;
+    uint8_t* d_pe_mid = nullptr;         // global scratch of the paired middle tiers (PE_MID_S, then PE_MID)
+    uint8_t* d_pe_mid2 = nullptr;
+    uint64_t pe_mid_warp_bytes = 0, pe_mid2_warp_bytes = 0;
+    uint32_t pe_mid_warps = 0, pe_mid2_warps = 0;
     uint64_t pe_heavy_warp_bytes = 0;
     uint32_t pe_heavy_warps = 0;
     fame_queue* queue = nullptr;         // the batched form's slots, if open
@@ -266,6 +269,8 @@ extern "C" int fame_gpu_close(fame_gpu* g)
     dev_free(g->hs.base);
     dev_free(g->ms.base);
     dev_free(g->d_pe_mid);
+    dev_free(g->d_pe_mid2);
+    dev_free(g->d_meth16);
     dev_free(g->d_pe_heavy);
     dev_free(g->d_pe_recs);
     dev_free(g->d_cand_flags);
@@ -536,12 +541,14 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
             return fail(set_err(g, FAME_ERR_CUDA, "k_dp_warp does not fit an SM"));
         g->dp_grid = (uint32_t)(g->sm_count * nb);
         g->dp_blocks = g->dp_grid;
-        uint64_t off[28], hoff[28], moff[28];
+        uint64_t off[28], hoff[28], moff[28], m2off[28];
         g->pe_warp_bytes = pe_layout(PE_LIGHT, off);
         pe_layout(PE_HEAVY, hoff);
-        g->pe_mid_warp_bytes = pe_layout(PE_MID, moff);
+        g->pe_mid_warp_bytes = pe_layout(PE_MID_S, moff);
+        g->pe_mid2_warp_bytes = pe_layout(PE_MID, m2off);
         // pe_kmers keeps its per-read arrays (8 * 256 + 96 bytes) in layout regions 11 .. 16
-        if (off[17] - off[11] < PE_KMER_AREA || hoff[17] - hoff[11] < PE_KMER_AREA || moff[17] - moff[11] < PE_KMER_AREA)
+        if (off[17] - off[11] < PE_KMER_AREA || hoff[17] - hoff[11] < PE_KMER_AREA ||
+            moff[17] - moff[11] < PE_KMER_AREA || m2off[17] - m2off[11] < PE_KMER_AREA)
             return fail(set_err(g, FAME_ERR_CUDA, "paired layout: k-mer area too small"));
         const size_t pe_smem = PE_SEED_WARPS * g->pe_warp_bytes;   // the largest layout (mates up to 255 bases)
         if (cudaFuncSetAttribute(k_pe_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pe_smem) != cudaSuccess ||
@@ -784,8 +791,10 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
     cb.heavy = g->d_heavy;
     cb.heavy2 = g->d_heavy2;
     if (!g->d_pe_mid) {
-        g->pe_mid_warps = (uint32_t)g->sm_count * 8;
+        g->pe_mid_warps = (uint32_t)g->sm_count * 16;
+        g->pe_mid2_warps = (uint32_t)g->sm_count * 4;
         CK(cudaMalloc((void**)&g->d_pe_mid, g->pe_mid_warp_bytes * g->pe_mid_warps));
+        CK(cudaMalloc((void**)&g->d_pe_mid2, g->pe_mid2_warp_bytes * g->pe_mid2_warps));
     }
     PeIndex px = g->px;
     px.ctx = (uint32_t)((double)maxpdist / WINLEN) + 1;
@@ -806,7 +815,10 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         cb.hit_n = g->d_hit_n;
         cb.cand_first = 0;
         CK(cudaMemsetAsync(g->d_ctr, 0, CTR_N * sizeof(unsigned long long), g->stream));
+        const int T = g->timing;
+        if (T) cudaEventRecord(g->ev[0], g->stream);
         k_pe_prep<<<(n + 255) / 256, 256, 0, g->stream>>>(cb, g->ix.readlen);
+        if (T) cudaEventRecord(g->ev[1], g->stream);
         g->launches++;
         if ((rc = sync_ctr())) return rc;
         if (g->h_ctr[CTR_TOO_LONG]) return set_err(g, FAME_ERR_READ, "mate longer than FAME_MAX_READ_LEN");
@@ -832,9 +844,17 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         k_pe_seed<<<grid, 32 * PE_SEED_WARPS, PE_SEED_WARPS * wbytes, g->stream>>>(g->ix, px, cb, g->d_pe_recs,
                                                                                   (uint32_t)wbytes, caps,
                                                                                   g->seed_mid_first);
+        if (T) cudaEventRecord(g->ev[2], g->stream);
+        // the paired middle tiers: cb.heavy2 -> (over PE_MID_S) cb.heavy -> (over PE_MID) per-pair path;
+        // cb.heavy takes the per-pair path's list only later, in k_pe_finish
         k_pe_seed_mid<<<g->pe_mid_warps / 4, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_recs, g->d_pe_mid,
-                                                                  g->pe_mid_warp_bytes, PE_MID);
-        g->launches += 2;
+                                                                  g->pe_mid_warp_bytes, PE_MID_S, cb.heavy2,
+                                                                  CTR_HEAVY2, CTR_QMID, cb.heavy, CTR_HEAVY3);
+        k_pe_seed_mid<<<g->pe_mid2_warps / 4, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_recs, g->d_pe_mid2,
+                                                                   g->pe_mid2_warp_bytes, PE_MID, cb.heavy,
+                                                                   CTR_HEAVY3, CTR_QMID2, nullptr, 0);
+        if (T) cudaEventRecord(g->ev[3], g->stream);
+        g->launches += 3;
         if ((rc = sync_ctr())) return rc;
         const uint64_t nc1 = g->h_ctr[CTR_CAND];
         if (nc1 > g->cap_cand) {
@@ -853,7 +873,9 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         };
         // B, C: first-walk scans, first walks, second-walk candidates
         scans(0, nc1);
+        if (T) cudaEventRecord(g->ev[4], g->stream);
         k_pe_walk1<<<(2 * n + 127) / 128, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_recs);
+        if (T) cudaEventRecord(g->ev[5], g->stream);
         g->launches++;
         if ((rc = sync_ctr())) return rc;
         const uint64_t nc2 = g->h_ctr[CTR_CAND];
@@ -863,7 +885,9 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         }
         // D, E: second-walk scans, second walks and the pair choice
         scans(nc1, nc2);
+        if (T) cudaEventRecord(g->ev[6], g->stream);
         k_pe_finish<<<(n + 127) / 128, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_recs);
+        if (T) cudaEventRecord(g->ev[7], g->stream);
         g->launches++;
         if ((rc = sync_ctr())) return rc;
         if (g->h_ctr[CTR_HEAVY]) {
@@ -878,9 +902,12 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
             g->launches++;
         }
         k_dp_warp<<<g->dp_grid, 128, 4 * DPW_BYTES, g->stream>>>(g->ix, cb);
+        if (T) cudaEventRecord(g->ev[8], g->stream);
         g->launches++;
         if ((rc = sync_ctr())) return rc;
         if (g->h_ctr[CTR_ERRFLAG]) return set_err(g, FAME_ERR_INDEX, "a read pair exceeds the paired path's capacities");
+        if (T)
+            for (int k = 0; k < FAME_PAIR_STAGES; ++k) cudaEventElapsedTime(&g->pe_stage_ms[k], g->ev[k], g->ev[k + 1]);
         if (cnt) {
             const unsigned long long* h = g->h_ctr;
             cnt->succ += h[CTR_SUCC];
@@ -937,22 +964,34 @@ extern "C" int fame_gpu_match_pairs(fame_gpu* g, const char* seqs1, const uint64
     return FAME_OK;
 }
 
+namespace {
+
+// Tallies of a tally array to the host as the reference's uint16 counts
+// (packed on the device, one copy), optionally reset; on the context's stream.
+int tally_copy_out(fame_gpu* g, uint32_t* meth_dev, uint16_t* meth, int reset)
+{
+    const uint64_t n4 = 4 * g->n_cpg;
+    if (meth && n4) {
+        if (!g->d_meth16) {
+            int rc;
+            if ((rc = dev_alloc(g, &g->d_meth16, n4))) return rc;
+        }
+        k_pack_tallies<<<g->sm_count * 8, 256, 0, g->stream>>>(meth_dev, n4, g->d_meth16);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(meth, g->d_meth16, n4 * 2, cudaMemcpyDeviceToHost, g->stream));
+    }
+    if (reset && n4) CK(cudaMemsetAsync(meth_dev, 0, n4 * 4, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    return FAME_OK;
+}
+
+}  // namespace
+
 extern "C" int fame_gpu_tallies(fame_gpu* g, uint16_t* meth, int reset)
 {
     if (!g) return FAME_ERR_ARG;
     CK(cudaSetDevice(g->device));
-    const uint64_t n4 = 4 * g->n_cpg;
-    if (meth && n4) {
-        std::vector<uint32_t> h(n4);
-        CK(cudaMemcpyAsync(h.data(), g->d_meth, n4 * 4, cudaMemcpyDeviceToHost, g->stream));
-        CK(cudaStreamSynchronize(g->stream));
-        for (uint64_t i = 0; i < n4; ++i) meth[i] = (uint16_t)(h[i] & 0xffffu);  // uint16 wrap-around
-    }
-    if (reset && n4) {
-        CK(cudaMemsetAsync(g->d_meth, 0, n4 * 4, g->stream));
-        CK(cudaStreamSynchronize(g->stream));
-    }
-    return FAME_OK;
+    return tally_copy_out(g, g->d_meth, meth, reset);
 }
 
 extern "C" int fame_gpu_alloc(fame_gpu* g, size_t bytes, void** p)
@@ -1037,6 +1076,13 @@ extern "C" int fame_gpu_map_order_probe(fame_gpu* g, const uint32_t* keys, uint3
     if (out[2]) return done(set_err(g, FAME_ERR_INDEX, "map order probe: a capacity was exceeded"));
     *final_buckets = out[1];
     return done((int)out[0]);
+}
+
+extern "C" int fame_gpu_pair_stage_times(fame_gpu* g, float* ms, int n)
+{
+    if (!g || !ms) return FAME_ERR_ARG;
+    for (int i = 0; i < n && i < FAME_PAIR_STAGES; ++i) ms[i] = g->pe_stage_ms[i];
+    return FAME_PAIR_STAGES;
 }
 
 extern "C" int fame_gpu_seed_tier_counts(const fame_gpu* g, uint64_t* out)

@@ -1183,6 +1183,14 @@ __global__ void k_build_rec(const uint32_t* tab, const uint32_t* entry, uint64_t
     }
 }
 
+// The uint16 tallies the reference keeps (its counters wrap at 2^16) from the
+// device's uint32 ones, packed for the copy to the host.
+__global__ void k_pack_tallies(const uint32_t* meth, uint64_t n4, uint16_t* out)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = (uint16_t)(meth[i] & 0xffffu);
+}
+
 // Largest bucket of the index (sizes the heavy path).
 __global__ void k_max_bucket(const uint32_t* tab, uint64_t n, unsigned int* out)
 {

@@ -81,6 +81,7 @@ struct PeMem {
     uint32_t* gt;
     uint8_t* gk;          // k-mer of each staged entry
     uint8_t* sv;          // staged entry survives the T-mask filter and the dedup
+    uint32_t area;        // bytes of regions 11 .. 16 (dead while the maps are built)
     PeCaps c;
 };
 
@@ -158,13 +159,17 @@ __device__ inline PeMem pe_mem(uint8_t* base, PeCaps c)
     s.gt = (uint32_t*)(base + off[25]);
     s.gk = base + off[26];
     s.sv = base + off[27];
+    s.area = (uint32_t)(off[17] - off[11]);
     return s;
 }
 
 // shared-memory caps of k_pe_seed (one warp; it keeps no matches)
 constexpr PeCaps PE_LIGHT{64, 256, 256 + NBHD - 1, 64, 0, 320, PE_KMAX};
-// caps of the paired middle tier (global scratch, many warps): genome-scale
-// indexes, about three entries per bucket, a few hundred keys per mate
+// caps of the paired middle tiers (global scratch): genome-scale indexes put
+// about three entries in a bucket and a few hundred keys in a mate's map.
+// The first holds the common pair with small tables (the value-table sweeps
+// of a pair cost in proportion to vcap), the second the rest.
+constexpr PeCaps PE_MID_S{256, 1024, 1024 + NBHD - 1 + 64, 256, 0, 2048, PE_KMAX};
 constexpr PeCaps PE_MID{1024, 4096, 4096 + NBHD - 1 + 64, 256, 0, 4096, PE_KMAX};
 
 __device__ __forceinline__ uint32_t vt_hash(uint32_t k, uint32_t mask) { return (k * 0x9E3779B1u) >> 8 & mask; }
@@ -1158,7 +1163,8 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
     __syncwarp();
     const uint32_t sigma2 = pe_kmers(ix, px, s, s.rd[1], n2);
     int par2 = 0;
-    if (sigma2 <= s.c.ecap && 2 * s.c.vcap * 4 <= PE_KMER_AREA) par2 = pe_count_par2(px, s, st, n2, sigma2);
+    // the lane-parallel count keeps two vcap-slot arrays in regions 11 .. 16
+    if (sigma2 <= s.c.ecap && 2 * s.c.vcap * 4 <= s.area) par2 = pe_count_par2(px, s, st, n2, sigma2);
     if (par2 < 0) return -1;
     if (par2 == 0 && lane == 0) pe_count_second(ix, px, s, st, n2, sigma2 <= s.c.ecap);
     if (__shfl_sync(0xffffffffu, st.over, 0)) return -1;
@@ -1534,27 +1540,35 @@ __global__ void k_pe_seed(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs
     }
 }
 
-// Stage A of the paired middle tier: the pairs of cb.heavy2 with the caps of a
-// genome-scale index, working memory in global scratch (warp_bytes per warp),
-// warp per pair, pairs taken from a work queue (counter CTR_QMID).  A pair
-// over these caps too is marked for the per-pair path (k_pe_heavy).
+// Stage A of a paired middle tier: the pairs of `list` (its length in counter
+// ctr_in) with the caps of a genome-scale index, working memory in global
+// scratch (warp_bytes per warp), warp per pair, pairs taken from a work queue
+// (counter ctr_q).  A pair over these caps goes to `spill` (counter
+// ctr_spill) for the next tier, or, without one, is marked for the per-pair
+// path (k_pe_heavy).
 __global__ void k_pe_seed_mid(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs, uint8_t* scratch,
-                              uint64_t warp_bytes, PeCaps caps)
+                              uint64_t warp_bytes, PeCaps caps, const uint32_t* list, int ctr_in, int ctr_q,
+                              uint32_t* spill, int ctr_spill)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const PeMem s = pe_mem(scratch + (uint64_t)wid * warp_bytes, caps);
-    const uint32_t npairs = (uint32_t)cb.ctr[CTR_HEAVY2];
+    const uint32_t npairs = (uint32_t)cb.ctr[ctr_in];
     while (true) {
         uint32_t k = 0;
-        if (lane == 0) k = (uint32_t)atomicAdd(cb.ctr + CTR_QMID, 1ull);
+        if (lane == 0) k = (uint32_t)atomicAdd(cb.ctr + ctr_q, 1ull);
         k = __shfl_sync(0xffffffffu, k, 0);
         if (k >= npairs) break;
-        const uint32_t r = cb.heavy2[k];
+        const uint32_t r = list[k];
         const bool over = pe_seed_pair(ix, px, cb, recs, s, caps, r);
         if (over && lane == 0) {
-            recs[2 * r].state = PT_FALLBACK;
-            recs[2 * r + 1].state = PT_FALLBACK;
+            if (spill) {
+                pe_rec_reset(recs, r);
+                spill[(uint32_t)atomicAdd(cb.ctr + ctr_spill, 1ull)] = r;
+            } else {
+                recs[2 * r].state = PT_FALLBACK;
+                recs[2 * r + 1].state = PT_FALLBACK;
+            }
         }
         __syncwarp();
     }

@@ -424,14 +424,7 @@ extern "C" int fame_gpu_tally_read(fame_gpu* g, const uint32_t* meth_dev, uint16
 {
     if (!g || !meth_dev) return FAME_ERR_ARG;
     CK(cudaSetDevice(g->device));
-    const uint64_t n4 = 4 * g->n_cpg;
-    if (meth && n4) {
-        std::vector<uint32_t> h(n4);
-        CK(cudaMemcpy(h.data(), meth_dev, n4 * 4, cudaMemcpyDeviceToHost));
-        for (uint64_t i = 0; i < n4; ++i) meth[i] = (uint16_t)(h[i] & 0xffffu);  // uint16 wrap-around
-    }
-    if (reset && n4) CK(cudaMemset((void*)meth_dev, 0, n4 * 4));
-    return FAME_OK;
+    return tally_copy_out(g, (uint32_t*)meth_dev, meth, reset);
 }
 
 extern "C" int fame_gpu_tally_free(fame_gpu* g, uint32_t* meth_dev)

@@ -303,6 +303,12 @@ int fame_gpu_stream(fame_gpu* g, void** stream);
 #define FAME_STAGES 9
 int fame_gpu_set_timing(fame_gpu* g, int enable);
 int fame_gpu_stage_times(fame_gpu* g, float* ms, int n);
+/* The same for the last paired-end call: 0 mate checks, 1 seeding in shared
+ * memory, 2 the paired middle tier, 3 first-mate window scans, 4 first walks,
+ * 5 second-mate window scans, 6 second walks and the pair choice, 7 the
+ * per-pair path and the banded DP.  Returns FAME_PAIR_STAGES. */
+#define FAME_PAIR_STAGES 8
+int fame_gpu_pair_stage_times(fame_gpu* g, float* ms, int n);
 /* Seeding tasks that entered each tier after the light one in the last
  * single-end chunk: out[0] the smaller shared-memory middle tier (up to 511
  * gathered bucket entries), out[1] the larger one (up to 1023), out[2] the
