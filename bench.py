@@ -395,9 +395,12 @@ def run_gb300(args):
     torch.cuda.synchronize()
     ev0.record(stream)
     tw0 = time.perf_counter()
+    host_steps = {"plain": [], "e2e": []}
     for k in range(args.steps):
         d_s, d_o, n = dev[steady[k % len(steady)]]
+        th = time.perf_counter()
         c = gm.match_reads_dev(d_s, d_o, n, flags, d_mat, d_inv)
+        host_steps["plain"].append(time.perf_counter() - th)
         stage += gm.stage_times()
         tiers += gm.seed_tier_counts()
         reads += n
@@ -435,7 +438,9 @@ def run_gb300(args):
     ev0.record(stream)
     for k in range(args.steps):
         hs, ho, n = pinned[steady[k % len(steady)]]
+        th = time.perf_counter()
         gm.match_reads(hs, ho, flags, mats=h_mat[:n], invalid=h_inv[:n])
+        host_steps["e2e"].append(time.perf_counter() - th)
         e_reads += n
         h2d += hs.nbytes + ho.nbytes
         d2h += 9 * n
@@ -536,6 +541,8 @@ def run_gb300(args):
         "e2e": {"value": e_reads * world / t_e2e, "unit": "reads/s", "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps), "h2d_copy_gbps": h2d_gbps},
         "gpu_launches": launches,
+        "host_step_ms": {k: [round(1e3 * min(v), 3), round(1e3 * float(np.median(v)), 3), round(1e3 * max(v), 3)]
+                         for k, v in host_steps.items() if v},
         "batched": batched,
         "fastq_file": fastq,
         "stage_seconds": st,
