@@ -997,7 +997,7 @@ __global__ void __launch_bounds__(128) k_seed(DevIndex ix, ChunkBufs cb, uint32_
 // shared memory.
 constexpr uint32_t MID_OVF = 256;
 template <uint32_t OPS, uint32_t DT, int WPB>
-__global__ void __launch_bounds__(32 * WPB) k_seed_mid(DevIndex ix, ChunkBufs cb, const uint32_t* list, int ctr_in,
+__global__ void __launch_bounds__(32 * WPB, 4) k_seed_mid(DevIndex ix, ChunkBufs cb, const uint32_t* list, int ctr_in,
                                                        int ctr_q, uint32_t* spill, int ctr_spill)
 {
     extern __shared__ __align__(16) uint8_t smem[];

@@ -281,52 +281,59 @@ __device__ bool sim_step_w(MapSim& m, const SeedMem& s)
     return sim_rehash_w(m, s, next);
 }
 
-// Inserts, in lane order, the keys ins[xb + lane] of the lanes in `todo`
-// (the stack empty on entry and on return).  Each step tries every pending
-// key at once: a key whose first empty bucket from its home lies in its
-// neighbourhood, that no earlier pending key wants too, and that keeps the
-// load under the rehash threshold is placed exactly where one insert_impl
-// after another would place it; the pending keys before the first one that
-// fails these tests go in together, and that one runs the full
-// insert_impl (displacements, overflow list, rehash) on its own.  False when
-// a cap is exceeded.
-__device__ bool sim_insert_batch_w(MapSim& m, const SeedMem& s, uint32_t xb, unsigned todo)
+// Runs insert_impl for the elements on the stack until it is empty, up to
+// 32 at a time: the top elements are tried at once (lane k the k-th from
+// the top); an element whose first empty bucket from its home lies in its
+// neighbourhood, that no element above it wants too, and that keeps the load
+// under the rehash threshold is placed exactly where one insert_impl after
+// another would place it.  The elements above the first one that fails these
+// tests go in together, and that one (then on top) runs the full insert_impl
+// (displacements, overflow list, or a rehash that pushes the table's
+// elements on top of the stack, which the next steps drain the same way).
+// False when a cap is exceeded.
+__device__ bool sim_drain_w(MapSim& m, const SeedMem& s)
 {
     constexpr uint32_t FULL = 0xffffffffu;
     const uint32_t lane = threadIdx.x & 31;
-    while (todo) {
-        const bool act = (todo >> lane) & 1u;
-        const uint32_t rank = __popc(todo & ((1u << lane) - 1));
+    while (m.sp > 0) {
+        const uint32_t n = min(32u, m.sp);
+        const bool act = lane < n;
+        const uint32_t x = act ? s.stk[m.sp - 1 - lane] : 0u;
         uint32_t ie = m.size;
         bool ok = false;
         if (act && m.size > 0) {
-            const uint32_t ib = sim_key(s, xb + lane) & m.mask;
+            const uint32_t ib = sim_key(s, x) & m.mask;
             const uint32_t lim = min(ib + MAX_PROBES, m.size);
             for (uint32_t b = ib; b < lim; ++b)
                 if (s.slot[b] == EMPTY_KEY) { ie = b; break; }
-            ok = ie < m.size && ie - ib < NBHD && m.nb + rank - m.novf < m.max_thr;
+            ok = ie < m.size && ie - ib < NBHD && m.nb + lane - m.novf < m.max_thr;
         }
-        // the first pending key that wants a bucket an earlier one wants too fails
-        const unsigned grp = __match_any_sync(FULL, act ? ie : 0xfffffff0u - lane) & todo;
-        if (act && (__ffs(grp) - 1) != (int)lane) ok = false;
+        // an element that wants a bucket an element above it wants too fails
+        const unsigned grp = __match_any_sync(FULL, act ? ie : 0xfffffff0u - lane);
+        if (act && (uint32_t)(__ffs(grp) - 1) != lane) ok = false;
         const unsigned bad = __ballot_sync(FULL, act && !ok);
-        const unsigned good = bad ? (todo & ((1u << (__ffs(bad) - 1)) - 1)) : todo;
-        if ((good >> lane) & 1u) s.slot[ie] = xb + lane;
-        m.nb += __popc(good);
-        todo &= ~good;
+        const uint32_t ngood = bad ? (uint32_t)(__ffs(bad) - 1) : n;
+        if (lane < ngood) s.slot[ie] = x;
+        m.nb += ngood;
+        m.sp -= ngood;
         __syncwarp();
-        if (bad) {
-            const uint32_t k = __ffs(bad) - 1;
-            todo &= ~(1u << k);
-            if (m.sp >= s.stk_cap) return false;
-            if (lane == 0) s.stk[m.sp] = xb + k;
-            m.sp++;
-            __syncwarp();
-            while (m.sp > 0)
-                if (!sim_step_w(m, s)) return false;
-        }
+        if (bad && !sim_step_w(m, s)) return false;
     }
     return true;
+}
+
+// Inserts, in lane order, the keys ins[xb + lane] of the lanes in `todo`
+// (the stack empty on entry and on return): they go on the stack, the first
+// on top, and the stack is drained.  False when a cap is exceeded.
+__device__ bool sim_insert_batch_w(MapSim& m, const SeedMem& s, uint32_t xb, unsigned todo)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t k = __popc(todo);
+    if (m.sp + k > s.stk_cap) return false;
+    if ((todo >> lane) & 1u) s.stk[m.sp + k - 1 - __popc(todo & ((1u << lane) - 1))] = xb + lane;
+    m.sp += k;
+    __syncwarp();
+    return sim_drain_w(m, s);
 }
 
 // A warp's reservation of candidate slots: tasks take contiguous runs from
@@ -714,21 +721,22 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
 // map (ReadQueue.cpp:2371, 2430) iff its first op's k-mer index is at most
 // maxQPos; ops come in k-mer order, so that holds iff some op of the key has
 // such an index, i.e. iff the key's count exceeds its count of ops from the
-// k-mers past maxQPos (both counts share one word).  When a strand map has
-// two or more candidates the insertion order is needed for the map replay:
-// the ops are then walked in order, 32 at a time, and each inserted key is
-// listed at its first op.
+// k-mers past maxQPos.  The same word keeps the dense index of the key's
+// first op (ops ordered by k-mer, then entry: within a sub-step the group's
+// leader, the lowest lane, holds the first), so when a strand map has two or
+// more candidates the insertion order the map replay needs is a rank of the
+// inserted keys by first op, through a bitmap.
 // ---------------------------------------------------------------------------
 struct SeedMemR {
     uint8_t* seq;        // oriented read, 256 bytes
     uint64_t* pre;       // prefix hashes (aliases the count table)
     uint16_t* ksz;       // bucket size per k-mer
     uint32_t* kpre;      // exclusive prefix of bucket sizes (nk + 1), for the replay order
-    uint32_t* kst;       // bucket start per k-mer, for the replay order
     uint32_t* dt_key;    // count table: distinct (window, strand) keys
-    uint32_t* dt_val;    //   count | count of ops past maxQPos << 13 | listed << 31
+    uint32_t* dt_val;    //   count | count of ops past maxQPos << 10 | first op << 20
     uint32_t* reached;   // [0, 32) count-table slots whose count reached QTHRESH,
                          // [33, 35) the staged candidates of the common case
+    uint32_t* bitmap;    // one bit per op (1024 bits): the first ops of the inserted keys (replay only)
     uint32_t* ins;       // inserted keys in first-touch order (replay only)
     uint16_t* ins_cnt;   //   and their counts
     uint32_t* slot;      // replayed buckets, pending stack, overflow list and the
@@ -738,10 +746,15 @@ struct SeedMemR {
     uint32_t ops_cap, dt_cap, slot_cap, stk_cap, ovf_cap;
 };
 
-constexpr uint32_t DTV_TAIL = 1u << 13;        // dt_val: one op from a k-mer past maxQPos (counts < 8192)
-constexpr uint32_t DTV_LISTED = 1u << 31;      // dt_val: the key is in the insertion order
-__device__ __forceinline__ uint32_t dtv_count(uint32_t v) { return v & (DTV_TAIL - 1); }
-__device__ __forceinline__ bool dtv_inserted(uint32_t v) { return dtv_count(v) > ((v >> 13) & (DTV_TAIL - 1)); }
+// count-table word: count (bits 0-9), count of ops from k-mers past maxQPos
+// (bits 10-19), dense index of the key's first op (bits 20-29; 1023 before
+// any), for at most 1023 gathered entries
+constexpr uint32_t DTV_TAIL = 1u << 10;
+constexpr uint32_t DTV_FIRST_SHIFT = 20;
+constexpr uint32_t DTV_EMPTY = 1023u << DTV_FIRST_SHIFT;
+__device__ __forceinline__ uint32_t dtv_count(uint32_t v) { return v & 1023u; }
+__device__ __forceinline__ uint32_t dtv_first(uint32_t v) { return (v >> DTV_FIRST_SHIFT) & 1023u; }
+__device__ __forceinline__ bool dtv_inserted(uint32_t v) { return dtv_count(v) > ((v >> 10) & 1023u); }
 
 // Shared-memory working set of one warp for seed_task_rec: up to OPS
 // gathered bucket entries, a DT-slot count table (a power of two >= 2 * OPS).
@@ -750,7 +763,7 @@ __device__ __forceinline__ bool dtv_inserted(uint32_t v) { return dtv_count(v) >
 // staged candidates share one region.
 template <uint32_t OPS, uint32_t DT, uint32_t OVF_N>
 struct SeedLayoutR {
-    static_assert(DT >= 2 * OPS && (DT & (DT - 1)) == 0 && OPS < DTV_TAIL, "count table too small");
+    static_assert(DT >= 2 * OPS && (DT & (DT - 1)) == 0 && OPS < 1024, "count table too small");
     static constexpr uint32_t R16(uint32_t b) { return (b + 15) / 16 * 16; }
     static constexpr uint32_t SLOT_N = DT + 64;    // replayed buckets: pow2_ceil(OPS + 1) + 61 at most
     static constexpr uint32_t SEQ = 0;             // 256 B
@@ -759,8 +772,8 @@ struct SeedLayoutR {
     static constexpr uint32_t DTK = KPRE + 912;
     static constexpr uint32_t DTV = DTK + DT * 4;
     static constexpr uint32_t END_U = DTV + DT * 4;
-    static constexpr uint32_t KST = END_U;         // 224 x u32
-    static constexpr uint32_t REACHED = KST + 896; // 36 x u32
+    static constexpr uint32_t BITMAP = END_U;      // 32 x u32
+    static constexpr uint32_t REACHED = BITMAP + 128; // 36 x u32
     static constexpr uint32_t INS = REACHED + 144;
     static constexpr uint32_t INSC = INS + R16(OPS * 4);
     static constexpr uint32_t BYTES = INSC + R16(OPS * 2);
@@ -781,7 +794,7 @@ __device__ __forceinline__ SeedMemR seed_mem_r(uint8_t* base)
     s.seq = base + L::SEQ;
     s.ksz = (uint16_t*)(base + L::KSZ);
     s.kpre = (uint32_t*)(base + L::KPRE);
-    s.kst = (uint32_t*)(base + L::KST);
+    s.bitmap = (uint32_t*)(base + L::BITMAP);
     s.pre = (uint64_t*)(base + L::DTK);
     s.dt_key = (uint32_t*)(base + L::DTK);
     s.dt_val = (uint32_t*)(base + L::DTV);
@@ -797,8 +810,7 @@ __device__ __forceinline__ SeedMemR seed_mem_r(uint8_t* base)
 }
 
 template <class L, uint32_t OPS, uint32_t DT, uint32_t OVF_N>
-__device__ __noinline__ int seed_rec_replay(uint8_t* base, const uint32_t* entry, unsigned long long* ctr,
-                                            uint32_t nk, uint32_t T, uint32_t maxQPos);
+__device__ __noinline__ int seed_rec_replay(uint8_t* base, unsigned long long* ctr, uint32_t T);
 
 // base: the warp's working memory (layout L).  Returns 0 when the task's
 // candidates are published, 1 when the task is over the caps.
@@ -855,7 +867,7 @@ __device__ __forceinline__ int seed_task_rec(const DevIndex& ix, const ChunkBufs
     __syncwarp();   // the prefix hashes are dead: the count table may take their memory
     for (uint32_t i = lane; i < DT; i += 32) {
         s.dt_key[i] = EMPTY_KEY;
-        s.dt_val[i] = 0;
+        s.dt_val[i] = DTV_EMPTY;
     }
     uint32_t T = 0;
     unsigned long long gb = 0;
@@ -864,7 +876,6 @@ __device__ __forceinline__ int seed_task_rec(const DevIndex& ix, const ChunkBufs
         const uint32_t p = lane + 32 * jj;
         if (p < nk) {
             s.ksz[p] = (uint16_t)lo[jj].y;
-            s.kst[p] = lo[jj].x;
             T += lo[jj].y;
             gb += 8 + 4ull * lo[jj].y;
         }
@@ -879,12 +890,29 @@ __device__ __forceinline__ int seed_task_rec(const DevIndex& ix, const ChunkBufs
     const uint32_t maxQPos = len - KMERLEN + 1 - QTHRESH;
     uint32_t nreached = 0;
     __syncwarp();
+    // dense op index of each k-mer's first entry: exclusive prefix of the bucket sizes
+    {
+        const uint32_t per = (nk + 31) / 32;
+        const uint32_t b = min(nk, lane * per), e = min(nk, b + per);
+        uint32_t loc = 0;
+        for (uint32_t p = b; p < e; ++p) loc += s.ksz[p];
+        uint32_t inc = loc;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(FULL, inc, d);
+            if (lane >= (uint32_t)d) inc += t;
+        }
+        uint32_t run = inc - loc;
+        for (uint32_t p = b; p < e; ++p) { s.kpre[p] = run; run += s.ksz[p]; }
+    }
+    __syncwarp();
     // 2-3. count the entries of every lane's buckets
 #pragma unroll
     for (int jj = 0; jj < KPL; ++jj) {
         if (32u * jj >= nk) continue;   // warp-uniform; no break, so the loop unrolls and lo / key stay in registers
         const uint32_t p = lane + 32 * jj;
         const uint32_t sz = lo[jj].y, start = lo[jj].x;
+        const uint32_t op0 = p < nk ? s.kpre[p] : 0u;   // dense index of the bucket's first op
         uint32_t q0 = lo[jj].z, q1 = lo[jj].w, q2 = 0, q3 = 0, q4 = 0, q5 = 0;
         if (sz > 2) {
             const uint4 hi = __ldg(ix.rec + 2ull * key[jj] + 1);
@@ -919,9 +947,12 @@ __device__ __forceinline__ int seed_task_rec(const DevIndex& ix, const ChunkBufs
                     }
                     h = (h + 1) & (DT - 1);
                 }
+                // the leader holds the group's lowest k-mer, so its op comes first
                 const uint32_t v = s.dt_val[h];
                 const uint32_t n = (uint32_t)__popc(grp);
-                s.dt_val[h] = v + n + (uint32_t)__popc(grp & tm) * DTV_TAIL;
+                const uint32_t first = min(dtv_first(v), op0 + j);
+                s.dt_val[h] = ((v & ((1u << DTV_FIRST_SHIFT) - 1)) + n + (uint32_t)__popc(grp & tm) * DTV_TAIL) |
+                              (first << DTV_FIRST_SHIFT);
                 reach = dtv_count(v) < QTHRESH && dtv_count(v) + n >= QTHRESH;
             }
             const unsigned rm = __ballot_sync(FULL, reach);
@@ -956,7 +987,7 @@ __device__ __forceinline__ int seed_task_rec(const DevIndex& ix, const ChunkBufs
             return 0;
         }
     }
-    const int staged = seed_rec_replay<L, OPS, DT, OVF_N>(base, ix.entry, cb.ctr, nk, T, maxQPos);
+    const int staged = seed_rec_replay<L, OPS, DT, OVF_N>(base, cb.ctr, T);
     if (staged < 0) return 1;
     seed_publish(cb, res, task, s.stage, (uint32_t)staged & 0xffffu, (uint32_t)staged >> 16);
     return 0;
@@ -968,69 +999,55 @@ __device__ __forceinline__ int seed_task_rec(const DevIndex& ix, const ChunkBufs
 // Returns nstage | nf << 16 with the candidates in s.stage, or -1 when a cap
 // is exceeded.
 template <class L, uint32_t OPS, uint32_t DT, uint32_t OVF_N>
-__device__ __noinline__ int seed_rec_replay(uint8_t* base, const uint32_t* entry, unsigned long long* ctr,
-                                            uint32_t nk, uint32_t T, uint32_t maxQPos)
+__device__ __noinline__ int seed_rec_replay(uint8_t* base, unsigned long long* ctr, uint32_t T)
 {
     constexpr uint32_t FULL = 0xffffffffu;
     const SeedMemR s = seed_mem_r<L, OPS, DT, OVF_N>(base);
     const uint32_t lane = threadIdx.x & 31;
     if (lane == 0) atomicAdd(ctr + CTR_REPLAY, 1ull);
-    // 4b. the inserted keys in first-touch order: the ops in order (dense index
-    //     = prefix of bucket sizes over the k-mers plus the entry), 32 at a
-    //     time; each inserted key is listed at its first op
-    {
-        const uint32_t per = (nk + 31) / 32;
-        const uint32_t b = min(nk, lane * per), e = min(nk, b + per);
-        uint32_t loc = 0;
-        for (uint32_t p = b; p < e; ++p) loc += s.ksz[p];
-        uint32_t inc = loc;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t t = __shfl_up_sync(FULL, inc, d);
-            if (lane >= (uint32_t)d) inc += t;
+    // 4b. the inserted keys in first-touch order: each inserted key marks the
+    //     dense index of its first op in a bitmap (first ops of distinct keys
+    //     are distinct ops); a key's rank is the number of marks below its own
+    s.bitmap[lane] = 0;
+    __syncwarp();
+    for (uint32_t b0 = 0; b0 < DT; b0 += 32) {
+        const uint32_t h = b0 + lane;
+        if (s.dt_key[h] != EMPTY_KEY) {
+            const uint32_t v = s.dt_val[h];
+            if (dtv_inserted(v)) {
+                const uint32_t d = dtv_first(v);
+                atomicOr(&s.bitmap[d >> 5], 1u << (d & 31));
+            }
         }
-        uint32_t run = inc - loc;
-        for (uint32_t p = b; p < e; ++p) { s.kpre[p] = run; run += s.ksz[p]; }
-        if (lane == 31) s.kpre[nk] = inc;
     }
     __syncwarp();
-    uint32_t nins = 0;
-    for (uint32_t q0 = 0; q0 < T; q0 += 32) {
-        const uint32_t q = q0 + lane;
-        bool valid = false;
-        uint32_t e = 0;
-        if (q < T) {
-            // the op's k-mer: the last p with kpre[p] <= q
-            uint32_t lo = 0, hi = nk;
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (s.kpre[mid] <= q) lo = mid;
-                else hi = mid;
-            }
-            const uint32_t j = q - s.kpre[lo];
-            const uint32_t* bk = entry + s.kst[lo];
-            e = __ldg(bk + j);
-            valid = !(j > 0 && __ldg(bk + j - 1) == e) && lo <= maxQPos;
-        }
-        const unsigned vm = __ballot_sync(FULL, valid);
-        const unsigned grp = __match_any_sync(FULL, valid ? e : EMPTY_KEY) & vm;
-        bool take = false;
-        uint32_t c = 0;
-        if (valid && (uint32_t)(__ffs(grp) - 1) == lane) {
-            uint32_t h = dt_hash(e, DT - 1);
-            while (s.dt_key[h] != e) h = (h + 1) & (DT - 1);
-            const uint32_t old = atomicOr(&s.dt_val[h], DTV_LISTED);
-            if (!(old & DTV_LISTED)) { take = true; c = dtv_count(old); }
-        }
-        const unsigned tm = __ballot_sync(FULL, take);
-        if (take) {
-            const uint32_t at = nins + __popc(tm & ((1u << lane) - 1));
-            s.ins[at] = e;
-            s.ins_cnt[at] = (uint16_t)c;
-        }
-        nins += __popc(tm);
-        __syncwarp();
+    const uint32_t word = s.bitmap[lane];
+    uint32_t wbase = __popc(word);
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, wbase, d);
+        if (lane >= (uint32_t)d) wbase += t;
     }
+    const uint32_t nins = __shfl_sync(FULL, wbase, 31);
+    wbase -= __popc(word);
+    for (uint32_t b0 = 0; b0 < DT; b0 += 32) {
+        const uint32_t h = b0 + lane;
+        const uint32_t kk = s.dt_key[h];
+        bool take = false;
+        uint32_t d = 0, v = 0;
+        if (kk != EMPTY_KEY) {
+            v = s.dt_val[h];
+            take = dtv_inserted(v);
+            d = dtv_first(v);
+        }
+        const uint32_t wb = __shfl_sync(FULL, wbase, take ? (d >> 5) : 0u);
+        if (take) {
+            const uint32_t rank = wb + __popc(s.bitmap[d >> 5] & ((1u << (d & 31)) - 1));
+            s.ins[rank] = kk;
+            s.ins_cnt[rank] = (uint16_t)dtv_count(v);
+        }
+    }
+    __syncwarp();
     // 5. replay both maps (forward map first, the order saQuerySeedSetRef
     //    walks); the count table and per-k-mer arrays are dead from here
     SeedMem sm{};
