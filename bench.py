@@ -55,10 +55,14 @@ DEFAULT_WORKLOAD = "se150_uneven_3gbp"
 # reported only while the hash of these files equals the one it was captured with.
 KERNEL_SOURCES = ("fame_gb300/csrc/seed.cuh", "fame_gb300/csrc/kernels.cuh", "fame_gb300/csrc/dev_common.cuh",
                   "fame_gb300/csrc/seedhash.h", "fame_gb300/csrc/qgram.h", "fame_gb300/csrc/editscan.h")
-# ncu figures per workload: DRAM bytes (read + write) of one steady-state k_seed
-# launch and the ALU-pipe utilisation of the two ALU-bound kernels, with the
-# source hash and the profile that holds the capture command.
-NCU_FIGURES = {}
+# ncu figures per workload: DRAM bytes (read + write) of the seeding launches
+# of one steady-state chunk and the ALU-pipe utilisation of the two ALU-bound
+# kernels, with the source hash and the profile that holds the capture command.
+NCU_FIGURES = {
+    "se150_uneven_3gbp": {"source_hash": "16eff2ef9d6f7da9", "seed_traffic_per_step": 3299303936,
+                          "shiftand_alu": 0.5597, "dp_alu": 0.7052,
+                          "profile": "profiles/seeding_se150_uneven_3gbp.md"},
+}
 
 
 def kernel_source_hash() -> str:
@@ -526,7 +530,7 @@ def run_gb300(args):
     fig = NCU_FIGURES.get(args.workload) if not args.reads else None
     src_hash = kernel_source_hash()
     fig_ok = bool(fig) and fig.get("source_hash") == src_hash
-    traffic = fig["seed_traffic_per_launch"] if fig_ok else None
+    traffic = fig["seed_traffic_per_step"] if fig_ok else None
     out = {
         "metric": METRIC, "value": total_reads / t_max, "unit": "reads/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
@@ -553,12 +557,12 @@ def run_gb300(args):
                                        "global": int(tiers[2]), "large_capacity": int(tiers[3]),
                                        "replayed_orders": int(tiers[4])},
                    "candidate_overflow_reruns": reruns},
-        "roofline": {"kernel": "k_seed (index gathers)", "bound": "hbm", "achieved": gbps, "peak": hbm,
+        "roofline": {"kernel": "seeding (k_seed_mid and the other seeding tiers: index gathers)", "bound": "hbm", "achieved": gbps, "peak": hbm,
                      "unit": "GB/s", "frac": gbps / hbm, "traffic": traffic,
                      "dram_achieved": traffic / (seed_s / args.steps) / 1e9 if (traffic and seed_s > 0) else None,
                      "note": "algorithmic bytes = 8 B bucket bounds + 4 B per bucket entry per k-mer lookup, "
-                             "counted on the device; peak %s; traffic = DRAM read + write of one steady-state "
-                             "launch from ncu (%s)" % (src, fig["profile"] if fig_ok else
+                             "counted on the device; peak %s; traffic = DRAM read + write of the seeding launches "
+                             "of one steady-state chunk from ncu (%s)" % (src, fig["profile"] if fig_ok else
                                                        "no capture of the current kernel sources")},
         "alu_bound_kernels": {
             "k_shiftand": {"stage_ms": 1e3 * st["shift_and"] / args.steps,
