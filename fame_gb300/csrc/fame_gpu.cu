@@ -76,7 +76,8 @@ struct fame_gpu {
     PeTaskRec* d_pe_recs = nullptr;      // per pair orientation
     uint64_t cap_pe_recs = 0;
     uint8_t* d_pe_heavy = nullptr;       // global scratch of k_pe_heavy
-    uint8_t* d_pe_mid2 = nullptr;        // global scratch of the second paired middle tier (PE_MID)
+    uint8_t* d_pe_mid = nullptr;         // global scratch of the paired middle tiers (PE_MID_S, then PE_MID)
+    uint8_t* d_pe_mid2 = nullptr;
     uint64_t pe_mid_warp_bytes = 0, pe_mid2_warp_bytes = 0;
     uint32_t pe_mid_warps = 0, pe_mid2_warps = 0;
     uint64_t pe_heavy_warp_bytes = 0;
@@ -267,6 +268,7 @@ extern "C" int fame_gpu_close(fame_gpu* g)
     dev_free(g->d_dp_orient); dev_free(g->d_heavy); dev_free(g->d_heavy2); dev_free(g->d_ctr); dev_free(g->d_meth);
     dev_free(g->hs.base);
     dev_free(g->ms.base);
+    dev_free(g->d_pe_mid);
     dev_free(g->d_pe_mid2);
     dev_free(g->d_meth16);
     dev_free(g->d_pe_heavy);
@@ -548,13 +550,6 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
         if (off[17] - off[11] < PE_KMER_AREA || hoff[17] - hoff[11] < PE_KMER_AREA ||
             moff[17] - moff[11] < PE_KMER_AREA || m2off[17] - m2off[11] < PE_KMER_AREA)
             return fail(set_err(g, FAME_ERR_CUDA, "paired layout: k-mer area too small"));
-        // the first paired middle tier keeps its working set in shared memory, one warp per block
-        if (cudaFuncSetAttribute(k_pe_seed_mid, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)g->pe_mid_warp_bytes) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pe_seed_mid, 32, g->pe_mid_warp_bytes) != cudaSuccess ||
-            nb < 1)
-            return fail(set_err(g, FAME_ERR_CUDA, "k_pe_seed_mid does not fit an SM"));
-        g->pe_mid_warps = (uint32_t)(g->sm_count * nb);
         const size_t pe_smem = PE_SEED_WARPS * g->pe_warp_bytes;   // the largest layout (mates up to 255 bases)
         if (cudaFuncSetAttribute(k_pe_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pe_smem) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pe_seed, 32 * PE_SEED_WARPS, pe_smem) != cudaSuccess || nb < 1)
@@ -795,8 +790,10 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
     cb.ctr = g->d_ctr;
     cb.heavy = g->d_heavy;
     cb.heavy2 = g->d_heavy2;
-    if (!g->d_pe_mid2) {
+    if (!g->d_pe_mid) {
+        g->pe_mid_warps = (uint32_t)g->sm_count * 16;
         g->pe_mid2_warps = (uint32_t)g->sm_count * 4;
+        CK(cudaMalloc((void**)&g->d_pe_mid, g->pe_mid_warp_bytes * g->pe_mid_warps));
         CK(cudaMalloc((void**)&g->d_pe_mid2, g->pe_mid2_warp_bytes * g->pe_mid2_warps));
     }
     PeIndex px = g->px;
@@ -850,9 +847,9 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         if (T) cudaEventRecord(g->ev[2], g->stream);
         // the paired middle tiers: cb.heavy2 -> (over PE_MID_S) cb.heavy -> (over PE_MID) per-pair path;
         // cb.heavy takes the per-pair path's list only later, in k_pe_finish
-        k_pe_seed_mid<<<g->pe_mid_warps, 32, g->pe_mid_warp_bytes, g->stream>>>(
-            g->ix, px, cb, g->d_pe_recs, nullptr, g->pe_mid_warp_bytes, PE_MID_S, cb.heavy2, CTR_HEAVY2, CTR_QMID,
-            cb.heavy, CTR_HEAVY3);
+        k_pe_seed_mid<<<g->pe_mid_warps / 4, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_recs, g->d_pe_mid,
+                                                                  g->pe_mid_warp_bytes, PE_MID_S, cb.heavy2,
+                                                                  CTR_HEAVY2, CTR_QMID, cb.heavy, CTR_HEAVY3);
         k_pe_seed_mid<<<g->pe_mid2_warps / 4, 128, 0, g->stream>>>(g->ix, px, cb, g->d_pe_recs, g->d_pe_mid2,
                                                                    g->pe_mid2_warp_bytes, PE_MID, cb.heavy,
                                                                    CTR_HEAVY3, CTR_QMID2, nullptr, 0);

@@ -169,7 +169,7 @@ constexpr PeCaps PE_LIGHT{64, 256, 256 + NBHD - 1, 64, 0, 320, PE_KMAX};
 // about three entries in a bucket and a few hundred keys in a mate's map.
 // The first holds the common pair with small tables (the value-table sweeps
 // of a pair cost in proportion to vcap), the second the rest.
-constexpr PeCaps PE_MID_S{256, 1024, 1024 + NBHD - 1 + 64, 256, 0, 512, PE_KMAX};
+constexpr PeCaps PE_MID_S{256, 1024, 1024 + NBHD - 1 + 64, 256, 0, 2048, PE_KMAX};
 constexpr PeCaps PE_MID{1024, 4096, 4096 + NBHD - 1 + 64, 256, 0, 4096, PE_KMAX};
 
 __device__ __forceinline__ uint32_t vt_hash(uint32_t k, uint32_t mask) { return (k * 0x9E3779B1u) >> 8 & mask; }
@@ -1541,21 +1541,18 @@ __global__ void k_pe_seed(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs
 }
 
 // Stage A of a paired middle tier: the pairs of `list` (its length in counter
-// ctr_in) with the caps of a genome-scale index, warp per pair, pairs taken
-// from a work queue (counter ctr_q).  Working memory: warp_bytes of dynamic
-// shared memory when scratch is null (blocks of one warp), else global
-// scratch, warp_bytes per warp.  A pair over these caps goes to `spill`
-// (counter ctr_spill) for the next tier, or, without one, is marked for the
-// per-pair path (k_pe_heavy).
+// ctr_in) with the caps of a genome-scale index, working memory in global
+// scratch (warp_bytes per warp), warp per pair, pairs taken from a work queue
+// (counter ctr_q).  A pair over these caps goes to `spill` (counter
+// ctr_spill) for the next tier, or, without one, is marked for the per-pair
+// path (k_pe_heavy).
 __global__ void k_pe_seed_mid(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs, uint8_t* scratch,
                               uint64_t warp_bytes, PeCaps caps, const uint32_t* list, int ctr_in, int ctr_q,
                               uint32_t* spill, int ctr_spill)
 {
-    extern __shared__ __align__(16) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const PeMem s = pe_mem(scratch ? scratch + (uint64_t)wid * warp_bytes : smem + (threadIdx.x >> 5) * warp_bytes,
-                           caps);
+    const PeMem s = pe_mem(scratch + (uint64_t)wid * warp_bytes, caps);
     const uint32_t npairs = (uint32_t)cb.ctr[ctr_in];
     while (true) {
         uint32_t k = 0;
