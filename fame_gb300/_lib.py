@@ -71,7 +71,8 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_fastq_close", "fame_queue_stage", "fame_queue_submit_staged", "fame_match_fastq",
            "fame_match_fastq_paired", "fame_index_write", "fame_gpu_index_bytes", "fame_queue_wait",
            "fame_gpu_set_seed_tier", "fame_gpu_autotune", "fame_gpu_load_tuning",
-           "fame_gpu_seed_tier_counts", "fame_gpu_map_order_probe", "fame_gpu_pair_stage_times"]
+           "fame_gpu_seed_tier_counts", "fame_gpu_map_order_probe", "fame_gpu_pair_stage_times",
+           "fame_gpu_open_layout", "fame_gpu_rec_layout"]
 
 _lib = None
 
@@ -95,6 +96,8 @@ def lib(build_if_missing: bool = True):
     L.fame_index_cpg_start.argtypes = [_P, _P, C.c_uint64]
     L.fame_index_cpg_start.restype = C.c_uint64
     L.fame_gpu_open.argtypes = [_P, C.c_int, _P]
+    L.fame_gpu_open_layout.argtypes = [_P, C.c_int, C.c_int, _P]
+    L.fame_gpu_rec_layout.argtypes = [_P, _P, _P]
     L.fame_gpu_close.argtypes = [_P]
     L.fame_gpu_last_error.argtypes = [_P]
     L.fame_gpu_last_error.restype = C.c_char_p
@@ -270,11 +273,21 @@ class HostIndex:
 class GpuMatcher:
     """The device context: index resident in HBM, chunk matching, tallies."""
 
-    def __init__(self, index: HostIndex, device: int = 0):
+    REC_AUTO, REC_DENSE, REC_HASHED = 0, 1, 2
+
+    def __init__(self, index: HostIndex, device: int = 0, rec_layout: int = 0):
+        """rec_layout: REC_AUTO (hashed bucket records when at most a quarter
+        of the buckets are non-empty), REC_DENSE or REC_HASHED."""
         self.index = index
         self.h = _P()
-        _check(lib().fame_gpu_open(C.byref(index.view), device, C.byref(self.h)))
+        _check(lib().fame_gpu_open_layout(C.byref(index.view), device, rec_layout, C.byref(self.h)))
         self.n_cpg = index.n_cpg
+
+    def rec_layout(self):
+        """(layout, record slots, non-empty buckets) of the device index."""
+        slots, nonempty = C.c_uint64(), C.c_uint64()
+        layout = lib().fame_gpu_rec_layout(self.h, C.byref(slots), C.byref(nonempty))
+        return layout, slots.value, nonempty.value
 
     def close(self):
         if self.h:

@@ -21,15 +21,25 @@ namespace fame {
 //            chromosomes concatenated at 32-base aligned offsets
 //   gnmask : one bit per base, set for N
 //   win    : {startPos, chrom, startInd, endInd} per window (metaWindows)
-constexpr uint32_t REC_INLINE = 6;   // bucket entries held in a bucket's record
+constexpr uint32_t REC_INLINE = 6;   // bucket entries held in a dense bucket record
+constexpr uint32_t EMPTY_REC_KEY = 0xffffffffu;   // key word of an empty hashed slot
 
 struct DevIndex {
     uint32_t readlen;
     uint32_t n_chrom;
-    // bucket records, 32 bytes per bucket k: rec[2k] = {start, size, e0, e1},
-    // rec[2k + 1] = {e2, e3, e4, e5} (the bucket's first REC_INLINE entries,
-    // 0 past its size); one aligned sector holds a lookup for most buckets
+    // bucket records, 32 bytes each, in one of two layouts:
+    //  dense (rec_hashed == 0): record k of bucket k, rec[2k] = {start, size,
+    //    e0, e1}, rec[2k + 1] = {e2, e3, e4, e5} (the bucket's first
+    //    REC_INLINE entries, 0 past its size);
+    //  hashed (rec_hashed == 1, small genomes): the non-empty buckets only,
+    //    open addressing with linear probing over rec_mask + 1 slots from
+    //    rec_slot(k), rec[2h] = {start, size, e0, e1}, rec[2h + 1] = {e2, e3,
+    //    e4, k} (five entries inline), an empty slot holding EMPTY_REC_KEY
+    //    in its key word.
+    // Either way one aligned sector holds a lookup for most buckets.
     const uint4* rec;
+    uint32_t rec_mask;
+    uint32_t rec_hashed;
     const uint32_t* entry;
     const uint32_t* gpack;
     const uint32_t* gnmask;
@@ -41,6 +51,36 @@ struct DevIndex {
     uint64_t n_cpg;
     uint64_t n_win;
 };
+
+// Home slot of bucket k in the hashed record layout.
+__host__ __device__ __forceinline__ uint32_t rec_slot(uint32_t k, uint32_t mask)
+{
+    return (k * 0x9E3779B1u) & mask;
+}
+
+// Record slot of bucket k and its first half {start, size, e0, e1} (zero for
+// an empty bucket); the second half is at rec[2 * slot + 1].
+__device__ __forceinline__ uint4 rec_lookup(const DevIndex& ix, uint32_t k, uint32_t& slot)
+{
+    if (!ix.rec_hashed) {
+        slot = k;
+        return __ldg(ix.rec + 2ull * k);
+    }
+    // at most half the slots are used, so a probe ends at the key or at an
+    // empty slot well before it has seen the whole table
+    uint32_t h = rec_slot(k, ix.rec_mask);
+    for (uint32_t i = 0; i <= ix.rec_mask; ++i) {
+        const uint32_t sk = __ldg(&ix.rec[2ull * h + 1].w);   // same sector as the first half
+        if (sk == k) {
+            slot = h;
+            return __ldg(ix.rec + 2ull * h);
+        }
+        if (sk == EMPTY_REC_KEY) break;
+        h = (h + 1) & ix.rec_mask;
+    }
+    slot = h;
+    return make_uint4(0, 0, 0, 0);
+}
 
 // Per-chunk buffers.
 struct ChunkBufs {

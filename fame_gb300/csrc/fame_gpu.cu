@@ -32,6 +32,9 @@ struct fame_gpu {
     DevIndex ix{};
     std::vector<void*> index_allocs;
     uint64_t index_bytes = 0;            // device bytes of the resident index tables
+    int rec_layout = FAME_REC_DENSE;     // bucket-record layout (FAME_REC_DENSE / FAME_REC_HASHED)
+    uint64_t rec_slots = 0;              // records (dense: HTABSIZE; hashed: slots of the table)
+    uint64_t nonempty_buckets = 0;
     uint64_t n_cpg = 0;
     uint32_t max_bucket = 0;
     // chunk buffers
@@ -283,7 +286,12 @@ extern "C" int fame_gpu_close(fame_gpu* g)
 
 extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** out)
 {
-    if (!v || !out) return FAME_ERR_ARG;
+    return fame_gpu_open_layout(v, device, FAME_REC_AUTO, out);
+}
+
+extern "C" int fame_gpu_open_layout(const fame_index_view* v, int device, int layout, fame_gpu** out)
+{
+    if (!v || !out || layout < FAME_REC_AUTO || layout > FAME_REC_HASHED) return FAME_ERR_ARG;
     *out = nullptr;
     fame_gpu* g = new (std::nothrow) fame_gpu();
     if (!g) return FAME_ERR_NOMEM;
@@ -359,11 +367,42 @@ extern "C" int fame_gpu_open(const fame_index_view* v, int device, fame_gpu** ou
             return fail(set_err(g, FAME_ERR_CUDA, "k-mer upload failed"));
     }
     g->ix.entry = d_entry;
-    // ---- bucket records: start, size and the first entries of each bucket in one sector
+    // ---- bucket records: start, size and the first entries of each bucket in one sector;
+    //      dense (one record per bucket) or hashed (the non-empty buckets only)
     {
+        unsigned long long* d_cnt;
+        if (cudaMalloc((void**)&d_cnt, 8) != cudaSuccess) return fail(set_err(g, FAME_ERR_NOMEM, "alloc"));
+        unsigned long long nne = 0;
+        cudaMemsetAsync(d_cnt, 0, 8, g->stream);
+        k_count_nonempty<<<g->sm_count * 8, 256, 0, g->stream>>>(d_tab, HTABSIZE, d_cnt);
+        cudaMemcpyAsync(&nne, d_cnt, 8, cudaMemcpyDeviceToHost, g->stream);
+        const cudaError_t ce = cudaStreamSynchronize(g->stream);
+        cudaFree(d_cnt);
+        if (ce != cudaSuccess) return fail(set_err(g, FAME_ERR_CUDA, "bucket count failed"));
+        g->nonempty_buckets = nne;
+        uint64_t slots = 1024;
+        while (slots < 2 * nne) slots <<= 1;
+        const bool hashed = layout == FAME_REC_HASHED || (layout == FAME_REC_AUTO && 4 * nne <= HTABSIZE);
+        if (hashed && slots > HTABSIZE)
+            return fail(set_err(g, FAME_ERR_INDEX, "hashed bucket records need at most HTABSIZE / 2 non-empty buckets"));
         uint4* d_rec;
-        if ((rc = alloc_idx((void**)&d_rec, HTABSIZE * 32))) return fail(rc);
-        k_build_rec<<<g->sm_count * 8, 256, 0, g->stream>>>(d_tab, d_entry, HTABSIZE, d_rec);
+        if (hashed) {
+            if ((rc = alloc_idx((void**)&d_rec, slots * 32))) return fail(rc);
+            cudaMemsetAsync(d_rec, 0xff, slots * 32, g->stream);
+            k_build_rec_hashed<<<g->sm_count * 8, 256, 0, g->stream>>>(d_tab, d_entry, HTABSIZE, d_rec,
+                                                                        (uint32_t)(slots - 1));
+            g->ix.rec_mask = (uint32_t)(slots - 1);
+            g->ix.rec_hashed = 1;
+            g->rec_layout = FAME_REC_HASHED;
+            g->rec_slots = slots;
+        } else {
+            if ((rc = alloc_idx((void**)&d_rec, HTABSIZE * 32))) return fail(rc);
+            k_build_rec<<<g->sm_count * 8, 256, 0, g->stream>>>(d_tab, d_entry, HTABSIZE, d_rec);
+            g->ix.rec_mask = (uint32_t)HTAB_MASK;
+            g->ix.rec_hashed = 0;
+            g->rec_layout = FAME_REC_DENSE;
+            g->rec_slots = HTABSIZE;
+        }
         if (cudaGetLastError() != cudaSuccess) return fail(set_err(g, FAME_ERR_CUDA, "bucket record build failed"));
         g->ix.rec = d_rec;
     }
@@ -1095,6 +1134,14 @@ extern "C" int fame_gpu_seed_tier_counts(const fame_gpu* g, uint64_t* out)
 extern "C" int fame_gpu_last_launches(const fame_gpu* g) { return g ? g->launches : 0; }
 
 extern "C" uint64_t fame_gpu_index_bytes(const fame_gpu* g) { return g ? g->index_bytes : 0; }
+
+extern "C" int fame_gpu_rec_layout(const fame_gpu* g, uint64_t* slots, uint64_t* nonempty)
+{
+    if (!g) return FAME_ERR_ARG;
+    if (slots) *slots = g->rec_slots;
+    if (nonempty) *nonempty = g->nonempty_buckets;
+    return g->rec_layout;
+}
 
 extern "C" int fame_gpu_set_seed_tier(fame_gpu* g, int mode)
 {

@@ -1191,6 +1191,37 @@ __global__ void k_pack_tallies(const uint32_t* meth, uint64_t n4, uint16_t* out)
         out[i] = (uint16_t)(meth[i] & 0xffffu);
 }
 
+// The hashed record layout (DevIndex::rec, small genomes) of buckets
+// 0 .. n - 1; rec (mask + 1 slots) starts with every word 0xffffffff.
+__global__ void k_build_rec_hashed(const uint32_t* tab, const uint32_t* entry, uint64_t n, uint4* rec, uint32_t mask)
+{
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b0 = tab[k], sz = tab[k + 1] - b0;
+        if (sz == 0) continue;
+        uint32_t e[5];
+#pragma unroll
+        for (uint32_t j = 0; j < 5; ++j) e[j] = j < sz ? entry[b0 + j] : 0u;
+        // the table has at least twice as many slots as non-empty buckets
+        uint32_t h = rec_slot((uint32_t)k, mask);
+        for (uint32_t i = 0; i <= mask && atomicCAS(&rec[2ull * h + 1].w, EMPTY_REC_KEY, (uint32_t)k) != EMPTY_REC_KEY; ++i)
+            h = (h + 1) & mask;
+        rec[2ull * h] = make_uint4(b0, sz, e[0], e[1]);
+        rec[2ull * h + 1].x = e[2];
+        rec[2ull * h + 1].y = e[3];
+        rec[2ull * h + 1].z = e[4];
+    }
+}
+
+// Non-empty buckets of the index.
+__global__ void k_count_nonempty(const uint32_t* tab, uint64_t n, unsigned long long* out)
+{
+    uint32_t c = 0;
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        c += tab[k + 1] > tab[k] ? 1u : 0u;
+    for (int d = 16; d > 0; d >>= 1) c += __shfl_xor_sync(0xffffffffu, c, d);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, (unsigned long long)c);
+}
+
 // Largest bucket of the index (sizes the heavy path).
 __global__ void k_max_bucket(const uint32_t* tab, uint64_t n, unsigned int* out)
 {

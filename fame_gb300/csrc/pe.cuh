@@ -281,7 +281,8 @@ __device__ uint32_t pe_kmers(const DevIndex& ix, const PeIndex& px, const PeMem&
         const uint32_t p = lane + 32 * jj;
         if (p < nk) {
             const uint32_t key = sh_prefix_hash([&](uint32_t j) { return P[j]; }, p, HTAB_MASK);
-            const uint2 t = __ldg((const uint2*)(ix.rec + 2ull * key));   // {start, size}
+            uint32_t slot;
+            const uint4 t = rec_lookup(ix, key, slot);   // {start, size, ...}
             b0[jj] = t.x;
             b1[jj] = t.x + t.y;
         }

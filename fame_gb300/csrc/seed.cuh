@@ -442,8 +442,8 @@ __device__ int seed_task(const DevIndex& ix, const ChunkBufs& cb, const SeedMem&
         for (int j = 0; j < KPL; ++j) {
             const uint32_t p = lane + 32 * j;
             if (p < nk) {
-                const uint32_t key = s.kst[p];
-                const uint4 t = __ldg(ix.rec + 2ull * key);
+                uint32_t slot;
+                const uint4 t = rec_lookup(ix, s.kst[p], slot);
                 b0[j] = t.x;
                 e0[j] = t.z;
                 b1[j] = t.x + t.y;
@@ -859,10 +859,21 @@ __device__ __forceinline__ int seed_task_rec(const DevIndex& ix, const ChunkBufs
         const uint32_t p = lane + 32 * jj;
         key[jj] = p < nk ? sh_prefix_hash([&](uint32_t j) { return P[j]; }, p, HTAB_MASK) : 0u;
     }
+    if (!ix.rec_hashed) {
 #pragma unroll
-    for (int jj = 0; jj < KPL; ++jj) {
-        const uint32_t p = lane + 32 * jj;
-        lo[jj] = p < nk ? __ldg(ix.rec + 2ull * key[jj]) : make_uint4(0, 0, 0, 0);
+        for (int jj = 0; jj < KPL; ++jj) {
+            const uint32_t p = lane + 32 * jj;
+            lo[jj] = p < nk ? __ldg(ix.rec + 2ull * key[jj]) : make_uint4(0, 0, 0, 0);
+        }
+    } else {
+        // hashed records (small genomes): probe, then keep the slot where the key was
+#pragma unroll
+        for (int jj = 0; jj < KPL; ++jj) {
+            const uint32_t p = lane + 32 * jj;
+            uint32_t slot = 0;
+            lo[jj] = p < nk ? rec_lookup(ix, key[jj], slot) : make_uint4(0, 0, 0, 0);
+            key[jj] = slot;
+        }
     }
     __syncwarp();   // the prefix hashes are dead: the count table may take their memory
     for (uint32_t i = lane; i < DT; i += 32) {
@@ -915,8 +926,10 @@ __device__ __forceinline__ int seed_task_rec(const DevIndex& ix, const ChunkBufs
         const uint32_t op0 = p < nk ? s.kpre[p] : 0u;   // dense index of the bucket's first op
         uint32_t q0 = lo[jj].z, q1 = lo[jj].w, q2 = 0, q3 = 0, q4 = 0, q5 = 0;
         if (sz > 2) {
-            const uint4 hi = __ldg(ix.rec + 2ull * key[jj] + 1);
-            q2 = hi.x; q3 = hi.y; q4 = hi.z; q5 = hi.w;
+            const uint4 hi = __ldg(ix.rec + 2ull * key[jj] + 1);   // key[jj]: the record's slot
+            q2 = hi.x; q3 = hi.y; q4 = hi.z;
+            // a hashed slot holds five entries (its last word is the key)
+            q5 = !ix.rec_hashed ? hi.w : (sz > 5 ? __ldg(ix.entry + start + 5) : 0u);
         }
         uint32_t jmax = sz;
 #pragma unroll

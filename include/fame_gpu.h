@@ -125,8 +125,23 @@ void fame_index_free(fame_host_index* ix);
 uint64_t fame_index_cpg_start(const fame_host_index* ix, fame_cpg* out, uint64_t cap);
 
 /* ---- device context ----------------------------------------------------- */
-/* Copy the index into HBM on `device` (resident until fame_gpu_close). */
+/* Copy the index into HBM on `device` (resident until fame_gpu_close).
+ * Replaces the index load of main.cpp (RefGenome::load / the index read) as
+ * far as the matching path is concerned: the tables stay on the device. */
 int fame_gpu_open(const fame_index_view* ix, int device, fame_gpu** out);
+
+/* Layout of the device's bucket records (no counterpart in the reference;
+ * results do not depend on it).  Each record holds a bucket's tabIndex start,
+ * its size and its first entries in one 32-byte sector. */
+#define FAME_REC_AUTO   0  /* hashed when the non-empty buckets are at most HTABSIZE / 4 */
+#define FAME_REC_DENSE  1  /* one record per bucket: 32 GiB whatever the genome */
+#define FAME_REC_HASHED 2  /* the non-empty buckets only, 2 to 4 slots each */
+/* fame_gpu_open with a chosen record layout (FAME_ERR_INDEX when hashed is
+ * asked for and more than HTABSIZE / 2 buckets are non-empty). */
+int fame_gpu_open_layout(const fame_index_view* ix, int device, int layout, fame_gpu** out);
+/* The context's record layout (FAME_REC_DENSE or FAME_REC_HASHED), its record
+ * count and the index's non-empty buckets (either pointer may be NULL). */
+int fame_gpu_rec_layout(const fame_gpu* g, uint64_t* slots, uint64_t* nonempty);
 int fame_gpu_close(fame_gpu* g);
 const char* fame_gpu_last_error(const fame_gpu* g);
 
