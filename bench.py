@@ -84,7 +84,47 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=60000, help="reads (pairs) of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fastq", action="store_true", help="skip the whole-file leg")
+    p.add_argument("--index-build", default="gpu", choices=["gpu", "host"],
+                   help="where the GB300 arms build the index (identical tables either way)")
+    p.add_argument("--index-check", action="store_true",
+                   help="build the index both ways, time both and compare every table")
     return p.parse_args()
+
+
+def build_index(args, seqs, readlen, device):
+    """The index for a GB300 arm: fame_index_build_gpu (default) or the
+    host build; with --index-check both, timed, every table compared.
+    Returns (index, seconds, report)."""
+    from fame_gb300 import HostIndex
+    gpu_first = args.index_build == "gpu"
+
+    def one(on_gpu):
+        t0 = time.time()
+        hi = (HostIndex.build_gpu(seqs, readlen=readlen, device=device) if on_gpu
+              else HostIndex.build(seqs, readlen=readlen, threads=0))
+        return hi, time.time() - t0
+
+    hi, t = one(gpu_first)
+    rep = {"where": args.index_build, "seconds": t}
+    if args.index_check:
+        other, t2 = one(not gpu_first)
+        rep["gpu_seconds"], rep["host_seconds"] = (t, t2) if gpu_first else (t2, t)
+        rep["host_threads"] = os.cpu_count()
+        rep["identical"] = same_index(hi, other)
+        other.close()
+    return hi, t, rep
+
+
+def same_index(a, b):
+    """Every table of two host indexes equal (bucket offsets, entries, T
+    masks, strandTable, windows, CpGs, filtered k-mers and their order)."""
+    import numpy as np
+    from fame_gb300._lib import HTABSIZE
+    ta, tb = a.tables(sparse=False), b.tables(sparse=False)
+    if any(not np.array_equal(ta[k], tb[k]) for k in ta):
+        return False
+    o32 = [x._arr(x.view.tab_index32, HTABSIZE + 1, np.uint32) for x in (a, b)]
+    return bool(np.array_equal(o32[0], o32[1]) and np.array_equal(a.filtered_order(), b.filtered_order()))
 
 
 # ---------------------------------------------------------------------------
@@ -344,9 +384,7 @@ def run_gb300(args):
     g = synth.genome_of(args.workload)
     rs, readlen = synth.reads_of(args.workload, g, args.reads)
     t_gen = time.time() - t0
-    t0 = time.time()
-    hi = HostIndex.build(g.seqs, readlen=readlen, threads=0)
-    t_build = time.time() - t0
+    hi, t_build, index_rep = build_index(args, g.seqs, readlen, local)
     genome_bp, n_chrom = int(g.total_len), len(g.seqs)
     del g
     gc.collect()
@@ -574,6 +612,7 @@ def run_gb300(args):
         "host": host_placement(local),
         "clocks": clk.summary(),
         "setup_seconds": {"generate": t_gen, "index_build": t_build, "upload": t_open},
+        "index_build": index_rep,
     }
     for i in used:
         gm.free(dev[i][0])
@@ -651,9 +690,7 @@ def run_gb300_serving(args):
             jobs.append(Job("cell%d" % i, seq[int(o[0]):int(o[-1])], o - o[0], arrival=float(arrivals[i])))
             a += int(n)
     t_gen = time.time() - t0
-    t0 = time.time()
-    hi = HostIndex.build(g.seqs, readlen=100, threads=0)
-    t_build = time.time() - t0
+    hi, t_build, index_rep = build_index(args, g.seqs, 100, 0)
     genome_bp = int(g.total_len)
     del g
     gc.collect()
@@ -689,6 +726,7 @@ def run_gb300_serving(args):
         "results_identical_to_plain": bool(same),
         "timing": "host clock over the whole trace (arrival-driven); per-job latency = completion - arrival",
         "clocks": clk.summary(), "setup_seconds": {"generate": t_gen, "index_build": t_build},
+        "index_build": index_rep,
     }
     emit(out)
 
@@ -707,9 +745,7 @@ def run_gb300_pe(args):
     g = synth.genome_of(args.workload)
     r1, r2 = synth.pairs_of(args.workload, g, args.reads)
     t_gen = time.time() - t0
-    t0 = time.time()
-    hi = HostIndex.build(g.seqs, readlen=100, threads=0)
-    t_build = time.time() - t0
+    hi, t_build, index_rep = build_index(args, g.seqs, 100, 0)
     genome_bp = int(g.total_len)
     del g
     gc.collect()
@@ -822,6 +858,7 @@ def run_gb300_pe(args):
         "stage_ms_one_chunk": pe_stages,
         "clocks": clk.summary(),
         "setup_seconds": {"generate": t_gen, "index_build": t_build, "upload": t_open},
+        "index_build": index_rep,
     }
     for d_s, d_o, _ in dev.values():
         gm.free(d_s)

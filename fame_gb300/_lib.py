@@ -72,7 +72,7 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_match_fastq_paired", "fame_index_write", "fame_gpu_index_bytes", "fame_queue_wait",
            "fame_gpu_set_seed_tier", "fame_gpu_autotune", "fame_gpu_load_tuning",
            "fame_gpu_seed_tier_counts", "fame_gpu_map_order_probe", "fame_gpu_pair_stage_times",
-           "fame_gpu_open_layout", "fame_gpu_rec_layout"]
+           "fame_gpu_open_layout", "fame_gpu_rec_layout", "fame_index_build_gpu", "fame_index_filtered_order"]
 
 _lib = None
 
@@ -90,11 +90,14 @@ def lib(build_if_missing: bool = True):
     L.fame_index_read.argtypes = [C.c_char_p, _P]
     L.fame_index_write.argtypes = [_P, C.c_char_p]
     L.fame_index_build.argtypes = [C.c_uint32, C.c_uint32, _P, _P, _P, C.c_int, C.c_int, _P]
+    L.fame_index_build_gpu.argtypes = [C.c_uint32, C.c_uint32, _P, _P, _P, C.c_int, C.c_int, _P]
     L.fame_index_view_of.argtypes = [_P, _P]
     L.fame_index_free.argtypes = [_P]
     L.fame_index_free.restype = None
     L.fame_index_cpg_start.argtypes = [_P, _P, C.c_uint64]
     L.fame_index_cpg_start.restype = C.c_uint64
+    L.fame_index_filtered_order.argtypes = [_P, _P, C.c_uint64]
+    L.fame_index_filtered_order.restype = C.c_uint64
     L.fame_gpu_open.argtypes = [_P, C.c_int, _P]
     L.fame_gpu_open_layout.argtypes = [_P, C.c_int, C.c_int, _P]
     L.fame_gpu_rec_layout.argtypes = [_P, _P, _P]
@@ -181,7 +184,16 @@ class HostIndex:
 
     @classmethod
     def build(cls, chrom_seqs, readlen: int = 100, names=None, noloss: bool = False, threads: int = 0) -> "HostIndex":
-        """Index build from chromosome sequences (uint8 arrays or bytes)."""
+        """Index build from chromosome sequences (uint8 arrays or bytes) on the host cores."""
+        return cls._build(lib().fame_index_build, chrom_seqs, readlen, names, noloss, threads)
+
+    @classmethod
+    def build_gpu(cls, chrom_seqs, readlen: int = 100, names=None, noloss: bool = False, device: int = 0) -> "HostIndex":
+        """The same index built on a GPU (identical tables)."""
+        return cls._build(lib().fame_index_build_gpu, chrom_seqs, readlen, names, noloss, device)
+
+    @classmethod
+    def _build(cls, fn, chrom_seqs, readlen, names, noloss, last):
         arrs = [np.ascontiguousarray(np.frombuffer(s, np.uint8) if isinstance(s, (bytes, bytearray)) else s,
                                      dtype=np.uint8) for s in chrom_seqs]
         ptrs = (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
@@ -191,8 +203,8 @@ class HostIndex:
             enc = [n.encode() for n in names]
             nm = (C.c_char_p * len(enc))(*enc)
         h = _P()
-        _check(lib().fame_index_build(readlen, len(arrs), C.cast(ptrs, _P), _ptr(lens),
-                                      C.cast(nm, _P) if nm is not None else None, int(noloss), threads, C.byref(h)))
+        _check(fn(readlen, len(arrs), C.cast(ptrs, _P), _ptr(lens), C.cast(nm, _P) if nm is not None else None,
+                  int(noloss), last, C.byref(h)))
         return cls(h)
 
     def close(self):
@@ -220,6 +232,13 @@ class HostIndex:
     @property
     def n_cpg(self) -> int:
         return int(self.view.n_cpg)
+
+    def filtered_order(self):
+        """filteredKmers in the order the reference's set received them."""
+        n = lib().fame_index_filtered_order(self.h, None, 0)
+        out = np.zeros(int(n), np.uint64)
+        lib().fame_index_filtered_order(self.h, _ptr(out), n)
+        return out
 
     def chrom_names(self):
         v = self.view

@@ -237,6 +237,80 @@ uint32_t tmask_repro(const fame_host_index& ix, const BaseBits& bb, uint32_t w, 
 // ---------------------------------------------------------------------------
 // builder
 // ---------------------------------------------------------------------------
+// readReference and generateWindows: normalised sequences, CpG tables and
+// windows (shared by the host and the device builder).
+void fame::index_build_front(fame_host_index* ix, uint32_t readlen, uint32_t n_chrom, const char* const* seq,
+                             const uint64_t* len, const char* const* names, int T)
+{
+    ix->readlen = readlen;
+    ix->seq.resize(n_chrom);
+    ix->names.resize(n_chrom);
+    // readLine (RefReader_istr.h:48-113): case folding, other letters -> N,
+    // CpGs at C - READLEN + 2 (or at C when too close to the start).
+    std::vector<std::vector<fame_cpg>> cpg(n_chrom), cpgs(n_chrom);
+    parallel_for(n_chrom, std::min<int>(T, (int)n_chrom), [&](uint64_t b, uint64_t e, int) {
+        for (uint64_t c = b; c < e; ++c) {
+            std::string& s = ix->seq[c];
+            s.resize(len[c]);
+            bool lastC = false;
+            for (uint64_t i = 0; i < len[c]; ++i) {
+                const char ch = seq[c][i];
+                switch (ch) {
+                    case 'g': case 'G':
+                        if (lastC) {
+                            if (i >= readlen - 2) cpg[c].push_back({(uint8_t)c, (uint32_t)i - readlen + 1});
+                            else cpgs[c].push_back({(uint8_t)c, (uint32_t)i - 1});
+                            lastC = false;
+                        }
+                        s[i] = 'G';
+                        break;
+                    case 'c': case 'C': s[i] = 'C'; lastC = true; break;
+                    case 'a': case 'A': s[i] = 'A'; lastC = false; break;
+                    case 't': case 'T': s[i] = 'T'; lastC = false; break;
+                    default: s[i] = 'N'; lastC = false; break;
+                }
+            }
+            ix->names[c] = names && names[c] ? std::string(names[c]) : ("chr" + std::to_string(c + 1));
+        }
+    });
+    for (uint32_t c = 0; c < n_chrom; ++c) {
+        ix->cpg.insert(ix->cpg.end(), cpg[c].begin(), cpg[c].end());
+        ix->cpg_start.insert(ix->cpg_start.end(), cpgs[c].begin(), cpgs[c].end());
+    }
+    // generateWindows (RefGenome.cpp:532-567); cpgTable[ci] is read even at
+    // ci == size there, which this treats as "no CpG".
+    {
+        const uint64_t ncpg = ix->cpg.size();
+        uint64_t ci = 0;
+        for (uint32_t c = 0; c < n_chrom; ++c) {
+            for (uint32_t ws = 0; ws < ix->seq[c].size(); ws = ws + WINLEN - readlen) {
+                const uint32_t we = ws + WINLEN;
+                uint32_t si = CPGDUMMY, ei = CPGDUMMY;
+                while (ci < ncpg && ix->cpg[ci].chrom == c && ix->cpg[ci].pos <= we) {
+                    if (si == CPGDUMMY) si = (uint32_t)ci;
+                    ei = (uint32_t)ci;
+                    ++ci;
+                }
+                while (ci > 0 && ci < ncpg && ix->cpg[ci].chrom == c && ix->cpg[ci].pos >= we - readlen) --ci;
+                if (ci > 0) ++ci;
+                ix->win.push_back({ws, (uint8_t)c, si, ei});
+            }
+        }
+    }
+}
+
+// filteredKmers from the k-mers in the order the reference's set received
+// them, and the chromosome name order.
+void fame::index_build_finish(fame_host_index* ix, std::vector<uint64_t>&& filtered_order)
+{
+    ix->filtered_order = std::move(filtered_order);
+    ix->filtered = ix->filtered_order;
+    std::sort(ix->filtered.begin(), ix->filtered.end());
+    ix->filtered.erase(std::unique(ix->filtered.begin(), ix->filtered.end()), ix->filtered.end());
+    ix->name_order.resize(ix->seq.size());
+    for (size_t c = 0; c < ix->seq.size(); ++c) ix->name_order[c] = (uint8_t)c;   // readReference inserts in order
+}
+
 extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* const* seq, const uint64_t* len,
                                 const char* const* names, int noloss, int n_threads, fame_host_index** out)
 {
@@ -256,65 +330,11 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
         t_last = now;
     };
     try {
-        ix->readlen = readlen;
-        ix->seq.resize(n_chrom);
-        ix->names.resize(n_chrom);
-        // readLine (RefReader_istr.h:48-113): case folding, other letters -> N,
-        // CpGs at C - READLEN + 2 (or at C when too close to the start).
-        std::vector<std::vector<fame_cpg>> cpg(n_chrom), cpgs(n_chrom);
-        parallel_for(n_chrom, std::min<int>(T, (int)n_chrom), [&](uint64_t b, uint64_t e, int) {
-            for (uint64_t c = b; c < e; ++c) {
-                std::string& s = ix->seq[c];
-                s.resize(len[c]);
-                bool lastC = false;
-                for (uint64_t i = 0; i < len[c]; ++i) {
-                    const char ch = seq[c][i];
-                    switch (ch) {
-                        case 'g': case 'G':
-                            if (lastC) {
-                                if (i >= readlen - 2) cpg[c].push_back({(uint8_t)c, (uint32_t)i - readlen + 1});
-                                else cpgs[c].push_back({(uint8_t)c, (uint32_t)i - 1});
-                                lastC = false;
-                            }
-                            s[i] = 'G';
-                            break;
-                        case 'c': case 'C': s[i] = 'C'; lastC = true; break;
-                        case 'a': case 'A': s[i] = 'A'; lastC = false; break;
-                        case 't': case 'T': s[i] = 'T'; lastC = false; break;
-                        default: s[i] = 'N'; lastC = false; break;
-                    }
-                }
-                ix->names[c] = names && names[c] ? std::string(names[c]) : ("chr" + std::to_string(c + 1));
-            }
-        });
-        for (uint32_t c = 0; c < n_chrom; ++c) {
-            ix->cpg.insert(ix->cpg.end(), cpg[c].begin(), cpg[c].end());
-            ix->cpg_start.insert(ix->cpg_start.end(), cpgs[c].begin(), cpgs[c].end());
-        }
-        phase("sequences, CpGs");
-        // generateWindows (RefGenome.cpp:532-567); cpgTable[ci] is read even at
-        // ci == size there, which this treats as "no CpG".
-        {
-            const uint64_t ncpg = ix->cpg.size();
-            uint64_t ci = 0;
-            for (uint32_t c = 0; c < n_chrom; ++c) {
-                for (uint32_t ws = 0; ws < ix->seq[c].size(); ws = ws + WINLEN - readlen) {
-                    const uint32_t we = ws + WINLEN;
-                    uint32_t si = CPGDUMMY, ei = CPGDUMMY;
-                    while (ci < ncpg && ix->cpg[ci].chrom == c && ix->cpg[ci].pos <= we) {
-                        if (si == CPGDUMMY) si = (uint32_t)ci;
-                        ei = (uint32_t)ci;
-                        ++ci;
-                    }
-                    while (ci > 0 && ci < ncpg && ix->cpg[ci].chrom == c && ix->cpg[ci].pos >= we - readlen) --ci;
-                    if (ci > 0) ++ci;
-                    ix->win.push_back({ws, (uint8_t)c, si, ei});
-                }
-            }
-        }
+        index_build_front(ix, readlen, n_chrom, seq, len, names, T);
+        phase("sequences, CpGs, windows");
         const uint64_t nwin = ix->win.size();
         const BaseBits bb(*ix, T);
-        phase("windows");
+        phase("base bits");
         // pass 1: bucket sizes (estimateTablesizes)
         BigVec<uint32_t> cnt(HTABSIZE + 1);
         parallel_for(HTABSIZE + 1, T, [&](uint64_t b, uint64_t e, int) { std::memset(&cnt[b], 0, (e - b) * 4); });
@@ -489,12 +509,9 @@ extern "C" int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* 
         }
         phase("T masks");
         // threads hold consecutive bucket ranges: their lists in thread order are the scan order
-        for (auto& f : filt) ix->filtered_order.insert(ix->filtered_order.end(), f.begin(), f.end());
-        ix->filtered = ix->filtered_order;
-        std::sort(ix->filtered.begin(), ix->filtered.end());
-        ix->filtered.erase(std::unique(ix->filtered.begin(), ix->filtered.end()), ix->filtered.end());
-        ix->name_order.resize(n_chrom);
-        for (uint32_t c = 0; c < n_chrom; ++c) ix->name_order[c] = (uint8_t)c;   // readReference inserts in order
+        std::vector<uint64_t> order;
+        for (auto& f : filt) order.insert(order.end(), f.begin(), f.end());
+        index_build_finish(ix, std::move(order));
         phase("filtered set");
     } catch (const std::bad_alloc&) {
         delete ix;
@@ -820,4 +837,11 @@ extern "C" uint64_t fame_index_cpg_start(const fame_host_index* ix, fame_cpg* ou
     if (!ix) return 0;
     for (uint64_t i = 0; i < ix->cpg_start.size() && i < cap; ++i) out[i] = ix->cpg_start[i];
     return ix->cpg_start.size();
+}
+
+extern "C" uint64_t fame_index_filtered_order(const fame_host_index* ix, uint64_t* out, uint64_t cap)
+{
+    if (!ix) return 0;
+    for (uint64_t i = 0; i < ix->filtered_order.size() && i < cap; ++i) out[i] = ix->filtered_order[i];
+    return ix->filtered_order.size();
 }

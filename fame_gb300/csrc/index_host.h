@@ -61,3 +61,13 @@ struct fame_host_index {
     std::vector<uint64_t> seq_lens;
     std::vector<const char*> name_ptrs;
 };
+
+namespace fame {
+// readReference and generateWindows (RefReader_istr.h:48-113,
+// RefGenome.cpp:532-567): fills seq, names, cpg, cpg_start and win on T
+// host threads.
+void index_build_front(fame_host_index* ix, uint32_t readlen, uint32_t n_chrom, const char* const* seq,
+                       const uint64_t* len, const char* const* names, int T);
+// filtered_order as given, filtered (sorted, unique) and name_order.
+void index_build_finish(fame_host_index* ix, std::vector<uint64_t>&& filtered_order);
+}  // namespace fame

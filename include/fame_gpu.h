@@ -108,6 +108,14 @@ int fame_index_read(const char* path, fame_host_index** out);
 int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* const* seq, const uint64_t* len,
                      const char* const* names, int noloss, int n_threads, fame_host_index** out);
 
+/* The same index, identical table for table, built on the GPU `device`
+ * (window hashing, bucket fill, bucket order, both filters, compaction and
+ * T masks on the device; the tables come back to host memory).  Needs about
+ * 24 bytes of device memory per k-mer entry plus 12 GiB for the bucket
+ * tables (3 Gbp: about 90 GB).  FAME_ERR_NOMEM when they do not fit. */
+int fame_index_build_gpu(uint32_t readlen, uint32_t n_chrom, const char* const* seq, const uint64_t* len,
+                         const char* const* names, int noloss, int device, fame_host_index** out);
+
 /* Write the index in the --load_index format to <path> and <path>_strands
  * (RefGenome::save, RefGenome.cpp:83-228): the reference's file for the same
  * index byte for byte, except the struct padding bytes (uninitialised there,
@@ -123,6 +131,11 @@ void fame_index_free(fame_host_index* ix);
 /* cpgStartTable (CpGs too close to a chromosome start to be reported,
  * RefReader_istr.h:66-76); returns the count, copies up to cap entries. */
 uint64_t fame_index_cpg_start(const fame_host_index* ix, fame_cpg* out, uint64_t cap);
+/* filteredKmers in the order the reference's unordered_set received them
+ * (RefGenome.cpp:2330; the index writer derives the set's iteration order,
+ * RefGenome.cpp:434-443, from it); returns the count, copies up to cap
+ * entries. */
+uint64_t fame_index_filtered_order(const fame_host_index* ix, uint64_t* out, uint64_t cap);
 
 /* ---- device context ----------------------------------------------------- */
 /* Copy the index into HBM on `device` (resident until fame_gpu_close).

@@ -32,3 +32,8 @@ def test_build_rejects_bad_arguments():
         HostIndex.build([], readlen=100)
     with pytest.raises(FameError):
         HostIndex.build([b"ACGT" * 100], readlen=20)
+    # the device build checks its arguments before touching a GPU
+    with pytest.raises(FameError):
+        HostIndex.build_gpu([], readlen=100)
+    with pytest.raises(FameError):
+        HostIndex.build_gpu([b"ACGT" * 100], readlen=4096)
