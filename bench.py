@@ -59,8 +59,8 @@ KERNEL_SOURCES = ("fame_gb300/csrc/seed.cuh", "fame_gb300/csrc/kernels.cuh", "fa
 # of one steady-state chunk and the ALU-pipe utilisation of the two ALU-bound
 # kernels, with the source hash and the profile that holds the capture command.
 NCU_FIGURES = {
-    "se150_uneven_3gbp": {"source_hash": "16eff2ef9d6f7da9", "seed_traffic_per_step": 3299303936,
-                          "shiftand_alu": 0.5597, "dp_alu": 0.7052,
+    "se150_uneven_3gbp": {"source_hash": "7a95f144a54c9c1d", "seed_traffic_per_step": 3300354048,
+                          "shiftand_alu": 0.5601, "dp_alu": 0.7051,
                           "profile": "profiles/seeding_se150_uneven_3gbp.md"},
 }
 
