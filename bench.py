@@ -366,12 +366,64 @@ def fastq_file_leg(gm, rs, slots=3):
             cnt, n = gm.match_fastq(path, False, 0, slots=slots, threads=0)
             times.append(time.perf_counter() - t0)
         gm.tallies(reset=True)
-        return {"value": n / times[-1], "unit": "reads/s", "reads": n, "file_bytes": size,
-                "first_call_reads_per_s": n / times[0], "write_seconds": t_write, "slots": slots,
-                "matched": int(cnt.succ),
-                "timing": "host clock around fame_match_fastq: parse + copy + match + tallies, file in page cache"}
+        out = {"value": n / times[-1], "unit": "reads/s", "reads": n, "file_bytes": size,
+               "first_call_reads_per_s": n / times[0], "write_seconds": t_write, "slots": slots,
+               "matched": int(cnt.succ),
+               "timing": "host clock around fame_match_fastq: parse + copy + match + tallies, file in page cache"}
+        out["bgzf"] = bgzf_leg(gm, rs, d, slots)
+        return out
     finally:
         shutil.rmtree(d, ignore_errors=True)
+
+
+def bgzf_leg(gm, rs, d, slots, n_reads=3_000_000):
+    """gzip input written as BGZF (the first n_reads reads, level 1): the
+    same file read by the native reader with its members inflated on the GPU
+    and with zlib on one host thread (read only), then matched whole through
+    fame_match_fastq (inflate on the GPU, parse, match, tallies); host clock,
+    file in the page cache, second of two calls."""
+    from fame_gb300 import synth
+    from fame_gb300._lib import FastqReader
+    sub = synth.ReadSet(seqs=rs.seqs[:n_reads], lens=rs.lens[:n_reads], chrom=rs.chrom[:n_reads],
+                        start=rs.start[:n_reads], fwd=rs.fwd[:n_reads]) if len(rs) > n_reads else rs
+    plain, path = os.path.join(d, "sub.fq"), os.path.join(d, "sub.fq.gz")
+    sub.write_fastq(plain)
+    t0 = time.perf_counter()
+    synth.bgzf_compress(plain, path, level=1)
+    t_comp = time.perf_counter() - t0
+    text = os.path.getsize(plain)
+    os.remove(plain)
+
+    def read_through(device):
+        r = FastqReader(path, is_gz=True, n_threads=0, max_reads=300000, max_len=256, device=device)
+        assert r.gpu_inflate == (device >= 0)
+        n = 0
+        t0 = time.perf_counter()
+        while True:
+            _, offs = r.read()
+            k = len(offs) - 1
+            n += k
+            if k < 300000:
+                break
+        dt = time.perf_counter() - t0
+        r.close()
+        return n, dt
+
+    read_through(0)
+    n_g, t_g = read_through(0)
+    n_z, t_z = read_through(-1)
+    times = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        cnt, n = gm.match_fastq(path, True, 0, slots=slots, threads=0)
+        times.append(time.perf_counter() - t0)
+    gm.tallies(reset=True)
+    return {"value": n / times[-1], "unit": "reads/s", "reads": n, "file_bytes": os.path.getsize(path),
+            "text_bytes": text, "compress_seconds": t_comp, "matched": int(cnt.succ),
+            "read_gpu_inflate": {"reads_per_s": n_g / t_g, "text_gb_per_s": text / t_g / 1e9},
+            "read_zlib_one_thread": {"reads_per_s": n_z / t_z, "text_gb_per_s": text / t_z / 1e9},
+            "timing": "host clock: reader alone (inflate + parse) both ways, then fame_match_fastq on the BGZF file "
+                      "(GPU inflate, parse, copy, match, tallies)"}
 
 
 def run_gb300(args):

@@ -72,7 +72,8 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_match_fastq_paired", "fame_index_write", "fame_gpu_index_bytes", "fame_queue_wait",
            "fame_gpu_set_seed_tier", "fame_gpu_autotune", "fame_gpu_load_tuning",
            "fame_gpu_seed_tier_counts", "fame_gpu_map_order_probe", "fame_gpu_pair_stage_times",
-           "fame_gpu_open_layout", "fame_gpu_rec_layout", "fame_index_build_gpu", "fame_index_filtered_order"]
+           "fame_gpu_open_layout", "fame_gpu_rec_layout", "fame_index_build_gpu", "fame_index_filtered_order",
+           "fame_fastq_open_dev", "fame_fastq_gpu_inflate"]
 
 _lib = None
 
@@ -142,6 +143,8 @@ def lib(build_if_missing: bool = True):
     L.fame_report_sc_header.argtypes = [_P, C.c_char_p]
     L.fame_report_sc_rows.argtypes = [_P, C.c_char_p, _P, C.c_char_p, C.c_int]
     L.fame_fastq_open.argtypes = [C.c_char_p, C.c_int, C.c_int, _P]
+    L.fame_fastq_open_dev.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, _P]
+    L.fame_fastq_gpu_inflate.argtypes = [_P]
     L.fame_fastq_read.argtypes = [_P, C.c_uint32, _P, C.c_uint64, _P, _P]
     L.fame_fastq_close.argtypes = [_P]
     L.fame_queue_stage.argtypes = [_P, _P, _P, _P, _P, _P]
@@ -497,9 +500,10 @@ class FastqReader:
     sequences packed with offsets, into page-locked buffers when given."""
 
     def __init__(self, path: str, is_gz: bool = False, n_threads: int = 0, max_reads: int = 300000,
-                 max_len: int = 256, seqs: np.ndarray = None, offs: np.ndarray = None):
+                 max_len: int = 256, seqs: np.ndarray = None, offs: np.ndarray = None, device: int = -1):
+        """device >= 0: BGZF input is inflated on that GPU (fame_fastq_open_dev)."""
         self.h = _P()
-        _check(lib().fame_fastq_open(path.encode(), int(is_gz), n_threads, C.byref(self.h)))
+        _check(lib().fame_fastq_open_dev(path.encode(), int(is_gz), n_threads, device, C.byref(self.h)))
         self.max_reads = max_reads
         self.seqs = np.zeros(max_reads * max_len, np.uint8) if seqs is None else seqs
         self.offs = np.zeros(max_reads + 1, np.uint64) if offs is None else offs
@@ -511,6 +515,11 @@ class FastqReader:
                                      C.byref(n)))
         k = n.value
         return self.seqs[: int(self.offs[k])], self.offs[: k + 1]
+
+    @property
+    def gpu_inflate(self) -> bool:
+        """True when the input is inflated on a GPU (BGZF)."""
+        return bool(lib().fame_fastq_gpu_inflate(self.h))
 
     def close(self):
         if self.h:

@@ -257,6 +257,7 @@ uint32_t pow2_ceil_host(uint64_t v)
 extern "C" const char* fame_gpu_last_error(const fame_gpu* g) { return g ? g->err.c_str() : "null context"; }
 
 int fame_gpu_fail(fame_gpu* g, int code, const char* msg) { return set_err(g, code, msg ? msg : ""); }
+int fame_gpu_device_of(const fame_gpu* g) { return g ? g->device : -1; }
 
 extern "C" int fame_gpu_close(fame_gpu* g)
 {

@@ -6,7 +6,10 @@
 //
 // Input: a regular uncompressed file is mapped and parsed in place (no copy
 // out of the page cache); gzip input and pipes are read into a buffer (gzip
-// inflated by zlib on the calling thread).  A call parses a region of whole
+// inflated by zlib on the calling thread, or, for BGZF input opened with a
+// device, member by member on the GPU: the compressed bytes are read in 64 MiB
+// pieces, the complete members found from their headers, and each refill
+// inflates enough of them in one launch).  A call parses a region of whole
 // lines sized from the bytes per record seen so far, in two parallel passes
 // over parts cut at line starts: the first counts each part's lines and, for
 // each of the four possible line phases, its sequence lines and their bytes;
@@ -33,6 +36,8 @@
 #include <vector>
 
 #include "../../include/fame_gpu.h"
+#include "bgzf.h"
+#include "inflate.h"
 
 namespace {
 
@@ -101,6 +106,7 @@ private:
 };
 
 constexpr size_t BLOCK = 64u << 20;     // first region, and the buffer's refill size
+constexpr size_t CREAD = 64u << 20;     // compressed bytes read at a time (BGZF input)
 constexpr size_t MIN_PART = 1u << 16;   // smallest part worth a thread
 
 }  // namespace
@@ -113,6 +119,12 @@ struct fame_fastq {
     // otherwise: FILE / gzip stream read into buf
     FILE* f = nullptr;
     gzFile gz = nullptr;
+    // BGZF input inflated on the GPU: compressed bytes [cpos, clen) of cbuf unread
+    FILE* cf = nullptr;
+    fame::BgzfGpu* bgzf = nullptr;
+    std::vector<uint8_t> cbuf;
+    size_t cpos = 0, clen = 0;
+    bool ceof = false;
     std::vector<char> buf;
     bool eof = false;
     size_t pos = 0, len = 0;  // unread bytes: [pos, len) of the mapping or of buf
@@ -123,6 +135,56 @@ struct fame_fastq {
 
 namespace {
 
+// More compressed input after the unread bytes; false on a read error.
+bool read_compressed(fame_fastq* q, size_t* scan)
+{
+    if (q->cpos > 0) {   // the unread compressed bytes to the front
+        std::memmove(q->cbuf.data(), q->cbuf.data() + q->cpos, q->clen - q->cpos);
+        *scan -= q->cpos;
+        q->clen -= q->cpos;
+        q->cpos = 0;
+    }
+    if (q->cbuf.size() < q->clen + CREAD) q->cbuf.resize(q->clen + CREAD);
+    const size_t r = std::fread(q->cbuf.data() + q->clen, 1, CREAD, q->cf);
+    if (r == 0) {
+        if (std::ferror(q->cf)) return false;
+        q->ceof = true;
+    }
+    q->clen += r;
+    return true;
+}
+
+// BGZF input: the complete members giving at least `want` bytes (or all that
+// are left) inflated on the GPU after the unread bytes.  False on a read
+// error, a malformed or truncated member, or a member that is not BGZF.
+bool fill_bgzf(fame_fastq* q, size_t want)
+{
+    std::vector<fame::BgzfMember> ms;
+    uint64_t out_total = 0;
+    size_t scan = q->cpos;
+    for (;;) {
+        while (out_total < want) {
+            uint32_t cd, cl, crc, isz;
+            const uint32_t tot = fame::bgzf_member(q->cbuf.data() + scan, q->clen - scan, &cd, &cl, &crc, &isz);
+            if (!tot) break;
+            ms.push_back(fame::BgzfMember{(uint64_t)(scan - q->cpos) + cd, cl, crc, out_total, isz, 0});
+            out_total += isz;
+            scan += tot;
+        }
+        if (out_total >= want || q->ceof) break;
+        if (!read_compressed(q, &scan)) return false;
+    }
+    if (q->ceof && out_total < want && scan < q->clen) return false;   // bytes left that are no complete member
+    if (q->buf.size() < q->len + out_total) q->buf.resize(q->len + out_total);
+    if (!ms.empty() && fame::bgzf_gpu_inflate(q->bgzf, q->cbuf.data() + q->cpos, scan - q->cpos, ms.data(),
+                                              (uint32_t)ms.size(), (uint8_t*)q->buf.data() + q->len, out_total) != FAME_OK)
+        return false;
+    q->len += out_total;
+    q->cpos = scan;
+    if (q->ceof && q->cpos == q->clen) q->eof = true;
+    return true;
+}
+
 // Appends up to `want` more bytes of buffered input after the unread ones.
 bool fill(fame_fastq* q, size_t want)
 {
@@ -131,6 +193,7 @@ bool fill(fame_fastq* q, size_t want)
         q->len -= q->pos;
         q->pos = 0;
     }
+    if (q->bgzf) return fill_bgzf(q, want);
     if (q->buf.size() < q->len + want) q->buf.resize(q->len + want);
     size_t got = 0;
     while (got < want && !q->eof) {
@@ -253,11 +316,36 @@ int parse_region(fame_fastq* q, const char* base, size_t end, uint32_t room, cha
 
 extern "C" int fame_fastq_open(const char* path, int is_gz, int n_threads, fame_fastq** out)
 {
+    return fame_fastq_open_dev(path, is_gz, n_threads, -1, out);
+}
+
+extern "C" int fame_fastq_open_dev(const char* path, int is_gz, int n_threads, int device, fame_fastq** out)
+{
     if (!path || !out) return FAME_ERR_ARG;
     *out = nullptr;
     fame_fastq* q = new (std::nothrow) fame_fastq();
     if (!q) return FAME_ERR_NOMEM;
-    if (is_gz) {
+    if (is_gz && device >= 0) {
+        // BGZF when the first member is complete and BGZF's (the first 64 MiB read either way)
+        q->cf = std::fopen(path, "rb");
+        if (q->cf) {
+            size_t scan = 0;
+            uint32_t cd, cl, crc, isz;
+            if (!read_compressed(q, &scan) || !fame::bgzf_member(q->cbuf.data(), q->clen, &cd, &cl, &crc, &isz)) {
+                std::fclose(q->cf);
+                q->cf = nullptr;
+                q->cbuf.clear();
+                q->clen = 0;
+                q->ceof = false;
+            } else if (!(q->bgzf = fame::bgzf_gpu_open(device))) {
+                fame_fastq_close(q);
+                return FAME_ERR_CUDA;
+            }
+        }
+    }
+    if (q->bgzf) {
+        // read through fill_bgzf
+    } else if (is_gz) {
         q->gz = gzopen(path, "rb");
         if (q->gz) gzbuffer(q->gz, 1u << 20);
     } else {
@@ -278,7 +366,7 @@ extern "C" int fame_fastq_open(const char* path, int is_gz, int n_threads, fame_
             ::close(fd);   // the mapping stays valid
         }
     }
-    if (!q->map && !q->f && !q->gz) {
+    if (!q->map && !q->f && !q->gz && !q->bgzf) {
         delete q;
         return FAME_ERR_IO;
     }
@@ -358,6 +446,10 @@ extern "C" int fame_fastq_close(fame_fastq* q)
     if (q->map) ::munmap((void*)q->map, q->map_len);
     if (q->f) std::fclose(q->f);
     if (q->gz) gzclose(q->gz);
+    if (q->bgzf) fame::bgzf_gpu_close(q->bgzf);
+    if (q->cf) std::fclose(q->cf);
     delete q;
     return FAME_OK;
 }
+
+extern "C" int fame_fastq_gpu_inflate(const fame_fastq* q) { return q && q->bgzf ? 1 : 0; }

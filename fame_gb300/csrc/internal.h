@@ -6,3 +6,5 @@
 
 // Records msg as the context's last error and returns code.
 int fame_gpu_fail(fame_gpu* g, int code, const char* msg);
+// The device of the context.
+int fame_gpu_device_of(const fame_gpu* g);

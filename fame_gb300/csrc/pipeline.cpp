@@ -70,7 +70,8 @@ extern "C" int fame_match_fastq(fame_gpu* g, const char* path, int is_gz, uint32
     *cnt = fame_counters{};
     if (n_reads) *n_reads = 0;
     Closer c;
-    int rc = fame_fastq_open(path, is_gz, n_threads, &c.f);
+    // BGZF input inflated on the context's GPU
+    int rc = fame_fastq_open_dev(path, is_gz, n_threads, fame_gpu_device_of(g), &c.f);
     if (rc) return fame_gpu_fail(g, rc, "cannot open the FASTQ file");
     rc = fame_queue_open(g, slots, chunk, (uint64_t)chunk * FAME_MAX_READ_LEN, &c.q);
     if (rc) return rc;
@@ -192,8 +193,8 @@ extern "C" int fame_match_fastq_paired(fame_gpu* g, const char* path1, const cha
     PairFiles pf;
     pf.g = g;
     int rc;
-    if ((rc = fame_fastq_open(path1, is_gz, n_threads, &pf.f[0])) ||
-        (rc = fame_fastq_open(path2, is_gz, n_threads, &pf.f[1])))
+    if ((rc = fame_fastq_open_dev(path1, is_gz, n_threads, fame_gpu_device_of(g), &pf.f[0])) ||
+        (rc = fame_fastq_open_dev(path2, is_gz, n_threads, fame_gpu_device_of(g), &pf.f[1])))
         return fame_gpu_fail(g, rc, "cannot open the mate FASTQ files");
     const uint64_t cap = (uint64_t)chunk * FAME_MAX_READ_LEN;
     PairChunk buf[2];

@@ -112,6 +112,31 @@ class ReadSet:
                 f.write(rec.tobytes())
 
 
+def bgzf_compress(src: str, dst: str, level: int = 1, block: int = 65280, threads: int = 0) -> None:
+    """Writes src as BGZF (the blocked gzip of bgzip: members of at most
+    64 KiB, each with a 'BC' extra subfield holding its size, then the empty
+    end-of-file member); members compressed on host threads."""
+    import os
+    import struct
+    import zlib
+    from concurrent.futures import ThreadPoolExecutor
+
+    def member(data: bytes) -> bytes:
+        co = zlib.compressobj(level, zlib.DEFLATED, -15)
+        cdata = co.compress(data) + co.flush()
+        head = struct.pack("<BBBBIBBHBBHH", 31, 139, 8, 4, 0, 0, 255, 6, ord("B"), ord("C"), 2, 18 + len(cdata) + 7)
+        return head + cdata + struct.pack("<II", zlib.crc32(data) & 0xFFFFFFFF, len(data))
+
+    with open(src, "rb") as f, open(dst, "wb") as g, ThreadPoolExecutor(threads or os.cpu_count() or 1) as ex:
+        while True:
+            piece = f.read(block * 1024)
+            if not piece:
+                break
+            for m in ex.map(member, [piece[i:i + block] for i in range(0, len(piece), block)]):
+                g.write(m)
+        g.write(member(b""))
+
+
 def _random_bases(rng, n, base_p):
     # exact per-mille composition through a lookup table (fast, platform independent)
     counts = np.round(np.asarray(base_p) * 1000).astype(int)

@@ -225,6 +225,16 @@ int fame_gpu_tallies(fame_gpu* g, uint16_t* meth, int reset);
  * threads at the same time. */
 typedef struct fame_fastq fame_fastq;
 int fame_fastq_open(const char* path, int is_gz, int n_threads, fame_fastq** out);
+/* fame_fastq_open, with gzip input written as BGZF (the blocked gzip of
+ * bgzip: members of at most 64 KiB whose headers and trailers give their
+ * sizes) inflated on GPU `device`, one warp per member, the CRC-32 and size
+ * of every member checked (a bad member fails the read with FAME_ERR_IO);
+ * other gzip input is inflated by zlib as with fame_fastq_open (one stream
+ * cannot be split).  device < 0 is fame_fastq_open.  FAME_ERR_CUDA when the
+ * input is BGZF and the device cannot be used. */
+int fame_fastq_open_dev(const char* path, int is_gz, int n_threads, int device, fame_fastq** out);
+/* 1 when the reader inflates its input on a GPU (BGZF), else 0. */
+int fame_fastq_gpu_inflate(const fame_fastq* f);
 int fame_fastq_read(fame_fastq* f, uint32_t max_reads, char* seqs, uint64_t seq_cap, uint64_t* offs, uint32_t* n);
 int fame_fastq_close(fame_fastq* f);
 
