@@ -831,7 +831,7 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
     cb.heavy = g->d_heavy;
     cb.heavy2 = g->d_heavy2;
     if (!g->d_pe_mid) {
-        g->pe_mid_warps = (uint32_t)g->sm_count * 16;
+        g->pe_mid_warps = (uint32_t)g->sm_count * 16;   // the register file's limit; 12, 8 and 4 were slower
         g->pe_mid2_warps = (uint32_t)g->sm_count * 4;
         CK(cudaMalloc((void**)&g->d_pe_mid, g->pe_mid_warp_bytes * g->pe_mid_warps));
         CK(cudaMalloc((void**)&g->d_pe_mid2, g->pe_mid2_warp_bytes * g->pe_mid2_warps));

@@ -282,7 +282,9 @@ __device__ uint32_t pe_kmers(const DevIndex& ix, const PeIndex& px, const PeMem&
         if (p < nk) {
             const uint32_t key = sh_prefix_hash([&](uint32_t j) { return P[j]; }, p, HTAB_MASK);
             uint32_t slot;
-            const uint4 t = rec_lookup(ix, key, slot);   // {start, size, ...}
+            // {start, size, ...}; a dense record is read once, evict-first, so that
+            // the index lines do not push the warps' working memory out of L2
+            const uint4 t = ix.rec_hashed ? rec_lookup(ix, key, slot) : __ldcs(ix.rec + 2ull * key);
             b0[jj] = t.x;
             b1[jj] = t.x + t.y;
         }
@@ -338,8 +340,8 @@ __device__ uint32_t pe_kmers(const DevIndex& ix, const PeIndex& px, const PeMem&
             if (i < sigma) {
                 const uint32_t p = s.gk[i];
                 const uint32_t src = s.kst[p] + (i - s.kpre[p]);
-                ev[j] = __ldg(ix.entry + src);
-                tv[j] = __ldg(px.tmask + src);
+                ev[j] = __ldcs(ix.entry + src);   // read once: evict-first
+                tv[j] = __ldcs(px.tmask + src);
             }
         }
 #pragma unroll
