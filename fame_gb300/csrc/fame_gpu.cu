@@ -581,7 +581,7 @@ extern "C" int fame_gpu_open_layout(const fame_index_view* v, int device, int la
             return fail(set_err(g, FAME_ERR_CUDA, "k_dp_warp does not fit an SM"));
         g->dp_grid = (uint32_t)(g->sm_count * nb);
         g->dp_blocks = g->dp_grid;
-        uint64_t off[28], hoff[28], moff[28], m2off[28];
+        uint64_t off[PE_LAYOUT_N], hoff[PE_LAYOUT_N], moff[PE_LAYOUT_N], m2off[PE_LAYOUT_N];
         g->pe_warp_bytes = pe_layout(PE_LIGHT, off);
         pe_layout(PE_HEAVY, hoff);
         g->pe_mid_warp_bytes = pe_layout(PE_MID_S, moff);
@@ -872,7 +872,7 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
                 if ((wmask >> w) & 1u) wmax = w;
             caps.kmax = std::min<uint32_t>(PE_KMAX, 64 * wmax - KMERLEN);
         }
-        uint64_t coff[28];
+        uint64_t coff[PE_LAYOUT_N];
         const uint64_t wbytes = pe_layout(caps, coff);
         uint32_t grid = g->pe_grid;
         {
@@ -932,7 +932,7 @@ int run_pairs(fame_gpu* g, const char* d_seqs, const uint64_t* d_offs, uint32_t 
         if ((rc = sync_ctr())) return rc;
         if (g->h_ctr[CTR_HEAVY]) {
             if (!g->d_pe_heavy) {
-                uint64_t off[28];
+                uint64_t off[PE_LAYOUT_N];
                 g->pe_heavy_warp_bytes = pe_layout(PE_HEAVY, off);
                 g->pe_heavy_warps = PE_HEAVY_WARPS;
                 CK(cudaMalloc((void**)&g->d_pe_heavy, g->pe_heavy_warp_bytes * g->pe_heavy_warps));

@@ -81,13 +81,17 @@ struct PeMem {
     uint32_t* gt;
     uint8_t* gk;          // k-mer of each staged entry
     uint8_t* sv;          // staged entry survives the T-mask filter and the dedup
+    uint16_t* occ[2];     // value-table slots holding a key, in insertion order (occn[dir] of them):
+    uint32_t* occn;       // the sweeps visit these, and the next pair clears only these
     uint32_t area;        // bytes of regions 11 .. 16 (dead while the maps are built)
     PeCaps c;
 };
 
 __host__ __device__ inline uint64_t pe_align16(uint64_t x) { return (x + 15) & ~15ull; }
 
-// Byte layout of PeMem for the given caps; returns the total.
+// Byte layout of PeMem for the given caps (PE_LAYOUT_N region offsets into
+// off); returns the total.
+constexpr int PE_LAYOUT_N = 31;
 __host__ __device__ inline uint64_t pe_layout(PeCaps c, uint64_t* off)
 {
     uint64_t o = 0;
@@ -121,12 +125,15 @@ __host__ __device__ inline uint64_t pe_layout(PeCaps c, uint64_t* off)
     put(4ull * c.ecap);                     // 25 gt
     put(c.ecap);                            // 26 gk
     put(c.ecap);                            // 27 sv
+    put(2ull * c.vcap);                     // 28 occ[0]
+    put(2ull * c.vcap);                     // 29 occ[1]
+    put(16);                                // 30 occn
     return o;
 }
 
 __device__ inline PeMem pe_mem(uint8_t* base, PeCaps c)
 {
-    uint64_t off[28];
+    uint64_t off[PE_LAYOUT_N];
     pe_layout(c, off);
     PeMem s;
     s.c = c;
@@ -159,8 +166,29 @@ __device__ inline PeMem pe_mem(uint8_t* base, PeCaps c)
     s.gt = (uint32_t*)(base + off[25]);
     s.gk = base + off[26];
     s.sv = base + off[27];
+    s.occ[0] = (uint16_t*)(base + off[28]);
+    s.occ[1] = (uint16_t*)(base + off[29]);
+    s.occn = (uint32_t*)(base + off[30]);
     s.area = (uint32_t)(off[17] - off[11]);
     return s;
+}
+
+// Empty value tables and slot lists (all lanes; once per warp and launch:
+// from then on each pair clears the slots it occupied when the next starts).
+__device__ inline void pe_tables_reset(const PeMem& s)
+{
+    const int lane = threadIdx.x & 31;
+    for (uint32_t i = lane; i < s.c.vcap; i += 32) {
+        s.vk[0][i] = EMPTY_KEY;
+        s.vk[1][i] = EMPTY_KEY;
+        s.vv[0][i] = 0;
+        s.vv[1][i] = 0;
+    }
+    if (lane == 0) {
+        s.occn[0] = 0;
+        s.occn[1] = 0;
+    }
+    __syncwarp();
 }
 
 // shared-memory caps of k_pe_seed (one warp; it keeps no matches)
@@ -207,7 +235,9 @@ __device__ __forceinline__ int pm_at(const PeMem& s, PeState& st, int dir, uint3
             if (4 * (st.nkeys[dir] + 1) > 3 * s.c.vcap) { st.over = true; return -1; }
             s.vk[dir][h] = key;
             s.vv[dir][h] = 0;
+            s.occ[dir][st.nkeys[dir]] = (uint16_t)h;
             st.nkeys[dir]++;
+            s.occn[dir] = st.nkeys[dir];
             break;
         }
     }
@@ -649,6 +679,7 @@ __device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint
         const unsigned grp = __match_any_sync(0xffffffffu, live ? e : EMPTY_KEY) & vm;
         const bool leader = live && (__ffs(grp) - 1) == lane;
         bool fresh = false, added = false;
+        uint32_t hs = 0;
         if (leader) {
             uint32_t h = vt_hash(id, mask);
             for (;; h = (h + 1) & mask) {
@@ -660,6 +691,7 @@ __device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint
                     if (old == id) break;
                 }
             }
+            hs = h;
             uint32_t v = s.vv[dir][h];
             if (!(v & PV_SEEN)) {
                 v |= PV_SEEN;
@@ -670,7 +702,9 @@ __device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint
         }
         for (int d = 0; d < 2; ++d) {
             const unsigned na = __ballot_sync(0xffffffffu, added && dir == d);
+            if (added && dir == d) s.occ[d][nkeys[d] + __popc(na & ((1u << lane) - 1))] = (uint16_t)hs;
             nkeys[d] += __popc(na);
+            if (lane == 0) s.occn[d] = nkeys[d];
             const unsigned bm = __ballot_sync(0xffffffffu, fresh && dir == d);
             if (fresh && dir == d) {
                 const uint32_t at = nins[d] + __popc(bm & ((1u << lane) - 1));
@@ -684,7 +718,8 @@ __device__ int pe_count_par(const PeIndex& px, const PeMem& s, PeState& st, uint
     if (over) return -1;
     // fold the op counts into count1 / count2 (8-bit wrap) and clear the scratch bits
     for (int dir = 0; dir < 2; ++dir)
-        for (uint32_t h = lane; h < s.c.vcap; h += 32) {
+        for (uint32_t x = lane; x < nkeys[dir]; x += 32) {
+            const uint32_t h = s.occ[dir][x];
             const uint32_t v = s.vv[dir][h];
             const uint32_t raw = ((v & PV_RAW_MASK) >> PV_RAW_SHIFT) & 0xffu;
             const uint32_t base_v = v & ~(PV_RAW_MASK | PV_SEEN);
@@ -747,6 +782,7 @@ __device__ int pe_count_par2(const PeIndex& px, const PeMem& s, PeState& st, uin
         const int dir = (int)(e >> 31);
         const uint32_t id = e & 0x7fffffffu;
         bool added = false;
+        uint32_t hs = 0;
         if (may) {
             uint32_t h = vt_hash(id, mask);
             for (;; h = (h + 1) & mask) {
@@ -758,6 +794,7 @@ __device__ int pe_count_par2(const PeIndex& px, const PeMem& s, PeState& st, uin
                     if (old == id) break;
                 }
             }
+            hs = h;
             if (!(s.vv[dir][h] & PV_PRESENT)) {
                 bool kept = false;
                 for (int c = -ctx; c <= ctx && !kept; ++c)
@@ -765,7 +802,12 @@ __device__ int pe_count_par2(const PeIndex& px, const PeMem& s, PeState& st, uin
                 if (kept) atomicMin(&at[dir][h], i);
             }
         }
-        for (int d = 0; d < 2; ++d) nkeys[d] += __popc(__ballot_sync(FULL, added && dir == d));
+        for (int d = 0; d < 2; ++d) {
+            const unsigned na = __ballot_sync(FULL, added && dir == d);
+            if (added && dir == d) s.occ[d][nkeys[d] + __popc(na & ((1u << lane) - 1))] = (uint16_t)hs;
+            nkeys[d] += __popc(na);
+            if (lane == 0) s.occn[d] = nkeys[d];
+        }
         __syncwarp();
     }
     // B: context from keys the second mate inserts earlier, to the fixed point
@@ -841,7 +883,8 @@ __device__ int pe_count_par2(const PeIndex& px, const PeMem& s, PeState& st, uin
     __syncwarp();
     // fold the op counts into count2 (8-bit wrap) and clear the scratch bits
     for (int dir = 0; dir < 2; ++dir)
-        for (uint32_t h = lane; h < s.c.vcap; h += 32) {
+        for (uint32_t x = lane; x < nkeys[dir]; x += 32) {
+            const uint32_t h = s.occ[dir][x];
             const uint32_t v = s.vv[dir][h];
             const uint32_t raw = ((v & PV_RAW_MASK) >> PV_RAW_SHIFT) & 0xffu;
             const uint32_t base_v = v & ~(PV_RAW_MASK | PV_SEEN);
@@ -1135,11 +1178,19 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
     // first = mate 1 (o = 0) or its reverse complement; second = the other strand of mate 2
     pe_orient(s.rd[0], cb.seqs + cb.offs[i1], n1, o);
     pe_orient(s.rd[1], cb.seqs + cb.offs[i2], n2, 1 - o);
-    for (uint32_t i = lane; i < s.c.vcap; i += 32) {
-        s.vk[0][i] = EMPTY_KEY;
-        s.vk[1][i] = EMPTY_KEY;
-        s.vv[0][i] = 0;
-        s.vv[1][i] = 0;
+    __syncwarp();
+    for (int dir = 0; dir < 2; ++dir) {   // the slots the previous pair occupied
+        const uint32_t no = s.occn[dir];
+        for (uint32_t x = lane; x < no; x += 32) {
+            const uint32_t h = s.occ[dir][x];
+            s.vk[dir][h] = EMPTY_KEY;
+            s.vv[dir][h] = 0;
+        }
+    }
+    __syncwarp();
+    if (lane == 0) {
+        s.occn[0] = 0;
+        s.occn[1] = 0;
     }
     __syncwarp();
     const uint32_t sigma = pe_kmers(ix, px, s, s.rd[0], n1);
@@ -1149,9 +1200,11 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
         pe_count_first(ix, px, s, st, n1, false);
     }
     if (__shfl_sync(0xffffffffu, st.over, 0)) return -1;
+    __syncwarp();
     // rebuild: keep count1 >= QTHRESH (order-independent)
     for (int dir = 0; dir < 2; ++dir)
-        for (uint32_t h = lane; h < s.c.vcap; h += 32) {
+        for (uint32_t x = lane; x < s.occn[dir]; x += 32) {
+            const uint32_t h = s.occ[dir][x];
             const uint32_t v = s.vv[dir][h];
             if (!(v & PV_PRESENT)) continue;
             s.vv[dir][h] = pv_c1(v) < QTHRESH ? 0u : (PV_PRESENT | pv_c1(v));
@@ -1176,7 +1229,8 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
     {
         const int ctx = (int)px.ctx;
         for (int dir = 0; dir < 2; ++dir)
-            for (uint32_t hh = lane; hh < s.c.vcap; hh += 32) {
+            for (uint32_t x = lane; x < s.occn[dir]; x += 32) {
+                const uint32_t hh = s.occ[dir][x];
                 const uint32_t v = s.vv[dir][hh];
                 const uint32_t key = s.vk[dir][hh];
                 if (key == EMPTY_KEY || !(v & PV_PRESENT) || pv_c2(v) < QTHRESH) continue;
@@ -1192,7 +1246,8 @@ __device__ int pe_maps(const DevIndex& ix, const PeIndex& px, const ChunkBufs& c
     __syncwarp();
     bool mine = false;
     for (int dir = 0; dir < 2; ++dir)
-        for (uint32_t hh = lane; hh < s.c.vcap; hh += 32) {
+        for (uint32_t x = lane; x < s.occn[dir]; x += 32) {
+            const uint32_t hh = s.occ[dir][x];
             const uint32_t v = s.vv[dir][hh];
             const uint32_t key = s.vk[dir][hh];
             mine |= key != EMPTY_KEY && (v & PV_PRESENT) && (v & PV_F2) && ix.win[key].z != CPGDUMMY;
@@ -1371,6 +1426,7 @@ __global__ void k_pe_heavy(DevIndex ix, PeIndex px, ChunkBufs cb, uint8_t* scrat
     const PeMem s = pe_mem(scratch + (uint64_t)wid * warp_bytes, caps);
     const uint32_t nheavy = (uint32_t)cb.ctr[CTR_HEAVY];
     for (uint32_t k = wid; k < nheavy; k += nw) {
+        if (k == wid) pe_tables_reset(s);   // the warp's first pair
         const uint32_t r = cb.heavy[k];
         if (!pe_pair<4>(ix, px, cb, s, r)) {
             if (lane == 0) atomicAdd(cb.ctr + CTR_ERRFLAG, 1ull);
@@ -1531,6 +1587,7 @@ __global__ void k_pe_seed(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* recs
     const uint32_t nw = gridDim.x * (blockDim.x >> 5);
     const PeMem s = pe_mem(smem + (threadIdx.x >> 5) * warp_bytes, caps);
     const uint32_t n = cb.n;
+    if (!route_mid && wid < n) pe_tables_reset(s);
     for (uint32_t r = wid; r < n; r += nw) {
         if (lane == 0) pe_rec_reset(recs, r);
         if ((cb.rflags[r] | cb.rflags[n + r]) & 7u) continue;   // k_pe_prep finished the pair
@@ -1557,11 +1614,14 @@ __global__ void k_pe_seed_mid(DevIndex ix, PeIndex px, ChunkBufs cb, PeTaskRec* 
     const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const PeMem s = pe_mem(scratch + (uint64_t)wid * warp_bytes, caps);
     const uint32_t npairs = (uint32_t)cb.ctr[ctr_in];
+    bool first = true;
     while (true) {
         uint32_t k = 0;
         if (lane == 0) k = (uint32_t)atomicAdd(cb.ctr + ctr_q, 1ull);
         k = __shfl_sync(0xffffffffu, k, 0);
         if (k >= npairs) break;
+        if (first) pe_tables_reset(s);   // the warp's first pair
+        first = false;
         const uint32_t r = list[k];
         const bool over = pe_seed_pair(ix, px, cb, recs, s, caps, r);
         if (over && lane == 0) {
