@@ -206,6 +206,17 @@ def host_placement(device):
                     out["cpus_allowed"] = line.split(":", 1)[1].strip()
     except Exception:
         pass
+    try:   # free memory per host node at the time of the call
+        import glob
+        free = {}
+        for path in sorted(glob.glob("/sys/devices/system/node/node*/meminfo")):
+            with open(path) as f:
+                for line in f:
+                    if "MemFree:" in line:
+                        free[path.split("/")[-2]] = round(int(line.split()[-2]) / 1e6, 1)   # kB -> GB
+        out["node_free_gb"] = free
+    except Exception:
+        pass
     return out
 
 
@@ -454,20 +465,27 @@ def run_gb300(args):
     d_mat = gm.alloc(8 * maxn)
     d_inv = gm.alloc(maxn)
     for i in used:
+        # each chunk in page-locked host memory, and the device copy filled from
+        # there (so every host buffer has served a copy before the timed loops,
+        # as a host's reused staging buffers have)
         base, o = chunks[i]
         nb = int(o[-1])
-        d_s = gm.alloc(nb)
-        d_o = gm.alloc(8 * len(o))
-        gm.memcpy(d_s, seq[base:].ctypes.data, nb, 1)
-        gm.memcpy(d_o, o.ctypes.data, 8 * len(o), 1)
-        dev[i] = (d_s, d_o, len(o) - 1)
         hs = gm.host_alloc(nb)
         ho = gm.host_alloc(8 * len(o)).view(np.uint64)
         hs[:] = seq[base:base + nb]
         ho[:] = o
         pinned[i] = (hs, ho, len(o) - 1)
+        d_s = gm.alloc(nb)
+        d_o = gm.alloc(8 * len(o))
+        gm.memcpy(d_s, hs.ctypes.data, nb, 1)
+        gm.memcpy(d_o, ho.ctypes.data, 8 * len(o), 1)
+        dev[i] = (d_s, d_o, len(o) - 1)
     h_mat = gm.host_alloc(8 * maxn).view(np.uint64)
     h_inv = gm.host_alloc(maxn)
+    # where the page-locked chunk buffers landed (a buffer off the GPU's near
+    # node copies over the CPU-to-CPU link)
+    near = gm.host_node()
+    buf_nodes = {i: sorted(set(gm.page_nodes(pinned[i][0]) + gm.page_nodes(pinned[i][1]))) for i in used}
     p_stream = ctypes.c_void_p()
     _L().fame_gpu_stream(gm.h, ctypes.byref(p_stream))
     stream = torch.cuda.ExternalStream(p_stream.value, device=local)
@@ -523,6 +541,7 @@ def run_gb300(args):
     h2d_gbps = 3 * hs0.nbytes / (time.perf_counter() - tc0) / 1e9
     # ---- timed: end to end from page-locked host memory
     e_reads = h2d = d2h = 0
+    e2e_steps = []
     for w in range(args.warmup):   # untimed: the host-buffer path's first calls (its device staging grows)
         hs, ho, n = pinned[steady[w % len(steady)]]
         gm.match_reads(hs, ho, flags, mats=h_mat[:n], invalid=h_inv[:n])
@@ -535,6 +554,7 @@ def run_gb300(args):
         th = time.perf_counter()
         gm.match_reads(hs, ho, flags, mats=h_mat[:n], invalid=h_inv[:n])
         host_steps["e2e"].append(time.perf_counter() - th)
+        e2e_steps.append((steady[k % len(steady)], time.perf_counter() - th))
         e_reads += n
         h2d += hs.nbytes + ho.nbytes
         d2h += 9 * n
@@ -661,7 +681,11 @@ def run_gb300(args):
                           "alu_pipe_of_peak": fig.get("dp_alu") if fig_ok else None},
             "note": "stages bound by the integer/logic pipe, not by HBM or tensor cores; ALU-pipe figures from "
                     "ncu captures of the same kernel sources (kernel source hash %s)" % src_hash},
-        "host": host_placement(local),
+        "host": dict(host_placement(local), near_node=near,
+                     e2e_steps=[{"chunk": c, "ms": round(1e3 * t, 3), "buffer_nodes": buf_nodes.get(c)}
+                                for c, t in e2e_steps],
+                     off_node_chunk_buffers=sum(1 for v in buf_nodes.values() if near >= 0 and any(x != near for x in v)),
+                     chunk_buffers=len(buf_nodes)),
         "clocks": clk.summary(),
         "setup_seconds": {"generate": t_gen, "index_build": t_build, "upload": t_open},
         "index_build": index_rep,
@@ -820,17 +844,21 @@ def run_gb300_pe(args):
         m1 = b1a[int(o1[a]):int(o1[b])]
         m2 = b2a[int(o2[a]):int(o2[b])]
         oo = np.concatenate([o1[a:b + 1] - o1[a], (o2[a + 1:b + 1] - o2[a]) + (o1[b] - o1[a])]).astype(np.uint64)
-        buf = np.concatenate([m1, m2])
-        d_s = gm.alloc(len(buf))
-        d_o = gm.alloc(8 * len(oo))
-        gm.memcpy(d_s, buf.ctypes.data, len(buf), 1)
-        gm.memcpy(d_o, oo.ctypes.data, 8 * len(oo), 1)
-        dev[i] = (d_s, d_o, b - a)
         h1 = gm.host_alloc(len(m1)); h1[:] = m1
         h2 = gm.host_alloc(len(m2)); h2[:] = m2
         ho1 = gm.host_alloc(8 * (b - a + 1)).view(np.uint64); ho1[:] = o1[a:b + 1] - o1[a]
         ho2 = gm.host_alloc(8 * (b - a + 1)).view(np.uint64); ho2[:] = o2[a:b + 1] - o2[a]
         pinned[i] = (h1, ho1, h2, ho2, b - a)
+        # the device copy (mates back to back) filled from the page-locked buffers, so
+        # that each has served a copy before the timed loops
+        d_s = gm.alloc(len(m1) + len(m2))
+        d_o = gm.alloc(8 * len(oo))
+        gm.memcpy(d_s, h1.ctypes.data, len(m1), 1)
+        gm.memcpy(d_s + len(m1), h2.ctypes.data, len(m2), 1)
+        gm.memcpy(d_o, ho1.ctypes.data, ho1.nbytes, 1)
+        gm.memcpy(d_o, ho2.ctypes.data, ho2.nbytes, 1)
+        gm.memcpy(d_o, oo.ctypes.data, 8 * len(oo), 1)
+        dev[i] = (d_s, d_o, b - a)
     p_stream = ctypes.c_void_p()
     _L().fame_gpu_stream(gm.h, ctypes.byref(p_stream))
     stream = torch.cuda.ExternalStream(p_stream.value, device=0)

@@ -73,7 +73,7 @@ EXPORTS = ["fame_index_read", "fame_index_build", "fame_index_view_of", "fame_in
            "fame_gpu_set_seed_tier", "fame_gpu_autotune", "fame_gpu_load_tuning",
            "fame_gpu_seed_tier_counts", "fame_gpu_map_order_probe", "fame_gpu_pair_stage_times",
            "fame_gpu_open_layout", "fame_gpu_rec_layout", "fame_index_build_gpu", "fame_index_filtered_order",
-           "fame_fastq_open_dev", "fame_fastq_gpu_inflate"]
+           "fame_fastq_open_dev", "fame_fastq_gpu_inflate", "fame_host_page_node", "fame_gpu_host_node"]
 
 _lib = None
 
@@ -143,6 +143,8 @@ def lib(build_if_missing: bool = True):
     L.fame_report_sc_header.argtypes = [_P, C.c_char_p]
     L.fame_report_sc_rows.argtypes = [_P, C.c_char_p, _P, C.c_char_p, C.c_int]
     L.fame_fastq_open.argtypes = [C.c_char_p, C.c_int, C.c_int, _P]
+    L.fame_host_page_node.argtypes = [_P]
+    L.fame_gpu_host_node.argtypes = [_P]
     L.fame_fastq_open_dev.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, _P]
     L.fame_fastq_gpu_inflate.argtypes = [_P]
     L.fame_fastq_read.argtypes = [_P, C.c_uint32, _P, C.c_uint64, _P, _P]
@@ -474,6 +476,18 @@ class GpuMatcher:
 
     def host_free(self, arr: np.ndarray):
         _check(lib().fame_gpu_host_free(self.h, arr.ctypes.data), self.h)
+
+    def host_node(self) -> int:
+        """Host NUMA node nearest the device (-1 when unknown)."""
+        return int(lib().fame_gpu_host_node(self.h))
+
+    @staticmethod
+    def page_nodes(arr: np.ndarray, samples: int = 3):
+        """NUMA nodes of a few pages of a host buffer (first, middle, last)."""
+        if arr.nbytes == 0:
+            return []
+        at = [0, arr.nbytes // 2, arr.nbytes - 1][:samples]
+        return [int(lib().fame_host_page_node(C.c_void_p(arr.ctypes.data + a))) for a in at]
 
     # separate tally arrays (one per job of a serving loop)
     def tally_alloc(self) -> int:

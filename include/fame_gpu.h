@@ -329,6 +329,13 @@ int fame_gpu_free(fame_gpu* g, void* ptr_dev);
 int fame_gpu_memcpy(fame_gpu* g, void* dst, const void* src, size_t bytes, int kind /* 1 H2D, 2 D2H, 3 D2D */);
 int fame_gpu_host_alloc(fame_gpu* g, size_t bytes, void** ptr);
 int fame_gpu_host_free(fame_gpu* g, void* ptr);
+/* Where host memory lies, for copy-rate diagnostics: the NUMA node holding
+ * the page at ptr (-1 when unknown), and the host node nearest the device
+ * (-1 when the device reports none).  A page-locked buffer whose pages the
+ * kernel placed on another node (the near node was short of memory) copies
+ * over the CPU-to-CPU link, at a fraction of the near node's rate. */
+int fame_host_page_node(const void* ptr);
+int fame_gpu_host_node(fame_gpu* g);
 /* The CUDA stream (cudaStream_t) all work of the context runs on. */
 int fame_gpu_stream(fame_gpu* g, void** stream);
 
