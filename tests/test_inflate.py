@@ -48,3 +48,38 @@ def test_bgzf_writer_is_gzip(tmp_path):
         p = tmp_path / ("r%d.fq.gz" % level)
         p.write_bytes(b)
         assert read_all(p, True, 700, 3) == [s for _, s, _, _ in recs]   # the zlib path, no device
+
+
+def _gpu_present():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_gpu_present(), reason="checks the behaviour without a GPU")
+def test_device_paths_fail_loudly_without_a_gpu(tmp_path):
+    """With no GPU, BGZF input opened for the device inflater and the device
+    index build return FAME_ERR_CUDA (no silent host fallback); plain gzip
+    opened with a device still reads through zlib (it never needs one)."""
+    from fame_gb300 import FameError, HostIndex
+    from fame_gb300._lib import FastqReader
+    rng = np.random.default_rng(9)
+    recs = records(rng, 500)
+    data = b"\n".join(x for r in recs for x in r) + b"\n"
+    p = tmp_path / "r.fq.gz"
+    p.write_bytes(bgzf(data, 6, 4000))
+    with pytest.raises(FameError) as e:
+        FastqReader(str(p), is_gz=True, device=0)
+    assert e.value.code == -2   # FAME_ERR_CUDA
+    q = tmp_path / "plain.fq.gz"
+    q.write_bytes(gzip.compress(data))
+    r = FastqReader(str(q), is_gz=True, max_reads=1000, max_len=300, device=0)
+    assert not r.gpu_inflate
+    seq, offs = r.read()
+    assert len(offs) - 1 == 500
+    r.close()
+    with pytest.raises(FameError) as e:
+        HostIndex.build_gpu([np.frombuffer(b"ACGT" * 50_000, np.uint8)], readlen=100, device=0)
+    assert e.value.code == -2
