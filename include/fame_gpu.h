@@ -110,9 +110,11 @@ int fame_index_build(uint32_t readlen, uint32_t n_chrom, const char* const* seq,
 
 /* The same index, identical table for table, built on the GPU `device`
  * (window hashing, bucket fill, bucket order, both filters, compaction and
- * T masks on the device; the tables come back to host memory).  Needs about
- * 24 bytes of device memory per k-mer entry plus 12 GiB for the bucket
- * tables (3 Gbp: about 90 GB).  FAME_ERR_NOMEM when they do not fit. */
+ * T masks on the device; the tables come back to host memory).  Needs at
+ * its peak about 16 bytes of device memory per k-mer entry before the
+ * filters, plus 8 GiB of bucket arrays, the genome (a byte per base) and up
+ * to 2 GiB of sort scratch: about 66 GB for a 3 Gbp genome.  FAME_ERR_NOMEM
+ * when they do not fit, FAME_ERR_CUDA without a usable device. */
 int fame_index_build_gpu(uint32_t readlen, uint32_t n_chrom, const char* const* seq, const uint64_t* len,
                          const char* const* names, int noloss, int device, fame_host_index** out);
 
