@@ -49,6 +49,24 @@ def test_argument_errors_without_gpu():
     assert L.fame_match_fastq(None, b"x.fq", 0, 0, 0, 2, 0, None, None, None) == -1
     assert L.fame_match_fastq_paired(None, b"1.fq", b"2.fq", 0, 0, 550, 0, 0, None, None) == -1
     assert L.fame_index_write(None, b"x.idx") == -1
+    # entry points of the device layouts, the device index build and reader, the diagnostics
+    assert L.fame_gpu_open_layout(None, 0, 0, None) == -1
+    assert L.fame_gpu_rec_layout(None, None, None) == -1
+    assert L.fame_index_build_gpu(100, 0, None, None, None, 0, 0, None) == -1
+    assert L.fame_fastq_open_dev(None, 1, 0, 0, None) == -1
+    assert L.fame_fastq_gpu_inflate(None) == 0
+    assert L.fame_index_filtered_order(None, None, 0) == 0
+    assert L.fame_host_page_node(None) == -1
+    assert L.fame_gpu_host_node(None) == -1
+
+
+def test_open_layout_rejects_unknown_layouts(product_index):
+    """An unknown record layout is an argument error, before any device call."""
+    import ctypes
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    for layout in (-1, 3, 99):
+        assert L.fame_gpu_open_layout(ctypes.byref(product_index.view), 0, layout, ctypes.byref(h)) == -1
 
 
 def test_index_read_errors(tmp_path):
