@@ -113,7 +113,7 @@ def build_index(args, seqs, readlen, device):
         hi, t = one(False)
         rep = {"where": "host", "seconds": t, "device_build_failed": str(e)[:200]}
         gpu_first = False
-    if args.index_check:
+    if args.index_check and "device_build_failed" not in rep:
         other, t2 = one(not gpu_first)
         rep["gpu_seconds"], rep["host_seconds"] = (t, t2) if gpu_first else (t2, t)
         rep["host_threads"] = os.cpu_count()
